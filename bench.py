@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 kNN path; prints one JSON line.
+
+Workload (default ``lidar``): the synthetic 64-beam lidar scan (about 1.15 M
+float32 points, 3-D), queried by the same scan after a random 2-degree
+rotation and a 0.1 m translation; k = 10, maxRadius = 1.0 m, self-match off,
+bucketSize 8 -- exact kNN through the CUDA kd-tree. ``--workload uniform``
+runs 1 M uniform points against 1 M uniform queries, k = 10.
+
+One step = one kNN search of every query of the batch.
+  value  queries/s with the cloud's tree and the queries already in HBM
+         (device API, CUDA events around each step, L2 flushed between steps)
+  e2e    the same search through the host API (nabo_cuda_knn) from pinned
+         host buffers: query upload, search, result download, per step
+  roofline  algorithmic bytes of the search kernel / its event-timed duration
+  cpu_baseline  the oracle's restatement of the reference's OpenMP
+         KDTREE_LINEAR_HEAP search timed on this host's cores
+
+``--impl reference`` times the reference algorithm on the host CPU instead
+(the C++ restatement in oracle/, all host threads) on the same workload.
+Multi-GPU (torchrun): every rank builds a replica of the tree and searches
+its own query batch (weak scaling, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "exact kNN queries/s (1M-pt 3D, k=10): learned-radius vs plain GPU kd-tree"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--workload", choices=["lidar", "uniform"], default="lidar")
+    p.add_argument("--k", type=int, default=10)
+    p.add_argument("--e2e-steps", type=int, default=None)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def workload(name: str, rank: int):
+    from libnabo_gb300 import synthetic as S
+    if name == "lidar":
+        cloud = S.lidar_scan()
+        q = S.lidar_queries(cloud, seed=S.SEED_BASE + 1 + 7919 * rank)
+        return cloud, q, dict(maxRadius=1.0, flags=0, label="lidar64_1.15M")
+    cloud = S.uniform(1_000_000, 3, seed=S.SEED_BASE + 5)
+    q = S.uniform(1_000_000, 3, seed=S.SEED_BASE + 6 + 7919 * rank)
+    return cloud, q, dict(maxRadius=float("inf"), flags=0, label="uniform_1M")
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(label: str, k: int):
+    """DRAM bytes per launch of the search kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", f"knn_kdtree_{label}_k{k}.txt")
+    if not os.path.exists(path):
+        return None, None
+    per_launch, nq = None, None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("dram_bytes_per_launch:"):
+                per_launch = float(line.split(":", 1)[1])
+            if line.startswith("queries_per_launch:"):
+                nq = float(line.split(":", 1)[1])
+    return per_launch, nq
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = f"/tmp/nabo_clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(cloud, q, k, cfg, reps=3):
+    """The reference's OpenMP KDTREE_LINEAR_HEAP search (oracle restatement)
+    on all host threads: build time and best-of-`reps` query throughput."""
+    from oracle import oracle as O
+    threads = O.num_threads()
+    t0 = time.perf_counter()
+    tree = O.OracleTree(cloud, bucket_size=8)
+    build_s = time.perf_counter() - t0
+    tree.knn(q[:10000], k, 0.0, cfg["flags"], cfg["maxRadius"], mode=O.MODE_REFERENCE)
+    best = None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        tree.knn(q, k, 0.0, cfg["flags"], cfg["maxRadius"], mode=O.MODE_REFERENCE)
+        dt = time.perf_counter() - t0
+        best = dt if best is None else min(best, dt)
+    stats_tree = O.OracleTree(cloud, bucket_size=8, creation_flags=O.TOUCH_STATISTICS)
+    sample = q[: min(len(q), 100000)]
+    _, _, touched = stats_tree.knn(sample, k, 0.0, cfg["flags"], cfg["maxRadius"], mode=O.MODE_REFERENCE)
+    return {"value": q.shape[0] / best, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"all {q.shape[0]} queries of the workload, best of {reps} after 1 warm-up; "
+                      f"tree build {build_s:.3f} s single-threaded",
+            "build_s": build_s, "touched_per_query": touched / sample.shape[0]}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    cloud, q, cfg = workload(args.workload, 0)
+    k = args.k
+    tree = O.OracleTree(cloud, bucket_size=8)
+    for _ in range(max(args.warmup, 1)):
+        tree.knn(q, k, 0.0, cfg["flags"], cfg["maxRadius"], mode=O.MODE_REFERENCE)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        tree.knn(q, k, 0.0, cfg["flags"], cfg["maxRadius"], mode=O.MODE_REFERENCE)
+        times.append(time.perf_counter() - t0)
+    per = sum(times) / len(times)
+    value = q.shape[0] / per
+    threads = O.num_threads()
+    out = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"{cfg['label']}_k{k}", "points": int(cloud.shape[0]), "queries": int(q.shape[0]),
+                   "k": k, "maxRadius": cfg["maxRadius"], "bucketSize": 8,
+                   "search": "KDTREE_LINEAR_HEAP restated in C++/OpenMP (oracle/nabo_oracle.cpp)"},
+        "cpu_baseline": {"value": value, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"all {q.shape[0]} queries per step"},
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import libnabo_gb300 as nb
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    k = args.k
+    cloud, q, cfg = workload(args.workload, rank)
+    nq = q.shape[0]
+    stream = torch.cuda.current_stream(dev)
+
+    # build (timed separately, reported as a side figure)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": 8})
+    build_s = time.perf_counter() - t0
+    # a second build after warm-up is the steady-state figure
+    s.close()
+    t0 = time.perf_counter()
+    s = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": 8})
+    build_s = min(build_s, time.perf_counter() - t0)
+    s_stats = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, creationOptionFlags=nb.TOUCH_STATISTICS)
+
+    tq = torch.from_numpy(q).to(dev)
+    idx = torch.empty((nq, k), dtype=torch.int32, device=dev)
+    d2 = torch.empty((nq, k), dtype=torch.float32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    touched = torch.zeros(1, dtype=torch.int64, device=dev)
+    s_stats.knn_device(tq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(idx, d2), touched=touched)
+    torch.cuda.synchronize()
+    p_bar = int(touched.item()) / nq
+    s.profile(True)
+
+    def step():
+        s.knn_device(tq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(idx, d2))
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kernel_ms = []
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            flush.zero_()
+            starts[i].record(stream)
+            step()
+            ends[i].record(stream)
+            kernel_ms.append(s.last_kernel_ms())
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * nq / (ms_per_step / 1e3)
+
+    # end to end through the host API, pinned host buffers
+    e2e_steps = args.e2e_steps or max(3, min(args.steps, 10))
+    hq = torch.from_numpy(q).pin_memory().numpy()
+    hidx = torch.empty((nq, k), dtype=torch.int32).pin_memory().numpy()
+    hd2 = torch.empty((nq, k), dtype=torch.float32).pin_memory().numpy()
+    for _ in range(2):
+        s.knn(hq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(hidx, hd2))
+    e2e_t = []
+    for _ in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.knn(hq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(hidx, hd2))
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_t) / len(e2e_t)
+    if world > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * nq / e2e_s
+
+    # roofline of the search kernel: algorithmic bytes per query
+    #   B_q = D*s + k*(4+s) + P*(D*s + 4)   (query, results, touched points)
+    dsz, D = 4, 3
+    b_q = D * dsz + k * (4 + dsz) + p_bar * (D * dsz + 4)
+    kern_s = statistics.mean(kernel_ms) / 1e3
+    achieved = nq * b_q / kern_s / 1e9
+    peak, peak_kind = measured_peaks()
+    traffic_launch, traffic_nq = profiled_traffic(cfg["label"], k)
+    traffic = None
+    if traffic_launch is not None and traffic_nq:
+        traffic = traffic_launch * nq / traffic_nq
+
+    if rank != 0:
+        return
+    base = None
+    if not args.no_cpu_baseline:
+        base = cpu_baseline(cloud, q, k, cfg)
+    clocks = clk.summary()
+    launches_per_step = 6 if nq >= 4096 else 1
+    out = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{cfg['label']}_k{k}", "points": int(cloud.shape[0]), "queries": int(nq),
+                   "k": k, "maxRadius": cfg["maxRadius"], "selfMatch": False, "bucketSize": 8,
+                   "form": "plain GPU kd-tree", "l2": "flushed between steps (256 MiB write)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
+                "d2h_bytes_per_step": int(hidx.nbytes + hd2.nbytes + 8)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "peak_source": peak_kind, "kernel": "k_knn_kdtree",
+                     "kernel_ms": kern_s * 1e3, "bytes_per_query": b_q, "touched_per_query": p_bar},
+        "cpu_baseline": base,
+        "clocks": clocks,
+        "gpu_launches": launches_per_step * args.steps,
+        "build_ms": build_s * 1e3,
+    }
+    if base is not None:
+        out["cpu_baseline"] = {kk: base[kk] for kk in ("value", "unit", "cores", "kind", "sample")}
+        out["cpu_baseline"]["build_s"] = base["build_s"]
+        out["cpu_baseline"]["touched_per_query"] = base["touched_per_query"]
+    print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,156 @@
+/* nabo_gb300.h -- C ABI of the GB300 kNN search library.
+ *
+ * A drop-in for the k-nearest-neighbour path of libnabo 1.1.2
+ * (Nabo::NearestNeighbourSearch<T>, nabo/nabo.h:257-441): the same build
+ * and search semantics, run on one NVIDIA GB300 (sm_103a). Plain pointers
+ * and sizes only; no C++ or framework types cross this boundary.
+ *
+ * Matrices use the reference's Eigen layout: a cloud or a query set is
+ * `rows x n`, column-major, one point per column, consecutive points
+ * `colStride` elements apart (colStride >= rows). Results are `k x nq`
+ * column-major: indices (int32) and squared distances (T) of the k
+ * neighbours of query i are at [i*k, i*k + k), ascending by distance.
+ * Unfound slots hold index -1 and distance +inf (nabo/nabo.h:216-226).
+ *
+ * Error handling: every function returns 0 on success or a NABO_CUDA_ERR_*
+ * code; nabo_cuda_last_error() returns the calling thread's message. The
+ * argument checks and their messages are those of the reference
+ * (nabo/nabo.cpp:102-131, :134-179; nabo/kdtree_cpu.cpp:234-251), which
+ * the C++ front end rethrows as exceptions.
+ */
+#ifndef NABO_GB300_H
+#define NABO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NABO_GB300_VERSION "0.1.0"
+#define NABO_GB300_REFERENCE_VERSION "1.1.2"
+
+/* Status codes. */
+#define NABO_CUDA_OK 0
+#define NABO_CUDA_ERR_ARGUMENT 1    /* the reference throws Nabo::runtime_error */
+#define NABO_CUDA_ERR_CUDA 2        /* CUDA runtime error (no GPU, out of memory, ...) */
+#define NABO_CUDA_ERR_UNSUPPORTED 3 /* valid for the reference, outside this library's limits */
+#define NABO_CUDA_ERR_INTERNAL 4
+
+/* Scalar types. */
+#define NABO_CUDA_FLOAT32 0
+#define NABO_CUDA_FLOAT64 1
+
+/* Search types: the reference's enum (nabo/nabo.h:290-299) extended with
+ * the CUDA types, placed after BRUTE_FORCE_CL. Only the CUDA types are
+ * implemented here; the CPU and OpenCL types stay in libnabo. */
+#define NABO_SEARCH_BRUTE_FORCE 0
+#define NABO_SEARCH_KDTREE_LINEAR_HEAP 1
+#define NABO_SEARCH_KDTREE_TREE_HEAP 2
+#define NABO_SEARCH_KDTREE_CL_PT_IN_NODES 3
+#define NABO_SEARCH_KDTREE_CL_PT_IN_LEAVES 4
+#define NABO_SEARCH_BRUTE_FORCE_CL 5
+#define NABO_SEARCH_KDTREE_CUDA 6
+#define NABO_SEARCH_BRUTE_FORCE_CUDA 7
+#define NABO_SEARCH_TYPE_COUNT 8
+
+/* Creation flags (nabo/nabo.h:302-305) and search flags (:308-312). */
+#define NABO_TOUCH_STATISTICS 1u
+#define NABO_ALLOW_SELF_MATCH 1u
+#define NABO_SORT_RESULTS 2u
+
+/* Additional parameters, the typed form of Nabo::Parameters
+ * (nabo/nabo.h:231-254). Initialise with nabo_cuda_params_init(). */
+typedef struct nabo_cuda_params {
+  uint32_t struct_size;   /* sizeof(nabo_cuda_params) */
+  uint32_t bucketSize;    /* "bucketSize", default 8 (nabo/kdtree_cpu.cpp:230) */
+  int32_t queryOrdering;  /* 1 (default): reorder queries along a Morton curve
+                             inside each search; 0: keep the given order */
+  int32_t reserved[5];
+} nabo_cuda_params;
+
+typedef struct nabo_cuda_search nabo_cuda_search; /* opaque */
+
+/* Fills `p` with the defaults. */
+void nabo_cuda_params_init(nabo_cuda_params* p);
+
+/* Builds a search object on the current CUDA device.
+ * Replaces NearestNeighbourSearch<T>::create (nabo/nabo.h:360,
+ * nabo/nabo.cpp:134-155) for the CUDA search types, and the constructors
+ * KDTreeUnbalancedPtInLeavesImplicitBoundsStackOpt (nabo/kdtree_cpu.cpp:
+ * 227-272) and BruteForceSearch (nabo/brute_force_cpu.cpp:44-60).
+ * `cloud` is HOST memory; it is copied to the device and not referenced
+ * after the call returns. `dim` is clamped to `rows` as in the reference.
+ * `params` may be NULL. */
+int nabo_cuda_create(int dtype, const void* cloud, int rows, int64_t n, int64_t colStride, int dim, int searchType,
+                     unsigned creationFlags, const nabo_cuda_params* params, nabo_cuda_search** out);
+
+/* Same, with `cloud` in DEVICE memory (read during the call only). */
+int nabo_cuda_create_device(int dtype, const void* cloud, int rows, int64_t n, int64_t colStride, int dim,
+                            int searchType, unsigned creationFlags, const nabo_cuda_params* params,
+                            nabo_cuda_search** out);
+
+/* Releases the object and its device memory. Accepts NULL.
+ * Replaces the virtual destructor (nabo/nabo.h:427). */
+int nabo_cuda_destroy(nabo_cuda_search* s);
+
+/* k-nearest-neighbour search with HOST buffers.
+ * Replaces NearestNeighbourSearch<T>::knn (nabo/nabo.h:338) when
+ * maxRadii == NULL (radius = maxRadius for every query) and the per-query
+ * radii overload (nabo/nabo.h:351) when maxRadii != NULL (nq values).
+ * query: qRows x nq column-major, column stride qStride (>= qRows).
+ * indices: k*nq int32; dists2: k*nq of the object's scalar type.
+ * touched (may be NULL): receives the reference's TOUCH_STATISTICS count
+ * (points examined in visited leaves; nq*n for brute force) when the
+ * object was created with NABO_TOUCH_STATISTICS, else 0.
+ * Results are always sorted ascending (SORT_RESULTS is accepted). */
+int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride, int k,
+                  double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii, int32_t* indices,
+                  void* dists2, uint64_t* touched);
+
+/* Same search with DEVICE buffers, stream-ordered on `stream` (a
+ * cudaStream_t; NULL = legacy default stream). Does not synchronise.
+ * touched (may be NULL) is a DEVICE uint64 to which the count is ADDED. */
+int nabo_cuda_knn_device(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride,
+                         int k, double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii,
+                         int32_t* indices, void* dists2, uint64_t* touched, void* stream);
+
+/* Object properties: the reference's public members dim, minBound,
+ * maxBound, creationOptionFlags (nabo/nabo.h:274-282) plus build facts.
+ * info[0]=dim info[1]=n info[2]=dtype info[3]=searchType
+ * info[4]=creationFlags info[5]=bucketSize info[6]=nodeCount
+ * info[7]=tree height (inner nodes on the longest root-to-leaf path). */
+int nabo_cuda_get_info(const nabo_cuda_search* s, int64_t info[8]);
+/* minBound/maxBound, `dim` values of the object's scalar type. */
+int nabo_cuda_get_bounds(const nabo_cuda_search* s, void* minBound, void* maxBound);
+
+/* Copies the kd-tree to host arrays (nodeCount entries each, pre-order):
+ * cutDim (-1 for a leaf), cutVal (scalar type), right child index,
+ * bucket start, bucket size; and `buckets` (n point indices in leaf
+ * order). Any pointer may be NULL. For parity checks against the
+ * reference's node array (nabo/nabo_private.h:138-177). */
+int nabo_cuda_export_tree(const nabo_cuda_search* s, int32_t* cutDim, void* cutVal, uint32_t* right,
+                          uint32_t* bucketStart, uint32_t* bucketSize, int32_t* buckets);
+
+/* Profiling aid (no reference counterpart; the reference times whole
+ * calls, tests/knnbench.cpp:134-169): when enabled, every later
+ * nabo_cuda_knn_device call on `s` records a pair of CUDA events right
+ * around its search kernel, and nabo_cuda_last_kernel_ms() waits for the
+ * second and returns the kernel's duration in milliseconds. Meant for
+ * single-threaded benchmarking; concurrent calls on one object overwrite
+ * each other's events. */
+int nabo_cuda_profile(nabo_cuda_search* s, int enable);
+int nabo_cuda_last_kernel_ms(const nabo_cuda_search* s, float* ms);
+
+/* Last error message of the calling thread ("" if none). */
+const char* nabo_cuda_last_error(void);
+
+/* Library version string. */
+const char* nabo_cuda_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NABO_GB300_H */

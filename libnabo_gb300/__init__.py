@@ -1,0 +1,298 @@
+"""libnabo_gb300 -- k-nearest-neighbour search on one NVIDIA GB300.
+
+A drop-in for the kNN path of libnabo 1.1.2. This module mirrors the
+reference's Python binding ``pynabo`` (python/nabo.cpp:95-218):
+``NearestNeighbourSearch(cloud, searchType, dim, creationOptionFlags,
+params)`` and ``.knn(query, k, epsilon, optionFlags, maxRadius)`` returning
+``(indices, dists2)``, plus the per-query radii overload of the C++ API
+(nabo/nabo.h:351). All compute runs in the CUDA library through the C ABI
+of include/nabo_gb300.h; there is no CPU path.
+
+Arrays: a cloud or query set is a C-contiguous numpy array of shape
+(n, dim) -- each point's coordinates contiguous, which is the reference's
+column-major dim x n layout. Results have shape (nq, k), ascending by
+distance; unfound slots hold index -1 and distance +inf.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+
+import numpy as np
+
+from ._native import lib as _lib
+from ._native import nabo_cuda_params
+
+__all__ = [
+    "SearchType", "SearchOptionFlags", "CreationOptionFlags", "NaboError", "NearestNeighbourSearch",
+    "InvalidIndex", "ALLOW_SELF_MATCH", "SORT_RESULTS", "TOUCH_STATISTICS", "version",
+]
+
+InvalidIndex = -1
+# default `dim`: numeric_limits<Index>::max(), clamped to the cloud rows (nabo/nabo.h:360)
+_DIM_ALL = 2**31 - 1
+
+
+class SearchType(enum.IntEnum):
+    """nabo/nabo.h:290-299, with the CUDA types after BRUTE_FORCE_CL."""
+    BRUTE_FORCE = 0
+    KDTREE_LINEAR_HEAP = 1
+    KDTREE_TREE_HEAP = 2
+    KDTREE_CL_PT_IN_NODES = 3
+    KDTREE_CL_PT_IN_LEAVES = 4
+    BRUTE_FORCE_CL = 5
+    KDTREE_CUDA = 6
+    BRUTE_FORCE_CUDA = 7
+    SEARCH_TYPE_COUNT = 8
+
+
+class SearchOptionFlags(enum.IntFlag):
+    """nabo/nabo.h:308-312."""
+    ALLOW_SELF_MATCH = 1
+    SORT_RESULTS = 2
+
+
+class CreationOptionFlags(enum.IntFlag):
+    """nabo/nabo.h:302-305."""
+    TOUCH_STATISTICS = 1
+
+
+ALLOW_SELF_MATCH = int(SearchOptionFlags.ALLOW_SELF_MATCH)
+SORT_RESULTS = int(SearchOptionFlags.SORT_RESULTS)
+TOUCH_STATISTICS = int(CreationOptionFlags.TOUCH_STATISTICS)
+
+_ERR_NAMES = {1: "argument", 2: "cuda", 3: "unsupported", 4: "internal"}
+
+
+class NaboError(RuntimeError):
+    """Error raised by the library; mirrors Nabo::runtime_error (nabo/nabo.cpp:50-66).
+
+    ``code`` is the C-ABI status (1 argument, 2 CUDA, 3 unsupported, 4 internal).
+    """
+
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+        self.kind = _ERR_NAMES.get(code, "unknown")
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise NaboError(rc, _lib.nabo_cuda_last_error().decode())
+
+
+def version() -> str:
+    return _lib.nabo_cuda_version().decode()
+
+
+def _dtype_code(dt) -> int:
+    dt = np.dtype(dt)
+    if dt == np.float32:
+        return 0
+    if dt == np.float64:
+        return 1
+    raise NaboError(1, f"unsupported scalar type {dt}; use float32 or float64")
+
+
+def _ptr(a) -> ctypes.c_void_p | None:
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+class NearestNeighbourSearch:
+    """A kNN search object on the current CUDA device.
+
+    Mirrors ``pynabo.NearestNeighbourSearch`` (python/nabo.cpp:98-130) and
+    ``Nabo::NearestNeighbourSearch<T>::create`` (nabo/nabo.h:360). ``cloud``
+    is a numpy array (host) or a CUDA torch tensor (device) of shape
+    (n, rows); it is copied into the search object. ``params`` accepts the
+    reference's ``bucketSize`` key and ``queryOrdering`` (1 = sort queries
+    along a Morton curve inside each search, the default).
+    """
+
+    def __init__(self, cloud, searchType: int = SearchType.KDTREE_CUDA, dim: int | None = None,
+                 creationOptionFlags: int = 0, params: dict | None = None):
+        self._h = ctypes.c_void_p()
+        p = nabo_cuda_params()
+        _lib.nabo_cuda_params_init(ctypes.byref(p))
+        for key, val in (params or {}).items():
+            if key == "bucketSize":
+                p.bucketSize = int(val)
+            elif key == "queryOrdering":
+                p.queryOrdering = int(val)
+            else:
+                raise NaboError(1, f"unknown parameter {key!r}")
+        self.searchType = int(searchType)
+        self.creationOptionFlags = int(creationOptionFlags)
+        if _is_torch(cloud):
+            import torch
+            if not cloud.is_cuda or cloud.dim() != 2:
+                raise NaboError(1, "a torch cloud must be a 2-D CUDA tensor")
+            cloud = cloud.contiguous()
+            self.dtype = np.dtype(str(cloud.dtype).replace("torch.", ""))
+            n, rows = cloud.shape
+            dimv = _DIM_ALL if dim is None else int(dim)
+            with torch.cuda.device(cloud.device):
+                torch.cuda.current_stream().synchronize()
+                _check(_lib.nabo_cuda_create_device(
+                    _dtype_code(self.dtype), ctypes.c_void_p(cloud.data_ptr()), rows, n, rows, dimv,
+                    self.searchType, self.creationOptionFlags, ctypes.byref(p), ctypes.byref(self._h)))
+        else:
+            cloud = np.asarray(cloud)
+            if cloud.ndim != 2:
+                raise NaboError(1, "cloud must be a 2-D array (points x coordinates)")
+            if cloud.dtype not in (np.float32, np.float64):
+                cloud = cloud.astype(np.float64)
+            cloud = np.ascontiguousarray(cloud)
+            self.dtype = cloud.dtype
+            n, rows = cloud.shape
+            dimv = _DIM_ALL if dim is None else int(dim)
+            _check(_lib.nabo_cuda_create(
+                _dtype_code(self.dtype), _ptr(cloud), rows, n, rows, dimv, self.searchType,
+                self.creationOptionFlags, ctypes.byref(p), ctypes.byref(self._h)))
+        info = (ctypes.c_int64 * 8)()
+        _check(_lib.nabo_cuda_get_info(self._h, info))
+        self.dim, self.n = int(info[0]), int(info[1])
+        self.bucketSize = int(info[5])
+        self.nodeCount, self.height = int(info[6]), int(info[7])
+        lo = np.zeros(self.dim, self.dtype)
+        hi = np.zeros(self.dim, self.dtype)
+        _check(_lib.nabo_cuda_get_bounds(self._h, _ptr(lo), _ptr(hi)))
+        self.minBound, self.maxBound = lo, hi
+        self.touched = 0
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            _lib.nabo_cuda_destroy(h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- search -----------------------------------------------------------
+    def knn(self, query, k: int = 1, epsilon: float = 0.0, optionFlags: int = 0, maxRadius: float = np.inf,
+            maxRadii=None, out=None):
+        """k nearest neighbours of each row of ``query``; returns (indices, dists2).
+
+        ``maxRadii`` (one radius per query) selects the reference's per-query
+        radius overload (nabo/nabo.h:351); otherwise ``maxRadius`` applies to
+        all queries (nabo/nabo.h:338). With TOUCH_STATISTICS the visited-point
+        count of the call is left in ``self.touched``. ``out`` may supply the
+        (indices, dists2) host arrays (C-contiguous, shape (nq, k)), e.g.
+        pinned buffers.
+        """
+        if _is_torch(query):
+            return self.knn_device(query, k, epsilon, optionFlags, maxRadius, maxRadii)
+        query = np.ascontiguousarray(np.asarray(query, dtype=self.dtype))
+        if query.ndim == 1:
+            query = query.reshape(1, -1)
+        nq, qrows = query.shape
+        kk = int(k)
+        if out is None:
+            idx = np.empty((nq, max(kk, 0)), np.int32)
+            d2 = np.empty((nq, max(kk, 0)), self.dtype)
+        else:
+            idx, d2 = out
+            if (idx.shape != (nq, kk) or d2.shape != (nq, kk) or idx.dtype != np.int32 or d2.dtype != self.dtype
+                    or not idx.flags.c_contiguous or not d2.flags.c_contiguous):
+                raise NaboError(1, "out arrays must be C-contiguous (nq, k) int32 / scalar arrays")
+        radii = None
+        if maxRadii is not None:
+            radii = np.ascontiguousarray(np.asarray(maxRadii, dtype=self.dtype).reshape(-1))
+            if radii.shape[0] != nq:
+                # nabo/nabo.cpp:126-127
+                raise NaboError(1, f"Maximum radii vector has not the same length ({radii.shape[0]}) "
+                                   f"than query has columns ({kk})")
+        touched = ctypes.c_uint64(0)
+        _check(_lib.nabo_cuda_knn(self._h, _ptr(query), qrows, nq, qrows, kk, float(epsilon), int(optionFlags),
+                                  float(maxRadius), _ptr(radii), _ptr(idx), _ptr(d2), ctypes.byref(touched)))
+        self.touched = int(touched.value)
+        return idx, d2
+
+    def knn_device(self, query, k: int = 1, epsilon: float = 0.0, optionFlags: int = 0,
+                   maxRadius: float = np.inf, maxRadii=None, out=None, touched=None, stream=None):
+        """Search with CUDA torch tensors, stream-ordered, no host synchronisation.
+
+        ``query`` is an (nq, rows) CUDA tensor; returns (indices, dists2) CUDA
+        tensors of shape (nq, k) (or fills ``out``). ``touched`` may be a
+        1-element int64 CUDA tensor to which the TOUCH_STATISTICS count is added.
+        """
+        import torch
+        if not query.is_cuda:
+            raise NaboError(1, "knn_device needs a CUDA tensor")
+        query = query.contiguous()
+        nq, qrows = query.shape
+        tdt = torch.float32 if self.dtype == np.float32 else torch.float64
+        if query.dtype != tdt:
+            raise NaboError(1, f"query dtype {query.dtype} does not match the cloud's {tdt}")
+        if out is None:
+            idx = torch.empty((nq, k), dtype=torch.int32, device=query.device)
+            d2 = torch.empty((nq, k), dtype=tdt, device=query.device)
+        else:
+            idx, d2 = out
+        rp = None
+        if maxRadii is not None:
+            maxRadii = maxRadii.contiguous()
+            if maxRadii.numel() != nq:
+                raise NaboError(1, f"Maximum radii vector has not the same length ({maxRadii.numel()}) "
+                                   f"than query has columns ({k})")
+            rp = ctypes.c_void_p(maxRadii.data_ptr())
+        st = stream if stream is not None else torch.cuda.current_stream(query.device).cuda_stream
+        tp = None if touched is None else ctypes.c_void_p(touched.data_ptr())
+        _check(_lib.nabo_cuda_knn_device(self._h, ctypes.c_void_p(query.data_ptr()), qrows, nq, qrows, int(k),
+                                         float(epsilon), int(optionFlags), float(maxRadius), rp,
+                                         ctypes.c_void_p(idx.data_ptr()), ctypes.c_void_p(d2.data_ptr()), tp,
+                                         ctypes.c_void_p(st)))
+        return idx, d2
+
+    def profile(self, enable: bool = True) -> None:
+        """Bracket the search kernel of later device searches with CUDA events."""
+        _check(_lib.nabo_cuda_profile(self._h, 1 if enable else 0))
+
+    def last_kernel_ms(self) -> float:
+        """Duration of the last device search's kernel (waits for it)."""
+        ms = ctypes.c_float(0.0)
+        _check(_lib.nabo_cuda_last_kernel_ms(self._h, ctypes.byref(ms)))
+        return float(ms.value)
+
+    def export_tree(self) -> dict:
+        """The kd-tree as numpy arrays in pre-order (for parity checks)."""
+        n = self.nodeCount
+        cut_dim = np.zeros(n, np.int32)
+        cut_val = np.zeros(n, self.dtype)
+        right = np.zeros(n, np.uint32)
+        b_start = np.zeros(n, np.uint32)
+        b_count = np.zeros(n, np.uint32)
+        buckets = np.zeros(self.n, np.int32)
+        _check(_lib.nabo_cuda_export_tree(self._h, _ptr(cut_dim), _ptr(cut_val), _ptr(right), _ptr(b_start),
+                                          _ptr(b_count), _ptr(buckets)))
+        return dict(cut_dim=cut_dim, cut_val=cut_val, right=right, bucket_start=b_start, bucket_count=b_count,
+                    buckets=buckets)
+
+    # Factory helpers named after the reference's (nabo/nabo.h:360-386).
+    @classmethod
+    def create(cls, cloud, dim=None, preferedType=SearchType.KDTREE_CUDA, creationOptionFlags=0,
+               additionalParameters=None):
+        return cls(cloud, preferedType, dim, creationOptionFlags, additionalParameters)
+
+    @classmethod
+    def createKDTreeCUDA(cls, cloud, dim=None, creationOptionFlags=0, additionalParameters=None):
+        return cls(cloud, SearchType.KDTREE_CUDA, dim, creationOptionFlags, additionalParameters)
+
+    @classmethod
+    def createBruteForceCUDA(cls, cloud, dim=None, creationOptionFlags=0):
+        return cls(cloud, SearchType.BRUTE_FORCE_CUDA, dim, creationOptionFlags, None)

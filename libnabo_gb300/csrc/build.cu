@@ -1,0 +1,1017 @@
+// build.cu -- kd-tree construction on the device.
+//
+// Produces exactly the tree of the reference constructor
+// KDTreeUnbalancedPtInLeavesImplicitBoundsStackOpt (nabo/kdtree_cpu.cpp:
+// 109-272): sliding-midpoint split on the widest box dimension, cut clamped
+// to the points' range, the two-pass in-place partition, the same leftCount
+// rules, pre-order node numbering with the left child at n+1, and leaf
+// buckets in the same point order. Points are stored in leaf order as
+// 16-byte-aligned records, so a bucket is a contiguous run.
+//
+// Phases:
+//   1. pack + bounds: records in cloud order, per-dimension min/max.
+//   2. top levels (segments larger than kSmallMax points), level by level,
+//      all segments of a level at once:
+//        prepare  cut dimension from the segment's box
+//        minmax   min/max of the cut coordinate over the segment
+//        cut      clamp the box midpoint into [min, max]
+//        count    #(< cut) and #(== cut)
+//        pass 1/2 the reference's two Hoare-style passes: the i-th misplaced
+//                 element from the left trades places with the i-th
+//                 misplaced element from the right. Ranks come from a
+//                 device-wide exclusive scan of the misplaced flags, the
+//                 pairs are written to two slot tables and swapped.
+//        finalize leftCount, node, children
+//   3. small segments: one thread each runs the reference's sequential
+//      recursion (as an explicit stack in global scratch) on its points,
+//      emitting a pre-order subtree into a private node range.
+//   4. renumber: subtree sizes bottom-up, pre-order positions top-down,
+//      then every node is written to its final slot.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <limits>
+#include <vector>
+
+#include "internal.cuh"
+
+namespace nabo_gb300 {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kSmallMax = 256;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int2 add2(int2 a, int2 b) { return make_int2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ uint32_t shfl_up(uint32_t v, int o) { return __shfl_up_sync(kFull, v, o); }
+__device__ __forceinline__ unsigned long long shfl_up(unsigned long long v, int o) {
+  return __shfl_up_sync(kFull, v, o);
+}
+__device__ __forceinline__ int2 shfl_up(int2 v, int o) {
+  return make_int2(__shfl_up_sync(kFull, v.x, o), __shfl_up_sync(kFull, v.y, o));
+}
+
+struct MinOp {
+  template <typename V>
+  __device__ V operator()(V a, V b) const { return a < b ? a : b; }
+};
+struct MaxOp {
+  template <typename V>
+  __device__ V operator()(V a, V b) const { return a > b ? a : b; }
+};
+struct AddOp {
+  __device__ int2 operator()(int2 a, int2 b) const { return add2(a, b); }
+};
+
+// Reduction over runs of equal segment id inside a warp (segments are
+// contiguous position ranges, so equal ids form one run). Returns the run's
+// reduction in the run's last lane (`tail`).
+template <typename V, typename Op>
+__device__ __forceinline__ V seg_warp_reduce(int s, V v, Op op, bool* tail) {
+  const int lane = threadIdx.x & 31;
+  const int prev = __shfl_up_sync(kFull, s, 1);
+  const bool head = (lane == 0) || (prev != s);
+  const unsigned heads = __ballot_sync(kFull, head);
+  const unsigned upto = heads & (kFull >> (31 - lane));
+  const int runStart = 31 - __clz(upto);
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const V y = shfl_up(v, o);
+    if (lane - o >= runStart) v = op(v, y);
+  }
+  *tail = (lane == 31) || ((heads >> (lane + 1)) & 1u);
+  return v;
+}
+
+__device__ __forceinline__ int2 warp_incl_scan(int2 v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int2 y = shfl_up(v, o);
+    if (lane >= o) v = add2(v, y);
+  }
+  return v;
+}
+
+// Exclusive scan over a block of kBlock threads.
+__device__ __forceinline__ int2 block_excl_scan(int2 v, int2* total) {
+  __shared__ int2 sw[kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int2 inc = warp_incl_scan(v, lane);
+  if (lane == 31) sw[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    int2 w = lane < kBlock / 32 ? sw[lane] : make_int2(0, 0);
+    w = warp_incl_scan(w, lane);
+    if (lane < kBlock / 32) sw[lane] = w;
+  }
+  __syncthreads();
+  const int2 wpre = warp > 0 ? sw[warp - 1] : make_int2(0, 0);
+  *total = sw[kBlock / 32 - 1];
+  __syncthreads();
+  return add2(wpre, make_int2(inc.x - v.x, inc.y - v.y));
+}
+
+template <typename T>
+struct Box {
+  T lo[kMaxDim];
+  T hi[kMaxDim];
+};
+
+// ---------------------------------------------------------------------------
+// Phase 1: packing and bounds.
+
+template <typename T, int D>
+__global__ void k_pack(const T* __restrict__ cloud, int64_t n, int64_t stride, int dim, Rec<T, D>* __restrict__ recs) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  Rec<T, D> r;
+#pragma unroll
+  for (int c = 0; c < RecSize<T, D>::chunks; ++c) r.v[c] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+  for (int d = 0; d < D; ++d) r.p.c[d] = d < dim ? cloud[p * stride + d] : T(0);
+  r.p.idx = (int32_t)p;
+  recs[p] = r;
+}
+
+template <typename K>
+__device__ __forceinline__ K warp_min(K v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const K y = __shfl_xor_sync(kFull, v, o);
+    v = y < v ? y : v;
+  }
+  return v;
+}
+template <typename K>
+__device__ __forceinline__ K warp_max(K v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const K y = __shfl_xor_sync(kFull, v, o);
+    v = y > v ? y : v;
+  }
+  return v;
+}
+
+template <typename T, int D>
+__global__ void k_bounds(const Rec<T, D>* __restrict__ recs, int64_t n, int dim, typename KeyOf<T>::type* mnK,
+                         typename KeyOf<T>::type* mxK) {
+  using Key = typename KeyOf<T>::type;
+  Key mn[D], mx[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    mn[d] = ordered_key(Ar<T>::inf());
+    mx[d] = ordered_key(-Ar<T>::inf());
+  }
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    Rec<T, D> r;
+    load_rec(recs, p, r);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const Key k = ordered_key(r.p.c[d]);
+      mn[d] = k < mn[d] ? k : mn[d];
+      mx[d] = k > mx[d] ? k : mx[d];
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    const Key a = warp_min(mn[d]);
+    const Key b = warp_max(mx[d]);
+    if ((threadIdx.x & 31) == 0 && d < dim) {
+      atomicMin(mnK + d, a);
+      atomicMax(mxK + d, b);
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_init_keys(typename KeyOf<T>::type* mnK, typename KeyOf<T>::type* mxK, int dim) {
+  const int d = threadIdx.x;
+  if (d < dim) {
+    mnK[d] = ordered_key(Ar<T>::inf());
+    mxK[d] = ordered_key(-Ar<T>::inf());
+  }
+}
+
+template <typename T>
+__global__ void k_decode_keys(const typename KeyOf<T>::type* mnK, const typename KeyOf<T>::type* mxK, int dim,
+                              T* lo, T* hi) {
+  const int d = threadIdx.x;
+  if (d < dim) {
+    lo[d] = ordered_val(mnK[d], T(0));
+    hi[d] = ordered_val(mxK[d], T(0));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Phase 2: top levels.
+
+template <typename T>
+struct SegLevel {
+  int* start;
+  int* count;
+  T* boxLo;  // [cap * kMaxDim]
+  T* boxHi;
+  int* cutDim;
+  typename KeyOf<T>::type* mnK;
+  typename KeyOf<T>::type* mxK;
+  T* cut;
+  int* mode;  // 0: midpoint inside range, 1: below min, 2: above max
+  int* lt;
+  int* eq;
+  int* leftCount;
+  int* newLeft;
+  int* newRight;
+};
+
+template <typename T>
+struct TopNodes {
+  int* dim;
+  T* cut;
+  int* left;   // >= 0: top node id; < 0: ~small segment id
+  int* right;
+  int* size;
+  int* pre;
+};
+
+template <typename T>
+struct SmallSegs {
+  int* start;
+  int* count;
+  int* depth;
+  T* boxLo;  // [cap * kMaxDim]
+  T* boxHi;
+  int* size;
+  int* base;
+};
+
+template <typename T>
+__global__ void k_root_segment(SegLevel<T> L, int n, Box<T> box, int dim) {
+  L.start[0] = 0;
+  L.count[0] = n;
+  for (int d = 0; d < dim; ++d) {
+    L.boxLo[d] = box.lo[d];
+    L.boxHi[d] = box.hi[d];
+  }
+}
+
+template <typename T>
+__global__ void k_root_small(SmallSegs<T> S, int n, Box<T> box, int dim) {
+  S.start[0] = 0;
+  S.count[0] = n;
+  S.depth[0] = 0;
+  for (int d = 0; d < dim; ++d) {
+    S.boxLo[d] = box.lo[d];
+    S.boxHi[d] = box.hi[d];
+  }
+}
+
+// argMax of the box extents (nabo/kdtree_cpu.cpp:76-90): first strict
+// maximum, starting from 0, so all-zero extents give dimension 0.
+template <typename T>
+__device__ __forceinline__ int arg_max_extent(const T* lo, const T* hi, int dim) {
+  T best = T(0);
+  int bd = 0;
+  for (int d = 0; d < dim; ++d) {
+    const T e = Ar<T>::sub(hi[d], lo[d]);
+    if (e > best) {
+      best = e;
+      bd = d;
+    }
+  }
+  return bd;
+}
+
+template <typename T>
+__global__ void k_prepare(SegLevel<T> L, int nseg, int dim) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  L.cutDim[s] = arg_max_extent(L.boxLo + (int64_t)s * kMaxDim, L.boxHi + (int64_t)s * kMaxDim, dim);
+  L.mnK[s] = ordered_key(std::numeric_limits<T>::max());
+  L.mxK[s] = ordered_key(std::numeric_limits<T>::lowest());
+  L.lt[s] = 0;
+  L.eq[s] = 0;
+}
+
+template <typename T, int D>
+__global__ void k_minmax(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L) {
+  using Key = typename KeyOf<T>::type;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = -1;
+  Key kmin = 0, kmax = 0;
+  if (p < n) {
+    s = segOf[p];
+    if (s >= 0) {
+      const T v = recs[p].p.c[L.cutDim[s]];
+      kmin = kmax = ordered_key(v);
+    }
+  }
+  bool tail;
+  kmin = seg_warp_reduce(s, kmin, MinOp(), &tail);
+  kmax = seg_warp_reduce(s, kmax, MaxOp(), &tail);
+  if (tail && s >= 0) {
+    atomicMin(L.mnK + s, kmin);
+    atomicMax(L.mxK + s, kmax);
+  }
+}
+
+template <typename T>
+__global__ void k_cut(SegLevel<T> L, int nseg) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const int cd = L.cutDim[s];
+  const T mn = ordered_val(L.mnK[s], T(0));
+  const T mx = ordered_val(L.mxK[s], T(0));
+  // (max + min) / 2 as the reference writes it (nabo/kdtree_cpu.cpp:135);
+  // halving is exact, so multiplying by 1/2 gives the same value.
+  const T ideal = Ar<T>::mul(Ar<T>::add(L.boxHi[(int64_t)s * kMaxDim + cd], L.boxLo[(int64_t)s * kMaxDim + cd]), T(0.5));
+  T cut;
+  int mode;
+  if (ideal < mn) {
+    cut = mn;
+    mode = 1;
+  } else if (ideal > mx) {
+    cut = mx;
+    mode = 2;
+  } else {
+    cut = ideal;
+    mode = 0;
+  }
+  L.cut[s] = cut;
+  L.mode[s] = mode;
+}
+
+template <typename T, int D>
+__global__ void k_count(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = -1;
+  int2 c = make_int2(0, 0);
+  if (p < n) {
+    s = segOf[p];
+    if (s >= 0) {
+      const T v = recs[p].p.c[L.cutDim[s]];
+      const T cut = L.cut[s];
+      c = make_int2(v < cut ? 1 : 0, v == cut ? 1 : 0);
+    }
+  }
+  bool tail;
+  c = seg_warp_reduce(s, c, AddOp(), &tail);
+  if (tail && s >= 0) {
+    if (c.x) atomicAdd(L.lt + s, c.x);
+    if (c.y) atomicAdd(L.eq + s, c.y);
+  }
+}
+
+// Misplaced flags of the reference's partition passes (nabo/kdtree_cpu.cpp
+// :149-177). Pass 1 scans the whole segment for `< cut`: a left element
+// that is not `< cut` inside the first L positions trades with a right
+// element that is not `>= cut`. Pass 2 scans from br1 = L for `<= cut`.
+template <typename T, int D>
+__device__ __forceinline__ int2 misplaced(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n,
+                                          const SegLevel<T>& L, int pass, int p, int* segOut) {
+  int2 f = make_int2(0, 0);
+  int s = -1;
+  if (p < n) {
+    s = segOf[p];
+    if (s >= 0) {
+      const T v = recs[p].p.c[L.cutDim[s]];
+      const T cut = L.cut[s];
+      const int loc = p - L.start[s];
+      const int lt = L.lt[s];
+      if (pass == 1) {
+        f.x = (loc < lt && !(v < cut)) ? 1 : 0;
+        f.y = (loc >= lt && !(v >= cut)) ? 1 : 0;
+      } else {
+        const int le = lt + L.eq[s];
+        f.x = (loc >= lt && loc < le && !(v <= cut)) ? 1 : 0;
+        f.y = (loc >= le && !(v > cut)) ? 1 : 0;
+      }
+    }
+  }
+  *segOut = s;
+  return f;
+}
+
+template <typename T, int D>
+__global__ void k_flag_sums(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
+                            int pass, int2* blockSums) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  int s;
+  const int2 f = misplaced(recs, segOf, n, L, pass, p, &s);
+  int2 total;
+  block_excl_scan(f, &total);
+  if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+}
+
+// Single block: exclusive scan of the per-block sums; the grand total goes
+// to *total.
+__global__ void k_scan_block_sums(int2* sums, int nb, int2* total) {
+  int2 carry = make_int2(0, 0);
+  for (int base = 0; base < nb; base += kBlock) {
+    const int i = base + threadIdx.x;
+    const int2 v = i < nb ? sums[i] : make_int2(0, 0);
+    int2 t;
+    const int2 ex = block_excl_scan(v, &t);
+    if (i < nb) sums[i] = add2(carry, ex);
+    carry = add2(carry, t);
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+template <typename T, int D>
+__global__ void k_flag_ranks(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
+                             int pass, const int2* blockPrefix, int2* S) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  int s;
+  const int2 f = misplaced(recs, segOf, n, L, pass, p, &s);
+  int2 total;
+  const int2 ex = block_excl_scan(f, &total);
+  if (p < n) S[p] = add2(ex, blockPrefix[blockIdx.x]);
+}
+
+template <typename T, int D>
+__global__ void k_pairs(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
+                        int pass, const int2* __restrict__ S, int* pairA, int* pairB) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  int s;
+  const int2 f = misplaced(recs, segOf, n, L, pass, p, &s);
+  if (f.x) pairA[S[p].x] = p;
+  if (f.y) {
+    const int st = L.start[s];
+    const int base = S[st].y;
+    const int m = S[st + L.count[s]].y - base;
+    const int j = S[p].y - base;
+    pairB[base + m - 1 - j] = p;
+  }
+}
+
+template <typename T, int D>
+__global__ void k_swap(Rec<T, D>* recs, const int* __restrict__ pairA, const int* __restrict__ pairB,
+                       const int2* __restrict__ total, int cap) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cap || t >= total->x) return;
+  const int a = pairA[t], b = pairB[t];
+  const Rec<T, D> ra = recs[a];
+  recs[a] = recs[b];
+  recs[b] = ra;
+}
+
+// nabo/kdtree_cpu.cpp:180-223: leftCount rule, node, children.
+template <typename T>
+__global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, int nseg, int levelBase, int nextLevelBase, int level,
+                           TopNodes<T> top, SmallSegs<T> small, int* counters, int dim) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nseg) return;
+  const int count = L.count[s];
+  const int start = L.start[s];
+  const int br1 = L.lt[s];
+  const int br2 = br1 + L.eq[s];
+  const int mode = L.mode[s];
+  int leftCount;
+  if (mode == 1)
+    leftCount = 1;
+  else if (mode == 2)
+    leftCount = count - 1;
+  else if (br1 > count / 2)
+    leftCount = br1;
+  else if (br2 < count / 2)
+    leftCount = br2;
+  else
+    leftCount = count / 2;
+  const int cd = L.cutDim[s];
+  const T cut = L.cut[s];
+  const int node = levelBase + s;
+  top.dim[node] = cd;
+  top.cut[node] = cut;
+  L.leftCount[s] = leftCount;
+  const T* lo = L.boxLo + (int64_t)s * kMaxDim;
+  const T* hi = L.boxHi + (int64_t)s * kMaxDim;
+  for (int side = 0; side < 2; ++side) {
+    const int cst = side == 0 ? start : start + leftCount;
+    const int ccount = side == 0 ? leftCount : count - leftCount;
+    int ref, newSeg = -1;
+    T* dLo;
+    T* dHi;
+    if (ccount > kSmallMax) {
+      const int id = atomicAdd(counters + 0, 1);
+      next.start[id] = cst;
+      next.count[id] = ccount;
+      dLo = next.boxLo + (int64_t)id * kMaxDim;
+      dHi = next.boxHi + (int64_t)id * kMaxDim;
+      ref = nextLevelBase + id;
+      newSeg = id;
+    } else {
+      const int sid = atomicAdd(counters + 1, 1);
+      small.start[sid] = cst;
+      small.count[sid] = ccount;
+      small.depth[sid] = level + 1;
+      dLo = small.boxLo + (int64_t)sid * kMaxDim;
+      dHi = small.boxHi + (int64_t)sid * kMaxDim;
+      ref = ~sid;
+    }
+    for (int d = 0; d < dim; ++d) {
+      dLo[d] = lo[d];
+      dHi[d] = hi[d];
+    }
+    if (side == 0) {
+      dHi[cd] = cut;
+      top.left[node] = ref;
+      L.newLeft[s] = newSeg;
+    } else {
+      dLo[cd] = cut;
+      top.right[node] = ref;
+      L.newRight[s] = newSeg;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_update_segof(int* segOf, int n, SegLevel<T> L) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  const int s = segOf[p];
+  if (s < 0) return;
+  const int loc = p - L.start[s];
+  segOf[p] = loc < L.leftCount[s] ? L.newLeft[s] : L.newRight[s];
+}
+
+// ---------------------------------------------------------------------------
+// Phase 3: one thread per small segment, the reference's recursion with an
+// explicit stack held in global scratch at the segment's own position range.
+
+template <typename T>
+struct SmallStack {
+  int* start;
+  int* count;
+  int* parent;
+  int* depth;
+  T* boxLo;  // [n * kMaxDim]
+  T* boxHi;
+};
+
+template <typename T, int D>
+__global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, int nSmall, Node<T>* scratch, SmallStack<T> stk,
+                        int dim, unsigned bucketSize, int* counters) {
+  const int sid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sid >= nSmall) return;
+  const int base = small.start[sid];
+  Node<T>* out = scratch + 2 * (int64_t)base;
+  int sp = 0;
+  {
+    const int e = base;
+    stk.start[e] = base;
+    stk.count[e] = small.count[sid];
+    stk.parent[e] = -1;
+    stk.depth[e] = small.depth[sid];
+    for (int d = 0; d < dim; ++d) {
+      stk.boxLo[(int64_t)e * kMaxDim + d] = small.boxLo[(int64_t)sid * kMaxDim + d];
+      stk.boxHi[(int64_t)e * kMaxDim + d] = small.boxHi[(int64_t)sid * kMaxDim + d];
+    }
+    sp = 1;
+  }
+  int emitted = 0;
+  int hmax = 0;
+  T lo[kMaxDim], hi[kMaxDim];
+  while (sp > 0) {
+    --sp;
+    const int e = base + sp;
+    const int st = stk.start[e];
+    const int count = stk.count[e];
+    const int parent = stk.parent[e];
+    const int depth = stk.depth[e];
+    const int local = emitted++;
+    if (parent >= 0) out[parent].meta = make_meta(node_dim(out[parent].meta), (uint32_t)local);
+    if (count <= (int)bucketSize) {
+      store_leaf(out + local, (uint32_t)count, (uint32_t)st);
+      hmax = depth > hmax ? depth : hmax;
+      continue;
+    }
+    for (int d = 0; d < dim; ++d) {
+      lo[d] = stk.boxLo[(int64_t)e * kMaxDim + d];
+      hi[d] = stk.boxHi[(int64_t)e * kMaxDim + d];
+    }
+    const int cd = arg_max_extent(lo, hi, dim);
+    const T ideal = Ar<T>::mul(Ar<T>::add(hi[cd], lo[cd]), T(0.5));
+    T mn = std::numeric_limits<T>::max(), mx = std::numeric_limits<T>::lowest();
+    for (int i = 0; i < count; ++i) {
+      const T v = recs[st + i].p.c[cd];
+      mn = (mn < v) ? mn : v;
+      mx = (v < mx) ? mx : v;
+    }
+    T cut;
+    if (ideal < mn)
+      cut = mn;
+    else if (ideal > mx)
+      cut = mx;
+    else
+      cut = ideal;
+    // two-pass partition, nabo/kdtree_cpu.cpp:149-177
+    Rec<T, D>* pts = recs + st;
+    int l = 0, r = count - 1;
+    for (;;) {
+      while (l < count && pts[l].p.c[cd] < cut) ++l;
+      while (r >= 0 && pts[r].p.c[cd] >= cut) --r;
+      if (l > r) break;
+      const Rec<T, D> tmp = pts[l];
+      pts[l] = pts[r];
+      pts[r] = tmp;
+      ++l;
+      --r;
+    }
+    const int br1 = l;
+    r = count - 1;
+    for (;;) {
+      while (l < count && pts[l].p.c[cd] <= cut) ++l;
+      while (r >= br1 && pts[r].p.c[cd] > cut) --r;
+      if (l > r) break;
+      const Rec<T, D> tmp = pts[l];
+      pts[l] = pts[r];
+      pts[r] = tmp;
+      ++l;
+      --r;
+    }
+    const int br2 = l;
+    int leftCount;
+    if (ideal < mn)
+      leftCount = 1;
+    else if (ideal > mx)
+      leftCount = count - 1;
+    else if (br1 > count / 2)
+      leftCount = br1;
+    else if (br2 < count / 2)
+      leftCount = br2;
+    else
+      leftCount = count / 2;
+    store_inner(out + local, (uint32_t)cd, 0u, cut);
+    // push right (processed after the whole left subtree), then left
+    {
+      const int f = base + sp;
+      stk.start[f] = st + leftCount;
+      stk.count[f] = count - leftCount;
+      stk.parent[f] = local;
+      stk.depth[f] = depth + 1;
+      for (int d = 0; d < dim; ++d) {
+        stk.boxLo[(int64_t)f * kMaxDim + d] = d == cd ? cut : lo[d];
+        stk.boxHi[(int64_t)f * kMaxDim + d] = hi[d];
+      }
+      ++sp;
+    }
+    {
+      const int f = base + sp;
+      stk.start[f] = st;
+      stk.count[f] = leftCount;
+      stk.parent[f] = -1;
+      stk.depth[f] = depth + 1;
+      for (int d = 0; d < dim; ++d) {
+        stk.boxLo[(int64_t)f * kMaxDim + d] = lo[d];
+        stk.boxHi[(int64_t)f * kMaxDim + d] = d == cd ? cut : hi[d];
+      }
+      ++sp;
+    }
+  }
+  small.size[sid] = emitted;
+  atomicMax(counters + 2, hmax);
+}
+
+// ---------------------------------------------------------------------------
+// Phase 4: pre-order numbering (single block).
+
+template <typename T>
+__device__ __forceinline__ int subtree_size(const TopNodes<T>& top, const SmallSegs<T>& small, int ref) {
+  return ref >= 0 ? top.size[ref] : small.size[~ref];
+}
+
+template <typename T>
+__global__ void k_renumber(TopNodes<T> top, SmallSegs<T> small, const int* lvStart, const int* lvCount, int nLevels,
+                           Node<T>* nodes, long long* total) {
+  if (nLevels == 0) {
+    if (threadIdx.x == 0) {
+      small.base[0] = 0;
+      *total = small.size[0];
+    }
+    return;
+  }
+  for (int l = nLevels - 1; l >= 0; --l) {
+    const int b = lvStart[l], c = lvCount[l];
+    for (int i = threadIdx.x; i < c; i += blockDim.x) {
+      const int t = b + i;
+      top.size[t] = 1 + subtree_size(top, small, top.left[t]) + subtree_size(top, small, top.right[t]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    top.pre[0] = 0;
+    *total = top.size[0];
+  }
+  __syncthreads();
+  for (int l = 0; l < nLevels; ++l) {
+    const int b = lvStart[l], c = lvCount[l];
+    for (int i = threadIdx.x; i < c; i += blockDim.x) {
+      const int t = b + i;
+      const int p = top.pre[t];
+      const int lref = top.left[t], rref = top.right[t];
+      const int lp = p + 1;
+      const int rp = p + 1 + subtree_size(top, small, lref);
+      if (lref >= 0)
+        top.pre[lref] = lp;
+      else
+        small.base[~lref] = lp;
+      if (rref >= 0)
+        top.pre[rref] = rp;
+      else
+        small.base[~rref] = rp;
+      store_inner(nodes + p, (uint32_t)top.dim[t], (uint32_t)rp, top.cut[t]);
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+__global__ void k_copy_small(const Node<T>* scratch, SmallSegs<T> small, int nSmall, Node<T>* nodes) {
+  const int sid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (sid >= nSmall) return;
+  const int base = small.base[sid];
+  const Node<T>* src = scratch + 2 * (int64_t)small.start[sid];
+  const int cnt = small.size[sid];
+  for (int i = 0; i < cnt; ++i) {
+    Node<T> nd = src[i];
+    if (!node_is_leaf(nd.meta)) nd.meta = make_meta(node_dim(nd.meta), (uint32_t)base + node_payload(nd.meta));
+    nodes[base + i] = nd;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+
+// Stream-ordered scratch that is released when the owner goes out of scope.
+struct Scratch {
+  cudaStream_t stream;
+  std::vector<void*> ptrs;
+  explicit Scratch(cudaStream_t s) : stream(s) {}
+  ~Scratch() {
+    for (void* p : ptrs) cudaFreeAsync(p, stream);
+  }
+  template <typename V>
+  cudaError_t get(V** out, int64_t count) {
+    void* p = nullptr;
+    const size_t bytes = (size_t)std::max<int64_t>(count, 1) * sizeof(V);
+    cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+    if (e == cudaSuccess) ptrs.push_back(p);
+    *out = static_cast<V*>(p);
+    return e;
+  }
+};
+
+template <typename T>
+cudaError_t alloc_level(Scratch& sc, SegLevel<T>* L, int64_t cap) {
+  cudaError_t e;
+  if ((e = sc.get(&L->start, cap))) return e;
+  if ((e = sc.get(&L->count, cap))) return e;
+  if ((e = sc.get(&L->boxLo, cap * kMaxDim))) return e;
+  if ((e = sc.get(&L->boxHi, cap * kMaxDim))) return e;
+  if ((e = sc.get(&L->cutDim, cap))) return e;
+  if ((e = sc.get(&L->mnK, cap))) return e;
+  if ((e = sc.get(&L->mxK, cap))) return e;
+  if ((e = sc.get(&L->cut, cap))) return e;
+  if ((e = sc.get(&L->mode, cap))) return e;
+  if ((e = sc.get(&L->lt, cap))) return e;
+  if ((e = sc.get(&L->eq, cap))) return e;
+  if ((e = sc.get(&L->leftCount, cap))) return e;
+  if ((e = sc.get(&L->newLeft, cap))) return e;
+  return sc.get(&L->newRight, cap);
+}
+
+template <typename T>
+double host_key_to_double(typename KeyOf<T>::type k);
+template <>
+double host_key_to_double<float>(uint32_t k) {
+  const uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+  float f;
+  std::memcpy(&f, &u, 4);
+  return (double)f;
+}
+template <>
+double host_key_to_double<double>(unsigned long long k) {
+  const unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+  double f;
+  std::memcpy(&f, &u, 8);
+  return f;
+}
+
+template <typename T, int D>
+int compute_bounds(const Rec<T, D>* recs, int64_t n, int dim, cudaStream_t stream, Scratch& sc, double* lo,
+                   double* hi) {
+  using Key = typename KeyOf<T>::type;
+  Key* keys;
+  NABO_CUDA_TRY(sc.get(&keys, 2 * kMaxDim));
+  k_init_keys<T><<<1, kMaxDim, 0, stream>>>(keys, keys + kMaxDim, dim);
+  const int grid = (int)std::min<int64_t>(ceil_div(n, kBlock), 152 * 8);
+  k_bounds<T, D><<<grid, kBlock, 0, stream>>>(recs, n, dim, keys, keys + kMaxDim);
+  NABO_CUDA_TRY(cudaGetLastError());
+  Key h[2 * kMaxDim];
+  NABO_CUDA_TRY(cudaMemcpyAsync(h, keys, sizeof(h), cudaMemcpyDeviceToHost, stream));
+  NABO_CUDA_TRY(cudaStreamSynchronize(stream));
+  for (int d = 0; d < kMaxDim; ++d) {
+    lo[d] = d < dim ? host_key_to_double<T>(h[d]) : 0.0;
+    hi[d] = d < dim ? host_key_to_double<T>(h[kMaxDim + d]) : 0.0;
+  }
+  return kOk;
+}
+
+}  // namespace
+
+template <typename T, int D>
+int pack_cloud(const T* dCloud, int64_t n, int64_t stride, int dim, cudaStream_t stream, DeviceCloud* out) {
+  Rec<T, D>* recs = nullptr;
+  NABO_CUDA_TRY(cudaMallocAsync((void**)&recs, (size_t)n * sizeof(Rec<T, D>), stream));
+  k_pack<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, recs);
+  NABO_CUDA_TRY(cudaGetLastError());
+  out->recs = recs;
+  Scratch sc(stream);
+  const int rc = compute_bounds<T, D>(recs, n, dim, stream, sc, out->lo, out->hi);
+  if (rc != kOk) return rc;
+  return kOk;
+}
+
+template <typename T, int D>
+int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, cudaStream_t stream,
+                 DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats) {
+  using Key = typename KeyOf<T>::type;
+  (void)sizeof(Key);
+  const int N = (int)n;
+  Scratch sc(stream);
+  Rec<T, D>* recs = nullptr;
+  NABO_CUDA_TRY(cudaMallocAsync((void**)&recs, (size_t)n * sizeof(Rec<T, D>), stream));
+  out->recs = recs;  // owned by the caller from here on
+  k_pack<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, recs);
+  NABO_CUDA_TRY(cudaGetLastError());
+
+  // Root box: true minimum, and max(numeric_limits<T>::min(), true maximum)
+  // because the reference starts its max bound at the smallest positive
+  // normal value (nabo/nabo.cpp:74, nabo/kdtree_cpu.cpp:256-267).
+  {
+    const int rc = compute_bounds<T, D>(recs, n, dim, stream, sc, out->lo, out->hi);
+    if (rc != kOk) return rc;
+  }
+  Box<T> root;
+  for (int d = 0; d < kMaxDim; ++d) {
+    root.lo[d] = d < dim ? (T)out->lo[d] : T(0);
+    root.hi[d] = d < dim ? std::max((T)out->hi[d], std::numeric_limits<T>::min()) : T(0);
+    rootMin[d] = (double)root.lo[d];
+    rootMax[d] = (double)root.hi[d];
+  }
+
+  // Working arrays.
+  int* segOf;
+  int2* S;
+  int2* blockSums;
+  int* pairA;
+  int* pairB;
+  int* counters;
+  const int nb = ceil_div(n, kBlock);
+  const int64_t pairCap = n / 2 + 1;
+  const int64_t segCap = n / (kSmallMax + 1) + 2;
+  const int64_t topCap = n + 1;
+  const int64_t smallCap = n + 1;
+  NABO_CUDA_TRY(sc.get(&segOf, n));
+  NABO_CUDA_TRY(sc.get(&S, n + 1));
+  NABO_CUDA_TRY(sc.get(&blockSums, nb));
+  NABO_CUDA_TRY(sc.get(&pairA, pairCap));
+  NABO_CUDA_TRY(sc.get(&pairB, pairCap));
+  NABO_CUDA_TRY(sc.get(&counters, 4));
+  NABO_CUDA_TRY(cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream));
+  SegLevel<T> cur, nxt;
+  NABO_CUDA_TRY(alloc_level(sc, &cur, segCap));
+  NABO_CUDA_TRY(alloc_level(sc, &nxt, segCap));
+  TopNodes<T> top;
+  NABO_CUDA_TRY(sc.get(&top.dim, topCap));
+  NABO_CUDA_TRY(sc.get(&top.cut, topCap));
+  NABO_CUDA_TRY(sc.get(&top.left, topCap));
+  NABO_CUDA_TRY(sc.get(&top.right, topCap));
+  NABO_CUDA_TRY(sc.get(&top.size, topCap));
+  NABO_CUDA_TRY(sc.get(&top.pre, topCap));
+  SmallSegs<T> small;
+  NABO_CUDA_TRY(sc.get(&small.start, smallCap));
+  NABO_CUDA_TRY(sc.get(&small.count, smallCap));
+  NABO_CUDA_TRY(sc.get(&small.depth, smallCap));
+  NABO_CUDA_TRY(sc.get(&small.boxLo, smallCap * kMaxDim));
+  NABO_CUDA_TRY(sc.get(&small.boxHi, smallCap * kMaxDim));
+  NABO_CUDA_TRY(sc.get(&small.size, smallCap));
+  NABO_CUDA_TRY(sc.get(&small.base, smallCap));
+
+  int nseg = 0;
+  int nSmall = 0;
+  if (N > kSmallMax) {
+    k_root_segment<T><<<1, 1, 0, stream>>>(cur, N, root, dim);
+    NABO_CUDA_TRY(cudaMemsetAsync(segOf, 0, (size_t)n * sizeof(int), stream));
+    nseg = 1;
+  } else {
+    k_root_small<T><<<1, 1, 0, stream>>>(small, N, root, dim);
+    nSmall = 1;
+    NABO_CUDA_TRY(cudaMemcpyAsync(counters + 1, &nSmall, sizeof(int), cudaMemcpyHostToDevice, stream));
+  }
+  NABO_CUDA_TRY(cudaGetLastError());
+
+  std::vector<int> lvStart, lvCount;
+  int levelBase = 0;
+  int level = 0;
+  int hctr[4];
+  while (nseg > 0) {
+    const int sg = ceil_div(nseg, 128);
+    k_prepare<T><<<sg, 128, 0, stream>>>(cur, nseg, dim);
+    k_minmax<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur);
+    k_cut<T><<<sg, 128, 0, stream>>>(cur, nseg);
+    k_count<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur);
+    for (int pass = 1; pass <= 2; ++pass) {
+      k_flag_sums<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, blockSums);
+      k_scan_block_sums<<<1, kBlock, 0, stream>>>(blockSums, nb, S + n);
+      k_flag_ranks<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, blockSums, S);
+      k_pairs<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, S, pairA, pairB);
+      k_swap<T, D><<<ceil_div(pairCap, kBlock), kBlock, 0, stream>>>(recs, pairA, pairB, S + n, (int)pairCap);
+    }
+    k_finalize<T><<<sg, 128, 0, stream>>>(cur, nxt, nseg, levelBase, levelBase + nseg, level, top, small, counters,
+                                          dim);
+    k_update_segof<T><<<nb, kBlock, 0, stream>>>(segOf, N, cur);
+    NABO_CUDA_TRY(cudaGetLastError());
+    NABO_CUDA_TRY(cudaMemcpyAsync(hctr, counters, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NABO_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int), stream));
+    NABO_CUDA_TRY(cudaStreamSynchronize(stream));
+    lvStart.push_back(levelBase);
+    lvCount.push_back(nseg);
+    levelBase += nseg;
+    nseg = hctr[0];
+    nSmall = hctr[1];
+    if (nseg > segCap || levelBase + nseg > topCap || nSmall > smallCap)
+      return set_error(kErrInternal, "kd-tree build: segment capacity exceeded");
+    std::swap(cur, nxt);
+    ++level;
+  }
+
+  // Small segments.
+  Node<T>* scratchNodes;
+  NABO_CUDA_TRY(sc.get(&scratchNodes, 2 * n));
+  SmallStack<T> stk;
+  NABO_CUDA_TRY(sc.get(&stk.start, n));
+  NABO_CUDA_TRY(sc.get(&stk.count, n));
+  NABO_CUDA_TRY(sc.get(&stk.parent, n));
+  NABO_CUDA_TRY(sc.get(&stk.depth, n));
+  NABO_CUDA_TRY(sc.get(&stk.boxLo, n * kMaxDim));
+  NABO_CUDA_TRY(sc.get(&stk.boxHi, n * kMaxDim));
+  k_small<T, D><<<ceil_div(nSmall, 64), 64, 0, stream>>>(recs, small, nSmall, scratchNodes, stk, dim, bucketSize,
+                                                         counters);
+  NABO_CUDA_TRY(cudaGetLastError());
+
+  // Renumber into pre-order.
+  const int nLevels = (int)lvStart.size();
+  int* dLv;
+  NABO_CUDA_TRY(sc.get(&dLv, 2 * std::max(nLevels, 1)));
+  if (nLevels > 0) {
+    NABO_CUDA_TRY(cudaMemcpyAsync(dLv, lvStart.data(), nLevels * sizeof(int), cudaMemcpyHostToDevice, stream));
+    NABO_CUDA_TRY(
+        cudaMemcpyAsync(dLv + nLevels, lvCount.data(), nLevels * sizeof(int), cudaMemcpyHostToDevice, stream));
+  }
+  long long* dTotal;
+  NABO_CUDA_TRY(sc.get(&dTotal, 1));
+  // Upper bound on the node count: every leaf holds at least one point.
+  Node<T>* nodes = nullptr;
+  const int64_t nodeCap = 2 * n;
+  NABO_CUDA_TRY(cudaMallocAsync((void**)&nodes, (size_t)nodeCap * sizeof(Node<T>), stream));
+  out->nodes = nodes;
+  k_renumber<T><<<1, 1024, 0, stream>>>(top, small, dLv, dLv + nLevels, nLevels, nodes, dTotal);
+  k_copy_small<T><<<ceil_div(nSmall, 128), 128, 0, stream>>>(scratchNodes, small, nSmall, nodes);
+  NABO_CUDA_TRY(cudaGetLastError());
+  long long total = 0;
+  NABO_CUDA_TRY(cudaMemcpyAsync(&total, dTotal, sizeof(long long), cudaMemcpyDeviceToHost, stream));
+  NABO_CUDA_TRY(cudaMemcpyAsync(hctr, counters, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+  NABO_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (total <= 0 || total > nodeCap) return set_error(kErrInternal, "kd-tree build: inconsistent node count");
+  if (total - 1 > (long long)kMaxNodeIndex)
+    return set_error(kErrUnsupported, "kd-tree build: the tree has more nodes than the device layout indexes");
+  out->nodeCount = total;
+  out->height = hctr[2];
+  if (stats) {
+    stats->topLevels = nLevels;
+    stats->topNodes = levelBase;
+    stats->smallSegments = nSmall;
+  }
+  return kOk;
+}
+
+#define NABO_BUILD_INSTANTIATE(T, D)                                                                          \
+  template int build_kdtree<T, D>(const T*, int64_t, int64_t, int, unsigned, cudaStream_t, DeviceCloud*,      \
+                                  double*, double*, BuildStats*);                                             \
+  template int pack_cloud<T, D>(const T*, int64_t, int64_t, int, cudaStream_t, DeviceCloud*);
+
+NABO_BUILD_INSTANTIATE(float, 2)
+NABO_BUILD_INSTANTIATE(float, 3)
+NABO_BUILD_INSTANTIATE(float, 4)
+NABO_BUILD_INSTANTIATE(float, 8)
+NABO_BUILD_INSTANTIATE(float, 16)
+NABO_BUILD_INSTANTIATE(double, 2)
+NABO_BUILD_INSTANTIATE(double, 3)
+NABO_BUILD_INSTANTIATE(double, 4)
+NABO_BUILD_INSTANTIATE(double, 8)
+NABO_BUILD_INSTANTIATE(double, 16)
+
+}  // namespace nabo_gb300

@@ -1,0 +1,519 @@
+// capi.cu -- the extern "C" boundary (include/nabo_gb300.h).
+//
+// Argument checks follow the reference in order and wording:
+//   create:  nabo/nabo.cpp:137-138 (dim <= 0), :76-79 (empty cloud),
+//            nabo/kdtree_cpu.cpp:234-235 (bucket size), :245-251 (node count)
+//   knn:     nabo/nabo.cpp:102-131 (checkSizesKnn)
+// so the C++ front end can rethrow them as the reference's exceptions.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "internal.cuh"
+#include "nabo_gb300.h"
+
+namespace nabo_gb300 {
+
+namespace {
+thread_local std::string g_lastError;
+}
+
+int set_error(int code, const std::string& msg) {
+  g_lastError = msg;
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  g_lastError = std::string("CUDA error in ") + what + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+  return kErrCuda;
+}
+
+}  // namespace nabo_gb300
+
+using namespace nabo_gb300;
+
+struct nabo_cuda_search {
+  DeviceCloud c;
+  int searchType = 0;
+  unsigned creationFlags = 0;
+  int rows = 0;
+  int device = 0;
+  int queryOrdering = 1;
+  double minBound[kMaxDim];
+  double maxBound[kMaxDim];
+  cudaEvent_t evStart = nullptr;  // profiling: bracket the search kernel
+  cudaEvent_t evStop = nullptr;
+};
+
+namespace {
+
+// Runs `body` with the object's device current, restoring the caller's.
+struct DeviceGuard {
+  int prev = -1;
+  bool ok = true;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      ok = false;
+      return;
+    }
+    if (prev != dev && cudaSetDevice(dev) != cudaSuccess) ok = false;
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+int pad_dim(int dim) {
+  if (dim <= 2) return 2;
+  if (dim == 3) return 3;
+  if (dim == 4) return 4;
+  if (dim <= 8) return 8;
+  if (dim <= 16) return 16;
+  return -1;
+}
+
+#define NABO_DISPATCH(dtype, dpad, CALL)                         \
+  do {                                                           \
+    if ((dtype) == NABO_CUDA_FLOAT32) {                          \
+      using T = float;                                           \
+      switch (dpad) {                                            \
+        case 2: { constexpr int D = 2; return CALL; }            \
+        case 3: { constexpr int D = 3; return CALL; }            \
+        case 4: { constexpr int D = 4; return CALL; }            \
+        case 8: { constexpr int D = 8; return CALL; }            \
+        case 16: { constexpr int D = 16; return CALL; }          \
+      }                                                          \
+    } else {                                                     \
+      using T = double;                                          \
+      switch (dpad) {                                            \
+        case 2: { constexpr int D = 2; return CALL; }            \
+        case 3: { constexpr int D = 3; return CALL; }            \
+        case 4: { constexpr int D = 4; return CALL; }            \
+        case 8: { constexpr int D = 8; return CALL; }            \
+        case 16: { constexpr int D = 16; return CALL; }          \
+      }                                                          \
+    }                                                            \
+    return set_error(kErrInternal, "bad dispatch");              \
+  } while (0)
+
+uint32_t storage_bit_count(uint32_t v) {
+  for (uint32_t i = 0; i < 64; ++i) {
+    if (v == 0) return i;
+    v >>= 1;
+  }
+  return 64;
+}
+
+int build_any(nabo_cuda_search* h, const void* dCloud, int64_t stride, cudaStream_t st) {
+  double rootMin[kMaxDim], rootMax[kMaxDim];
+  if (h->searchType == NABO_SEARCH_KDTREE_CUDA) {
+    NABO_DISPATCH(h->c.dtype, h->c.dpad,
+                  (build_kdtree<T, D>(static_cast<const T*>(dCloud), h->c.n, stride, h->c.dim, h->c.bucketSize, st,
+                                      &h->c, rootMin, rootMax, nullptr)));
+  }
+  NABO_DISPATCH(h->c.dtype, h->c.dpad, (pack_cloud<T, D>(static_cast<const T*>(dCloud), h->c.n, stride, h->c.dim, st, &h->c)));
+}
+
+int knn_any(const nabo_cuda_search* h, const KnnArgs& a, cudaStream_t st) {
+  if (h->searchType == NABO_SEARCH_KDTREE_CUDA) {
+    NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_kdtree<T, D>(h->c, a, st)));
+  }
+  NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_bruteforce<T, D>(h->c, a, st)));
+}
+
+void free_events(nabo_cuda_search* s) {
+  if (s->evStart) cudaEventDestroy(s->evStart);
+  if (s->evStop) cudaEventDestroy(s->evStop);
+  s->evStart = s->evStop = nullptr;
+}
+
+void free_cloud(DeviceCloud& c) {
+  if (c.recs) cudaFree(c.recs);
+  if (c.nodes) cudaFree(c.nodes);
+  c.recs = nullptr;
+  c.nodes = nullptr;
+}
+
+int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int64_t n, int64_t colStride, int dimIn,
+                int searchType, unsigned creationFlags, const nabo_cuda_params* params, nabo_cuda_search** out) {
+  if (!out) return set_error(kErrArgument, "output handle pointer is NULL");
+  *out = nullptr;
+  if (dtype != NABO_CUDA_FLOAT32 && dtype != NABO_CUDA_FLOAT64) return set_error(kErrArgument, "unknown scalar type");
+  nabo_cuda_params p;
+  nabo_cuda_params_init(&p);
+  if (params) {
+    p.bucketSize = params->bucketSize;
+    p.queryOrdering = params->queryOrdering;
+  }
+  // NearestNeighbourSearch::create (nabo/nabo.cpp:137-138)
+  if (dimIn <= 0) return set_error(kErrArgument, "Your space must have at least one dimension");
+  if (searchType < 0 || searchType >= NABO_SEARCH_TYPE_COUNT) return set_error(kErrArgument, "Unknown search type");
+  if (searchType != NABO_SEARCH_KDTREE_CUDA && searchType != NABO_SEARCH_BRUTE_FORCE_CUDA)
+    return set_error(kErrUnsupported,
+                     "this library provides only the CUDA search types (KDTREE_CUDA, BRUTE_FORCE_CUDA); "
+                     "the CPU and OpenCL types are provided by libnabo");
+  // base constructor (nabo/nabo.cpp:69-80)
+  if (n == 0) return set_error(kErrArgument, "Cloud has no points");
+  if (rows == 0) return set_error(kErrArgument, "Cloud has 0 dimensions");
+  if (n < 0 || rows < 0) return set_error(kErrArgument, "negative cloud size");
+  if (!cloud) return set_error(kErrArgument, "cloud pointer is NULL");
+  if (colStride < rows) return set_error(kErrArgument, "cloud column stride is smaller than its row count");
+  const int dim = std::min(dimIn, rows);
+  if (searchType == NABO_SEARCH_KDTREE_CUDA) {
+    // nabo/kdtree_cpu.cpp:234-251
+    if (p.bucketSize < 2)
+      return set_error(kErrArgument,
+                       "Requested bucket size " + std::to_string(p.bucketSize) + ", but must be larger than 2");
+    if (n > (int64_t)p.bucketSize) {
+      const uint32_t dimBitCount = storage_bit_count((uint32_t)dim);
+      const uint64_t maxNodeCount = (0x1ULL << (32 - dimBitCount)) - 1;
+      const uint64_t estimatedNodeCount = (uint64_t)n / (p.bucketSize / 2);
+      if (estimatedNodeCount > maxNodeCount)
+        return set_error(kErrArgument, "Cloud has a risk to have more nodes (" + std::to_string(estimatedNodeCount) +
+                                           ") than the kd-tree allows (" + std::to_string(maxNodeCount) +
+                                           "). The kd-tree has " + std::to_string(dimBitCount) +
+                                           " bits for dimensions and " + std::to_string(32 - dimBitCount) +
+                                           " bits for node indices");
+    }
+  }
+  const int dpad = pad_dim(dim);
+  if (dpad < 0) return set_error(kErrUnsupported, "the CUDA search types support at most 16 dimensions");
+  if (n > (int64_t)std::numeric_limits<int32_t>::max())
+    return set_error(kErrUnsupported, "clouds are indexed with int (nabo/nabo.h:267): at most 2^31-1 points");
+  if (searchType == NABO_SEARCH_KDTREE_CUDA && std::min<int64_t>(n, p.bucketSize) > (int64_t)kMaxNodeIndex)
+    return set_error(kErrUnsupported, "bucket size too large for the device node layout");
+
+  nabo_cuda_search* h = new nabo_cuda_search();
+  h->searchType = searchType;
+  h->creationFlags = creationFlags;
+  h->rows = rows;
+  h->queryOrdering = p.queryOrdering;
+  h->c.dtype = dtype;
+  h->c.dim = dim;
+  h->c.dpad = dpad;
+  h->c.n = n;
+  h->c.bucketSize = p.bucketSize;
+  if (cudaGetDevice(&h->device) != cudaSuccess) {
+    const cudaError_t e = cudaGetLastError();
+    delete h;
+    return cuda_error(e, "cudaGetDevice");
+  }
+  cudaStream_t st = cudaStreamPerThread;
+  const size_t es = dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  const size_t bytes = (size_t)((n - 1) * colStride + rows) * es;
+  const void* dCloud = cloud;
+  void* tmp = nullptr;
+  int rc = kOk;
+  if (!cloudOnDevice) {
+    cudaError_t e = cudaMallocAsync(&tmp, bytes, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(tmp, cloud, bytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "cloud upload");
+    dCloud = tmp;
+  }
+  if (rc == kOk) rc = build_any(h, dCloud, colStride, st);
+  if (tmp) cudaFreeAsync(tmp, st);
+  if (rc == kOk) {
+    const cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_error(e, "create");
+  }
+  if (rc != kOk) {
+    cudaStreamSynchronize(st);
+    free_cloud(h->c);
+    delete h;
+    return rc;
+  }
+  // Public bounds (nabo/nabo.h:280-282): brute force stores the true
+  // bounds (nabo/brute_force_cpu.cpp:48-50); the kd-tree leaves the base
+  // constructor's initial values when the cloud fits one bucket
+  // (nabo/kdtree_cpu.cpp:236-243), else min over points and
+  // max(numeric_limits<T>::min(), max over points) (nabo/nabo.cpp:73-74).
+  for (int d = 0; d < kMaxDim; ++d) {
+    h->minBound[d] = h->c.lo[d];
+    h->maxBound[d] = h->c.hi[d];
+  }
+  if (searchType == NABO_SEARCH_KDTREE_CUDA) {
+    const double tmin = dtype == NABO_CUDA_FLOAT32 ? (double)std::numeric_limits<float>::min()
+                                                   : std::numeric_limits<double>::min();
+    const double tmax = dtype == NABO_CUDA_FLOAT32 ? (double)std::numeric_limits<float>::max()
+                                                   : std::numeric_limits<double>::max();
+    for (int d = 0; d < dim; ++d) {
+      if (n <= (int64_t)p.bucketSize) {
+        h->minBound[d] = tmax;
+        h->maxBound[d] = tmin;
+      } else {
+        h->maxBound[d] = std::max(h->maxBound[d], tmin);
+      }
+    }
+  }
+  *out = h;
+  return kOk;
+}
+
+int check_knn(const nabo_cuda_search* h, int qRows, int64_t nq, int64_t qStride, int k, unsigned optionFlags,
+              const void* maxRadii) {
+  const bool allowSelf = optionFlags & NABO_ALLOW_SELF_MATCH;
+  const int64_t cols = h->c.n;
+  // nabo/nabo.cpp:105-115
+  if (allowSelf) {
+    if (k > cols)
+      return set_error(kErrArgument, "Requesting more points (" + std::to_string(k) + ") than available in cloud (" +
+                                         std::to_string(cols) + ")");
+  } else {
+    if (k > cols - 1)
+      return set_error(kErrArgument, "Requesting more points (" + std::to_string(k) +
+                                         ") than available in cloud minus 1 (" + std::to_string(cols - 1) +
+                                         ") (as self match is forbidden)");
+  }
+  // nabo/nabo.cpp:116-117
+  if (qRows < h->c.dim)
+    return set_error(kErrArgument, "Query has less dimensions (" + std::to_string(qRows) +
+                                       ") than requested for cloud (" + std::to_string(h->c.dim) + ")");
+  // nabo/nabo.cpp:128-130
+  const unsigned maxFlags = NABO_ALLOW_SELF_MATCH | NABO_SORT_RESULTS;
+  if (optionFlags > maxFlags)
+    return set_error(kErrArgument, "OR-ed value of option flags (" + std::to_string(optionFlags) +
+                                       ") is larger than maximal valid value (" + std::to_string(maxFlags) + ")");
+  (void)maxRadii;
+  if (k < 1) return set_error(kErrArgument, "k must be at least 1");
+  if (nq < 0) return set_error(kErrArgument, "negative query count");
+  if (qStride < qRows) return set_error(kErrArgument, "query column stride is smaller than its row count");
+  if (nq > (int64_t)std::numeric_limits<int32_t>::max())
+    return set_error(kErrUnsupported, "at most 2^31-1 queries per call");
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
+
+void nabo_cuda_params_init(nabo_cuda_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->struct_size = sizeof(nabo_cuda_params);
+  p->bucketSize = 8;
+  p->queryOrdering = 1;
+}
+
+int nabo_cuda_create(int dtype, const void* cloud, int rows, int64_t n, int64_t colStride, int dim, int searchType,
+                     unsigned creationFlags, const nabo_cuda_params* params, nabo_cuda_search** out) {
+  return create_impl(dtype, cloud, false, rows, n, colStride, dim, searchType, creationFlags, params, out);
+}
+
+int nabo_cuda_create_device(int dtype, const void* cloud, int rows, int64_t n, int64_t colStride, int dim,
+                            int searchType, unsigned creationFlags, const nabo_cuda_params* params,
+                            nabo_cuda_search** out) {
+  return create_impl(dtype, cloud, true, rows, n, colStride, dim, searchType, creationFlags, params, out);
+}
+
+int nabo_cuda_destroy(nabo_cuda_search* s) {
+  if (!s) return kOk;
+  DeviceGuard g(s->device);
+  free_events(s);
+  free_cloud(s->c);
+  delete s;
+  return kOk;
+}
+
+int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride, int k,
+                  double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii, int32_t* indices,
+                  void* dists2, uint64_t* touched) {
+  if (!s) return set_error(kErrArgument, "search object is NULL");
+  int rc = check_knn(s, qRows, nq, qStride, k, optionFlags, maxRadii);
+  if (rc != kOk) return rc;
+  if (touched) *touched = 0;
+  if (nq == 0) return kOk;
+  if (!query || !indices || !dists2) return set_error(kErrArgument, "NULL query or result buffer");
+  DeviceGuard g(s->device);
+  if (!g.ok) return cuda_error(cudaGetLastError(), "cudaSetDevice");
+  cudaStream_t st = cudaStreamPerThread;
+  const size_t es = s->c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  const size_t qBytes = (size_t)((nq - 1) * qStride + qRows) * es;
+  const size_t outN = (size_t)nq * (size_t)k;
+  void *dq = nullptr, *dr = nullptr, *dd = nullptr;
+  int32_t* di = nullptr;
+  unsigned long long* dt = nullptr;
+  cudaError_t e = cudaMallocAsync(&dq, qBytes, st);
+  if (e == cudaSuccess && maxRadii) e = cudaMallocAsync(&dr, (size_t)nq * es, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&di, outN * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = cudaMallocAsync(&dd, outN * es, st);
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dt, sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dq, query, qBytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && maxRadii) e = cudaMemcpyAsync(dr, maxRadii, (size_t)nq * es, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dt, 0, sizeof(unsigned long long), st);
+  if (e != cudaSuccess) rc = cuda_error(e, "knn setup");
+  if (rc == kOk) {
+    KnnArgs a;
+    a.query = dq;
+    a.nq = nq;
+    a.qStride = qStride;
+    a.k = k;
+    a.eps = epsilon;
+    a.optionFlags = optionFlags;
+    a.touchStats = (s->creationFlags & NABO_TOUCH_STATISTICS) != 0;
+    a.maxRadius = maxRadius;
+    a.maxRadii = dr;
+    a.indices = di;
+    a.dists2 = dd;
+    a.touched = dt;
+    a.sortQueries = s->queryOrdering != 0;
+    rc = knn_any(s, a, st);
+  }
+  unsigned long long ht = 0;
+  if (rc == kOk) {
+    e = cudaMemcpyAsync(indices, di, outN * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dists2, dd, outN * es, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&ht, dt, sizeof(ht), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "knn results");
+  }
+  if (dq) cudaFreeAsync(dq, st);
+  if (dr) cudaFreeAsync(dr, st);
+  if (di) cudaFreeAsync(di, st);
+  if (dd) cudaFreeAsync(dd, st);
+  if (dt) cudaFreeAsync(dt, st);
+  e = cudaStreamSynchronize(st);
+  if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, "knn");
+  if (rc == kOk && touched) {
+    if (!(s->creationFlags & NABO_TOUCH_STATISTICS))
+      *touched = 0;
+    else if (s->searchType == NABO_SEARCH_BRUTE_FORCE_CUDA)
+      *touched = (uint64_t)nq * (uint64_t)s->c.n;  // nabo/brute_force_cpu.cpp:99-100
+    else
+      *touched = ht;
+  }
+  return rc;
+}
+
+int nabo_cuda_knn_device(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride,
+                         int k, double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii,
+                         int32_t* indices, void* dists2, uint64_t* touched, void* stream) {
+  if (!s) return set_error(kErrArgument, "search object is NULL");
+  int rc = check_knn(s, qRows, nq, qStride, k, optionFlags, maxRadii);
+  if (rc != kOk) return rc;
+  if (nq == 0) return kOk;
+  if (!query || !indices || !dists2) return set_error(kErrArgument, "NULL query or result buffer");
+  DeviceGuard g(s->device);
+  if (!g.ok) return cuda_error(cudaGetLastError(), "cudaSetDevice");
+  KnnArgs a;
+  a.query = query;
+  a.nq = nq;
+  a.qStride = qStride;
+  a.k = k;
+  a.eps = epsilon;
+  a.optionFlags = optionFlags;
+  a.touchStats = (s->creationFlags & NABO_TOUCH_STATISTICS) != 0 && s->searchType == NABO_SEARCH_KDTREE_CUDA;
+  a.maxRadius = maxRadius;
+  a.maxRadii = maxRadii;
+  a.indices = indices;
+  a.dists2 = dists2;
+  a.touched = reinterpret_cast<unsigned long long*>(touched);
+  a.sortQueries = s->queryOrdering != 0;
+  a.evStart = s->evStart;
+  a.evStop = s->evStop;
+  return knn_any(s, a, static_cast<cudaStream_t>(stream));
+}
+
+int nabo_cuda_profile(nabo_cuda_search* s, int enable) {
+  if (!s) return set_error(kErrArgument, "search object is NULL");
+  DeviceGuard g(s->device);
+  free_events(s);
+  if (enable) {
+    cudaError_t e = cudaEventCreate(&s->evStart);
+    if (e == cudaSuccess) e = cudaEventCreate(&s->evStop);
+    if (e != cudaSuccess) {
+      free_events(s);
+      return cuda_error(e, "cudaEventCreate");
+    }
+  }
+  return kOk;
+}
+
+int nabo_cuda_last_kernel_ms(const nabo_cuda_search* s, float* ms) {
+  if (!s || !ms) return set_error(kErrArgument, "NULL argument");
+  if (!s->evStart) return set_error(kErrArgument, "profiling is not enabled on this search object");
+  DeviceGuard g(s->device);
+  cudaError_t e = cudaEventSynchronize(s->evStop);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(ms, s->evStart, s->evStop);
+  if (e != cudaSuccess) return cuda_error(e, "kernel timing");
+  return kOk;
+}
+
+int nabo_cuda_get_info(const nabo_cuda_search* s, int64_t info[8]) {
+  if (!s || !info) return set_error(kErrArgument, "NULL argument");
+  info[0] = s->c.dim;
+  info[1] = s->c.n;
+  info[2] = s->c.dtype;
+  info[3] = s->searchType;
+  info[4] = s->creationFlags;
+  info[5] = s->c.bucketSize;
+  info[6] = s->c.nodeCount;
+  info[7] = s->c.height;
+  return kOk;
+}
+
+int nabo_cuda_get_bounds(const nabo_cuda_search* s, void* minBound, void* maxBound) {
+  if (!s) return set_error(kErrArgument, "search object is NULL");
+  for (int d = 0; d < s->c.dim; ++d) {
+    if (s->c.dtype == NABO_CUDA_FLOAT32) {
+      if (minBound) static_cast<float*>(minBound)[d] = (float)s->minBound[d];
+      if (maxBound) static_cast<float*>(maxBound)[d] = (float)s->maxBound[d];
+    } else {
+      if (minBound) static_cast<double*>(minBound)[d] = s->minBound[d];
+      if (maxBound) static_cast<double*>(maxBound)[d] = s->maxBound[d];
+    }
+  }
+  return kOk;
+}
+
+int nabo_cuda_export_tree(const nabo_cuda_search* s, int32_t* cutDim, void* cutVal, uint32_t* right,
+                          uint32_t* bucketStart, uint32_t* bucketSize, int32_t* buckets) {
+  if (!s) return set_error(kErrArgument, "search object is NULL");
+  if (s->searchType != NABO_SEARCH_KDTREE_CUDA) return set_error(kErrArgument, "not a kd-tree search object");
+  DeviceGuard g(s->device);
+  const bool f32 = s->c.dtype == NABO_CUDA_FLOAT32;
+  const size_t nodeBytes = f32 ? 8 : 16;
+  std::vector<unsigned char> nodes((size_t)s->c.nodeCount * nodeBytes);
+  cudaError_t e = cudaMemcpy(nodes.data(), s->c.nodes, nodes.size(), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "export nodes");
+  for (int64_t i = 0; i < s->c.nodeCount; ++i) {
+    const unsigned char* p = nodes.data() + i * nodeBytes;
+    uint32_t meta, start;
+    std::memcpy(&meta, p, 4);
+    std::memcpy(&start, p + 4, 4);
+    const bool leaf = node_is_leaf(meta);
+    if (cutDim) cutDim[i] = leaf ? -1 : (int32_t)node_dim(meta);
+    if (right) right[i] = leaf ? 0u : node_payload(meta);
+    if (bucketStart) bucketStart[i] = leaf ? start : 0u;
+    if (bucketSize) bucketSize[i] = leaf ? node_payload(meta) : 0u;
+    if (cutVal) {
+      if (f32) {
+        float v = 0.0f;
+        if (!leaf) std::memcpy(&v, p + 4, 4);
+        static_cast<float*>(cutVal)[i] = v;
+      } else {
+        double v = 0.0;
+        if (!leaf) std::memcpy(&v, p + 8, 8);
+        static_cast<double*>(cutVal)[i] = v;
+      }
+    }
+  }
+  if (buckets) {
+    const size_t es = f32 ? 4 : 8;
+    const size_t recBytes = ((size_t)s->c.dpad * es + 4 + 15) / 16 * 16;
+    std::vector<unsigned char> recs((size_t)s->c.n * recBytes);
+    e = cudaMemcpy(recs.data(), s->c.recs, recs.size(), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "export buckets");
+    for (int64_t i = 0; i < s->c.n; ++i) std::memcpy(buckets + i, recs.data() + i * recBytes + s->c.dpad * es, 4);
+  }
+  return kOk;
+}
+
+const char* nabo_cuda_last_error(void) { return g_lastError.c_str(); }
+
+const char* nabo_cuda_version(void) { return NABO_GB300_VERSION; }
+
+}  // extern "C"

@@ -1,0 +1,101 @@
+// internal.cuh -- declarations shared by the build, search and C-ABI units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "common.cuh"
+
+namespace nabo_gb300 {
+
+// Status codes (mirrored in include/nabo_gb300.h).
+enum Status : int {
+  kOk = 0,
+  kErrArgument = 1,
+  kErrCuda = 2,
+  kErrUnsupported = 3,
+  kErrInternal = 4,
+};
+
+// Sets the calling thread's last-error message; returns `code`.
+int set_error(int code, const std::string& msg);
+int cuda_error(cudaError_t e, const char* what);
+
+#define NABO_CUDA_TRY(expr)                                        \
+  do {                                                             \
+    cudaError_t e__ = (expr);                                      \
+    if (e__ != cudaSuccess) return ::nabo_gb300::cuda_error(e__, #expr); \
+  } while (0)
+
+// Device-resident kd-tree (or, for brute force, the packed cloud only).
+struct DeviceCloud {
+  int dtype = 0;        // 0 = f32, 1 = f64
+  int dim = 0;          // dimensions searched (<= cloud rows)
+  int dpad = 0;         // compiled record dimension (>= dim)
+  int64_t n = 0;        // points
+  unsigned bucketSize = 8;
+  void* recs = nullptr;   // Rec<T,dpad>[n], leaf order (kd-tree) or cloud order (brute force)
+  void* nodes = nullptr;  // Node<T>[nodeCount] (kd-tree only)
+  int64_t nodeCount = 0;
+  int height = 0;         // max inner nodes on a root-to-leaf path
+  double lo[kMaxDim];     // true per-dimension bounds of the points (for query ordering)
+  double hi[kMaxDim];
+};
+
+struct BuildStats {
+  int topLevels = 0;
+  int64_t topNodes = 0;
+  int64_t smallSegments = 0;
+};
+
+// Builds the kd-tree of `n` points (dim coordinates each, column stride
+// `stride` elements) held in device memory at `dCloud`. Produces the same
+// tree as the reference's KDTreeUnbalancedPtInLeavesImplicitBoundsStackOpt
+// constructor (nabo/kdtree_cpu.cpp:109-272): same nodes, cut values and
+// bucket order. `rootMin/rootMax` receive the root box the reference uses
+// (with its max-bound initialisation), as doubles.
+template <typename T, int D>
+int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, cudaStream_t stream,
+                 DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats);
+
+// Packs the cloud into records in cloud order (brute force) and computes
+// its true bounds.
+template <typename T, int D>
+int pack_cloud(const T* dCloud, int64_t n, int64_t stride, int dim, cudaStream_t stream, DeviceCloud* out);
+
+struct KnnArgs {
+  const void* query = nullptr;  // device, dim rows x nq, column stride qStride
+  int64_t nq = 0;
+  int64_t qStride = 0;
+  int k = 1;
+  double eps = 0.0;
+  unsigned optionFlags = 0;
+  bool touchStats = false;
+  double maxRadius = 0.0;        // used when maxRadii == nullptr
+  const void* maxRadii = nullptr;  // device, nq values, or nullptr
+  int32_t* indices = nullptr;    // device, k x nq column-major
+  void* dists2 = nullptr;        // device, k x nq column-major
+  unsigned long long* touched = nullptr;  // device counter (accumulated), may be null
+  bool sortQueries = true;       // reorder queries along a space-filling curve
+  int32_t* found = nullptr;      // optional device output: neighbours found per query
+  cudaEvent_t evStart = nullptr; // optional: recorded right before / after the search kernel
+  cudaEvent_t evStop = nullptr;
+};
+
+template <typename T, int D>
+int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream);
+template <typename T, int D>
+int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream);
+
+// Query ordering: writes a permutation of [0, nq) grouping nearby queries.
+template <typename T>
+int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
+                  int32_t* dOrder, cudaStream_t stream);
+
+// Device-wide exclusive scan of uint32 values (in place), returns total via
+// a device pointer. Scratch is stream-ordered.
+int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t stream);
+
+}  // namespace nabo_gb300

@@ -1,0 +1,254 @@
+// search.cuh -- kd-tree and brute-force kNN kernels (templates).
+//
+// One thread per query. The traversal is the reference's recurseKnn
+// (nabo/kdtree_cpu.cpp:367-447) turned into a loop with an explicit stack:
+// at an inner node the near child is entered at once and the far child is
+// pushed with its incremental box distance
+//     rd_far = rd + (-(old_off*old_off) + new_off*new_off)
+// and the offset vector it must see; a popped far child is visited iff
+//     rd_far <= maxRadius^2  and  rd_far * (1+eps)^2 <= head.
+// The far child is pushed only if that test already holds, which changes no
+// decision because head never grows. Every +,-,* is separately rounded
+// (no FMA contraction) so distances are bit-identical to the CPU oracle.
+//
+// Top-k: K (dist2, index) pairs in registers, kept in descending order so
+// the head (largest) is slot 0; slots >= k hold -inf so one instantiation
+// serves every k <= K. Pairs are ordered by (dist2, index): among equal
+// distances the lower index is kept, which makes the result independent of
+// visit order (the reference's IndexHeapBruteForceVector keeps the first
+// visited, nabo/index_heap.h:322-334).
+#pragma once
+
+#include "common.cuh"
+
+namespace nabo_gb300 {
+
+template <typename T>
+__device__ __forceinline__ bool pair_greater(T da, int ia, T db, int ib) {
+  return da > db || (da == db && ia > ib);
+}
+
+template <typename T, int K>
+struct TopK {
+  T d[K];
+  int i[K];
+  __device__ __forceinline__ void init(int k) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      d[j] = j < k ? Ar<T>::inf() : -Ar<T>::inf();
+      i[j] = -1;
+    }
+  }
+  __device__ __forceinline__ T head() const { return d[0]; }
+  __device__ __forceinline__ bool accepts(T dist, int idx) const { return pair_greater(d[0], i[0], dist, idx); }
+  // Drops the head and inserts (dist, idx); requires accepts(dist, idx).
+  // Slot j takes its successor while that is still larger than the new
+  // pair, then the new pair, then keeps its own value.
+  __device__ __forceinline__ void insert(T dist, int idx) {
+#pragma unroll
+    for (int j = 0; j + 1 < K; ++j) {
+      if (pair_greater(d[j + 1], i[j + 1], dist, idx)) {
+        d[j] = d[j + 1];
+        i[j] = i[j + 1];
+      } else if (pair_greater(d[j], i[j], dist, idx)) {
+        d[j] = dist;
+        i[j] = idx;
+      }
+    }
+    if (pair_greater(d[K - 1], i[K - 1], dist, idx)) {
+      d[K - 1] = dist;
+      i[K - 1] = idx;
+    }
+  }
+  // Writes the k entries in ascending order; returns how many are valid.
+  __device__ __forceinline__ int store(int k, int32_t* __restrict__ oi, T* __restrict__ od) const {
+    int found = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (j < k) {
+        oi[k - 1 - j] = i[j];
+        od[k - 1 - j] = d[j];
+        found += i[j] >= 0 ? 1 : 0;
+      }
+    }
+    return found;
+  }
+};
+
+template <typename T, int D>
+__device__ __forceinline__ T pick(const T (&v)[D], int c) {
+  T r = v[0];
+#pragma unroll
+  for (int d = 1; d < D; ++d)
+    if (c == d) r = v[d];
+  return r;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T dist2_seq(const T (&q)[D], const Rec<T, D>& r) {
+  // (q0-p0)^2 first, then +(q1-p1)^2, ... (nabo/kdtree_cpu.cpp:383-391)
+  T diff = Ar<T>::sub(q[0], r.p.c[0]);
+  T dist = Ar<T>::mul(diff, diff);
+#pragma unroll
+  for (int d = 1; d < D; ++d) {
+    diff = Ar<T>::sub(q[d], r.p.c[d]);
+    dist = Ar<T>::add(dist, Ar<T>::mul(diff, diff));
+  }
+  return dist;
+}
+
+struct KnnLaunch {
+  const void* nodes;
+  const void* recs;
+  const void* query;
+  int64_t nq;
+  int64_t qStride;
+  int dim;
+  const int32_t* order;
+  int k;
+  double maxError2;
+  double maxRadius2;
+  const void* maxRadii;
+  int32_t* outIdx;
+  void* outD2;
+  unsigned long long* touched;
+  int32_t* found;
+  int64_t n;  // points (brute force)
+  int allowSelf;
+  int stats;
+};
+
+template <typename T, int D, int K, int STACK>
+__global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
+  const bool selfOk = a.allowSelf != 0;
+  const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
+  const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
+  const T* __restrict__ query = static_cast<const T*>(a.query);
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  unsigned long long touched = 0;
+  if (t < a.nq) {
+    const int64_t qi = a.order ? (int64_t)a.order[t] : t;
+    T q[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) q[d] = d < a.dim ? query[qi * a.qStride + d] : T(0);
+    T maxRadius2 = (T)a.maxRadius2;
+    if (a.maxRadii) {
+      const T r = static_cast<const T*>(a.maxRadii)[qi];
+      maxRadius2 = Ar<T>::mul(r, r);
+    }
+    const T maxError2 = (T)a.maxError2;
+    TopK<T, K> heap;
+    heap.init(a.k);
+    T off[D];
+#pragma unroll
+    for (int d = 0; d < D; ++d) off[d] = T(0);
+    uint32_t sNode[STACK];
+    T sRd[STACK];
+    T sOff[STACK][D];
+    int sp = 0;
+    uint32_t node = 0;
+    T rd = T(0);
+    for (;;) {
+      const Node<T> nd = load_node(nodes, node);
+      if (!node_is_leaf(nd.meta)) {
+        const int cd = (int)node_dim(nd.meta);
+        const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
+        const T oldOff = pick(off, cd);
+        const T rdFar = Ar<T>::add(rd, Ar<T>::add(-Ar<T>::mul(oldOff, oldOff), Ar<T>::mul(newOff, newOff)));
+        const uint32_t right = node_payload(nd.meta);
+        const uint32_t nearN = newOff > T(0) ? right : node + 1;
+        const uint32_t farN = newOff > T(0) ? node + 1 : right;
+        if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head()) {
+          sNode[sp] = farN;
+          sRd[sp] = rdFar;
+#pragma unroll
+          for (int d = 0; d < D; ++d) sOff[sp][d] = d == cd ? newOff : off[d];
+          ++sp;
+        }
+        node = nearN;
+        continue;
+      }
+      const uint32_t cnt = node_payload(nd.meta);
+      const uint32_t st = node_start(nd);
+      for (uint32_t j = 0; j < cnt; ++j) {
+        Rec<T, D> r;
+        load_rec(recs, (int64_t)st + j, r);
+        const T dist = dist2_seq(q, r);
+        if (dist <= maxRadius2 && heap.accepts(dist, r.p.idx) && (selfOk || dist > Ar<T>::eps()))
+          heap.insert(dist, r.p.idx);
+      }
+      touched += cnt;
+      bool more = false;
+      while (sp > 0) {
+        --sp;
+        const T e = sRd[sp];
+        if (Ar<T>::mul(e, maxError2) <= heap.head()) {
+          rd = e;
+          node = sNode[sp];
+#pragma unroll
+          for (int d = 0; d < D; ++d) off[d] = sOff[sp][d];
+          more = true;
+          break;
+        }
+      }
+      if (!more) break;
+    }
+    const int f = heap.store(a.k, a.outIdx + qi * a.k, static_cast<T*>(a.outD2) + qi * a.k);
+    if (a.found) a.found[qi] = f;
+  }
+  if (a.stats) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) touched += __shfl_xor_sync(0xffffffffu, touched, o);
+    if ((threadIdx.x & 31) == 0 && touched) atomicAdd(a.touched, touched);
+  }
+}
+
+// Brute force (nabo/brute_force_cpu.cpp:63-103): every query against every
+// point, points staged through shared memory in tiles; each thread owns one
+// query and its top-k. Points are offered in index order.
+template <typename T, int D, int K>
+__global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a) {
+  const bool selfOk = a.allowSelf != 0;
+  constexpr int kTile = (int)((24 * 1024) / sizeof(Rec<T, D>));
+  __shared__ Rec<T, D> tile[kTile];
+  const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
+  const T* __restrict__ query = static_cast<const T*>(a.query);
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool active = t < a.nq;
+  const int64_t qi = active ? (a.order ? (int64_t)a.order[t] : t) : 0;
+  T q[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) q[d] = (active && d < a.dim) ? query[qi * a.qStride + d] : T(0);
+  T maxRadius2 = (T)a.maxRadius2;
+  if (a.maxRadii && active) {
+    const T r = static_cast<const T*>(a.maxRadii)[qi];
+    maxRadius2 = Ar<T>::mul(r, r);
+  }
+  TopK<T, K> heap;
+  heap.init(a.k);
+  for (int64_t base = 0; base < a.n; base += kTile) {
+    const int m = (int)((a.n - base) < kTile ? (a.n - base) : kTile);
+    __syncthreads();
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(recs + base);
+      uint4* dst = reinterpret_cast<uint4*>(tile);
+      const int words = m * RecSize<T, D>::chunks;
+      for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = __ldg(src + w);
+    }
+    __syncthreads();
+    if (active) {
+      for (int j = 0; j < m; ++j) {
+        const Rec<T, D>& r = tile[j];
+        const T dist = dist2_seq(q, r);
+        if (dist <= maxRadius2 && heap.accepts(dist, r.p.idx) && (selfOk || dist > Ar<T>::eps()))
+          heap.insert(dist, r.p.idx);
+      }
+    }
+  }
+  if (active) {
+    const int f = heap.store(a.k, a.outIdx + qi * a.k, static_cast<T*>(a.outD2) + qi * a.k);
+    if (a.found) a.found[qi] = f;
+  }
+}
+
+}  // namespace nabo_gb300

@@ -1,0 +1,113 @@
+// search_impl.cuh -- host-side dispatch of the kNN kernels for one (T, D).
+// Included by one translation unit per (T, D) so they compile in parallel.
+#pragma once
+
+#include "internal.cuh"
+#include "search.cuh"
+
+namespace nabo_gb300 {
+
+// Register top-k sizes compiled; a request for k uses the smallest K >= k.
+#define NABO_K_LIST(X) X(1) X(2) X(5) X(8) X(10) X(16) X(32)
+constexpr int kMaxK = 32;
+// Traversal stack depths compiled; the tree's height selects one.
+constexpr int kStackSmall = 64;
+constexpr int kStackLarge = 256;
+
+inline int round_k(int k) {
+#define NABO_ROUND(KK) \
+  if (k <= KK) return KK;
+  NABO_K_LIST(NABO_ROUND)
+#undef NABO_ROUND
+  return -1;
+}
+
+template <typename T, int D>
+KnnLaunch make_launch(const DeviceCloud& c, const KnnArgs& a, const int32_t* order) {
+  KnnLaunch L;
+  L.nodes = c.nodes;
+  L.recs = c.recs;
+  L.query = a.query;
+  L.nq = a.nq;
+  L.qStride = a.qStride;
+  L.dim = c.dim;
+  L.order = order;
+  L.k = a.k;
+  const T eps = (T)a.eps;
+  const T one = T(1);
+  const T e1 = one + eps;
+  L.maxError2 = (double)(T)(e1 * e1);
+  const T r = (T)a.maxRadius;
+  L.maxRadius2 = (double)(T)(r * r);
+  L.maxRadii = a.maxRadii;
+  L.outIdx = a.indices;
+  L.outD2 = a.dists2;
+  L.touched = a.touched;
+  L.found = a.found;
+  L.n = c.n;
+  L.allowSelf = (a.optionFlags & 1u) ? 1 : 0;
+  L.stats = (a.touchStats && a.touched) ? 1 : 0;
+  return L;
+}
+
+template <typename T, int D>
+int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
+  if (a.nq == 0) return kOk;
+  const int K = round_k(a.k);
+  if (K < 0) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+  if (c.height > kStackLarge)
+    return set_error(kErrUnsupported, "kd-tree height exceeds the traversal stack of the CUDA search");
+  int32_t* order = nullptr;
+  if (a.sortQueries && a.nq >= 4096) {
+    NABO_CUDA_TRY(cudaMallocAsync((void**)&order, (size_t)a.nq * sizeof(int32_t), stream));
+    const int rc = order_queries<T>(static_cast<const T*>(a.query), a.nq, a.qStride, c.dim, c.lo, c.hi, order, stream);
+    if (rc != kOk) {
+      cudaFreeAsync(order, stream);
+      return rc;
+    }
+  }
+  const KnnLaunch L = make_launch<T, D>(c, a, order);
+  const int grid = ceil_div(a.nq, 128);
+  const bool small = c.height <= kStackSmall;
+  if (a.evStart) cudaEventRecord(a.evStart, stream);
+#define NABO_LAUNCH(KK)                                                       \
+  case KK:                                                                    \
+    if (small)                                                                \
+      k_knn_kdtree<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);       \
+    else                                                                      \
+      k_knn_kdtree<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);       \
+    break;
+  switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+#undef NABO_LAUNCH
+  if (a.evStop) cudaEventRecord(a.evStop, stream);
+  const cudaError_t e = cudaGetLastError();
+  if (order) cudaFreeAsync(order, stream);
+  if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree launch");
+  return kOk;
+}
+
+template <typename T, int D>
+int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
+  if (a.nq == 0) return kOk;
+  const int K = round_k(a.k);
+  if (K < 0) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+  const KnnLaunch L = make_launch<T, D>(c, a, nullptr);
+  const int grid = ceil_div(a.nq, 128);
+  if (a.evStart) cudaEventRecord(a.evStart, stream);
+#define NABO_LAUNCH(KK)                                              \
+  case KK:                                                           \
+    k_knn_bruteforce<T, D, KK><<<grid, 128, 0, stream>>>(L);         \
+    break;
+  switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+#undef NABO_LAUNCH
+  if (a.evStop) cudaEventRecord(a.evStop, stream);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "k_knn_bruteforce launch");
+  return kOk;
+}
+
+#define NABO_SEARCH_INSTANTIATE(T, D)                                              \
+  template int knn_kdtree<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
+  template int knn_bruteforce<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t);
+
+}  // namespace nabo_gb300
