@@ -155,9 +155,10 @@ __device__ __forceinline__ K warp_max(K v) {
 
 template <typename T, int D>
 __global__ void k_bounds(const Rec<T, D>* __restrict__ recs, int64_t n, int dim, typename KeyOf<T>::type* mnK,
-                         typename KeyOf<T>::type* mxK) {
+                         typename KeyOf<T>::type* mxK, int* nonFinite) {
   using Key = typename KeyOf<T>::type;
   Key mn[D], mx[D];
+  int bad = 0;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     mn[d] = ordered_key(Ar<T>::inf());
@@ -171,8 +172,10 @@ __global__ void k_bounds(const Rec<T, D>* __restrict__ recs, int64_t n, int dim,
       const Key k = ordered_key(r.p.c[d]);
       mn[d] = k < mn[d] ? k : mn[d];
       mx[d] = k > mx[d] ? k : mx[d];
+      bad |= (d < dim && !isfinite(r.p.c[d])) ? 1 : 0;
     }
   }
+  if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(nonFinite, 1);
 #pragma unroll
   for (int d = 0; d < D; ++d) {
     const Key a = warp_min(mn[d]);
@@ -442,7 +445,8 @@ __global__ void k_pairs(const Rec<T, D>* __restrict__ recs, const int* __restric
     const int base = S[st].y;
     const int m = S[st + L.count[s]].y - base;
     const int j = S[p].y - base;
-    pairB[base + m - 1 - j] = p;
+    const int slot = base + m - 1 - j;
+    if (slot >= 0 && slot < n) pairB[slot] = p;
   }
 }
 
@@ -450,7 +454,7 @@ template <typename T, int D>
 __global__ void k_swap(Rec<T, D>* recs, const int* __restrict__ pairA, const int* __restrict__ pairB,
                        const int2* __restrict__ total, int cap) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= cap || t >= total->x) return;
+  if (t >= cap || t >= total->x || t >= total->y) return;
   const int a = pairA[t], b = pairB[t];
   const Rec<T, D> ra = recs[a];
   recs[a] = recs[b];
@@ -460,7 +464,7 @@ __global__ void k_swap(Rec<T, D>* recs, const int* __restrict__ pairA, const int
 // nabo/kdtree_cpu.cpp:180-223: leftCount rule, node, children.
 template <typename T>
 __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, int nseg, int levelBase, int nextLevelBase, int level,
-                           TopNodes<T> top, SmallSegs<T> small, int* counters, int dim) {
+                           TopNodes<T> top, SmallSegs<T> small, int* counters, int dim, int segCap, int smallCap) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= nseg) return;
   const int count = L.count[s];
@@ -479,6 +483,9 @@ __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, int nseg, int levelB
     leftCount = br2;
   else
     leftCount = count / 2;
+  // finite coordinates guarantee 1 <= leftCount < count; keep the split
+  // productive whatever happens
+  leftCount = leftCount < 1 ? 1 : (leftCount > count - 1 ? count - 1 : leftCount);
   const int cd = L.cutDim[s];
   const T cut = L.cut[s];
   const int node = levelBase + s;
@@ -495,6 +502,10 @@ __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, int nseg, int levelB
     T* dHi;
     if (ccount > kSmallMax) {
       const int id = atomicAdd(counters + 0, 1);
+      if (id >= segCap) {
+        atomicOr(counters + 3, 1);
+        return;
+      }
       next.start[id] = cst;
       next.count[id] = ccount;
       dLo = next.boxLo + (int64_t)id * kMaxDim;
@@ -503,6 +514,10 @@ __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, int nseg, int levelB
       newSeg = id;
     } else {
       const int sid = atomicAdd(counters + 1, 1);
+      if (sid >= smallCap) {
+        atomicOr(counters + 3, 1);
+        return;
+      }
       small.start[sid] = cst;
       small.count[sid] = ccount;
       small.depth[sid] = level + 1;
@@ -556,6 +571,7 @@ __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, int nSmall, Node<T>
   const int sid = blockIdx.x * blockDim.x + threadIdx.x;
   if (sid >= nSmall) return;
   const int base = small.start[sid];
+  const int segN = small.count[sid];
   Node<T>* out = scratch + 2 * (int64_t)base;
   int sp = 0;
   {
@@ -643,6 +659,11 @@ __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, int nSmall, Node<T>
       leftCount = br2;
     else
       leftCount = count / 2;
+    leftCount = leftCount < 1 ? 1 : (leftCount > count - 1 ? count - 1 : leftCount);
+    if (sp + 2 > segN || local + 2 >= 2 * segN) {  // cannot happen for a valid split; never overrun
+      atomicOr(counters + 3, 2);
+      break;
+    }
     store_inner(out + local, (uint32_t)cd, 0u, cut);
     // push right (processed after the whole left subtree), then left
     {
@@ -799,19 +820,28 @@ double host_key_to_double<double>(unsigned long long k) {
   return f;
 }
 
+// Per-dimension bounds; fails on NaN or infinite coordinates, for which
+// the reference's split loop does not terminate (idealCutVal becomes NaN
+// and leftCount 0, nabo/kdtree_cpu.cpp:180-190).
 template <typename T, int D>
 int compute_bounds(const Rec<T, D>* recs, int64_t n, int dim, cudaStream_t stream, Scratch& sc, double* lo,
                    double* hi) {
   using Key = typename KeyOf<T>::type;
   Key* keys;
+  int* flag;
   NABO_CUDA_TRY(sc.get(&keys, 2 * kMaxDim));
+  NABO_CUDA_TRY(sc.get(&flag, 1));
+  NABO_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), stream));
   k_init_keys<T><<<1, kMaxDim, 0, stream>>>(keys, keys + kMaxDim, dim);
   const int grid = (int)std::min<int64_t>(ceil_div(n, kBlock), 152 * 8);
-  k_bounds<T, D><<<grid, kBlock, 0, stream>>>(recs, n, dim, keys, keys + kMaxDim);
+  k_bounds<T, D><<<grid, kBlock, 0, stream>>>(recs, n, dim, keys, keys + kMaxDim, flag);
   NABO_CUDA_TRY(cudaGetLastError());
   Key h[2 * kMaxDim];
+  int hflag = 0;
   NABO_CUDA_TRY(cudaMemcpyAsync(h, keys, sizeof(h), cudaMemcpyDeviceToHost, stream));
+  NABO_CUDA_TRY(cudaMemcpyAsync(&hflag, flag, sizeof(int), cudaMemcpyDeviceToHost, stream));
   NABO_CUDA_TRY(cudaStreamSynchronize(stream));
+  if (hflag) return set_error(kErrArgument, "Cloud has non-finite (NaN or infinite) coordinates");
   for (int d = 0; d < kMaxDim; ++d) {
     lo[d] = d < dim ? host_key_to_double<T>(h[d]) : 0.0;
     hi[d] = d < dim ? host_key_to_double<T>(h[kMaxDim + d]) : 0.0;
@@ -870,7 +900,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   int* pairB;
   int* counters;
   const int nb = ceil_div(n, kBlock);
-  const int64_t pairCap = n / 2 + 1;
+  const int64_t pairCap = n + 1;
   const int64_t segCap = n / (kSmallMax + 1) + 2;
   const int64_t topCap = n + 1;
   const int64_t smallCap = n + 1;
@@ -931,7 +961,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
       k_swap<T, D><<<ceil_div(pairCap, kBlock), kBlock, 0, stream>>>(recs, pairA, pairB, S + n, (int)pairCap);
     }
     k_finalize<T><<<sg, 128, 0, stream>>>(cur, nxt, nseg, levelBase, levelBase + nseg, level, top, small, counters,
-                                          dim);
+                                          dim, (int)segCap, (int)smallCap);
     k_update_segof<T><<<nb, kBlock, 0, stream>>>(segOf, N, cur);
     NABO_CUDA_TRY(cudaGetLastError());
     NABO_CUDA_TRY(cudaMemcpyAsync(hctr, counters, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
@@ -942,7 +972,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
     levelBase += nseg;
     nseg = hctr[0];
     nSmall = hctr[1];
-    if (nseg > segCap || levelBase + nseg > topCap || nSmall > smallCap)
+    if (hctr[3] || nseg > segCap || levelBase + nseg > topCap || nSmall > smallCap)
       return set_error(kErrInternal, "kd-tree build: segment capacity exceeded");
     std::swap(cur, nxt);
     ++level;
@@ -985,7 +1015,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   NABO_CUDA_TRY(cudaMemcpyAsync(&total, dTotal, sizeof(long long), cudaMemcpyDeviceToHost, stream));
   NABO_CUDA_TRY(cudaMemcpyAsync(hctr, counters, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
   NABO_CUDA_TRY(cudaStreamSynchronize(stream));
-  if (total <= 0 || total > nodeCap) return set_error(kErrInternal, "kd-tree build: inconsistent node count");
+  if (hctr[3] || total <= 0 || total > nodeCap) return set_error(kErrInternal, "kd-tree build: inconsistent node count");
   if (total - 1 > (long long)kMaxNodeIndex)
     return set_error(kErrUnsupported, "kd-tree build: the tree has more nodes than the device layout indexes");
   out->nodeCount = total;

@@ -158,7 +158,9 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
         const uint32_t right = node_payload(nd.meta);
         const uint32_t nearN = newOff > T(0) ? right : node + 1;
         const uint32_t farN = newOff > T(0) ? node + 1 : right;
-        if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head()) {
+        // sp <= tree height <= STACK (checked on the host); the test only
+        // makes the bound explicit
+        if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < STACK) {
           sNode[sp] = farN;
           sRd[sp] = rdFar;
 #pragma unroll
