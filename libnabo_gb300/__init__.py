@@ -109,8 +109,9 @@ class NearestNeighbourSearch:
     ``Nabo::NearestNeighbourSearch<T>::create`` (nabo/nabo.h:360). ``cloud``
     is a numpy array (host) or a CUDA torch tensor (device) of shape
     (n, rows); it is copied into the search object. ``params`` accepts the
-    reference's ``bucketSize`` key and ``queryOrdering`` (1 = sort queries
-    along a Morton curve inside each search, the default).
+    reference's ``bucketSize`` key, ``queryOrdering`` (1 = sort queries
+    along a Morton curve inside each search, the default) and ``traversal``
+    (0 auto, 1 the reference's visit order, 2 the warp packet).
     """
 
     def __init__(self, cloud, searchType: int = SearchType.KDTREE_CUDA, dim: int | None = None,
@@ -123,6 +124,8 @@ class NearestNeighbourSearch:
                 p.bucketSize = int(val)
             elif key == "queryOrdering":
                 p.queryOrdering = int(val)
+            elif key == "traversal":
+                p.traversal = int(val)
             else:
                 raise NaboError(1, f"unknown parameter {key!r}")
         self.searchType = int(searchType)

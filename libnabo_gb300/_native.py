@@ -40,7 +40,8 @@ class nabo_cuda_params(ctypes.Structure):
         ("struct_size", ctypes.c_uint32),
         ("bucketSize", ctypes.c_uint32),
         ("queryOrdering", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("traversal", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
 

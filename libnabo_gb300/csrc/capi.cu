@@ -43,6 +43,7 @@ struct nabo_cuda_search {
   int rows = 0;
   int device = 0;
   int queryOrdering = 1;
+  int traversal = 0;
   double minBound[kMaxDim];
   double maxBound[kMaxDim];
   cudaEvent_t evStart = nullptr;  // profiling: bracket the search kernel
@@ -149,6 +150,7 @@ int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int6
   if (params) {
     p.bucketSize = params->bucketSize;
     p.queryOrdering = params->queryOrdering;
+    p.traversal = params->traversal;
   }
   // NearestNeighbourSearch::create (nabo/nabo.cpp:137-138)
   if (dimIn <= 0) return set_error(kErrArgument, "Your space must have at least one dimension");
@@ -193,6 +195,11 @@ int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int6
   h->creationFlags = creationFlags;
   h->rows = rows;
   h->queryOrdering = p.queryOrdering;
+  h->traversal = p.traversal;
+  if (p.traversal < 0 || p.traversal > 2) {
+    delete h;
+    return set_error(kErrArgument, "traversal must be 0, 1 or 2");
+  }
   h->c.dtype = dtype;
   h->c.dim = dim;
   h->c.dpad = dpad;
@@ -361,6 +368,7 @@ int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64
     a.dists2 = dd;
     a.touched = dt;
     a.sortQueries = s->queryOrdering != 0;
+    a.traversal = s->traversal;
     rc = knn_any(s, a, st);
   }
   unsigned long long ht = 0;
@@ -412,6 +420,7 @@ int nabo_cuda_knn_device(const nabo_cuda_search* s, const void* query, int qRows
   a.dists2 = dists2;
   a.touched = reinterpret_cast<unsigned long long*>(touched);
   a.sortQueries = s->queryOrdering != 0;
+  a.traversal = s->traversal;
   a.evStart = s->evStart;
   a.evStop = s->evStop;
   return knn_any(s, a, static_cast<cudaStream_t>(stream));

@@ -80,6 +80,7 @@ struct KnnArgs {
   unsigned long long* touched = nullptr;  // device counter (accumulated), may be null
   bool sortQueries = true;       // reorder queries along a space-filling curve
   int32_t* found = nullptr;      // optional device output: neighbours found per query
+  int traversal = 0;             // 0 auto, 1 reference order, 2 warp packet (exact search only)
   cudaEvent_t evStart = nullptr; // optional: recorded right before / after the search kernel
   cudaEvent_t evStop = nullptr;
 };

@@ -205,6 +205,143 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
   }
 }
 
+// Warp-packet traversal for exact search (epsilon = 0).
+//
+// The 32 queries of a warp (neighbours along the Morton order) walk the
+// tree together: one node sequence for the warp, chosen so that at each
+// inner node the child that most lanes see as their near side comes first;
+// every lane keeps its own offsets, box distance and top-k, and decides for
+// itself whether a node can hold a better neighbour. A node is skipped only
+// when no lane wants it, so every lane still examines every point that can
+// enter its result. Leaf records are read with warp-uniform addresses
+// (broadcast loads) and candidates are inserted after the whole leaf has
+// been filtered, so the warp pays for the largest number of insertions of
+// any one lane rather than for every point where some lane inserts.
+//
+// The box distance of a cell is the sequential sum over d of off[d]^2,
+// rounded exactly as the point distance is. Rounding is monotone, so a
+// point inside the cell is never closer than its cell's bound, and the
+// pruning test rd <= head never drops an acceptable point: the result is
+// the exact k smallest (dist2, index) pairs -- the brute-force answer.
+template <typename T, int D>
+__device__ __forceinline__ T box_dist2(const T (&off)[D]) {
+  T rd = Ar<T>::mul(off[0], off[0]);
+#pragma unroll
+  for (int d = 1; d < D; ++d) rd = Ar<T>::add(rd, Ar<T>::mul(off[d], off[d]));
+  return rd;
+}
+
+template <typename T, int D, int K, int STACK>
+__global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
+  constexpr unsigned kAll = 0xffffffffu;
+  constexpr int kChunk = 8;
+  const bool selfOk = a.allowSelf != 0;
+  const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
+  const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
+  const T* __restrict__ query = static_cast<const T*>(a.query);
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const bool active = t < a.nq;
+  const int64_t qi = active ? (a.order ? (int64_t)a.order[t] : t) : 0;
+  T q[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) q[d] = (active && d < a.dim) ? query[qi * a.qStride + d] : T(0);
+  T maxRadius2 = (T)a.maxRadius2;
+  if (a.maxRadii && active) {
+    const T r = static_cast<const T*>(a.maxRadii)[qi];
+    maxRadius2 = Ar<T>::mul(r, r);
+  }
+  if (!active) maxRadius2 = -Ar<T>::inf();  // wants nothing
+  TopK<T, K> heap;
+  heap.init(a.k);
+  T off[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) off[d] = T(0);
+  uint32_t sNode[STACK];
+  T sOff[STACK][D];
+  int sp = 0;
+  uint32_t node = 0;
+  for (;;) {
+    const T rd = box_dist2(off);
+    const bool want = rd <= maxRadius2 && rd <= heap.head();
+    if (__any_sync(kAll, want)) {
+      const Node<T> nd = load_node(nodes, node);
+      if (!node_is_leaf(nd.meta)) {
+        const int cd = (int)node_dim(nd.meta);
+        const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
+        const bool nearRight = newOff > T(0);
+        const int votesRight = __popc(__ballot_sync(kAll, want && nearRight));
+        const int votes = __popc(__ballot_sync(kAll, want));
+        const bool firstRight = 2 * votesRight > votes;
+        const uint32_t right = node_payload(nd.meta);
+        const uint32_t first = firstRight ? right : node + 1;
+        const uint32_t second = firstRight ? node + 1 : right;
+        // the second child is this lane's far side iff the first is its near side
+        const bool secondFar = nearRight == firstRight;
+        T offS[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) offS[d] = (d == cd && secondFar) ? newOff : off[d];
+        const T rdS = box_dist2(offS);
+        const bool wantS = want && rdS <= maxRadius2 && rdS <= heap.head();
+        if (__any_sync(kAll, wantS) && sp < STACK) {
+          sNode[sp] = second;
+#pragma unroll
+          for (int d = 0; d < D; ++d) sOff[sp][d] = offS[d];
+          ++sp;
+        }
+#pragma unroll
+        for (int d = 0; d < D; ++d)  // the first child is this lane's far side
+          if (d == cd && !secondFar) off[d] = newOff;
+        node = first;
+        continue;
+      }
+      const uint32_t cnt = node_payload(nd.meta);
+      const uint32_t st = node_start(nd);
+      for (uint32_t base = 0; base < cnt; base += kChunk) {
+        T dj[kChunk];
+        int ij[kChunk];
+        unsigned mask = 0;
+#pragma unroll
+        for (int j = 0; j < kChunk; ++j) {
+          dj[j] = Ar<T>::inf();
+          ij[j] = -1;
+          if (base + j < cnt) {
+            Rec<T, D> r;
+            load_rec(recs, (int64_t)st + base + j, r);
+            dj[j] = dist2_seq(q, r);
+            ij[j] = r.p.idx;
+            const bool ok = want && dj[j] <= maxRadius2 && heap.accepts(dj[j], ij[j]) &&
+                            (selfOk || dj[j] > Ar<T>::eps());
+            mask |= ok ? (1u << j) : 0u;
+          }
+        }
+        while (mask) {
+          const int j = __ffs(mask) - 1;
+          mask &= mask - 1;
+          T dv = dj[0];
+          int iv = ij[0];
+#pragma unroll
+          for (int m = 1; m < kChunk; ++m) {
+            if (j == m) {
+              dv = dj[m];
+              iv = ij[m];
+            }
+          }
+          if (heap.accepts(dv, iv)) heap.insert(dv, iv);
+        }
+      }
+    }
+    if (sp == 0) break;
+    --sp;
+    node = sNode[sp];
+#pragma unroll
+    for (int d = 0; d < D; ++d) off[d] = sOff[sp][d];
+  }
+  if (active) {
+    const int f = heap.store(a.k, a.outIdx + qi * a.k, static_cast<T*>(a.outD2) + qi * a.k);
+    if (a.found) a.found[qi] = f;
+  }
+}
+
 // Brute force (nabo/brute_force_cpu.cpp:63-103): every query against every
 // point, points staged through shared memory in tiles; each thread owns one
 // query and its top-k. Points are offered in index order.

@@ -69,13 +69,25 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
   const KnnLaunch L = make_launch<T, D>(c, a, order);
   const int grid = ceil_div(a.nq, 128);
   const bool small = c.height <= kStackSmall;
+  // The reference visit order is needed when it defines the answer: the
+  // touched-point count and approximate (epsilon > 0) search.
+  const bool packet = a.traversal == 2 || (a.traversal == 0 && a.eps == 0.0 && !L.stats);
+  if (packet && (a.eps != 0.0 || L.stats))
+    return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
   if (a.evStart) cudaEventRecord(a.evStart, stream);
-#define NABO_LAUNCH(KK)                                                       \
-  case KK:                                                                    \
-    if (small)                                                                \
-      k_knn_kdtree<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);       \
-    else                                                                      \
-      k_knn_kdtree<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);       \
+#define NABO_LAUNCH(KK)                                                            \
+  case KK:                                                                         \
+    if (packet) {                                                                  \
+      if (small)                                                                   \
+        k_knn_kdtree_packet<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);   \
+      else                                                                         \
+        k_knn_kdtree_packet<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);   \
+    } else {                                                                       \
+      if (small)                                                                   \
+        k_knn_kdtree<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);          \
+      else                                                                         \
+        k_knn_kdtree<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);          \
+    }                                                                              \
     break;
   switch (K) { NABO_K_LIST(NABO_LAUNCH) }
 #undef NABO_LAUNCH

@@ -81,16 +81,23 @@ def test_knnvalidate_cases_gpu(ref_scans, case):
             assert s.touched == q.shape[0] * cloud.shape[0]
 
 
-def _check_against_oracle(cloud, q, k, eps=0.0, flags=0, max_radius=np.inf, radii=None, bucket=8, stats=True):
+def _check_against_oracle(cloud, q, k, eps=0.0, flags=0, max_radius=np.inf, radii=None, bucket=8):
+    """Both kd-tree traversals against the oracle: the reference-order kernel
+    (selected by TOUCH_STATISTICS, or forced) must match indices, dists2 and
+    the touched count; the default kernel (warp packet for exact searches)
+    must match indices and dists2; brute force must match the oracle's."""
     nb = _nb()
-    cf = H.TOUCH_STATISTICS if stats else 0
-    orc = O.OracleTree(cloud, bucket_size=bucket, creation_flags=cf)
+    orc = O.OracleTree(cloud, bucket_size=bucket, creation_flags=H.TOUCH_STATISTICS)
     oi, od, ot = orc.knn(q, k, eps, flags, max_radius, max_radii=radii, mode=O.MODE_CANONICAL)
-    s = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, creationOptionFlags=cf,
+    s = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, creationOptionFlags=nb.TOUCH_STATISTICS,
                                   params={"bucketSize": bucket})
     gi, gd = s.knn(q, k, eps, flags, max_radius, maxRadii=radii)
-    H.assert_identical(gi, gd, oi, od, f"kd-tree k={k} eps={eps} flags={flags}")
+    H.assert_identical(gi, gd, oi, od, f"kd-tree (reference order) k={k} eps={eps} flags={flags}")
     assert s.touched == ot, f"touched {s.touched} vs {ot}"
+    for trav in (0, 1):
+        p = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": bucket, "traversal": trav})
+        pi, pd = p.knn(q, k, eps, flags, max_radius, maxRadii=radii)
+        H.assert_identical(pi, pd, oi, od, f"kd-tree (traversal {trav}) k={k} eps={eps} flags={flags}")
     if eps == 0.0:
         bi, bd, _ = O.bf_knn(cloud, q, k, flags, max_radius, max_radii=radii, mode=O.MODE_CANONICAL)
         b = nb.NearestNeighbourSearch(cloud, nb.SearchType.BRUTE_FORCE_CUDA)
@@ -264,3 +271,21 @@ def test_full_size_properties(which):
     sample = np.random.default_rng(1).choice(q.shape[0], 20000, replace=False)
     oi, od, _ = orc.knn(q[sample], k, 0.0, flags, r, mode=O.MODE_CANONICAL)
     H.assert_identical(gi[sample], gd[sample], oi, od, f"{which} sample")
+    # the default (warp-packet) search gives the same answer on every query
+    p = nb.NearestNeighbourSearch(cloud)
+    pi, pd = p.knn(q, k, 0.0, flags, r)
+    H.assert_identical(pi, pd, gi, gd, f"{which} packet vs reference order")
+
+
+def test_non_finite_cloud_is_rejected():
+    nb = _nb()
+    cloud = np.random.default_rng(3).random((500, 3)).astype(np.float32)
+    for bad in (np.nan, np.inf, -np.inf):
+        c = cloud.copy()
+        c[123, 1] = bad
+        with pytest.raises(nb.NaboError, match="non-finite"):
+            nb.NearestNeighbourSearch(c)
+    # a non-finite value in a row beyond `dim` is not searched and is accepted
+    c = np.concatenate([cloud, np.full((500, 1), np.nan, np.float32)], axis=1)
+    s = nb.NearestNeighbourSearch(c, dim=3)
+    assert s.dim == 3
