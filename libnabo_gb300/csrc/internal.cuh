@@ -95,6 +95,11 @@ template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
                   int32_t* dOrder, cudaStream_t stream);
 
+// Counting-sort placement: dHist holds per-cell counts (turned into offsets
+// in place), dCell/dRank each query's cell and rank inside it.
+int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist, int64_t bins, int64_t nq,
+                   int32_t* dOrder, cudaStream_t stream);
+
 // Device-wide exclusive scan of uint32 values (in place), returns total via
 // a device pointer. Scratch is stream-ordered.
 int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t stream);

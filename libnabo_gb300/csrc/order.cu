@@ -1,11 +1,13 @@
 // order.cu -- query ordering for warp coherence, and a device-wide scan.
 //
-// Queries are grouped by the cell of a Morton (Z-order) curve over the
-// cloud's bounding box: each query gets the top B bits of its interleaved
-// coordinate key (B ~ log2(nq) + 1), a counting sort by cell gives the
-// permutation. Threads of one warp then start from nearby points and walk
-// similar paths down the kd-tree. The order inside a cell is whatever the
-// atomics produce; results do not depend on it, only timing does.
+// A query ordering is a counting sort by cell: every query gets a cell id
+// and a rank inside its cell (an atomic increment of the cell's count), the
+// counts are scanned into offsets and each query is placed at offset+rank.
+// The kd-tree search uses the leaf each query descends to as its cell
+// (k_leaf_cells in search.cuh), which groups queries at the scale of the
+// data's own buckets. order_queries() offers a Morton (Z-order) cell over
+// the bounding box for searches without a tree. The order inside a cell is
+// whatever the atomics produce; results do not depend on it, only timing.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -127,6 +129,16 @@ int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t
   const cudaError_t e = cudaGetLastError();
   cudaFreeAsync(sums, stream);
   if (e != cudaSuccess) return cuda_error(e, "scan_exclusive_u32");
+  return kOk;
+}
+
+int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist, int64_t bins, int64_t nq,
+                   int32_t* dOrder, cudaStream_t stream) {
+  const int rc = scan_exclusive_u32(dHist, bins, nullptr, stream);
+  if (rc != kOk) return rc;
+  k_place<<<ceil_div(nq, kB), kB, 0, stream>>>(dCell, dRank, dHist, nq, dOrder);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "order_by_cells");
   return kOk;
 }
 

@@ -97,6 +97,29 @@ __device__ __forceinline__ T dist2_seq(const T (&q)[D], const Rec<T, D>& r) {
   return dist;
 }
 
+// Query ordering for the kd-tree: each query's cell is the leaf it reaches
+// by always taking its near side (new_off > 0 -> right, as the search
+// does). Leaves are numbered in pre-order, so queries sorted by leaf are
+// grouped at the scale of the data's own buckets.
+template <typename T, int D>
+__global__ void k_leaf_cells(const Node<T>* __restrict__ nodes, const T* __restrict__ query, int64_t nq,
+                             int64_t qStride, int dim, uint32_t* cell, uint32_t* rank, uint32_t* hist) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  T q[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) q[d] = d < dim ? query[i * qStride + d] : T(0);
+  uint32_t node = 0;
+  for (;;) {
+    const Node<T> nd = load_node(nodes, node);
+    if (node_is_leaf(nd.meta)) break;
+    const T newOff = Ar<T>::sub(pick(q, (int)node_dim(nd.meta)), nd.cut);
+    node = newOff > T(0) ? node_payload(nd.meta) : node + 1;
+  }
+  cell[i] = node;
+  rank[i] = atomicAdd(hist + node, 1u);
+}
+
 struct KnnLaunch {
   const void* nodes;
   const void* recs;

@@ -59,10 +59,27 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
     return set_error(kErrUnsupported, "kd-tree height exceeds the traversal stack of the CUDA search");
   int32_t* order = nullptr;
   if (a.sortQueries && a.nq >= 4096) {
-    NABO_CUDA_TRY(cudaMallocAsync((void**)&order, (size_t)a.nq * sizeof(int32_t), stream));
-    const int rc = order_queries<T>(static_cast<const T*>(a.query), a.nq, a.qStride, c.dim, c.lo, c.hi, order, stream);
+    // counting sort of the queries by the leaf they descend to
+    uint32_t *hist = nullptr, *cell = nullptr, *rank = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&order, (size_t)a.nq * sizeof(int32_t), stream);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&hist, (size_t)c.nodeCount * sizeof(uint32_t), stream);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&cell, (size_t)a.nq * sizeof(uint32_t), stream);
+    if (e == cudaSuccess) e = cudaMallocAsync((void**)&rank, (size_t)a.nq * sizeof(uint32_t), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, (size_t)c.nodeCount * sizeof(uint32_t), stream);
+    int rc = kOk;
+    if (e == cudaSuccess) {
+      k_leaf_cells<T, D><<<ceil_div(a.nq, 256), 256, 0, stream>>>(static_cast<const Node<T>*>(c.nodes),
+                                                                  static_cast<const T*>(a.query), a.nq, a.qStride,
+                                                                  c.dim, cell, rank, hist);
+      rc = order_by_cells(cell, rank, hist, c.nodeCount, a.nq, order, stream);
+    } else {
+      rc = cuda_error(e, "query ordering");
+    }
+    if (hist) cudaFreeAsync(hist, stream);
+    if (cell) cudaFreeAsync(cell, stream);
+    if (rank) cudaFreeAsync(rank, stream);
     if (rc != kOk) {
-      cudaFreeAsync(order, stream);
+      if (order) cudaFreeAsync(order, stream);
       return rc;
     }
   }

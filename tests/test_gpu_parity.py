@@ -82,10 +82,17 @@ def test_knnvalidate_cases_gpu(ref_scans, case):
 
 
 def _check_against_oracle(cloud, q, k, eps=0.0, flags=0, max_radius=np.inf, radii=None, bucket=8):
-    """Both kd-tree traversals against the oracle: the reference-order kernel
-    (selected by TOUCH_STATISTICS, or forced) must match indices, dists2 and
-    the touched count; the default kernel (warp packet for exact searches)
-    must match indices and dists2; brute force must match the oracle's."""
+    """Both kd-tree traversals and brute force against the oracle.
+
+    The reference-order kernel (used with TOUCH_STATISTICS or epsilon > 0,
+    or forced with traversal=1) must match the oracle's kd-tree search:
+    indices, dists2 and the touched count. The warp-packet kernel (default
+    for exact searches) prunes with a bound that provably never exceeds a
+    point's distance, so it must match the oracle's brute force exactly;
+    the reference's incremental box distance can round above a point's
+    distance, so on rare ties-at-rounding inputs the oracle's kd-tree search
+    misses a point that brute force keeps (see test_empty_query_and_far_queries).
+    """
     nb = _nb()
     orc = O.OracleTree(cloud, bucket_size=bucket, creation_flags=H.TOUCH_STATISTICS)
     oi, od, ot = orc.knn(q, k, eps, flags, max_radius, max_radii=radii, mode=O.MODE_CANONICAL)
@@ -94,15 +101,20 @@ def _check_against_oracle(cloud, q, k, eps=0.0, flags=0, max_radius=np.inf, radi
     gi, gd = s.knn(q, k, eps, flags, max_radius, maxRadii=radii)
     H.assert_identical(gi, gd, oi, od, f"kd-tree (reference order) k={k} eps={eps} flags={flags}")
     assert s.touched == ot, f"touched {s.touched} vs {ot}"
-    for trav in (0, 1):
-        p = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": bucket, "traversal": trav})
-        pi, pd = p.knn(q, k, eps, flags, max_radius, maxRadii=radii)
-        H.assert_identical(pi, pd, oi, od, f"kd-tree (traversal {trav}) k={k} eps={eps} flags={flags}")
+    r = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": bucket, "traversal": 1})
+    ri, rd = r.knn(q, k, eps, flags, max_radius, maxRadii=radii)
+    H.assert_identical(ri, rd, oi, od, f"kd-tree (traversal 1) k={k} eps={eps} flags={flags}")
+    p = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": bucket})
+    pi, pd = p.knn(q, k, eps, flags, max_radius, maxRadii=radii)
     if eps == 0.0:
         bi, bd, _ = O.bf_knn(cloud, q, k, flags, max_radius, max_radii=radii, mode=O.MODE_CANONICAL)
+        H.assert_identical(pi, pd, bi, bd, f"kd-tree (warp packet) vs oracle brute force k={k}")
+        H.assert_equal_up_to_ties(pi, pd, oi, od, f"kd-tree (warp packet) vs oracle kd-tree k={k}")
         b = nb.NearestNeighbourSearch(cloud, nb.SearchType.BRUTE_FORCE_CUDA)
         gbi, gbd = b.knn(q, k, 0.0, flags, max_radius, maxRadii=radii)
         H.assert_identical(gbi, gbd, bi, bd, f"brute force k={k}")
+    else:
+        H.assert_identical(pi, pd, oi, od, f"kd-tree (default, epsilon > 0) k={k}")
     return gi, gd
 
 
@@ -170,6 +182,12 @@ def test_degenerate_clouds():
 
 
 def test_empty_query_and_far_queries():
+    """Queries 1e7 away from a unit cloud: every squared distance rounds to
+    one of a few float values, so most neighbours tie. The brute-force /
+    warp-packet answer keeps the lowest indices among the tied points; the
+    reference-order traversal can prune a cell whose incrementally updated
+    box distance rounded above the head while a point inside it ties the
+    head, which the oracle's kd-tree reproduces."""
     nb = _nb()
     rng = np.random.default_rng(13)
     cloud = rng.random((1000, 3)).astype(np.float32)
