@@ -52,7 +52,7 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--traversal", type=int, default=0,
-                   help="kd-tree traversal: 0 auto (warp packet for exact search), 1 reference order")
+                   help="kd-tree traversal: 0/1 reference visit order (default), 2 warp packet")
     return p.parse_args()
 
 
@@ -320,7 +320,7 @@ def run_ours(args):
         "config": {"workload": f"{cfg['label']}_k{k}", "points": int(cloud.shape[0]), "queries": int(nq),
                    "k": k, "maxRadius": cfg["maxRadius"], "selfMatch": False, "bucketSize": 8,
                    "form": "plain GPU kd-tree",
-                   "traversal": "warp packet" if args.traversal in (0, 2) else "reference order",
+                   "traversal": "warp packet" if args.traversal == 2 else "reference order",
                    "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),

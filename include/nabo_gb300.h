@@ -67,12 +67,12 @@ typedef struct nabo_cuda_params {
   uint32_t bucketSize;    /* "bucketSize", default 8 (nabo/kdtree_cpu.cpp:230) */
   int32_t queryOrdering;  /* 1 (default): reorder queries along a Morton curve
                              inside each search; 0: keep the given order */
-  int32_t traversal;      /* kd-tree search order. 0 (default): the warp-packet
-                             traversal for exact searches (epsilon 0) without
-                             TOUCH_STATISTICS, else the reference's visit order;
-                             1: always the reference's visit order; 2: always
-                             the warp packet (exact searches without touch
-                             statistics only) */
+  int32_t traversal;      /* kd-tree search order. 0 (default) or 1: the
+                             reference's visit order (nabo/kdtree_cpu.cpp:
+                             367-447), one query per thread; 2: the warp
+                             packet -- the 32 queries of a warp walk one node
+                             sequence, each pruning for itself -- for exact
+                             searches (epsilon 0) without TOUCH_STATISTICS */
   int32_t reserved[4];
 } nabo_cuda_params;
 

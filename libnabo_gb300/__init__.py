@@ -111,7 +111,8 @@ class NearestNeighbourSearch:
     (n, rows); it is copied into the search object. ``params`` accepts the
     reference's ``bucketSize`` key, ``queryOrdering`` (1 = sort queries
     along a Morton curve inside each search, the default) and ``traversal``
-    (0 auto, 1 the reference's visit order, 2 the warp packet).
+    (0 or 1 the reference's visit order, 2 the warp packet for exact
+    searches without touch statistics).
     """
 
     def __init__(self, cloud, searchType: int = SearchType.KDTREE_CUDA, dim: int | None = None,

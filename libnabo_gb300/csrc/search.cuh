@@ -141,6 +141,56 @@ struct KnnLaunch {
   int stats;
 };
 
+// Leaf scan shared by the kernels: the bucket's records are read in chunks
+// of 8 (independent loads in flight), candidates that beat the current head
+// are collected in a bit mask and inserted afterwards. The order of
+// insertion inside a leaf does not change the heap after the leaf (the k
+// smallest pairs of the union), so this matches the reference's point-by-
+// point loop (nabo/kdtree_cpu.cpp:378-398); the warp pays for the largest
+// number of insertions of any lane instead of for every point where some
+// lane inserts.
+template <typename T, int D, int K>
+__device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, uint32_t st, uint32_t cnt,
+                                          const T (&q)[D], T maxRadius2, bool selfOk, bool want, TopK<T, K>& heap) {
+  constexpr int kChunk = 8;
+  for (uint32_t base = 0; base < cnt; base += kChunk) {
+    T dj[kChunk];
+    int ij[kChunk];
+    unsigned mask = 0;
+#pragma unroll
+    for (int j = 0; j < kChunk; ++j) {
+      dj[j] = Ar<T>::inf();
+      ij[j] = -1;
+      if (base + j < cnt) {
+        Rec<T, D> r;
+        load_rec(recs, (int64_t)st + base + j, r);
+        dj[j] = dist2_seq(q, r);
+        ij[j] = r.p.idx;
+        const bool ok = want && dj[j] <= maxRadius2 && heap.accepts(dj[j], ij[j]) &&
+                        (selfOk || dj[j] > Ar<T>::eps());
+        mask |= ok ? (1u << j) : 0u;
+      }
+    }
+    while (mask) {
+      const int j = __ffs(mask) - 1;
+      mask &= mask - 1;
+      T dv = dj[0];
+      int iv = ij[0];
+#pragma unroll
+      for (int m = 1; m < kChunk; ++m) {
+        if (j == m) {
+          dv = dj[m];
+          iv = ij[m];
+        }
+      }
+      if (heap.accepts(dv, iv)) heap.insert(dv, iv);
+    }
+  }
+}
+
+// Reference-order traversal, structured descend / leaf / pop so the lanes
+// of a warp run each phase together: all lanes descend until every lane
+// stands on a leaf, then all scan their leaves, then all pop.
 template <typename T, int D, int K, int STACK>
 __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
   const bool selfOk = a.allowSelf != 0;
@@ -172,8 +222,9 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
     uint32_t node = 0;
     T rd = T(0);
     for (;;) {
-      const Node<T> nd = load_node(nodes, node);
-      if (!node_is_leaf(nd.meta)) {
+      // descend to a leaf, pushing far children
+      Node<T> nd = load_node(nodes, node);
+      while (!node_is_leaf(nd.meta)) {
         const int cd = (int)node_dim(nd.meta);
         const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
         const T oldOff = pick(off, cd);
@@ -191,18 +242,13 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
           ++sp;
         }
         node = nearN;
-        continue;
+        nd = load_node(nodes, node);
       }
+      // leaf
       const uint32_t cnt = node_payload(nd.meta);
-      const uint32_t st = node_start(nd);
-      for (uint32_t j = 0; j < cnt; ++j) {
-        Rec<T, D> r;
-        load_rec(recs, (int64_t)st + j, r);
-        const T dist = dist2_seq(q, r);
-        if (dist <= maxRadius2 && heap.accepts(dist, r.p.idx) && (selfOk || dist > Ar<T>::eps()))
-          heap.insert(dist, r.p.idx);
-      }
+      scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, selfOk, true, heap);
       touched += cnt;
+      // pop the next far child that can still hold a better neighbour
       bool more = false;
       while (sp > 0) {
         --sp;
@@ -257,7 +303,6 @@ __device__ __forceinline__ T box_dist2(const T (&off)[D]) {
 template <typename T, int D, int K, int STACK>
 __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
   constexpr unsigned kAll = 0xffffffffu;
-  constexpr int kChunk = 8;
   const bool selfOk = a.allowSelf != 0;
   const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
@@ -317,41 +362,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
         node = first;
         continue;
       }
-      const uint32_t cnt = node_payload(nd.meta);
-      const uint32_t st = node_start(nd);
-      for (uint32_t base = 0; base < cnt; base += kChunk) {
-        T dj[kChunk];
-        int ij[kChunk];
-        unsigned mask = 0;
-#pragma unroll
-        for (int j = 0; j < kChunk; ++j) {
-          dj[j] = Ar<T>::inf();
-          ij[j] = -1;
-          if (base + j < cnt) {
-            Rec<T, D> r;
-            load_rec(recs, (int64_t)st + base + j, r);
-            dj[j] = dist2_seq(q, r);
-            ij[j] = r.p.idx;
-            const bool ok = want && dj[j] <= maxRadius2 && heap.accepts(dj[j], ij[j]) &&
-                            (selfOk || dj[j] > Ar<T>::eps());
-            mask |= ok ? (1u << j) : 0u;
-          }
-        }
-        while (mask) {
-          const int j = __ffs(mask) - 1;
-          mask &= mask - 1;
-          T dv = dj[0];
-          int iv = ij[0];
-#pragma unroll
-          for (int m = 1; m < kChunk; ++m) {
-            if (j == m) {
-              dv = dj[m];
-              iv = ij[m];
-            }
-          }
-          if (heap.accepts(dv, iv)) heap.insert(dv, iv);
-        }
-      }
+      scan_leaf<T, D, K>(recs, node_start(nd), node_payload(nd.meta), q, maxRadius2, selfOk, want, heap);
     }
     if (sp == 0) break;
     --sp;

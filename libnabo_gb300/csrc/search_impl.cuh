@@ -86,9 +86,9 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
   const KnnLaunch L = make_launch<T, D>(c, a, order);
   const int grid = ceil_div(a.nq, 128);
   const bool small = c.height <= kStackSmall;
-  // The reference visit order is needed when it defines the answer: the
-  // touched-point count and approximate (epsilon > 0) search.
-  const bool packet = a.traversal == 2 || (a.traversal == 0 && a.eps == 0.0 && !L.stats);
+  // Default: the reference visit order (it is also the faster one on the
+  // measured workloads); the warp packet is opt-in for exact searches.
+  const bool packet = a.traversal == 2;
   if (packet && (a.eps != 0.0 || L.stats))
     return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
   if (a.evStart) cudaEventRecord(a.evStart, stream);

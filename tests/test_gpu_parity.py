@@ -84,14 +84,14 @@ def test_knnvalidate_cases_gpu(ref_scans, case):
 def _check_against_oracle(cloud, q, k, eps=0.0, flags=0, max_radius=np.inf, radii=None, bucket=8):
     """Both kd-tree traversals and brute force against the oracle.
 
-    The reference-order kernel (used with TOUCH_STATISTICS or epsilon > 0,
-    or forced with traversal=1) must match the oracle's kd-tree search:
-    indices, dists2 and the touched count. The warp-packet kernel (default
-    for exact searches) prunes with a bound that provably never exceeds a
-    point's distance, so it must match the oracle's brute force exactly;
-    the reference's incremental box distance can round above a point's
-    distance, so on rare ties-at-rounding inputs the oracle's kd-tree search
-    misses a point that brute force keeps (see test_empty_query_and_far_queries).
+    The default reference-order kernel must match the oracle's kd-tree
+    search: indices, dists2 and the touched count. The opt-in warp-packet
+    kernel (traversal=2, exact searches) prunes with a bound that provably
+    never exceeds a point's distance, so it must match the oracle's brute
+    force exactly; the reference's incrementally updated box distance can
+    round above a point's distance, so on rare inputs where a point ties the
+    head at that rounding the kd-tree search misses a point that brute force
+    keeps (see test_empty_query_and_far_queries).
     """
     nb = _nb()
     orc = O.OracleTree(cloud, bucket_size=bucket, creation_flags=H.TOUCH_STATISTICS)
@@ -99,22 +99,20 @@ def _check_against_oracle(cloud, q, k, eps=0.0, flags=0, max_radius=np.inf, radi
     s = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, creationOptionFlags=nb.TOUCH_STATISTICS,
                                   params={"bucketSize": bucket})
     gi, gd = s.knn(q, k, eps, flags, max_radius, maxRadii=radii)
-    H.assert_identical(gi, gd, oi, od, f"kd-tree (reference order) k={k} eps={eps} flags={flags}")
+    H.assert_identical(gi, gd, oi, od, f"kd-tree k={k} eps={eps} flags={flags}")
     assert s.touched == ot, f"touched {s.touched} vs {ot}"
-    r = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": bucket, "traversal": 1})
+    r = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": bucket})
     ri, rd = r.knn(q, k, eps, flags, max_radius, maxRadii=radii)
-    H.assert_identical(ri, rd, oi, od, f"kd-tree (traversal 1) k={k} eps={eps} flags={flags}")
-    p = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": bucket})
-    pi, pd = p.knn(q, k, eps, flags, max_radius, maxRadii=radii)
+    H.assert_identical(ri, rd, oi, od, f"kd-tree without statistics k={k} eps={eps} flags={flags}")
     if eps == 0.0:
         bi, bd, _ = O.bf_knn(cloud, q, k, flags, max_radius, max_radii=radii, mode=O.MODE_CANONICAL)
+        p = nb.NearestNeighbourSearch(cloud, nb.SearchType.KDTREE_CUDA, params={"bucketSize": bucket, "traversal": 2})
+        pi, pd = p.knn(q, k, eps, flags, max_radius, maxRadii=radii)
         H.assert_identical(pi, pd, bi, bd, f"kd-tree (warp packet) vs oracle brute force k={k}")
         H.assert_equal_up_to_ties(pi, pd, oi, od, f"kd-tree (warp packet) vs oracle kd-tree k={k}")
         b = nb.NearestNeighbourSearch(cloud, nb.SearchType.BRUTE_FORCE_CUDA)
         gbi, gbd = b.knn(q, k, 0.0, flags, max_radius, maxRadii=radii)
         H.assert_identical(gbi, gbd, bi, bd, f"brute force k={k}")
-    else:
-        H.assert_identical(pi, pd, oi, od, f"kd-tree (default, epsilon > 0) k={k}")
     return gi, gd
 
 
@@ -183,8 +181,8 @@ def test_degenerate_clouds():
 
 def test_empty_query_and_far_queries():
     """Queries 1e7 away from a unit cloud: every squared distance rounds to
-    one of a few float values, so most neighbours tie. The brute-force /
-    warp-packet answer keeps the lowest indices among the tied points; the
+    one of a few float values, so most neighbours tie. The brute-force and
+    warp-packet answers keep the lowest indices among the tied points; the
     reference-order traversal can prune a cell whose incrementally updated
     box distance rounded above the head while a point inside it ties the
     head, which the oracle's kd-tree reproduces."""
@@ -289,10 +287,12 @@ def test_full_size_properties(which):
     sample = np.random.default_rng(1).choice(q.shape[0], 20000, replace=False)
     oi, od, _ = orc.knn(q[sample], k, 0.0, flags, r, mode=O.MODE_CANONICAL)
     H.assert_identical(gi[sample], gd[sample], oi, od, f"{which} sample")
-    # the default (warp-packet) search gives the same answer on every query
-    p = nb.NearestNeighbourSearch(cloud)
-    pi, pd = p.knn(q, k, 0.0, flags, r)
-    H.assert_identical(pi, pd, gi, gd, f"{which} packet vs reference order")
+    # without statistics, and with the warp-packet traversal, every query
+    # gets the same answer
+    for params in ({}, {"traversal": 2}):
+        p = nb.NearestNeighbourSearch(cloud, params=params)
+        pi, pd = p.knn(q, k, 0.0, flags, r)
+        H.assert_identical(pi, pd, gi, gd, f"{which} {params} vs statistics run")
 
 
 def test_non_finite_cloud_is_rejected():
