@@ -771,13 +771,13 @@ struct Scratch {
   std::vector<void*> ptrs;
   explicit Scratch(cudaStream_t s) : stream(s) {}
   ~Scratch() {
-    for (void* p : ptrs) cudaFreeAsync(p, stream);
+    for (void* p : ptrs) scratch_free(p, stream);
   }
   template <typename V>
   cudaError_t get(V** out, int64_t count) {
     void* p = nullptr;
     const size_t bytes = (size_t)std::max<int64_t>(count, 1) * sizeof(V);
-    cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+    cudaError_t e = scratch_alloc(&p, bytes, stream);
     if (e == cudaSuccess) ptrs.push_back(p);
     *out = static_cast<V*>(p);
     return e;
@@ -854,10 +854,10 @@ int compute_bounds(const Rec<T, D>* recs, int64_t n, int dim, cudaStream_t strea
 template <typename T, int D>
 int pack_cloud(const T* dCloud, int64_t n, int64_t stride, int dim, cudaStream_t stream, DeviceCloud* out) {
   Rec<T, D>* recs = nullptr;
-  NABO_CUDA_TRY(cudaMallocAsync((void**)&recs, (size_t)n * sizeof(Rec<T, D>), stream));
+  NABO_CUDA_TRY(cudaMalloc((void**)&recs, (size_t)n * sizeof(Rec<T, D>)));
+  out->recs = recs;
   k_pack<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, recs);
   NABO_CUDA_TRY(cudaGetLastError());
-  out->recs = recs;
   Scratch sc(stream);
   const int rc = compute_bounds<T, D>(recs, n, dim, stream, sc, out->lo, out->hi);
   if (rc != kOk) return rc;
@@ -872,7 +872,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   const int N = (int)n;
   Scratch sc(stream);
   Rec<T, D>* recs = nullptr;
-  NABO_CUDA_TRY(cudaMallocAsync((void**)&recs, (size_t)n * sizeof(Rec<T, D>), stream));
+  NABO_CUDA_TRY(cudaMalloc((void**)&recs, (size_t)n * sizeof(Rec<T, D>)));
   out->recs = recs;  // owned by the caller from here on
   k_pack<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, recs);
   NABO_CUDA_TRY(cudaGetLastError());
@@ -1006,7 +1006,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   // Upper bound on the node count: every leaf holds at least one point.
   Node<T>* nodes = nullptr;
   const int64_t nodeCap = 2 * n;
-  NABO_CUDA_TRY(cudaMallocAsync((void**)&nodes, (size_t)nodeCap * sizeof(Node<T>), stream));
+  NABO_CUDA_TRY(cudaMalloc((void**)&nodes, (size_t)nodeCap * sizeof(Node<T>)));
   out->nodes = nodes;
   k_renumber<T><<<1, 1024, 0, stream>>>(top, small, dLv, dLv + nLevels, nLevels, nodes, dTotal);
   k_copy_small<T><<<ceil_div(nSmall, 128), 128, 0, stream>>>(scratchNodes, small, nSmall, nodes);

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <limits>
 #include <string>
 #include <vector>
@@ -26,6 +27,47 @@ int set_error(int code, const std::string& msg) {
   g_lastError = msg;
   return code;
 }
+
+namespace {
+std::mutex g_poolMutex;
+cudaMemPool_t g_pools[64] = {};
+}  // namespace
+
+static cudaError_t library_pool(cudaMemPool_t* pool) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_poolMutex);
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p;
+    e = cudaMemPoolCreate(&p, &props);
+    if (e != cudaSuccess) return e;
+    uint64_t keep = ~0ull;
+    e = cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+      cudaMemPoolDestroy(p);
+      return e;
+    }
+    g_pools[dev] = p;
+  }
+  *pool = g_pools[dev];
+  return cudaSuccess;
+}
+
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
+  cudaMemPool_t pool;
+  const cudaError_t e = library_pool(&pool);
+  if (e != cudaSuccess) return e;
+  return cudaMallocFromPoolAsync(p, bytes, pool, stream);
+}
+
+cudaError_t scratch_free(void* p, cudaStream_t stream) { return cudaFreeAsync(p, stream); }
 
 int cuda_error(cudaError_t e, const char* what) {
   g_lastError = std::string("CUDA error in ") + what + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
@@ -217,13 +259,13 @@ int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int6
   void* tmp = nullptr;
   int rc = kOk;
   if (!cloudOnDevice) {
-    cudaError_t e = cudaMallocAsync(&tmp, bytes, st);
+    cudaError_t e = scratch_alloc(&tmp, bytes, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(tmp, cloud, bytes, cudaMemcpyHostToDevice, st);
     if (e != cudaSuccess) rc = cuda_error(e, "cloud upload");
     dCloud = tmp;
   }
   if (rc == kOk) rc = build_any(h, dCloud, colStride, st);
-  if (tmp) cudaFreeAsync(tmp, st);
+  if (tmp) scratch_free(tmp, st);
   if (rc == kOk) {
     const cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) rc = cuda_error(e, "create");
@@ -344,11 +386,11 @@ int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64
   void *dq = nullptr, *dr = nullptr, *dd = nullptr;
   int32_t* di = nullptr;
   unsigned long long* dt = nullptr;
-  cudaError_t e = cudaMallocAsync(&dq, qBytes, st);
-  if (e == cudaSuccess && maxRadii) e = cudaMallocAsync(&dr, (size_t)nq * es, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&di, outN * sizeof(int32_t), st);
-  if (e == cudaSuccess) e = cudaMallocAsync(&dd, outN * es, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void**)&dt, sizeof(unsigned long long), st);
+  cudaError_t e = scratch_alloc(&dq, qBytes, st);
+  if (e == cudaSuccess && maxRadii) e = scratch_alloc(&dr, (size_t)nq * es, st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&di, outN * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = scratch_alloc(&dd, outN * es, st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&dt, sizeof(unsigned long long), st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dq, query, qBytes, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && maxRadii) e = cudaMemcpyAsync(dr, maxRadii, (size_t)nq * es, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(dt, 0, sizeof(unsigned long long), st);
@@ -378,11 +420,11 @@ int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64
     if (e == cudaSuccess) e = cudaMemcpyAsync(&ht, dt, sizeof(ht), cudaMemcpyDeviceToHost, st);
     if (e != cudaSuccess) rc = cuda_error(e, "knn results");
   }
-  if (dq) cudaFreeAsync(dq, st);
-  if (dr) cudaFreeAsync(dr, st);
-  if (di) cudaFreeAsync(di, st);
-  if (dd) cudaFreeAsync(dd, st);
-  if (dt) cudaFreeAsync(dt, st);
+  if (dq) scratch_free(dq, st);
+  if (dr) scratch_free(dr, st);
+  if (di) scratch_free(di, st);
+  if (dd) scratch_free(dd, st);
+  if (dt) scratch_free(dt, st);
   e = cudaStreamSynchronize(st);
   if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, "knn");
   if (rc == kOk && touched) {

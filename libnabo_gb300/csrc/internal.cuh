@@ -29,6 +29,14 @@ int cuda_error(cudaError_t e, const char* what);
     if (e__ != cudaSuccess) return ::nabo_gb300::cuda_error(e__, #expr); \
   } while (0)
 
+// Stream-ordered scratch from a library-owned memory pool of the current
+// device. The pool keeps freed memory mapped (release threshold: unlimited)
+// so repeated searches do not remap their scratch after every
+// synchronisation; it is separate from the device's default pool, so other
+// users of cudaMallocAsync are unaffected.
+cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream);
+cudaError_t scratch_free(void* p, cudaStream_t stream);
+
 // Device-resident kd-tree (or, for brute force, the packed cloud only).
 struct DeviceCloud {
   int dtype = 0;        // 0 = f32, 1 = f64

@@ -122,12 +122,12 @@ __global__ void k_place(const uint32_t* __restrict__ cell, const uint32_t* __res
 int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t stream) {
   const int nb = ceil_div(n, kB);
   uint32_t* sums = nullptr;
-  NABO_CUDA_TRY(cudaMallocAsync((void**)&sums, (size_t)std::max(nb, 1) * sizeof(uint32_t), stream));
+  NABO_CUDA_TRY(scratch_alloc((void**)&sums, (size_t)std::max(nb, 1) * sizeof(uint32_t), stream));
   k_block_sums<<<nb, kB, 0, stream>>>(data, n, sums);
   k_scan_sums<<<1, kB, 0, stream>>>(sums, nb, dTotal);
   k_apply<<<nb, kB, 0, stream>>>(data, n, sums);
   const cudaError_t e = cudaGetLastError();
-  cudaFreeAsync(sums, stream);
+  scratch_free(sums, stream);
   if (e != cudaSuccess) return cuda_error(e, "scan_exclusive_u32");
   return kOk;
 }
@@ -165,9 +165,9 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
   }
   const int64_t bins = int64_t(1) << B;
   uint32_t *hist = nullptr, *cell = nullptr, *rank = nullptr;
-  NABO_CUDA_TRY(cudaMallocAsync((void**)&hist, (size_t)bins * sizeof(uint32_t), stream));
-  NABO_CUDA_TRY(cudaMallocAsync((void**)&cell, (size_t)nq * sizeof(uint32_t), stream));
-  NABO_CUDA_TRY(cudaMallocAsync((void**)&rank, (size_t)nq * sizeof(uint32_t), stream));
+  NABO_CUDA_TRY(scratch_alloc((void**)&hist, (size_t)bins * sizeof(uint32_t), stream));
+  NABO_CUDA_TRY(scratch_alloc((void**)&cell, (size_t)nq * sizeof(uint32_t), stream));
+  NABO_CUDA_TRY(scratch_alloc((void**)&rank, (size_t)nq * sizeof(uint32_t), stream));
   NABO_CUDA_TRY(cudaMemsetAsync(hist, 0, (size_t)bins * sizeof(uint32_t), stream));
   k_cells<T><<<ceil_div(nq, kB), kB, 0, stream>>>(dQuery, nq, qStride, p, cell, rank, hist);
   int rc = scan_exclusive_u32(hist, bins, nullptr, stream);
@@ -176,9 +176,9 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = cuda_error(e, "order_queries");
   }
-  cudaFreeAsync(hist, stream);
-  cudaFreeAsync(cell, stream);
-  cudaFreeAsync(rank, stream);
+  scratch_free(hist, stream);
+  scratch_free(cell, stream);
+  scratch_free(rank, stream);
   return rc;
 }
 

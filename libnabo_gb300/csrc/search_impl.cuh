@@ -61,10 +61,10 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
   if (a.sortQueries && a.nq >= 4096) {
     // counting sort of the queries by the leaf they descend to
     uint32_t *hist = nullptr, *cell = nullptr, *rank = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&order, (size_t)a.nq * sizeof(int32_t), stream);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&hist, (size_t)c.nodeCount * sizeof(uint32_t), stream);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&cell, (size_t)a.nq * sizeof(uint32_t), stream);
-    if (e == cudaSuccess) e = cudaMallocAsync((void**)&rank, (size_t)a.nq * sizeof(uint32_t), stream);
+    cudaError_t e = scratch_alloc((void**)&order, (size_t)a.nq * sizeof(int32_t), stream);
+    if (e == cudaSuccess) e = scratch_alloc((void**)&hist, (size_t)c.nodeCount * sizeof(uint32_t), stream);
+    if (e == cudaSuccess) e = scratch_alloc((void**)&cell, (size_t)a.nq * sizeof(uint32_t), stream);
+    if (e == cudaSuccess) e = scratch_alloc((void**)&rank, (size_t)a.nq * sizeof(uint32_t), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, (size_t)c.nodeCount * sizeof(uint32_t), stream);
     int rc = kOk;
     if (e == cudaSuccess) {
@@ -75,11 +75,11 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
     } else {
       rc = cuda_error(e, "query ordering");
     }
-    if (hist) cudaFreeAsync(hist, stream);
-    if (cell) cudaFreeAsync(cell, stream);
-    if (rank) cudaFreeAsync(rank, stream);
+    if (hist) scratch_free(hist, stream);
+    if (cell) scratch_free(cell, stream);
+    if (rank) scratch_free(rank, stream);
     if (rc != kOk) {
-      if (order) cudaFreeAsync(order, stream);
+      if (order) scratch_free(order, stream);
       return rc;
     }
   }
@@ -110,7 +110,7 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
 #undef NABO_LAUNCH
   if (a.evStop) cudaEventRecord(a.evStop, stream);
   const cudaError_t e = cudaGetLastError();
-  if (order) cudaFreeAsync(order, stream);
+  if (order) scratch_free(order, stream);
   if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree launch");
   return kOk;
 }
