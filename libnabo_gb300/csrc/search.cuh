@@ -192,7 +192,7 @@ __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, ui
 // of a warp run each phase together: all lanes descend until every lane
 // stands on a leaf, then all scan their leaves, then all pop.
 template <typename T, int D, int K, int STACK>
-__global__ void __launch_bounds__(128, 8) k_knn_kdtree(KnnLaunch a) {
+__global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
   const bool selfOk = a.allowSelf != 0;
   const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
