@@ -122,6 +122,38 @@ int nabo_cuda_knn_device(const nabo_cuda_search* s, const void* query, int qRows
                          int k, double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii,
                          int32_t* indices, void* dists2, uint64_t* touched, void* stream);
 
+/* Search that allocates no device memory (no counterpart in the reference,
+ * whose CPU search needs no device memory at all).
+ *
+ * nabo_cuda_knn_device takes its query-ordering scratch from a memory
+ * pool, which may call into the CUDA allocator. Some callers must not do
+ * that once they are running: a robot's real-time perception loop (for
+ * example ICP registering every lidar scan) that fixes its GPU memory at
+ * start-up because allocation can block or synchronise the device, and
+ * applications whose device memory is owned by their own arena. For them
+ * this entry point takes its scratch from a fixed array inside the library,
+ * NABO_CUDA_NOALLOC_SCRATCH_BYTES (3.25 MiB) per GPU, held by every GPU
+ * that loads the library until the process exits. The caller passes device
+ * inputs and outputs exactly as for nabo_cuda_knn_device; the results are
+ * identical.
+ *
+ * Limits and rules:
+ *  - nq <= NABO_CUDA_NOALLOC_MAX_QUERIES per call; larger requests fail
+ *    with NABO_CUDA_ERR_ARGUMENT (split the batch);
+ *  - the first call on a device looks up the array's device address
+ *    (cudaGetSymbolAddress); make that first call before any stream
+ *    capture;
+ *  - every call on a device shares the one array: calls whose work
+ *    overlaps on the GPU (different streams or threads without ordering
+ *    between them) race and corrupt each other's results. Order them on
+ *    one stream or synchronise between them. */
+#define NABO_CUDA_NOALLOC_MAX_QUERIES 262144
+#define NABO_CUDA_NOALLOC_SCRATCH_BYTES 3407872
+int nabo_cuda_knn_device_noalloc(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq,
+                                 int64_t qStride, int k, double epsilon, unsigned optionFlags, double maxRadius,
+                                 const void* maxRadii, int32_t* indices, void* dists2, uint64_t* touched,
+                                 void* stream);
+
 /* Object properties: the reference's public members dim, minBound,
  * maxBound, creationOptionFlags (nabo/nabo.h:274-282) plus build facts.
  * info[0]=dim info[1]=n info[2]=dtype info[3]=searchType

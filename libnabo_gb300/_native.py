@@ -25,6 +25,7 @@ SIGNATURES = {
     "nabo_cuda_destroy": (_I, [_P]),
     "nabo_cuda_knn": (_I, [_P, _P, _I, _I64, _I64, _I, _D, _U, _D, _P, _P, _P, _P]),
     "nabo_cuda_knn_device": (_I, [_P, _P, _I, _I64, _I64, _I, _D, _U, _D, _P, _P, _P, _P, _P]),
+    "nabo_cuda_knn_device_noalloc": (_I, [_P, _P, _I, _I64, _I64, _I, _D, _U, _D, _P, _P, _P, _P, _P]),
     "nabo_cuda_get_info": (_I, [_P, _P]),
     "nabo_cuda_get_bounds": (_I, [_P, _P, _P]),
     "nabo_cuda_export_tree": (_I, [_P, _P, _P, _P, _P, _P, _P]),

@@ -338,6 +338,23 @@ int check_knn(const nabo_cuda_search* h, int qRows, int64_t nq, int64_t qStride,
 
 }  // namespace
 
+namespace nabo_gb300 {
+HandleView handle_view(const nabo_cuda_search* s) {
+  HandleView v;
+  v.cloud = &s->c;
+  v.searchType = s->searchType;
+  v.creationFlags = s->creationFlags;
+  v.device = s->device;
+  v.traversal = s->traversal;
+  return v;
+}
+
+int handle_check_knn(const nabo_cuda_search* s, int qRows, int64_t nq, int64_t qStride, int k, unsigned optionFlags,
+                     const void* maxRadii) {
+  return check_knn(s, qRows, nq, qStride, k, optionFlags, maxRadii);
+}
+}  // namespace nabo_gb300
+
 extern "C" {
 
 void nabo_cuda_params_init(nabo_cuda_params* p) {

@@ -8,6 +8,8 @@
 
 #include "common.cuh"
 
+struct nabo_cuda_search;
+
 namespace nabo_gb300 {
 
 // Status codes (mirrored in include/nabo_gb300.h).
@@ -97,6 +99,22 @@ template <typename T, int D>
 int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream);
 template <typename T, int D>
 int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream);
+
+template <typename T, int D>
+int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream);
+
+// Read access to a search object for the allocation-free entry point, and
+// the search-argument checks every entry point applies.
+struct HandleView {
+  const DeviceCloud* cloud;
+  int searchType;
+  unsigned creationFlags;
+  int device;
+  int traversal;
+};
+HandleView handle_view(const struct ::nabo_cuda_search* s);
+int handle_check_knn(const struct ::nabo_cuda_search* s, int qRows, int64_t nq, int64_t qStride, int k,
+                     unsigned optionFlags, const void* maxRadii);
 
 // Query ordering: writes a permutation of [0, nq) grouping nearby queries.
 template <typename T>

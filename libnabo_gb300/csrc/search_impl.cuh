@@ -135,8 +135,45 @@ int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) 
   return kOk;
 }
 
+// kd-tree search with a query order computed by the caller (`order` may be
+// null); launches the search kernel only and allocates nothing.
+template <typename T, int D>
+int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream) {
+  if (a.nq == 0) return kOk;
+  const int K = round_k(a.k);
+  if (K < 0) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+  if (c.height > kStackLarge)
+    return set_error(kErrUnsupported, "kd-tree height exceeds the traversal stack of the CUDA search");
+  const KnnLaunch L = make_launch<T, D>(c, a, order);
+  const int grid = ceil_div(a.nq, 128);
+  const bool small = c.height <= kStackSmall;
+  const bool packet = a.traversal == 2;
+  if (packet && (a.eps != 0.0 || L.stats))
+    return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
+#define NABO_LAUNCH(KK)                                                            \
+  case KK:                                                                         \
+    if (packet) {                                                                  \
+      if (small)                                                                   \
+        k_knn_kdtree_packet<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);   \
+      else                                                                         \
+        k_knn_kdtree_packet<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);   \
+    } else {                                                                       \
+      if (small)                                                                   \
+        k_knn_kdtree<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);          \
+      else                                                                         \
+        k_knn_kdtree<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);          \
+    }                                                                              \
+    break;
+  switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+#undef NABO_LAUNCH
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree launch");
+  return kOk;
+}
+
 #define NABO_SEARCH_INSTANTIATE(T, D)                                              \
   template int knn_kdtree<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
-  template int knn_bruteforce<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t);
+  template int knn_bruteforce<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
+  template int knn_kdtree_given_order<T, D>(const DeviceCloud&, const KnnArgs&, const int32_t*, cudaStream_t);
 
 }  // namespace nabo_gb300
