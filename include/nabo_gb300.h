@@ -154,6 +154,80 @@ int nabo_cuda_knn_device_noalloc(const nabo_cuda_search* s, const void* query, i
                                  const void* maxRadii, int32_t* indices, void* dists2, uint64_t* touched,
                                  void* stream);
 
+/* ---------------------------------------------------------------------
+ * Learned search radius (no counterpart in the reference; it feeds the
+ * reference's per-query radius overload, nabo/nabo.h:351).
+ *
+ * A radius model is a small network (inputs padded to 16: the normalised
+ * coordinates, plus 8 coarse-voxel occupancies of the cloud around the
+ * query for 3-D clouds; two hidden layers of 64 SiLU units; BF16 weights,
+ * FP32 sums) trained on the GPU to predict log(d_k), the log distance of a
+ * query's k-th neighbour, from training queries whose d_k the exact kd-tree
+ * search computes. A learned search runs the kd-tree search with the
+ * per-query radius safety * exp(prediction) (capped at maxRadius) and
+ * searches again without it every query that found fewer than k
+ * neighbours inside its radius, so results equal nabo_cuda_knn's. */
+typedef struct nabo_cuda_radius_model nabo_cuda_radius_model; /* opaque */
+#define NABO_CUDA_RADIUS_MODEL_INPUTS 16
+#define NABO_CUDA_RADIUS_MODEL_PARAMS 5313 /* W1[64][16] b1[64] W2[64][64] b2[64] w3[64] b3 */
+
+typedef struct nabo_cuda_train_params {
+  uint32_t struct_size;
+  int32_t epochs;  /* passes over the training queries, default 30 */
+  int32_t batch;   /* minibatch, default 4096 */
+  float lr;        /* Adam learning rate (cosine-decayed), default 3e-3 */
+  float safety;    /* radius = safety * exp(prediction), default 1.2 */
+  uint32_t reserved0;
+  uint64_t seed;   /* weight initialisation and shuffling, default 1234 */
+  int32_t reserved[4];
+} nabo_cuda_train_params;
+
+void nabo_cuda_train_params_init(nabo_cuda_train_params* p);
+
+/* Trains a model for k-NN searches of `s` (a KDTREE_CUDA object) from
+ * `n` training queries in DEVICE memory (qRows x n, column stride qStride).
+ * Training queries without k neighbours within maxRadius are left out. */
+int nabo_cuda_radius_model_train(const nabo_cuda_search* s, const void* trainQueries, int qRows, int64_t n,
+                                 int64_t qStride, int k, unsigned optionFlags, double maxRadius,
+                                 const nabo_cuda_train_params* params, nabo_cuda_radius_model** out);
+int nabo_cuda_radius_model_destroy(nabo_cuda_radius_model* m);
+
+/* Per-query radii (DEVICE; the search object's scalar type), capped at
+ * maxRadius; `raw` (DEVICE float, may be NULL) receives the standardised
+ * network outputs. Stream-ordered. */
+int nabo_cuda_radius_model_predict_device(const nabo_cuda_radius_model* m, const void* query, int qRows, int64_t nq,
+                                          int64_t qStride, double maxRadius, void* radii, float* raw, void* stream);
+
+/* Learned search with DEVICE buffers (stream-ordered, no host sync).
+ * Same arguments and results as nabo_cuda_knn_device; `fallbacks` (DEVICE
+ * int32, may be NULL) receives the number of queries searched again. With
+ * TOUCH_STATISTICS, `touched` accumulates the points examined by both
+ * searches (not the reference's count for an unbounded search). */
+int nabo_cuda_knn_learned_device(const nabo_cuda_search* s, const nabo_cuda_radius_model* m, const void* query,
+                                 int qRows, int64_t nq, int64_t qStride, int k, double epsilon, unsigned optionFlags,
+                                 double maxRadius, int32_t* indices, void* dists2, uint64_t* touched,
+                                 int32_t* fallbacks, void* stream);
+/* Same with HOST buffers; `fallbacks` is a host int64. */
+int nabo_cuda_knn_learned(const nabo_cuda_search* s, const nabo_cuda_radius_model* m, const void* query, int qRows,
+                          int64_t nq, int64_t qStride, int k, double epsilon, unsigned optionFlags, double maxRadius,
+                          int32_t* indices, void* dists2, uint64_t* touched, int64_t* fallbacks);
+
+/* Network inputs of queries (DEVICE float, nq x 16), for checks. */
+int nabo_cuda_radius_model_features_device(const nabo_cuda_radius_model* m, const void* query, int qRows, int64_t nq,
+                                           int64_t qStride, float* features, void* stream);
+/* Gradient (HOST, NABO_CUDA_RADIUS_MODEL_PARAMS floats) of the mean squared
+ * error of the network over n samples: features (DEVICE float, n x 16) and
+ * standardised targets (DEVICE float, n); `loss` (HOST) receives the summed
+ * squared error. For gradient checks against an independent computation. */
+int nabo_cuda_radius_model_gradients(const nabo_cuda_radius_model* m, const float* features, const float* targets,
+                                     int64_t n, float* grad, float* loss);
+/* Save / load: params (HOST, NABO_CUDA_RADIUS_MODEL_PARAMS FP32 master
+ * weights) and meta (HOST, 8 floats: mu, sigma, safety, k, final training
+ * loss, training samples, inputs used, parameter count); either may be
+ * NULL. set() takes mu, sigma and safety from meta. */
+int nabo_cuda_radius_model_get(const nabo_cuda_radius_model* m, float* params, float* meta);
+int nabo_cuda_radius_model_set(nabo_cuda_radius_model* m, const float* params, const float* meta);
+
 /* Object properties: the reference's public members dim, minBound,
  * maxBound, creationOptionFlags (nabo/nabo.h:274-282) plus build facts.
  * info[0]=dim info[1]=n info[2]=dtype info[3]=searchType

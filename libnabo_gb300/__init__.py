@@ -21,12 +21,16 @@ import enum
 import numpy as np
 
 from ._native import lib as _lib
-from ._native import nabo_cuda_params
+from ._native import nabo_cuda_params, nabo_cuda_train_params
 
 __all__ = [
     "SearchType", "SearchOptionFlags", "CreationOptionFlags", "NaboError", "NearestNeighbourSearch",
-    "InvalidIndex", "ALLOW_SELF_MATCH", "SORT_RESULTS", "TOUCH_STATISTICS", "version",
+    "InvalidIndex", "ALLOW_SELF_MATCH", "SORT_RESULTS", "TOUCH_STATISTICS", "version", "RadiusModel",
+    "RADIUS_MODEL_PARAMS", "RADIUS_MODEL_INPUTS",
 ]
+
+RADIUS_MODEL_PARAMS = 5313
+RADIUS_MODEL_INPUTS = 16
 
 InvalidIndex = -1
 # default `dim`: numeric_limits<Index>::max(), clamped to the cloud rows (nabo/nabo.h:360)
@@ -300,3 +304,169 @@ class NearestNeighbourSearch:
     @classmethod
     def createBruteForceCUDA(cls, cloud, dim=None, creationOptionFlags=0):
         return cls(cloud, SearchType.BRUTE_FORCE_CUDA, dim, creationOptionFlags, None)
+
+
+def _torch_device_array(x, dtype):
+    """A CUDA tensor of `x` (numpy or torch) with the given torch dtype."""
+    import torch
+    if _is_torch(x):
+        return x.to(device="cuda" if not x.is_cuda else x.device, dtype=dtype).contiguous()
+    return torch.from_numpy(np.ascontiguousarray(x)).to(device="cuda", dtype=dtype)
+
+
+class RadiusModel:
+    """Learned per-query search radius for a KDTREE_CUDA search object.
+
+    A small BF16 network, trained on the GPU by the library's own kernels,
+    predicts log(d_k) for a query (from its coordinates and, in 3-D, the
+    occupancy of the coarse voxels around it). ``knn`` searches with the
+    per-query radius ``safety * exp(prediction)`` and searches again,
+    without the bound, every query that found fewer than k neighbours inside
+    it, so the results equal ``NearestNeighbourSearch.knn``. ``fallbacks``
+    holds how many queries the last search had to repeat.
+    """
+
+    def __init__(self, search: NearestNeighbourSearch, train_queries, k: int, optionFlags: int = 0,
+                 maxRadius: float = np.inf, epochs: int = 30, batch: int = 4096, lr: float = 3e-3,
+                 safety: float = 1.2, seed: int = 1234):
+        import torch
+        self.search = search
+        self.k = int(k)
+        self._m = ctypes.c_void_p()
+        tdt = torch.float32 if search.dtype == np.float32 else torch.float64
+        tq = _torch_device_array(train_queries, tdt)
+        n, rows = tq.shape
+        p = nabo_cuda_train_params()
+        _lib.nabo_cuda_train_params_init(ctypes.byref(p))
+        p.epochs, p.batch, p.lr, p.safety, p.seed = int(epochs), int(batch), float(lr), float(safety), int(seed)
+        torch.cuda.synchronize()
+        _check(_lib.nabo_cuda_radius_model_train(search._h, ctypes.c_void_p(tq.data_ptr()), rows, n, rows, self.k,
+                                                 int(optionFlags), float(maxRadius), ctypes.byref(p),
+                                                 ctypes.byref(self._m)))
+        self.fallbacks = 0
+        self.touched = 0
+
+    def close(self) -> None:
+        m = getattr(self, "_m", None)
+        if m is not None and m.value:
+            _lib.nabo_cuda_radius_model_destroy(m)
+            self._m = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def meta(self) -> dict:
+        meta = (ctypes.c_float * 8)()
+        _check(_lib.nabo_cuda_radius_model_get(self._m, None, meta))
+        return dict(mu=meta[0], sigma=meta[1], safety=meta[2], k=int(meta[3]), train_loss=meta[4],
+                    train_samples=int(meta[5]), inputs=int(meta[6]))
+
+    def get_params(self):
+        params = np.zeros(RADIUS_MODEL_PARAMS, np.float32)
+        meta = np.zeros(8, np.float32)
+        _check(_lib.nabo_cuda_radius_model_get(self._m, _ptr(params), _ptr(meta)))
+        return params, meta
+
+    def set_params(self, params, meta=None):
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        if params.shape != (RADIUS_MODEL_PARAMS,):
+            raise NaboError(1, f"expected {RADIUS_MODEL_PARAMS} parameters")
+        m = None if meta is None else np.ascontiguousarray(meta, dtype=np.float32)
+        _check(_lib.nabo_cuda_radius_model_set(self._m, _ptr(params), _ptr(m)))
+
+    def save(self, path: str) -> None:
+        params, meta = self.get_params()
+        np.savez(path, params=params, meta=meta)
+
+    def load(self, path: str) -> None:
+        with np.load(path) as z:
+            self.set_params(z["params"], z["meta"])
+
+    def _tq(self, query):
+        import torch
+        tdt = torch.float32 if self.search.dtype == np.float32 else torch.float64
+        return _torch_device_array(query, tdt)
+
+    def features(self, query):
+        """Network inputs (nq, 16) float32 CUDA tensor."""
+        import torch
+        tq = self._tq(query)
+        nq, rows = tq.shape
+        X = torch.empty((nq, RADIUS_MODEL_INPUTS), dtype=torch.float32, device=tq.device)
+        st = torch.cuda.current_stream(tq.device).cuda_stream
+        _check(_lib.nabo_cuda_radius_model_features_device(self._m, ctypes.c_void_p(tq.data_ptr()), rows, nq, rows,
+                                                           ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(st)))
+        return X
+
+    def predict(self, query, maxRadius: float = np.inf, raw: bool = False):
+        """Per-query radii (CUDA tensor); with raw=True also the standardised outputs."""
+        import torch
+        tq = self._tq(query)
+        nq, rows = tq.shape
+        radii = torch.empty(nq, dtype=tq.dtype, device=tq.device)
+        out = torch.empty(nq, dtype=torch.float32, device=tq.device) if raw else None
+        st = torch.cuda.current_stream(tq.device).cuda_stream
+        _check(_lib.nabo_cuda_radius_model_predict_device(
+            self._m, ctypes.c_void_p(tq.data_ptr()), rows, nq, rows, float(maxRadius),
+            ctypes.c_void_p(radii.data_ptr()), None if out is None else ctypes.c_void_p(out.data_ptr()),
+            ctypes.c_void_p(st)))
+        return (radii, out) if raw else radii
+
+    def gradients(self, features, targets):
+        """(grad[RADIUS_MODEL_PARAMS], summed squared error) of the MSE over the samples."""
+        import torch
+        X = _torch_device_array(features, torch.float32)
+        Y = _torch_device_array(targets, torch.float32)
+        grad = np.zeros(RADIUS_MODEL_PARAMS, np.float32)
+        loss = ctypes.c_float(0.0)
+        torch.cuda.synchronize()
+        _check(_lib.nabo_cuda_radius_model_gradients(self._m, ctypes.c_void_p(X.data_ptr()),
+                                                     ctypes.c_void_p(Y.data_ptr()), X.shape[0], _ptr(grad),
+                                                     ctypes.byref(loss)))
+        return grad, float(loss.value)
+
+    def knn(self, query, k: int | None = None, epsilon: float = 0.0, optionFlags: int = 0,
+            maxRadius: float = np.inf, out=None):
+        """Learned search with host arrays; returns (indices, dists2)."""
+        k = self.k if k is None else int(k)
+        if _is_torch(query):
+            return self.knn_device(query, k, epsilon, optionFlags, maxRadius)
+        query = np.ascontiguousarray(np.asarray(query, dtype=self.search.dtype))
+        nq, qrows = query.shape
+        if out is None:
+            idx = np.empty((nq, k), np.int32)
+            d2 = np.empty((nq, k), self.search.dtype)
+        else:
+            idx, d2 = out
+        touched = ctypes.c_uint64(0)
+        fb = ctypes.c_int64(0)
+        _check(_lib.nabo_cuda_knn_learned(self.search._h, self._m, _ptr(query), qrows, nq, qrows, k, float(epsilon),
+                                          int(optionFlags), float(maxRadius), _ptr(idx), _ptr(d2),
+                                          ctypes.byref(touched), ctypes.byref(fb)))
+        self.touched = int(touched.value)
+        self.fallbacks = int(fb.value)
+        return idx, d2
+
+    def knn_device(self, query, k: int | None = None, epsilon: float = 0.0, optionFlags: int = 0,
+                   maxRadius: float = np.inf, out=None, touched=None, fallbacks=None, stream=None):
+        """Learned search with CUDA tensors, stream-ordered; returns (indices, dists2)."""
+        import torch
+        k = self.k if k is None else int(k)
+        query = query.contiguous()
+        nq, qrows = query.shape
+        if out is None:
+            idx = torch.empty((nq, k), dtype=torch.int32, device=query.device)
+            d2 = torch.empty((nq, k), dtype=query.dtype, device=query.device)
+        else:
+            idx, d2 = out
+        st = stream if stream is not None else torch.cuda.current_stream(query.device).cuda_stream
+        _check(_lib.nabo_cuda_knn_learned_device(
+            self.search._h, self._m, ctypes.c_void_p(query.data_ptr()), qrows, nq, qrows, k, float(epsilon),
+            int(optionFlags), float(maxRadius), ctypes.c_void_p(idx.data_ptr()), ctypes.c_void_p(d2.data_ptr()),
+            None if touched is None else ctypes.c_void_p(touched.data_ptr()),
+            None if fallbacks is None else ctypes.c_void_p(fallbacks.data_ptr()), ctypes.c_void_p(st)))
+        return idx, d2

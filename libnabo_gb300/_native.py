@@ -26,6 +26,16 @@ SIGNATURES = {
     "nabo_cuda_knn": (_I, [_P, _P, _I, _I64, _I64, _I, _D, _U, _D, _P, _P, _P, _P]),
     "nabo_cuda_knn_device": (_I, [_P, _P, _I, _I64, _I64, _I, _D, _U, _D, _P, _P, _P, _P, _P]),
     "nabo_cuda_knn_device_noalloc": (_I, [_P, _P, _I, _I64, _I64, _I, _D, _U, _D, _P, _P, _P, _P, _P]),
+    "nabo_cuda_train_params_init": (None, [_P]),
+    "nabo_cuda_radius_model_train": (_I, [_P, _P, _I, _I64, _I64, _I, _U, _D, _P, _P]),
+    "nabo_cuda_radius_model_destroy": (_I, [_P]),
+    "nabo_cuda_radius_model_predict_device": (_I, [_P, _P, _I, _I64, _I64, _D, _P, _P, _P]),
+    "nabo_cuda_knn_learned_device": (_I, [_P, _P, _P, _I, _I64, _I64, _I, _D, _U, _D, _P, _P, _P, _P, _P]),
+    "nabo_cuda_knn_learned": (_I, [_P, _P, _P, _I, _I64, _I64, _I, _D, _U, _D, _P, _P, _P, _P]),
+    "nabo_cuda_radius_model_features_device": (_I, [_P, _P, _I, _I64, _I64, _P, _P]),
+    "nabo_cuda_radius_model_gradients": (_I, [_P, _P, _P, _I64, _P, _P]),
+    "nabo_cuda_radius_model_get": (_I, [_P, _P, _P]),
+    "nabo_cuda_radius_model_set": (_I, [_P, _P, _P]),
     "nabo_cuda_get_info": (_I, [_P, _P]),
     "nabo_cuda_get_bounds": (_I, [_P, _P, _P]),
     "nabo_cuda_export_tree": (_I, [_P, _P, _P, _P, _P, _P, _P]),
@@ -34,6 +44,19 @@ SIGNATURES = {
     "nabo_cuda_last_error": (ctypes.c_char_p, []),
     "nabo_cuda_version": (ctypes.c_char_p, []),
 }
+
+
+class nabo_cuda_train_params(ctypes.Structure):
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("epochs", ctypes.c_int32),
+        ("batch", ctypes.c_int32),
+        ("lr", ctypes.c_float),
+        ("safety", ctypes.c_float),
+        ("reserved0", ctypes.c_uint32),
+        ("seed", ctypes.c_uint64),
+        ("reserved", ctypes.c_int32 * 4),
+    ]
 
 
 class nabo_cuda_params(ctypes.Structure):

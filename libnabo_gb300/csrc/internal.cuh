@@ -7,6 +7,7 @@
 #include <string>
 
 #include "common.cuh"
+#include "nabo_gb300.h"
 
 struct nabo_cuda_search;
 
@@ -91,6 +92,7 @@ struct KnnArgs {
   bool sortQueries = true;       // reorder queries along a space-filling curve
   int32_t* found = nullptr;      // optional device output: neighbours found per query
   int traversal = 0;             // 0 auto, 1 reference order, 2 warp packet (exact search only)
+  const int32_t* nqDevice = nullptr;  // optional device count: only the first *nqDevice of nq run
   cudaEvent_t evStart = nullptr; // optional: recorded right before / after the search kernel
   cudaEvent_t evStop = nullptr;
 };
@@ -115,6 +117,25 @@ struct HandleView {
 HandleView handle_view(const struct ::nabo_cuda_search* s);
 int handle_check_knn(const struct ::nabo_cuda_search* s, int qRows, int64_t nq, int64_t qStride, int k,
                      unsigned optionFlags, const void* maxRadii);
+
+// Learned search radius (learned.cu).
+struct RadiusModel;
+int radius_model_train(const struct ::nabo_cuda_search* s, const void* dTrain, int64_t nTrain, int64_t qStride, int k,
+                       unsigned optionFlags, double maxRadius, const nabo_cuda_train_params& tp, RadiusModel** out,
+                       cudaStream_t st);
+void radius_model_free(RadiusModel* m);
+int radius_model_predict(const RadiusModel& m, const void* query, int64_t nq, int64_t qStride, double maxRadius,
+                         void* radii, float* raw, cudaStream_t st);
+int knn_learned(const struct ::nabo_cuda_search* s, const RadiusModel& m, const KnnArgs& base, int32_t* dFallbacks,
+                cudaStream_t st);
+int radius_model_gradients(const RadiusModel& m, const float* dX, const float* dY, int64_t n, float* hGrad,
+                           float* hLoss, cudaStream_t st);
+int radius_model_features(const RadiusModel& m, const void* query, int64_t nq, int64_t qStride, float* dX,
+                          cudaStream_t st);
+int radius_model_get(const RadiusModel& m, float* params, float* meta);
+int radius_model_set(RadiusModel& m, const float* params, const float* meta);
+const void* radius_model_owner(const RadiusModel& m);
+int radius_model_k(const RadiusModel& m);
 
 // Query ordering: writes a permutation of [0, nq) grouping nearby queries.
 template <typename T>

@@ -1,0 +1,1143 @@
+// learned.cu -- learned per-query search radius for exact kNN.
+//
+// A small MLP predicts, for each query, the log of its k-th neighbour
+// distance; the search then runs with a per-query radius of
+// safety * exp(prediction) (the reference's per-query maxRadii overload,
+// nabo/nabo.h:351, nabo/kdtree_cpu.cpp:306-336). A query that finds fewer
+// than k points inside its radius is searched again without the learned
+// bound, so every result equals the plain search's.
+//
+// Network: inputs padded to kF = 16, two hidden layers of kH = 64 SiLU
+// units, one output. Weights are BF16, sums are FP32.
+//   3-D clouds: inputs = 3 normalised coordinates + 8 coarse-voxel
+//               occupancies (log counts of the 2x2x2 voxels around the
+//               query in a grid of about 128 voxels along the longest side)
+//   other dims: inputs = the normalised coordinates.
+// Training: targets are log(d_k) of training queries, computed by the exact
+// GPU kd-tree search; MSE on the standardised target; Adam. The training
+// kernel runs on the FP32 cores and rounds weights, inputs and the first
+// hidden layer to BF16 exactly where the inference kernel does, so training
+// fits the network that inference evaluates. Inference uses the tensor
+// cores (mma.sync m16n8k16, BF16 in, FP32 accumulate), 16 queries per warp.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "internal.cuh"
+#include "nabo_gb300.h"
+
+namespace nabo_gb300 {
+namespace {
+
+constexpr int kF = 16;
+constexpr int kH = 64;
+constexpr int kOffW1 = 0;                  // W1[kH][kF]
+constexpr int kOffB1 = kOffW1 + kH * kF;   // b1[kH]
+constexpr int kOffW2 = kOffB1 + kH;        // W2[kH][kH]
+constexpr int kOffB2 = kOffW2 + kH * kH;   // b2[kH]
+constexpr int kOffW3 = kOffB2 + kH;        // w3[kH]
+constexpr int kOffB3 = kOffW3 + kH;        // b3
+constexpr int kParams = kOffB3 + 1;        // 5313
+constexpr int kGridMax = 128;
+
+struct FeatureSpace {
+  int dim;
+  int nIn;
+  float center[kMaxDim];
+  float invHalf[kMaxDim];
+  int useGrid;
+  float lo[3];
+  float invH;
+  int nx, ny, nz;
+  float invLogMax;
+  const uint32_t* grid;
+};
+
+__device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
+__device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
+
+template <typename T>
+__device__ __forceinline__ void features(const T* __restrict__ q, const FeatureSpace& fs, float (&out)[kF]) {
+#pragma unroll
+  for (int f = 0; f < kF; ++f) out[f] = 0.0f;
+  for (int d = 0; d < fs.dim && d < kF; ++d) out[d] = fminf(fmaxf(((float)q[d] - fs.center[d]) * fs.invHalf[d], -4.f), 4.f);
+  if (fs.useGrid) {
+    int i0[3];
+    const int nn[3] = {fs.nx, fs.ny, fs.nz};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) i0[d] = (int)floorf(((float)q[d] - fs.lo[d]) * fs.invH - 0.5f);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      int v[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) v[d] = min(max(i0[d] + ((c >> d) & 1), 0), nn[d] - 1);
+      const uint32_t cnt = fs.grid[((int64_t)v[0] * fs.ny + v[1]) * fs.nz + v[2]];
+      out[3 + c] = log1pf((float)cnt) * fs.invLogMax;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// voxel grid
+
+template <typename T, int D>
+__global__ void k_grid_count(const Rec<T, D>* __restrict__ recs, int64_t n, FeatureSpace fs, uint32_t* grid) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Rec<T, D> r = recs[i];
+  int v[3];
+  const int nn[3] = {fs.nx, fs.ny, fs.nz};
+#pragma unroll
+  for (int d = 0; d < 3; ++d) v[d] = min(max((int)floorf(((float)r.p.c[d] - fs.lo[d]) * fs.invH), 0), nn[d] - 1);
+  atomicAdd(grid + ((int64_t)v[0] * fs.ny + v[1]) * fs.nz + v[2], 1u);
+}
+
+__global__ void k_grid_max(const uint32_t* grid, int64_t cells, uint32_t* mx) {
+  uint32_t m = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cells; i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, grid[i]);
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+}
+
+// ---------------------------------------------------------------------------
+// training data
+
+template <typename T>
+__global__ void k_features(const T* __restrict__ query, int64_t nq, int64_t qStride, FeatureSpace fs, float* X) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  float f[kF];
+  features(query + i * qStride, fs, f);
+#pragma unroll
+  for (int j = 0; j < kF; ++j) X[i * kF + j] = f[j];
+}
+
+// y = log(d_k) from the k-th squared distance; queries without k
+// neighbours (d2 = inf) get a NaN target and are left out of training.
+template <typename T>
+__global__ void k_targets(const T* __restrict__ d2, int64_t nq, int k, double minD2, float* y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  const double v = (double)d2[i * k + (k - 1)];
+  y[i] = isinf(v) ? __int_as_float(0x7fc00000) : (float)(0.5 * log(v > minD2 ? v : minD2));
+}
+
+// ---------------------------------------------------------------------------
+// training step: gradient of the mean squared error over `count` samples
+// (indices idx[0..count)), accumulated into grad[kParams]. One block of 256
+// threads handles kSamplesPerBlock samples in tiles of 32.
+
+constexpr int kTile = 32;
+constexpr int kTrainThreads = 256;
+constexpr int kSamplesPerBlock = 256;
+
+struct TrainSmem {
+  float W1[kH * kF];   // [j][f]
+  float W2T[kH * kH];  // [i][j] = W2[j][i]
+  float b1[kH], b2[kH], w3[kH];
+  float b3;
+  float x[kTile][kF];
+  float z1[kTile][kH];
+  float a1[kTile][kH];
+  float z2[kTile][kH];
+  float a2[kTile][kH];
+  float dz2[kTile][kH];
+  float y[kTile], yhat[kTile], dy[kTile];
+  float gW1[kH * kF];
+  float gb1[kH], gb2[kH], gw3[kH];
+  float gb3;
+  float loss;
+};
+
+__global__ void __launch_bounds__(kTrainThreads) k_mlp_grad(const float* __restrict__ X, const float* __restrict__ Y,
+                                                            const int32_t* __restrict__ idx, int count,
+                                                            const __nv_bfloat16* __restrict__ Wb, float* grad,
+                                                            float* lossOut, float invBatch) {
+  extern __shared__ float smemRaw[];
+  TrainSmem& S = *reinterpret_cast<TrainSmem*>(smemRaw);
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kH * kF; i += kTrainThreads) {
+    S.W1[i] = __bfloat162float(Wb[kOffW1 + i]);
+    S.gW1[i] = 0.0f;
+  }
+  for (int i = tid; i < kH * kH; i += kTrainThreads) {
+    const int j = i / kH, c = i % kH;
+    S.W2T[c * kH + j] = __bfloat162float(Wb[kOffW2 + i]);
+  }
+  for (int i = tid; i < kH; i += kTrainThreads) {
+    S.b1[i] = __bfloat162float(Wb[kOffB1 + i]);
+    S.b2[i] = __bfloat162float(Wb[kOffB2 + i]);
+    S.w3[i] = __bfloat162float(Wb[kOffW3 + i]);
+    S.gb1[i] = S.gb2[i] = S.gw3[i] = 0.0f;
+  }
+  if (tid == 0) {
+    S.b3 = __bfloat162float(Wb[kOffB3]);
+    S.gb3 = 0.0f;
+    S.loss = 0.0f;
+  }
+  // W2 gradient: thread owns entries o = tid + 256 r, r < 16 (row j = o / 64, col i = o % 64)
+  float gW2[(kH * kH) / kTrainThreads];
+#pragma unroll
+  for (int r = 0; r < (kH * kH) / kTrainThreads; ++r) gW2[r] = 0.0f;
+  __syncthreads();
+
+  const int first = blockIdx.x * kSamplesPerBlock;
+  for (int t0 = first; t0 < min(first + kSamplesPerBlock, count); t0 += kTile) {
+    const int m = min(kTile, count - t0);
+    // inputs
+    for (int i = tid; i < kTile * kF; i += kTrainThreads) {
+      const int s = i / kF, f = i % kF;
+      S.x[s][f] = s < m ? bf16r(X[(int64_t)idx[t0 + s] * kF + f]) : 0.0f;
+    }
+    if (tid < kTile) S.y[tid] = tid < m ? Y[idx[t0 + tid]] : 0.0f;
+    __syncthreads();
+    // layer 1
+    for (int o = tid; o < kTile * kH; o += kTrainThreads) {
+      const int s = o / kH, j = o % kH;
+      float z = S.b1[j];
+#pragma unroll
+      for (int f = 0; f < kF; ++f) z += S.W1[j * kF + f] * S.x[s][f];
+      S.z1[s][j] = z;
+      S.a1[s][j] = bf16r(z * sigm(z));
+    }
+    __syncthreads();
+    // layer 2
+    for (int o = tid; o < kTile * kH; o += kTrainThreads) {
+      const int s = o / kH, j = o % kH;
+      float z = S.b2[j];
+#pragma unroll 8
+      for (int i = 0; i < kH; ++i) z += S.W2T[i * kH + j] * S.a1[s][i];
+      S.z2[s][j] = z;
+      S.a2[s][j] = z * sigm(z);
+    }
+    __syncthreads();
+    // output and loss: one warp per 4 samples
+    {
+      const int warp = tid >> 5, lane = tid & 31;
+      for (int s = warp; s < kTile; s += kTrainThreads / 32) {
+        float acc = S.w3[lane] * S.a2[s][lane] + S.w3[lane + 32] * S.a2[s][lane + 32];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+          const float yh = acc + S.b3;
+          const float e = s < m ? yh - S.y[s] : 0.0f;
+          S.yhat[s] = yh;
+          S.dy[s] = 2.0f * e * invBatch;
+          atomicAdd(&S.loss, e * e);
+        }
+      }
+    }
+    __syncthreads();
+    // output layer gradients and dz2
+    if (tid < kH) {
+      float g = 0.0f;
+      for (int s = 0; s < m; ++s) g += S.dy[s] * S.a2[s][tid];
+      S.gw3[tid] += g;
+    }
+    if (tid == kH) {
+      float g = 0.0f;
+      for (int s = 0; s < m; ++s) g += S.dy[s];
+      S.gb3 += g;
+    }
+    for (int o = tid; o < kTile * kH; o += kTrainThreads) {
+      const int s = o / kH, j = o % kH;
+      const float z = S.z2[s][j];
+      const float sg = sigm(z);
+      S.dz2[s][j] = s < m ? S.dy[s] * S.w3[j] * sg * (1.0f + z * (1.0f - sg)) : 0.0f;
+    }
+    __syncthreads();
+    // W2, b2 gradients
+#pragma unroll
+    for (int r = 0; r < (kH * kH) / kTrainThreads; ++r) {
+      const int o = tid + kTrainThreads * r;
+      const int j = o / kH, i = o % kH;
+      float g = 0.0f;
+      for (int s = 0; s < m; ++s) g += S.dz2[s][j] * S.a1[s][i];
+      gW2[r] += g;
+    }
+    if (tid < kH) {
+      float g = 0.0f;
+      for (int s = 0; s < m; ++s) g += S.dz2[s][tid];
+      S.gb2[tid] += g;
+    }
+    // back through layer 2 into dz1 (stored in z1; the rounding of a1 to
+    // BF16 is passed straight through)
+    for (int o = tid; o < kTile * kH; o += kTrainThreads) {
+      const int s = o / kH, i = o % kH;
+      float g = 0.0f;
+#pragma unroll 8
+      for (int j = 0; j < kH; ++j) g += S.W2T[i * kH + j] * S.dz2[s][j];
+      const float z = S.z1[s][i];
+      const float sg = sigm(z);
+      S.a2[s][i] = g * sg * (1.0f + z * (1.0f - sg));  // reuse a2 as dz1
+    }
+    __syncthreads();
+    // W1, b1 gradients
+    for (int o = tid; o < kH * kF; o += kTrainThreads) {
+      const int j = o / kF, f = o % kF;
+      float g = 0.0f;
+      for (int s = 0; s < m; ++s) g += S.a2[s][j] * S.x[s][f];
+      S.gW1[o] += g;
+    }
+    if (tid < kH) {
+      float g = 0.0f;
+      for (int s = 0; s < m; ++s) g += S.a2[s][tid];
+      S.gb1[tid] += g;
+    }
+    __syncthreads();
+  }
+  // flush
+#pragma unroll
+  for (int r = 0; r < (kH * kH) / kTrainThreads; ++r) atomicAdd(grad + kOffW2 + tid + kTrainThreads * r, gW2[r]);
+  for (int i = tid; i < kH * kF; i += kTrainThreads) atomicAdd(grad + kOffW1 + i, S.gW1[i]);
+  if (tid < kH) {
+    atomicAdd(grad + kOffB1 + tid, S.gb1[tid]);
+    atomicAdd(grad + kOffB2 + tid, S.gb2[tid]);
+    atomicAdd(grad + kOffW3 + tid, S.gw3[tid]);
+  }
+  if (tid == 0) {
+    atomicAdd(grad + kOffB3, S.gb3);
+    if (lossOut) atomicAdd(lossOut, S.loss);
+  }
+}
+
+__global__ void k_adam(float* p, float* m, float* v, float* g, __nv_bfloat16* pb, int n, float lr, float b1,
+                       float b2, float c1, float c2, float eps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.0f - b1) * gi;
+  const float vi = b2 * v[i] + (1.0f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float pi = p[i] - lr * (mi * c1) / (sqrtf(vi * c2) + eps);
+  p[i] = pi;
+  pb[i] = __float2bfloat16_rn(pi);
+  g[i] = 0.0f;
+}
+
+__global__ void k_to_bf16(const float* p, __nv_bfloat16* pb, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) pb[i] = __float2bfloat16_rn(p[i]);
+}
+
+// ---------------------------------------------------------------------------
+// inference: 16 queries per warp on the tensor cores
+
+__device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+struct RadiusOut {
+  float mu, sigma, safety;
+  double maxRadius;
+};
+
+constexpr int kInferWarps = 8;
+
+template <typename T>
+__global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __restrict__ query, int64_t nq,
+                                                                 int64_t qStride, FeatureSpace fs,
+                                                                 const __nv_bfloat16* __restrict__ Wb, RadiusOut ro,
+                                                                 T* radii, float* rawOut) {
+  __shared__ __align__(16) __nv_bfloat16 sW1[kH * kF];
+  __shared__ __align__(16) __nv_bfloat16 sW2[kH * kH];
+  __shared__ float sb1[kH], sb2[kH], sw3[kH];
+  __shared__ __align__(16) __nv_bfloat16 sX[kInferWarps][16 * kF];
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kH * kF; i += blockDim.x) sW1[i] = Wb[kOffW1 + i];
+  for (int i = tid; i < kH * kH; i += blockDim.x) sW2[i] = Wb[kOffW2 + i];
+  for (int i = tid; i < kH; i += blockDim.x) {
+    sb1[i] = __bfloat162float(Wb[kOffB1 + i]);
+    sb2[i] = __bfloat162float(Wb[kOffB2 + i]);
+    sw3[i] = __bfloat162float(Wb[kOffW3 + i]);
+  }
+  const float b3 = __bfloat162float(Wb[kOffB3]);
+  __syncthreads();
+  const int warp = tid >> 5, lane = tid & 31;
+  const int g = lane >> 2, tig = lane & 3;
+  const int64_t tiles = (nq + 15) / 16;
+  for (int64_t tile = (int64_t)blockIdx.x * kInferWarps + warp; tile < tiles; tile += (int64_t)gridDim.x * kInferWarps) {
+    const int64_t q0 = tile * 16;
+    // features of the tile's 16 queries (lanes 0..15)
+    if (lane < 16) {
+      float f[kF];
+      const int64_t qi = q0 + lane;
+      if (qi < nq) {
+        features(query + qi * qStride, fs, f);
+      } else {
+#pragma unroll
+        for (int j = 0; j < kF; ++j) f[j] = 0.0f;
+      }
+#pragma unroll
+      for (int j = 0; j < kF; ++j) sX[warp][lane * kF + j] = __float2bfloat16_rn(f[j]);
+    }
+    __syncwarp();
+    const uint32_t* X32 = reinterpret_cast<const uint32_t*>(sX[warp]);  // row = 8 words
+    uint32_t a[4];
+    a[0] = X32[g * 8 + tig];
+    a[1] = X32[(g + 8) * 8 + tig];
+    a[2] = X32[g * 8 + 4 + tig];
+    a[3] = X32[(g + 8) * 8 + 4 + tig];
+    // layer 1: 8 n-tiles of 8 hidden units
+    const uint32_t* W1w = reinterpret_cast<const uint32_t*>(sW1);  // row j = 8 words
+    float z1[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      z1[j][0] = z1[j][1] = z1[j][2] = z1[j][3] = 0.0f;
+      const int n = 8 * j + g;
+      mma16816(z1[j], a, W1w[n * 8 + tig], W1w[n * 8 + 4 + tig]);
+    }
+    // SiLU, BF16, repacked as the A operand of layer 2 (4 k-steps)
+    uint32_t a1[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int j = 2 * s + h;
+        const int c = 8 * j + 2 * tig;
+        float v[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float z = z1[j][e] + sb1[c + (e & 1)];
+          v[e] = z * sigm(z);
+        }
+        a1[s][2 * h + 0] = pack2(v[0], v[1]);
+        a1[s][2 * h + 1] = pack2(v[2], v[3]);
+      }
+    }
+    // fragment order for m16n8k16 A: {row g k0-7, row g+8 k0-7, row g k8-15, row g+8 k8-15}
+    uint32_t A2[4][4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      A2[s][0] = a1[s][0];
+      A2[s][1] = a1[s][1];
+      A2[s][2] = a1[s][2];
+      A2[s][3] = a1[s][3];
+    }
+    // layer 2
+    const uint32_t* W2w = reinterpret_cast<const uint32_t*>(sW2);  // row j = 32 words
+    float z2[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      z2[j][0] = z2[j][1] = z2[j][2] = z2[j][3] = 0.0f;
+      const int n = 8 * j + g;
+#pragma unroll
+      for (int s = 0; s < 4; ++s) mma16816(z2[j], A2[s], W2w[n * 32 + 8 * s + tig], W2w[n * 32 + 8 * s + 4 + tig]);
+    }
+    // output layer: rows g and g+8
+    float y0 = 0.0f, y1 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int c = 8 * j + 2 * tig;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float z = z2[j][e] + sb2[c + (e & 1)];
+        const float act = z * sigm(z) * sw3[c + (e & 1)];
+        if (e < 2)
+          y0 += act;
+        else
+          y1 += act;
+      }
+    }
+    y0 += __shfl_xor_sync(0xffffffffu, y0, 1);
+    y0 += __shfl_xor_sync(0xffffffffu, y0, 2);
+    y1 += __shfl_xor_sync(0xffffffffu, y1, 1);
+    y1 += __shfl_xor_sync(0xffffffffu, y1, 2);
+    if (tig == 0) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int64_t qi = q0 + g + 8 * h;
+        if (qi < nq) {
+          const float yn = (h == 0 ? y0 : y1) + b3;
+          if (rawOut) rawOut[qi] = yn;
+          const double r = (double)ro.safety * exp((double)ro.mu + (double)ro.sigma * (double)yn);
+          radii[qi] = (T)(r < ro.maxRadius ? r : ro.maxRadius);
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Queries whose bounded search found fewer than k neighbours although
+// their learned radius was below the caller's radius.
+template <typename T>
+__global__ void k_collect_misses(const int32_t* __restrict__ found, const T* __restrict__ radii, int64_t nq, int k,
+                                 double maxRadius, int32_t* list, int32_t* count) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  if (found[i] < k && (double)radii[i] < maxRadius) list[atomicAdd(count, 1)] = (int32_t)i;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+
+struct RadiusModel {
+  int dtype = 0;
+  int dim = 0;
+  int dpad = 0;
+  int k = 1;
+  const void* owner = nullptr;  // the search object the model was trained on
+  FeatureSpace fs{};
+  uint32_t* grid = nullptr;
+  float* params = nullptr;  // FP32 master
+  float* adamM = nullptr;
+  float* adamV = nullptr;
+  float* grad = nullptr;
+  __nv_bfloat16* pb = nullptr;
+  float mu = 0.0f, sigma = 1.0f, safety = 1.2f;
+  float trainLoss = 0.0f;
+  int64_t trainSamples = 0;
+};
+
+namespace {
+
+void free_model(RadiusModel* m) {
+  if (m->grid) cudaFree(m->grid);
+  if (m->params) cudaFree(m->params);
+  if (m->adamM) cudaFree(m->adamM);
+  if (m->adamV) cudaFree(m->adamV);
+  if (m->grad) cudaFree(m->grad);
+  if (m->pb) cudaFree(m->pb);
+}
+
+template <typename T, int D>
+int build_grid(const DeviceCloud& c, RadiusModel* m, cudaStream_t st) {
+  FeatureSpace& fs = m->fs;
+  fs.dim = c.dim;
+  for (int d = 0; d < kMaxDim; ++d) {
+    const double lo = d < c.dim ? c.lo[d] : 0.0, hi = d < c.dim ? c.hi[d] : 0.0;
+    fs.center[d] = (float)(0.5 * (lo + hi));
+    const double half = 0.5 * (hi - lo);
+    fs.invHalf[d] = half > 0.0 ? (float)(1.0 / half) : 0.0f;
+  }
+  fs.useGrid = (c.dim == 3) ? 1 : 0;
+  fs.nIn = fs.useGrid ? 11 : std::min(c.dim, kF);
+  fs.grid = nullptr;
+  if (!fs.useGrid) return kOk;
+  double ext = 0.0;
+  for (int d = 0; d < 3; ++d) ext = std::max(ext, c.hi[d] - c.lo[d]);
+  if (!(ext > 0.0)) ext = 1.0;
+  const double h = ext / kGridMax;
+  fs.invH = (float)(1.0 / h);
+  int nn[3];
+  for (int d = 0; d < 3; ++d) {
+    fs.lo[d] = (float)c.lo[d];
+    nn[d] = std::max(1, std::min(kGridMax, (int)std::ceil((c.hi[d] - c.lo[d]) / h + 1e-9)));
+  }
+  fs.nx = nn[0];
+  fs.ny = nn[1];
+  fs.nz = nn[2];
+  const int64_t cells = (int64_t)nn[0] * nn[1] * nn[2];
+  NABO_CUDA_TRY(cudaMalloc((void**)&m->grid, (size_t)cells * sizeof(uint32_t) + sizeof(uint32_t)));
+  NABO_CUDA_TRY(cudaMemsetAsync(m->grid, 0, (size_t)cells * sizeof(uint32_t) + sizeof(uint32_t), st));
+  if constexpr (D == 3) {
+    k_grid_count<T, D><<<ceil_div(c.n, 256), 256, 0, st>>>(static_cast<const Rec<T, D>*>(c.recs), c.n, fs, m->grid);
+  } else {
+    return set_error(kErrInternal, "voxel features need 3-D records");
+  }
+  k_grid_max<<<(int)std::min<int64_t>(ceil_div(cells, 256), 1024), 256, 0, st>>>(m->grid, cells, m->grid + cells);
+  uint32_t mx = 0;
+  NABO_CUDA_TRY(cudaMemcpyAsync(&mx, m->grid + cells, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  NABO_CUDA_TRY(cudaStreamSynchronize(st));
+  fs.invLogMax = (float)(1.0 / std::log1p((double)std::max(mx, 1u)));
+  fs.grid = m->grid;
+  return kOk;
+}
+
+int launch_radius(const RadiusModel& m, const void* query, int64_t nq, int64_t qStride, double maxRadius, void* radii,
+                  float* raw, cudaStream_t st) {
+  if (nq == 0) return kOk;
+  RadiusOut ro;
+  ro.mu = m.mu;
+  ro.sigma = m.sigma;
+  ro.safety = m.safety;
+  ro.maxRadius = maxRadius;
+  const int64_t tiles = (nq + 15) / 16;
+  const int grid = (int)std::min<int64_t>(ceil_div(tiles, kInferWarps), 152 * 16);
+  if (m.dtype == NABO_CUDA_FLOAT32)
+    k_mlp_radius<float><<<grid, kInferWarps * 32, 0, st>>>(static_cast<const float*>(query), nq, qStride, m.fs, m.pb,
+                                                             ro, static_cast<float*>(radii), raw);
+  else
+    k_mlp_radius<double><<<grid, kInferWarps * 32, 0, st>>>(static_cast<const double*>(query), nq, qStride, m.fs,
+                                                              m.pb, ro, static_cast<double*>(radii), raw);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "learned radius kernel");
+  return kOk;
+}
+
+int launch_features(const RadiusModel& m, const void* query, int64_t nq, int64_t qStride, float* X, cudaStream_t st) {
+  if (m.dtype == NABO_CUDA_FLOAT32)
+    k_features<float><<<ceil_div(nq, 256), 256, 0, st>>>(static_cast<const float*>(query), nq, qStride, m.fs, X);
+  else
+    k_features<double><<<ceil_div(nq, 256), 256, 0, st>>>(static_cast<const double*>(query), nq, qStride, m.fs, X);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "features kernel");
+  return kOk;
+}
+
+size_t train_smem() { return sizeof(TrainSmem); }
+
+int grad_step(const RadiusModel& m, const float* X, const float* Y, const int32_t* idx, int count, float* lossDev,
+              cudaStream_t st) {
+  NABO_CUDA_TRY(cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
+  const int blocks = ceil_div(count, kSamplesPerBlock);
+  k_mlp_grad<<<blocks, kTrainThreads, train_smem(), st>>>(X, Y, idx, count, m.pb, m.grad, lossDev,
+                                                          1.0f / (float)count);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "training kernel");
+  return kOk;
+}
+
+// Initial weights: uniform(+-1/sqrt(fan_in)) from a seeded generator.
+std::vector<float> init_params(uint64_t seed, int nIn) {
+  std::mt19937_64 rng(seed);
+  std::vector<float> p(kParams, 0.0f);
+  auto fill = [&](int off, int count, double bound) {
+    std::uniform_real_distribution<double> u(-bound, bound);
+    for (int i = 0; i < count; ++i) p[off + i] = (float)u(rng);
+  };
+  fill(kOffW1, kH * kF, 1.0 / std::sqrt((double)std::max(nIn, 1)));
+  for (int j = 0; j < kH; ++j)
+    for (int f = nIn; f < kF; ++f) p[kOffW1 + j * kF + f] = 0.0f;
+  fill(kOffW2, kH * kH, 1.0 / std::sqrt((double)kH));
+  fill(kOffW3, kH, 1.0 / std::sqrt((double)kH));
+  return p;
+}
+
+template <typename T>
+int dispatch_grid(const DeviceCloud& c, RadiusModel* m, cudaStream_t st) {
+  switch (c.dpad) {
+    case 2: return build_grid<T, 2>(c, m, st);
+    case 3: return build_grid<T, 3>(c, m, st);
+    case 4: return build_grid<T, 4>(c, m, st);
+    case 8: return build_grid<T, 8>(c, m, st);
+    case 16: return build_grid<T, 16>(c, m, st);
+  }
+  return set_error(kErrInternal, "bad dispatch");
+}
+
+int search_plain(const DeviceCloud& c, const KnnArgs& a, cudaStream_t st) {
+#define NABO_L_CASE(TT, DD) \
+  if (c.dpad == DD) return knn_kdtree<TT, DD>(c, a, st);
+  if (c.dtype == NABO_CUDA_FLOAT32) {
+    NABO_L_CASE(float, 2) NABO_L_CASE(float, 3) NABO_L_CASE(float, 4) NABO_L_CASE(float, 8) NABO_L_CASE(float, 16)
+  } else {
+    NABO_L_CASE(double, 2) NABO_L_CASE(double, 3) NABO_L_CASE(double, 4) NABO_L_CASE(double, 8)
+    NABO_L_CASE(double, 16)
+  }
+#undef NABO_L_CASE
+  return set_error(kErrInternal, "bad dispatch");
+}
+
+int search_given(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t st) {
+#define NABO_L_CASE(TT, DD) \
+  if (c.dpad == DD) return knn_kdtree_given_order<TT, DD>(c, a, order, st);
+  if (c.dtype == NABO_CUDA_FLOAT32) {
+    NABO_L_CASE(float, 2) NABO_L_CASE(float, 3) NABO_L_CASE(float, 4) NABO_L_CASE(float, 8) NABO_L_CASE(float, 16)
+  } else {
+    NABO_L_CASE(double, 2) NABO_L_CASE(double, 3) NABO_L_CASE(double, 4) NABO_L_CASE(double, 8)
+    NABO_L_CASE(double, 16)
+  }
+#undef NABO_L_CASE
+  return set_error(kErrInternal, "bad dispatch");
+}
+
+}  // namespace
+
+// Trains a radius model for k-NN searches of `s` on `nTrain` training
+// queries (device memory).
+int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nTrain, int64_t qStride, int k,
+                       unsigned optionFlags, double maxRadius, const nabo_cuda_train_params& tp, RadiusModel** out,
+                       cudaStream_t st) {
+  const HandleView h = handle_view(s);
+  const DeviceCloud& c = *h.cloud;
+  RadiusModel* m = new RadiusModel();
+  m->dtype = c.dtype;
+  m->dim = c.dim;
+  m->dpad = c.dpad;
+  m->k = k;
+  m->owner = s;
+  m->safety = tp.safety;
+  const size_t es = c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  int rc = c.dtype == NABO_CUDA_FLOAT32 ? dispatch_grid<float>(c, m, st) : dispatch_grid<double>(c, m, st);
+  auto fail = [&](int code) {
+    cudaStreamSynchronize(st);
+    free_model(m);
+    delete m;
+    return code;
+  };
+  if (rc != kOk) return fail(rc);
+  cudaError_t e = cudaMalloc((void**)&m->params, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->adamM, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->adamV, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->grad, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->pb, kParams * sizeof(__nv_bfloat16));
+  if (e != cudaSuccess) return fail(cuda_error(e, "model allocation"));
+  const std::vector<float> p0 = init_params(tp.seed, m->fs.nIn);
+  e = cudaMemcpyAsync(m->params, p0.data(), kParams * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->adamM, 0, kParams * sizeof(float), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->adamV, 0, kParams * sizeof(float), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->grad, 0, kParams * sizeof(float), st);
+  if (e != cudaSuccess) return fail(cuda_error(e, "model init"));
+  k_to_bf16<<<ceil_div(kParams, 256), 256, 0, st>>>(m->params, m->pb, kParams);
+
+  // exact k-th distances of the training queries
+  int32_t* idx = nullptr;
+  void* d2 = nullptr;
+  float *X = nullptr, *Y = nullptr, *loss = nullptr;
+  int32_t* order = nullptr;
+  e = scratch_alloc((void**)&idx, (size_t)nTrain * k * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = scratch_alloc(&d2, (size_t)nTrain * k * es, st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&X, (size_t)nTrain * kF * sizeof(float), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&Y, (size_t)nTrain * sizeof(float), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&loss, sizeof(float), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&order, (size_t)nTrain * sizeof(int32_t), st);
+  if (e != cudaSuccess) rc = cuda_error(e, "training buffers");
+  if (rc == kOk) {
+    KnnArgs a;
+    a.query = dTrain;
+    a.nq = nTrain;
+    a.qStride = qStride;
+    a.k = k;
+    a.optionFlags = optionFlags;
+    a.maxRadius = maxRadius;
+    a.indices = idx;
+    a.dists2 = d2;
+    a.traversal = h.traversal;
+    rc = search_plain(c, a, st);
+  }
+  if (rc == kOk) rc = launch_features(*m, dTrain, nTrain, qStride, X, st);
+  std::vector<float> hy;
+  if (rc == kOk) {
+    double minD2 = 1e-30;
+    if (m->dtype == NABO_CUDA_FLOAT32)
+      k_targets<float><<<ceil_div(nTrain, 256), 256, 0, st>>>(static_cast<const float*>(d2), nTrain, k, minD2, Y);
+    else
+      k_targets<double><<<ceil_div(nTrain, 256), 256, 0, st>>>(static_cast<const double*>(d2), nTrain, k, minD2, Y);
+    hy.resize((size_t)nTrain);
+    e = cudaMemcpyAsync(hy.data(), Y, (size_t)nTrain * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_error(e, "training targets");
+  }
+  // standardise the targets; keep samples with a k-th neighbour
+  std::vector<int32_t> valid;
+  if (rc == kOk) {
+    double sum = 0.0, sq = 0.0;
+    for (int64_t i = 0; i < nTrain; ++i) {
+      if (std::isnan(hy[(size_t)i])) continue;
+      valid.push_back((int32_t)i);
+      sum += hy[(size_t)i];
+      sq += (double)hy[(size_t)i] * hy[(size_t)i];
+    }
+    if (valid.size() < 16) rc = set_error(kErrArgument, "too few training queries have k neighbours within maxRadius");
+    if (rc == kOk) {
+      const double mean = sum / valid.size();
+      const double var = std::max(sq / valid.size() - mean * mean, 1e-12);
+      m->mu = (float)mean;
+      m->sigma = (float)std::sqrt(var);
+      for (int64_t i = 0; i < nTrain; ++i)
+        if (!std::isnan(hy[(size_t)i])) hy[(size_t)i] = (float)((hy[(size_t)i] - mean) / m->sigma);
+      e = cudaMemcpyAsync(Y, hy.data(), (size_t)nTrain * sizeof(float), cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) rc = cuda_error(e, "training targets upload");
+    }
+  }
+  // Adam with a cosine learning-rate decay
+  if (rc == kOk) {
+    std::mt19937_64 rng(tp.seed ^ 0x9e3779b97f4a7c15ull);
+    const int nValid = (int)valid.size();
+    const int batch = std::max(32, std::min(tp.batch, nValid));
+    const int stepsPerEpoch = std::max(1, nValid / batch);
+    const int total = std::max(1, tp.epochs) * stepsPerEpoch;
+    std::vector<int32_t> perm(valid);
+    int step = 0;
+    float lastLoss = 0.0f;
+    for (int ep = 0; ep < std::max(1, tp.epochs) && rc == kOk; ++ep) {
+      std::shuffle(perm.begin(), perm.end(), rng);
+      e = cudaMemcpyAsync(order, perm.data(), perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+      if (e != cudaSuccess) {
+        rc = cuda_error(e, "batch upload");
+        break;
+      }
+      const bool lastEpoch = ep + 1 == std::max(1, tp.epochs);
+      if (lastEpoch) cudaMemsetAsync(loss, 0, sizeof(float), st);
+      for (int b = 0; b < stepsPerEpoch && rc == kOk; ++b, ++step) {
+        rc = grad_step(*m, X, Y, order + (size_t)b * batch, batch, lastEpoch ? loss : nullptr, st);
+        const double lr = tp.lr * 0.5 * (1.0 + std::cos(3.14159265358979323846 * step / total));
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = (float)(1.0 / (1.0 - std::pow(b1, step + 1)));
+        const float c2 = (float)(1.0 / (1.0 - std::pow(b2, step + 1)));
+        k_adam<<<ceil_div(kParams, 256), 256, 0, st>>>(m->params, m->adamM, m->adamV, m->grad, m->pb, kParams,
+                                                       (float)lr, b1, b2, c1, c2, 1e-8f);
+      }
+      if (lastEpoch && rc == kOk) {
+        e = cudaMemcpyAsync(&lastLoss, loss, sizeof(float), cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = cuda_error(e, "training");
+      }
+    }
+    m->trainLoss = lastLoss / (float)((size_t)stepsPerEpoch * batch);
+    m->trainSamples = nValid;
+  }
+  if (idx) scratch_free(idx, st);
+  if (d2) scratch_free(d2, st);
+  if (X) scratch_free(X, st);
+  if (Y) scratch_free(Y, st);
+  if (loss) scratch_free(loss, st);
+  if (order) scratch_free(order, st);
+  if (rc != kOk) return fail(rc);
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(cuda_error(e, "training"));
+  *out = m;
+  return kOk;
+}
+
+void radius_model_free(RadiusModel* m) {
+  if (!m) return;
+  free_model(m);
+  delete m;
+}
+
+int radius_model_predict(const RadiusModel& m, const void* query, int64_t nq, int64_t qStride, double maxRadius,
+                         void* radii, float* raw, cudaStream_t st) {
+  return launch_radius(m, query, nq, qStride, maxRadius, radii, raw, st);
+}
+
+// Bounded search with the learned radii, then the exact search again for
+// the queries that found fewer than k neighbours inside their radius.
+int knn_learned(const nabo_cuda_search* s, const RadiusModel& m, const KnnArgs& base, int32_t* dFallbacks,
+                cudaStream_t st) {
+  const HandleView h = handle_view(s);
+  const DeviceCloud& c = *h.cloud;
+  if (base.nq == 0) return kOk;
+  const size_t es = c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  void* radii = nullptr;
+  int32_t *found = nullptr, *list = nullptr, *count = nullptr;
+  cudaError_t e = scratch_alloc(&radii, (size_t)base.nq * es, st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&found, (size_t)base.nq * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&list, (size_t)base.nq * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&count, sizeof(int32_t), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(int32_t), st);
+  int rc = e == cudaSuccess ? kOk : cuda_error(e, "learned search buffers");
+  if (rc == kOk) rc = launch_radius(m, base.query, base.nq, base.qStride, base.maxRadius, radii, nullptr, st);
+  if (rc == kOk) {
+    KnnArgs a = base;
+    a.maxRadii = radii;
+    a.found = found;
+    rc = search_plain(c, a, st);
+  }
+  if (rc == kOk) {
+    if (c.dtype == NABO_CUDA_FLOAT32)
+      k_collect_misses<float><<<ceil_div(base.nq, 256), 256, 0, st>>>(found, static_cast<const float*>(radii), base.nq,
+                                                                        base.k, base.maxRadius, list, count);
+    else
+      k_collect_misses<double><<<ceil_div(base.nq, 256), 256, 0, st>>>(
+          found, static_cast<const double*>(radii), base.nq, base.k, base.maxRadius, list, count);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_error(e, "miss compaction");
+  }
+  if (rc == kOk) {
+    KnnArgs a = base;
+    a.maxRadii = nullptr;
+    a.nqDevice = count;
+    rc = search_given(c, a, list, st);
+  }
+  if (rc == kOk && dFallbacks) {
+    e = cudaMemcpyAsync(dFallbacks, count, sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "fallback count");
+  }
+  if (radii) scratch_free(radii, st);
+  if (found) scratch_free(found, st);
+  if (list) scratch_free(list, st);
+  if (count) scratch_free(count, st);
+  return rc;
+}
+
+// Gradient of the training loss for given features/targets (for checks).
+int radius_model_gradients(const RadiusModel& m, const float* dX, const float* dY, int64_t n, float* hGrad,
+                           float* hLoss, cudaStream_t st) {
+  int32_t* idx = nullptr;
+  float* loss = nullptr;
+  cudaError_t e = scratch_alloc((void**)&idx, (size_t)n * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&loss, sizeof(float), st);
+  if (e != cudaSuccess) return cuda_error(e, "gradient buffers");
+  std::vector<int32_t> seq((size_t)n);
+  for (int64_t i = 0; i < n; ++i) seq[(size_t)i] = (int32_t)i;
+  e = cudaMemcpyAsync(idx, seq.data(), (size_t)n * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(loss, 0, sizeof(float), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m.grad, 0, kParams * sizeof(float), st);
+  int rc = e == cudaSuccess ? kOk : cuda_error(e, "gradient setup");
+  if (rc == kOk) rc = grad_step(m, dX, dY, idx, (int)n, loss, st);
+  if (rc == kOk) {
+    e = cudaMemcpyAsync(hGrad, m.grad, kParams * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hLoss, loss, sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m.grad, 0, kParams * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_error(e, "gradient readback");
+  }
+  scratch_free(idx, st);
+  scratch_free(loss, st);
+  cudaStreamSynchronize(st);
+  return rc;
+}
+
+int radius_model_features(const RadiusModel& m, const void* query, int64_t nq, int64_t qStride, float* dX,
+                          cudaStream_t st) {
+  return launch_features(m, query, nq, qStride, dX, st);
+}
+
+int radius_model_get(const RadiusModel& m, float* params, float* meta) {
+  if (params) {
+    const cudaError_t e = cudaMemcpy(params, m.params, kParams * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "model read");
+  }
+  if (meta) {
+    meta[0] = m.mu;
+    meta[1] = m.sigma;
+    meta[2] = m.safety;
+    meta[3] = (float)m.k;
+    meta[4] = m.trainLoss;
+    meta[5] = (float)m.trainSamples;
+    meta[6] = (float)m.fs.nIn;
+    meta[7] = (float)kParams;
+  }
+  return kOk;
+}
+
+int radius_model_set(RadiusModel& m, const float* params, const float* meta) {
+  if (params) {
+    cudaError_t e = cudaMemcpy(m.params, params, kParams * sizeof(float), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_error(e, "model write");
+    k_to_bf16<<<ceil_div(kParams, 256), 256>>>(m.params, m.pb, kParams);
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_error(e, "model write");
+  }
+  if (meta) {
+    m.mu = meta[0];
+    m.sigma = meta[1];
+    m.safety = meta[2];
+  }
+  return kOk;
+}
+
+const void* radius_model_owner(const RadiusModel& m) { return m.owner; }
+int radius_model_k(const RadiusModel& m) { return m.k; }
+
+}  // namespace nabo_gb300
+
+// ---------------------------------------------------------------------------
+// C ABI
+
+struct nabo_cuda_radius_model {
+  nabo_gb300::RadiusModel* m;
+  int device;
+};
+
+using namespace nabo_gb300;
+
+namespace {
+struct DevGuard {
+  int prev = -1;
+  explicit DevGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+  }
+  ~DevGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+}  // namespace
+
+extern "C" {
+
+void nabo_cuda_train_params_init(nabo_cuda_train_params* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->struct_size = sizeof(nabo_cuda_train_params);
+  p->epochs = 30;
+  p->batch = 4096;
+  p->lr = 3e-3f;
+  p->safety = 1.2f;
+  p->seed = 1234;
+}
+
+int nabo_cuda_radius_model_train(const nabo_cuda_search* s, const void* trainQueries, int qRows, int64_t n,
+                                 int64_t qStride, int k, unsigned optionFlags, double maxRadius,
+                                 const nabo_cuda_train_params* params, nabo_cuda_radius_model** out) {
+  if (!s || !out) return set_error(kErrArgument, "NULL search object or output pointer");
+  *out = nullptr;
+  const HandleView h = handle_view(s);
+  if (h.searchType != NABO_SEARCH_KDTREE_CUDA)
+    return set_error(kErrArgument, "a radius model is trained for a kd-tree search object");
+  int rc = handle_check_knn(s, qRows, n, qStride, k, optionFlags, nullptr);
+  if (rc != kOk) return rc;
+  if (n < 16 || !trainQueries) return set_error(kErrArgument, "at least 16 training queries are needed");
+  if (n > (int64_t)1 << 30) return set_error(kErrUnsupported, "too many training queries");
+  nabo_cuda_train_params tp;
+  nabo_cuda_train_params_init(&tp);
+  if (params) {
+    tp.epochs = params->epochs;
+    tp.batch = params->batch;
+    tp.lr = params->lr;
+    tp.safety = params->safety;
+    tp.seed = params->seed;
+  }
+  if (tp.epochs < 1 || tp.batch < 32 || !(tp.lr > 0.0f) || !(tp.safety >= 1.0f))
+    return set_error(kErrArgument, "training parameters: epochs >= 1, batch >= 32, lr > 0, safety >= 1");
+  DevGuard g(h.device);
+  RadiusModel* m = nullptr;
+  rc = radius_model_train(s, trainQueries, n, qStride, k, optionFlags, maxRadius, tp, &m, cudaStreamPerThread);
+  if (rc != kOk) return rc;
+  *out = new nabo_cuda_radius_model{m, h.device};
+  return kOk;
+}
+
+int nabo_cuda_radius_model_destroy(nabo_cuda_radius_model* m) {
+  if (!m) return kOk;
+  DevGuard g(m->device);
+  radius_model_free(m->m);
+  delete m;
+  return kOk;
+}
+
+int nabo_cuda_radius_model_predict_device(const nabo_cuda_radius_model* m, const void* query, int qRows, int64_t nq,
+                                          int64_t qStride, double maxRadius, void* radii, float* raw, void* stream) {
+  if (!m) return set_error(kErrArgument, "radius model is NULL");
+  if (nq < 0 || qStride < qRows || qRows < m->m->dim) return set_error(kErrArgument, "bad query shape");
+  if (nq == 0) return kOk;
+  if (!query || !radii) return set_error(kErrArgument, "NULL query or radii buffer");
+  DevGuard g(m->device);
+  return radius_model_predict(*m->m, query, nq, qStride, maxRadius, radii, raw, static_cast<cudaStream_t>(stream));
+}
+
+int nabo_cuda_knn_learned_device(const nabo_cuda_search* s, const nabo_cuda_radius_model* m, const void* query,
+                                 int qRows, int64_t nq, int64_t qStride, int k, double epsilon, unsigned optionFlags,
+                                 double maxRadius, int32_t* indices, void* dists2, uint64_t* touched,
+                                 int32_t* fallbacks, void* stream) {
+  if (!s || !m) return set_error(kErrArgument, "NULL search object or radius model");
+  if (radius_model_owner(*m->m) != s)
+    return set_error(kErrArgument, "the radius model was trained for another search object");
+  int rc = handle_check_knn(s, qRows, nq, qStride, k, optionFlags, nullptr);
+  if (rc != kOk) return rc;
+  if (nq == 0) return kOk;
+  if (!query || !indices || !dists2) return set_error(kErrArgument, "NULL query or result buffer");
+  const HandleView h = handle_view(s);
+  DevGuard g(h.device);
+  KnnArgs a;
+  a.query = query;
+  a.nq = nq;
+  a.qStride = qStride;
+  a.k = k;
+  a.eps = epsilon;
+  a.optionFlags = optionFlags;
+  a.touchStats = (h.creationFlags & NABO_TOUCH_STATISTICS) != 0;
+  a.touched = reinterpret_cast<unsigned long long*>(touched);
+  a.maxRadius = maxRadius;
+  a.indices = indices;
+  a.dists2 = dists2;
+  a.traversal = h.traversal == 2 ? 1 : h.traversal;
+  return knn_learned(s, *m->m, a, fallbacks, static_cast<cudaStream_t>(stream));
+}
+
+int nabo_cuda_knn_learned(const nabo_cuda_search* s, const nabo_cuda_radius_model* m, const void* query, int qRows,
+                          int64_t nq, int64_t qStride, int k, double epsilon, unsigned optionFlags, double maxRadius,
+                          int32_t* indices, void* dists2, uint64_t* touched, int64_t* fallbacks) {
+  if (!s || !m) return set_error(kErrArgument, "NULL search object or radius model");
+  int rc = handle_check_knn(s, qRows, nq, qStride, k, optionFlags, nullptr);
+  if (rc != kOk) return rc;
+  if (touched) *touched = 0;
+  if (fallbacks) *fallbacks = 0;
+  if (nq == 0) return kOk;
+  if (!query || !indices || !dists2) return set_error(kErrArgument, "NULL query or result buffer");
+  const HandleView h = handle_view(s);
+  DevGuard g(h.device);
+  cudaStream_t st = cudaStreamPerThread;
+  const size_t es = h.cloud->dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  const size_t qBytes = (size_t)((nq - 1) * qStride + qRows) * es;
+  const size_t outN = (size_t)nq * (size_t)k;
+  void *dq = nullptr, *dd = nullptr;
+  int32_t *di = nullptr, *dfb = nullptr;
+  unsigned long long* dt = nullptr;
+  cudaError_t e = scratch_alloc(&dq, qBytes, st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&di, outN * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = scratch_alloc(&dd, outN * es, st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&dt, sizeof(unsigned long long), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&dfb, sizeof(int32_t), st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dq, query, qBytes, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dt, 0, sizeof(unsigned long long), st);
+  rc = e == cudaSuccess ? kOk : cuda_error(e, "learned knn setup");
+  if (rc == kOk)
+    rc = nabo_cuda_knn_learned_device(s, m, dq, qRows, nq, qStride, k, epsilon, optionFlags, maxRadius, di, dd,
+                                      reinterpret_cast<uint64_t*>(dt), dfb, st);
+  unsigned long long ht = 0;
+  int32_t hfb = 0;
+  if (rc == kOk) {
+    e = cudaMemcpyAsync(indices, di, outN * sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dists2, dd, outN * es, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&ht, dt, sizeof(ht), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hfb, dfb, sizeof(hfb), cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "learned knn results");
+  }
+  if (dq) scratch_free(dq, st);
+  if (di) scratch_free(di, st);
+  if (dd) scratch_free(dd, st);
+  if (dt) scratch_free(dt, st);
+  if (dfb) scratch_free(dfb, st);
+  e = cudaStreamSynchronize(st);
+  if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, "learned knn");
+  if (rc == kOk) {
+    if (touched) *touched = (h.creationFlags & NABO_TOUCH_STATISTICS) ? ht : 0;
+    if (fallbacks) *fallbacks = hfb;
+  }
+  return rc;
+}
+
+int nabo_cuda_radius_model_features_device(const nabo_cuda_radius_model* m, const void* query, int qRows, int64_t nq,
+                                           int64_t qStride, float* features, void* stream) {
+  if (!m) return set_error(kErrArgument, "radius model is NULL");
+  if (nq < 0 || qStride < qRows || qRows < m->m->dim) return set_error(kErrArgument, "bad query shape");
+  if (nq == 0) return kOk;
+  DevGuard g(m->device);
+  return radius_model_features(*m->m, query, nq, qStride, features, static_cast<cudaStream_t>(stream));
+}
+
+int nabo_cuda_radius_model_gradients(const nabo_cuda_radius_model* m, const float* features, const float* targets,
+                                     int64_t n, float* grad, float* loss) {
+  if (!m || !features || !targets || !grad || !loss) return set_error(kErrArgument, "NULL argument");
+  if (n < 1 || n > (int64_t)1 << 28) return set_error(kErrArgument, "bad sample count");
+  DevGuard g(m->device);
+  return radius_model_gradients(*m->m, features, targets, n, grad, loss, cudaStreamPerThread);
+}
+
+int nabo_cuda_radius_model_get(const nabo_cuda_radius_model* m, float* params, float* meta) {
+  if (!m) return set_error(kErrArgument, "radius model is NULL");
+  DevGuard g(m->device);
+  return radius_model_get(*m->m, params, meta);
+}
+
+int nabo_cuda_radius_model_set(nabo_cuda_radius_model* m, const float* params, const float* meta) {
+  if (!m) return set_error(kErrArgument, "radius model is NULL");
+  DevGuard g(m->device);
+  return radius_model_set(*m->m, params, meta);
+}
+
+}  // extern "C"

@@ -139,6 +139,7 @@ struct KnnLaunch {
   int64_t n;  // points (brute force)
   int allowSelf;
   int stats;
+  const int32_t* nqDevice;  // if set, only threads t < *nqDevice search (t < nq still bounds the grid)
 };
 
 // Leaf scan shared by the kernels: the bucket's records are read in chunks
@@ -199,7 +200,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
   const T* __restrict__ query = static_cast<const T*>(a.query);
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   unsigned long long touched = 0;
-  if (t < a.nq) {
+  if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
     const int64_t qi = a.order ? (int64_t)a.order[t] : t;
     T q[D];
 #pragma unroll

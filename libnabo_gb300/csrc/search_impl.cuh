@@ -47,6 +47,7 @@ KnnLaunch make_launch(const DeviceCloud& c, const KnnArgs& a, const int32_t* ord
   L.n = c.n;
   L.allowSelf = (a.optionFlags & 1u) ? 1 : 0;
   L.stats = (a.touchStats && a.touched) ? 1 : 0;
+  L.nqDevice = a.nqDevice;
   return L;
 }
 
