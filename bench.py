@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-order", action="store_true", help="keep the queries in their given order")
+    p.add_argument("--no-learned", action="store_true", help="skip the learned-radius form")
+    p.add_argument("--train-queries", type=int, default=200000)
     p.add_argument("--traversal", type=int, default=0,
                    help="kd-tree traversal: 0/1 reference visit order (default), 2 warp packet")
     return p.parse_args()
@@ -66,6 +68,18 @@ def workload(name: str, rank: int):
     cloud = S.uniform(1_000_000, 3, seed=S.SEED_BASE + 5)
     q = S.uniform(1_000_000, 3, seed=S.SEED_BASE + 6 + 7919 * rank)
     return cloud, q, dict(maxRadius=float("inf"), flags=0, label="uniform_1M")
+
+
+def training_queries(name: str, cloud, count: int):
+    """Training queries from the same distribution as the workload's but not
+    the benchmark queries themselves: another random transform of the scan,
+    or fresh uniform samples."""
+    from libnabo_gb300 import synthetic as S
+    rng = np.random.default_rng(S.SEED_BASE + 4242)
+    if name == "lidar":
+        t = S.lidar_queries(cloud, seed=S.SEED_BASE + 4242)
+        return t[rng.choice(t.shape[0], min(count, t.shape[0]), replace=False)]
+    return S.uniform(count, 3, seed=S.SEED_BASE + 4243)
 
 
 def measured_peaks():
@@ -242,36 +256,72 @@ def run_ours(args):
     p_bar = int(touched.item()) / nq
     s.profile(True)
 
-    def step():
-        s.knn_device(tq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(idx, d2))
-
-    for _ in range(args.warmup):
-        flush.zero_()
-        step()
-    torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    kernel_ms = []
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    def timed(step_fn, kernel_ms_fn=None):
+        """W warm-up steps, then K steps timed with CUDA events (L2 flushed
+        before each); returns (per-step ms list, kernel ms list)."""
+        for _ in range(args.warmup):
+            flush.zero_()
+            step_fn()
+        torch.cuda.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        kms = []
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
         for i in range(args.steps):
             flush.zero_()
             starts[i].record(stream)
-            step()
+            step_fn()
             ends[i].record(stream)
-            kernel_ms.append(s.last_kernel_ms())
+            if kernel_ms_fn is not None:
+                kms.append(kernel_ms_fn())
         torch.cuda.synchronize()
-    if world > 1:
-        dist.barrier()
-    step_ms = [a.elapsed_time(b) for a, b in zip(starts, ends)]
-    total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    ms_per_step = total_ms / args.steps
+        if world > 1:
+            dist.barrier()
+        return [a.elapsed_time(b) for a, b in zip(starts, ends)], kms
+
+    def max_over_ranks(x):
+        if world > 1:
+            t = torch.tensor([x], dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return x
+
+    def plain_step():
+        s.knn_device(tq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(idx, d2))
+
+    with ClockSampler(local) as clk:
+        step_ms, kernel_ms = timed(plain_step, s.last_kernel_ms)
+        plain_ms = max_over_ranks(sum(step_ms)) / args.steps
+        learned = None
+        if not args.no_learned:
+            tr = training_queries(args.workload, cloud, args.train_queries)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            model = nb.RadiusModel(s, tr, k=k, optionFlags=cfg["flags"], maxRadius=cfg["maxRadius"])
+            torch.cuda.synchronize()
+            train_s = time.perf_counter() - t0
+            fb = torch.zeros(1, dtype=torch.int32, device=dev)
+            li = torch.empty_like(idx)
+            ld = torch.empty_like(d2)
+
+            def learned_step():
+                model.knn_device(tq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(li, ld), fallbacks=fb)
+
+            lstep_ms, lkernel_ms = timed(learned_step, s.last_kernel_ms)
+            learned_ms = max_over_ranks(sum(lstep_ms)) / args.steps
+            torch.cuda.synchronize()
+            exact = bool(torch.equal(li, idx) and torch.equal(ld, d2))
+            learned = {"ms_per_step": learned_ms, "queries_per_s": world * nq / (learned_ms / 1e3),
+                       "fallbacks": int(fb.item()), "fallback_rate": int(fb.item()) / nq,
+                       "identical_to_plain": exact, "train_s": train_s, "train_queries": int(tr.shape[0]),
+                       "bounded_kernel_ms": statistics.mean(lkernel_ms),
+                       "model": {kk: (round(v, 6) if isinstance(v, float) else v) for kk, v in model.meta.items()}}
+    plain_value = world * nq / (plain_ms / 1e3)
+    plain_kernel_ms = statistics.mean(kernel_ms)
+    use_learned = learned is not None and learned["identical_to_plain"] and learned["ms_per_step"] < plain_ms
+    ms_per_step = learned["ms_per_step"] if use_learned else plain_ms
     value = world * nq / (ms_per_step / 1e3)
 
     # end to end through the host API, pinned host buffers
@@ -279,27 +329,26 @@ def run_ours(args):
     hq = torch.from_numpy(q).pin_memory().numpy()
     hidx = torch.empty((nq, k), dtype=torch.int32).pin_memory().numpy()
     hd2 = torch.empty((nq, k), dtype=torch.float32).pin_memory().numpy()
+    search_api = model if use_learned else s
     for _ in range(2):
-        s.knn(hq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(hidx, hd2))
+        search_api.knn(hq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(hidx, hd2))
     e2e_t = []
     for _ in range(e2e_steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        s.knn(hq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(hidx, hd2))
+        search_api.knn(hq, k, 0.0, cfg["flags"], cfg["maxRadius"], out=(hidx, hd2))
         e2e_t.append(time.perf_counter() - t0)
-    e2e_s = sum(e2e_t) / len(e2e_t)
-    if world > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(sum(e2e_t) / len(e2e_t))
     e2e_value = world * nq / e2e_s
 
     # roofline of the search kernel: algorithmic bytes per query
     #   B_q = D*s + k*(4+s) + P*(D*s + 4)   (query, results, touched points)
+    # with P the reference algorithm's touched points (TOUCH_STATISTICS of
+    # the unbounded search on the same input)
     dsz, D = 4, 3
     b_q = D * dsz + k * (4 + dsz) + p_bar * (D * dsz + 4)
-    kern_s = statistics.mean(kernel_ms) / 1e3
+    kern_s = statistics.mean(lkernel_ms if use_learned else kernel_ms) / 1e3
     achieved = nq * b_q / kern_s / 1e9
     peak, peak_kind = measured_peaks()
     traffic_launch, traffic_nq = profiled_traffic(cfg["label"], k)
@@ -314,13 +363,15 @@ def run_ours(args):
         base = cpu_baseline(cloud, q, k, cfg)
     clocks = clk.summary()
     launches_per_step = 6 if (nq >= 4096 and not args.no_order) else 1
+    if use_learned:
+        launches_per_step += 3  # radius network, miss compaction, fallback search
     out = {
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{cfg['label']}_k{k}", "points": int(cloud.shape[0]), "queries": int(nq),
                    "k": k, "maxRadius": cfg["maxRadius"], "selfMatch": False, "bucketSize": 8,
-                   "form": "plain GPU kd-tree",
+                   "form": "learned radius (MLP) + kd-tree" if use_learned else "plain GPU kd-tree",
                    "traversal": "warp packet" if args.traversal == 2 else "reference order",
                    "query_order": "given" if args.no_order else "kd-tree leaf",
                    "l2": "flushed between steps (256 MiB write)",
@@ -328,8 +379,12 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
                 "d2h_bytes_per_step": int(hidx.nbytes + hd2.nbytes + 8)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": traffic, "peak_source": peak_kind, "kernel": "k_knn_kdtree",
-                     "kernel_ms": kern_s * 1e3, "bytes_per_query": b_q, "touched_per_query": p_bar},
+                     "traffic": traffic, "peak_source": peak_kind,
+                     "kernel": "k_knn_kdtree (bounded search of the learned form)" if use_learned
+                     else "k_knn_kdtree", "kernel_ms": kern_s * 1e3, "bytes_per_query": b_q,
+                     "touched_per_query": p_bar},
+        "forms": {"plain": {"ms_per_step": plain_ms, "queries_per_s": plain_value, "kernel_ms": plain_kernel_ms},
+                  "learned": learned},
         "cpu_baseline": base,
         "clocks": clocks,
         "gpu_launches": launches_per_step * args.steps,

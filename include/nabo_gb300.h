@@ -159,12 +159,13 @@ int nabo_cuda_knn_device_noalloc(const nabo_cuda_search* s, const void* query, i
  * reference's per-query radius overload, nabo/nabo.h:351).
  *
  * A radius model is a small network (inputs padded to 16: the normalised
- * coordinates, plus 8 coarse-voxel occupancies of the cloud around the
- * query for 3-D clouds; two hidden layers of 64 SiLU units; BF16 weights,
- * FP32 sums) trained on the GPU to predict log(d_k), the log distance of a
- * query's k-th neighbour, from training queries whose d_k the exact kd-tree
- * search computes. A learned search runs the kd-tree search with the
- * per-query radius safety * exp(prediction) (capped at maxRadius) and
+ * coordinates, plus for 3-D clouds the occupancy of the voxel holding the
+ * query at 8 octave scales; two hidden layers of 64 SiLU units; BF16
+ * weights, FP32 sums) trained on the GPU to predict log(d_k), the log
+ * distance of a query's k-th neighbour, from training queries whose d_k the
+ * exact kd-tree search computes. A learned search runs the kd-tree search
+ * with the per-query radius safety * exp(prediction + calibrated margin)
+ * (capped at maxRadius) and
  * searches again without it every query that found fewer than k
  * neighbours inside its radius, so results equal nabo_cuda_knn's. */
 typedef struct nabo_cuda_radius_model nabo_cuda_radius_model; /* opaque */
@@ -177,7 +178,9 @@ typedef struct nabo_cuda_train_params {
   int32_t batch;   /* minibatch, default 4096 */
   float lr;        /* Adam learning rate (cosine-decayed), default 3e-3 */
   float safety;    /* radius = safety * exp(prediction), default 1.2 */
-  uint32_t reserved0;
+  float targetMissRate; /* after training, widen the radius until about this
+                           fraction of the training queries would fall outside
+                           it (default 0.03; 0 keeps the plain safety factor) */
   uint64_t seed;   /* weight initialisation and shuffling, default 1234 */
   int32_t reserved[4];
 } nabo_cuda_train_params;
@@ -223,8 +226,9 @@ int nabo_cuda_radius_model_gradients(const nabo_cuda_radius_model* m, const floa
                                      int64_t n, float* grad, float* loss);
 /* Save / load: params (HOST, NABO_CUDA_RADIUS_MODEL_PARAMS FP32 master
  * weights) and meta (HOST, 8 floats: mu, sigma, safety, k, final training
- * loss, training samples, inputs used, parameter count); either may be
- * NULL. set() takes mu, sigma and safety from meta. */
+ * loss, training samples, inputs used, margin); either may be
+ * NULL; meta[7] is the calibrated margin. set() takes mu, sigma, safety
+ * and the margin from meta. */
 int nabo_cuda_radius_model_get(const nabo_cuda_radius_model* m, float* params, float* meta);
 int nabo_cuda_radius_model_set(nabo_cuda_radius_model* m, const float* params, const float* meta);
 

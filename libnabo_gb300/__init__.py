@@ -328,7 +328,7 @@ class RadiusModel:
 
     def __init__(self, search: NearestNeighbourSearch, train_queries, k: int, optionFlags: int = 0,
                  maxRadius: float = np.inf, epochs: int = 30, batch: int = 4096, lr: float = 3e-3,
-                 safety: float = 1.2, seed: int = 1234):
+                 safety: float = 1.2, seed: int = 1234, targetMissRate: float = 0.03):
         import torch
         self.search = search
         self.k = int(k)
@@ -339,6 +339,7 @@ class RadiusModel:
         p = nabo_cuda_train_params()
         _lib.nabo_cuda_train_params_init(ctypes.byref(p))
         p.epochs, p.batch, p.lr, p.safety, p.seed = int(epochs), int(batch), float(lr), float(safety), int(seed)
+        p.targetMissRate = float(targetMissRate)
         torch.cuda.synchronize()
         _check(_lib.nabo_cuda_radius_model_train(search._h, ctypes.c_void_p(tq.data_ptr()), rows, n, rows, self.k,
                                                  int(optionFlags), float(maxRadius), ctypes.byref(p),
@@ -363,7 +364,7 @@ class RadiusModel:
         meta = (ctypes.c_float * 8)()
         _check(_lib.nabo_cuda_radius_model_get(self._m, None, meta))
         return dict(mu=meta[0], sigma=meta[1], safety=meta[2], k=int(meta[3]), train_loss=meta[4],
-                    train_samples=int(meta[5]), inputs=int(meta[6]))
+                    train_samples=int(meta[5]), inputs=int(meta[6]), margin=meta[7])
 
     def get_params(self):
         params = np.zeros(RADIUS_MODEL_PARAMS, np.float32)

@@ -53,7 +53,7 @@ class nabo_cuda_train_params(ctypes.Structure):
         ("batch", ctypes.c_int32),
         ("lr", ctypes.c_float),
         ("safety", ctypes.c_float),
-        ("reserved0", ctypes.c_uint32),
+        ("targetMissRate", ctypes.c_float),
         ("seed", ctypes.c_uint64),
         ("reserved", ctypes.c_int32 * 4),
     ]

@@ -346,6 +346,8 @@ HandleView handle_view(const nabo_cuda_search* s) {
   v.creationFlags = s->creationFlags;
   v.device = s->device;
   v.traversal = s->traversal;
+  v.evStart = s->evStart;
+  v.evStop = s->evStop;
   return v;
 }
 

@@ -113,6 +113,8 @@ struct HandleView {
   unsigned creationFlags;
   int device;
   int traversal;
+  cudaEvent_t evStart;  // profiling events (null when profiling is off)
+  cudaEvent_t evStop;
 };
 HandleView handle_view(const struct ::nabo_cuda_search* s);
 int handle_check_knn(const struct ::nabo_cuda_search* s, int qRows, int64_t nq, int64_t qStride, int k,

@@ -9,10 +9,15 @@
 //
 // Network: inputs padded to kF = 16, two hidden layers of kH = 64 SiLU
 // units, one output. Weights are BF16, sums are FP32.
-//   3-D clouds: inputs = 3 normalised coordinates + 8 coarse-voxel
-//               occupancies (log counts of the 2x2x2 voxels around the
-//               query in a grid of about 128 voxels along the longest side)
+//   3-D clouds: inputs = 3 normalised coordinates + 8 voxel occupancies:
+//               the log point count of the voxel holding the query at 8
+//               octave scales h0 * 2^s, h0 half the median k-th distance of
+//               the training queries. Each scale's counts sit in a hash
+//               table (open addressing) holding only occupied voxels.
 //   other dims: inputs = the normalised coordinates.
+// Radius: safety * exp(mu + sigma * (output + margin)); `margin` is set
+// after training so that about `targetMissRate` of the training queries
+// would fall outside their radius (0 when that rate is met already).
 // Training: targets are log(d_k) of training queries, computed by the exact
 // GPU kd-tree search; MSE on the standardised target; Adam. The training
 // kernel runs on the FP32 cores and rounds weights, inputs and the first
@@ -44,7 +49,7 @@ constexpr int kOffB2 = kOffW2 + kH * kH;   // b2[kH]
 constexpr int kOffW3 = kOffB2 + kH;        // w3[kH]
 constexpr int kOffB3 = kOffW3 + kH;        // b3
 constexpr int kParams = kOffB3 + 1;        // 5313
-constexpr int kGridMax = 128;
+constexpr int kScales = 8;
 
 struct FeatureSpace {
   int dim;
@@ -53,14 +58,52 @@ struct FeatureSpace {
   float invHalf[kMaxDim];
   int useGrid;
   float lo[3];
-  float invH;
-  int nx, ny, nz;
-  float invLogMax;
-  const uint32_t* grid;
+  float invH0;                     // 1 / finest voxel size
+  float invLogN;                   // 1 / log1p(points)
+  unsigned long long* keys[kScales];  // hash tables: voxel key (0 = empty)
+  uint32_t* counts[kScales];
+  uint32_t mask[kScales];          // capacity - 1 (capacity a power of two)
 };
+
+// Voxel key of integer coordinates (21 bits each); 0 is reserved for empty.
+__device__ __forceinline__ unsigned long long voxel_key(int x, int y, int z) {
+  return ((((unsigned long long)x & 0x1FFFFFull) << 42) | (((unsigned long long)y & 0x1FFFFFull) << 21) |
+          ((unsigned long long)z & 0x1FFFFFull)) + 1ull;
+}
+// 64-bit finaliser (splitmix64) for the slot.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+constexpr int kVoxelCoordMax = (1 << 21) - 1;
 
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
+
+// Count of the voxel at scale s holding point (x, y, z); 0 outside the
+// cloud's voxels. Probing is bounded by the table size (a table is at most
+// half full, so a lookup ends at the key or at an empty slot long before).
+__device__ __forceinline__ uint32_t voxel_count(const FeatureSpace& fs, int s, const float (&p)[3]) {
+  const float inv = fs.invH0 * __int_as_float((127 - s) << 23);  // invH0 / 2^s
+  int c[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float v = floorf((p[d] - fs.lo[d]) * inv);
+    if (!(v >= 0.0f && v <= (float)kVoxelCoordMax)) return 0u;
+    c[d] = (int)v;
+  }
+  const unsigned long long key = voxel_key(c[0], c[1], c[2]);
+  const uint32_t mask = fs.mask[s];
+  uint32_t slot = (uint32_t)mix64(key) & mask;
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    const unsigned long long k = fs.keys[s][slot];
+    if (k == key) return fs.counts[s][slot];
+    if (k == 0ull) return 0u;
+    slot = (slot + 1u) & mask;
+  }
+  return 0u;
+}
 
 template <typename T>
 __device__ __forceinline__ void features(const T* __restrict__ q, const FeatureSpace& fs, float (&out)[kF]) {
@@ -68,42 +111,40 @@ __device__ __forceinline__ void features(const T* __restrict__ q, const FeatureS
   for (int f = 0; f < kF; ++f) out[f] = 0.0f;
   for (int d = 0; d < fs.dim && d < kF; ++d) out[d] = fminf(fmaxf(((float)q[d] - fs.center[d]) * fs.invHalf[d], -4.f), 4.f);
   if (fs.useGrid) {
-    int i0[3];
-    const int nn[3] = {fs.nx, fs.ny, fs.nz};
+    const float p[3] = {(float)q[0], (float)q[1], (float)q[2]};
 #pragma unroll
-    for (int d = 0; d < 3; ++d) i0[d] = (int)floorf(((float)q[d] - fs.lo[d]) * fs.invH - 0.5f);
-#pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      int v[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) v[d] = min(max(i0[d] + ((c >> d) & 1), 0), nn[d] - 1);
-      const uint32_t cnt = fs.grid[((int64_t)v[0] * fs.ny + v[1]) * fs.nz + v[2]];
-      out[3 + c] = log1pf((float)cnt) * fs.invLogMax;
-    }
+    for (int s = 0; s < kScales; ++s) out[3 + s] = log1pf((float)voxel_count(fs, s, p)) * fs.invLogN;
   }
 }
 
 // ---------------------------------------------------------------------------
 // voxel grid
 
+// Inserts every point into the scale-s table (counts its voxel). A table
+// holds at least twice as many slots as there are points, so an insert
+// finds its key or a free slot; the bound only makes the loop finite.
 template <typename T, int D>
-__global__ void k_grid_count(const Rec<T, D>* __restrict__ recs, int64_t n, FeatureSpace fs, uint32_t* grid) {
+__global__ void k_voxel_insert(const Rec<T, D>* __restrict__ recs, int64_t n, FeatureSpace fs, int s,
+                               int* overflow) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
   const Rec<T, D> r = recs[i];
-  int v[3];
-  const int nn[3] = {fs.nx, fs.ny, fs.nz};
+  const float inv = fs.invH0 * __int_as_float((127 - s) << 23);
+  int c[3];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) v[d] = min(max((int)floorf(((float)r.p.c[d] - fs.lo[d]) * fs.invH), 0), nn[d] - 1);
-  atomicAdd(grid + ((int64_t)v[0] * fs.ny + v[1]) * fs.nz + v[2], 1u);
-}
-
-__global__ void k_grid_max(const uint32_t* grid, int64_t cells, uint32_t* mx) {
-  uint32_t m = 0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < cells; i += (int64_t)gridDim.x * blockDim.x)
-    m = max(m, grid[i]);
-  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(mx, m);
+  for (int d = 0; d < 3; ++d) c[d] = min(max((int)floorf(((float)r.p.c[d] - fs.lo[d]) * inv), 0), kVoxelCoordMax);
+  const unsigned long long key = voxel_key(c[0], c[1], c[2]);
+  const uint32_t mask = fs.mask[s];
+  uint32_t slot = (uint32_t)mix64(key) & mask;
+  for (uint32_t probe = 0; probe <= mask; ++probe) {
+    const unsigned long long prev = atomicCAS(fs.keys[s] + slot, 0ull, key);
+    if (prev == 0ull || prev == key) {
+      atomicAdd(fs.counts[s] + slot, 1u);
+      return;
+    }
+    slot = (slot + 1u) & mask;
+  }
+  atomicOr(overflow, 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -345,7 +386,7 @@ __device__ __forceinline__ uint32_t pack2(float lo, float hi) {
 }
 
 struct RadiusOut {
-  float mu, sigma, safety;
+  float mu, sigma, safety, margin;
   double maxRadius;
 };
 
@@ -467,7 +508,7 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __rest
         if (qi < nq) {
           const float yn = (h == 0 ? y0 : y1) + b3;
           if (rawOut) rawOut[qi] = yn;
-          const double r = (double)ro.safety * exp((double)ro.mu + (double)ro.sigma * (double)yn);
+          const double r = (double)ro.safety * exp((double)ro.mu + (double)ro.sigma * ((double)yn + ro.margin));
           radii[qi] = (T)(r < ro.maxRadius ? r : ro.maxRadius);
         }
       }
@@ -498,7 +539,8 @@ struct RadiusModel {
   int k = 1;
   const void* owner = nullptr;  // the search object the model was trained on
   FeatureSpace fs{};
-  uint32_t* grid = nullptr;
+  void* tables = nullptr;   // all scales' keys and counts
+  float margin = 0.0f;      // calibration offset added to the standardised output
   float* params = nullptr;  // FP32 master
   float* adamM = nullptr;
   float* adamV = nullptr;
@@ -512,7 +554,7 @@ struct RadiusModel {
 namespace {
 
 void free_model(RadiusModel* m) {
-  if (m->grid) cudaFree(m->grid);
+  if (m->tables) cudaFree(m->tables);
   if (m->params) cudaFree(m->params);
   if (m->adamM) cudaFree(m->adamM);
   if (m->adamV) cudaFree(m->adamV);
@@ -520,8 +562,10 @@ void free_model(RadiusModel* m) {
   if (m->pb) cudaFree(m->pb);
 }
 
+// Feature normalisation, and for 3-D clouds the voxel tables at the
+// scales h0 * 2^s.
 template <typename T, int D>
-int build_grid(const DeviceCloud& c, RadiusModel* m, cudaStream_t st) {
+int build_grid(const DeviceCloud& c, RadiusModel* m, double h0, cudaStream_t st) {
   FeatureSpace& fs = m->fs;
   fs.dim = c.dim;
   for (int d = 0; d < kMaxDim; ++d) {
@@ -531,37 +575,53 @@ int build_grid(const DeviceCloud& c, RadiusModel* m, cudaStream_t st) {
     fs.invHalf[d] = half > 0.0 ? (float)(1.0 / half) : 0.0f;
   }
   fs.useGrid = (c.dim == 3) ? 1 : 0;
-  fs.nIn = fs.useGrid ? 11 : std::min(c.dim, kF);
-  fs.grid = nullptr;
+  fs.nIn = fs.useGrid ? 3 + kScales : std::min(c.dim, kF);
   if (!fs.useGrid) return kOk;
-  double ext = 0.0;
-  for (int d = 0; d < 3; ++d) ext = std::max(ext, c.hi[d] - c.lo[d]);
-  if (!(ext > 0.0)) ext = 1.0;
-  const double h = ext / kGridMax;
-  fs.invH = (float)(1.0 / h);
-  int nn[3];
-  for (int d = 0; d < 3; ++d) {
-    fs.lo[d] = (float)c.lo[d];
-    nn[d] = std::max(1, std::min(kGridMax, (int)std::ceil((c.hi[d] - c.lo[d]) / h + 1e-9)));
-  }
-  fs.nx = nn[0];
-  fs.ny = nn[1];
-  fs.nz = nn[2];
-  const int64_t cells = (int64_t)nn[0] * nn[1] * nn[2];
-  NABO_CUDA_TRY(cudaMalloc((void**)&m->grid, (size_t)cells * sizeof(uint32_t) + sizeof(uint32_t)));
-  NABO_CUDA_TRY(cudaMemsetAsync(m->grid, 0, (size_t)cells * sizeof(uint32_t) + sizeof(uint32_t), st));
   if constexpr (D == 3) {
-    k_grid_count<T, D><<<ceil_div(c.n, 256), 256, 0, st>>>(static_cast<const Rec<T, D>*>(c.recs), c.n, fs, m->grid);
+    double ext = 0.0;
+    for (int d = 0; d < 3; ++d) ext = std::max(ext, c.hi[d] - c.lo[d]);
+    if (!(ext > 0.0)) ext = 1.0;
+    // the finest voxel: at least ext / 2^20 so voxel coordinates fit 21 bits
+    h0 = std::max(h0, ext / (double)(1 << 20));
+    fs.invH0 = (float)(1.0 / h0);
+    fs.invLogN = (float)(1.0 / std::log1p((double)c.n));
+    for (int d = 0; d < 3; ++d) fs.lo[d] = (float)c.lo[d];
+    size_t total = 0;
+    uint32_t cap[kScales];
+    for (int s = 0; s < kScales; ++s) {
+      double cells = 1.0;
+      for (int d = 0; d < 3; ++d) cells *= std::floor((c.hi[d] - c.lo[d]) / (h0 * std::ldexp(1.0, s))) + 1.0;
+      const double need = 2.0 * std::min((double)c.n, cells);
+      uint32_t cp = 64;
+      while ((double)cp < need && cp < (1u << 30)) cp <<= 1;
+      cap[s] = cp;
+      fs.mask[s] = cp - 1;
+      total += (size_t)cp * (sizeof(unsigned long long) + sizeof(uint32_t));
+    }
+    NABO_CUDA_TRY(cudaMalloc(&m->tables, total + sizeof(int)));
+    NABO_CUDA_TRY(cudaMemsetAsync(m->tables, 0, total + sizeof(int), st));
+    unsigned char* p = static_cast<unsigned char*>(m->tables);
+    for (int s = 0; s < kScales; ++s) {
+      fs.keys[s] = reinterpret_cast<unsigned long long*>(p);
+      p += (size_t)cap[s] * sizeof(unsigned long long);
+    }
+    for (int s = 0; s < kScales; ++s) {
+      fs.counts[s] = reinterpret_cast<uint32_t*>(p);
+      p += (size_t)cap[s] * sizeof(uint32_t);
+    }
+    int* overflow = reinterpret_cast<int*>(p);
+    for (int s = 0; s < kScales; ++s)
+      k_voxel_insert<T, D><<<ceil_div(c.n, 256), 256, 0, st>>>(static_cast<const Rec<T, D>*>(c.recs), c.n, fs, s,
+                                                               overflow);
+    int hov = 0;
+    NABO_CUDA_TRY(cudaGetLastError());
+    NABO_CUDA_TRY(cudaMemcpyAsync(&hov, overflow, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NABO_CUDA_TRY(cudaStreamSynchronize(st));
+    if (hov) return set_error(kErrInternal, "voxel table overflow");
+    return kOk;
   } else {
     return set_error(kErrInternal, "voxel features need 3-D records");
   }
-  k_grid_max<<<(int)std::min<int64_t>(ceil_div(cells, 256), 1024), 256, 0, st>>>(m->grid, cells, m->grid + cells);
-  uint32_t mx = 0;
-  NABO_CUDA_TRY(cudaMemcpyAsync(&mx, m->grid + cells, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  NABO_CUDA_TRY(cudaStreamSynchronize(st));
-  fs.invLogMax = (float)(1.0 / std::log1p((double)std::max(mx, 1u)));
-  fs.grid = m->grid;
-  return kOk;
 }
 
 int launch_radius(const RadiusModel& m, const void* query, int64_t nq, int64_t qStride, double maxRadius, void* radii,
@@ -571,6 +631,7 @@ int launch_radius(const RadiusModel& m, const void* query, int64_t nq, int64_t q
   ro.mu = m.mu;
   ro.sigma = m.sigma;
   ro.safety = m.safety;
+  ro.margin = m.margin;
   ro.maxRadius = maxRadius;
   const int64_t tiles = (nq + 15) / 16;
   const int grid = (int)std::min<int64_t>(ceil_div(tiles, kInferWarps), 152 * 16);
@@ -625,13 +686,13 @@ std::vector<float> init_params(uint64_t seed, int nIn) {
 }
 
 template <typename T>
-int dispatch_grid(const DeviceCloud& c, RadiusModel* m, cudaStream_t st) {
+int dispatch_grid(const DeviceCloud& c, RadiusModel* m, double h0, cudaStream_t st) {
   switch (c.dpad) {
-    case 2: return build_grid<T, 2>(c, m, st);
-    case 3: return build_grid<T, 3>(c, m, st);
-    case 4: return build_grid<T, 4>(c, m, st);
-    case 8: return build_grid<T, 8>(c, m, st);
-    case 16: return build_grid<T, 16>(c, m, st);
+    case 2: return build_grid<T, 2>(c, m, h0, st);
+    case 3: return build_grid<T, 3>(c, m, h0, st);
+    case 4: return build_grid<T, 4>(c, m, h0, st);
+    case 8: return build_grid<T, 8>(c, m, h0, st);
+    case 16: return build_grid<T, 16>(c, m, h0, st);
   }
   return set_error(kErrInternal, "bad dispatch");
 }
@@ -679,39 +740,34 @@ int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nT
   m->owner = s;
   m->safety = tp.safety;
   const size_t es = c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
-  int rc = c.dtype == NABO_CUDA_FLOAT32 ? dispatch_grid<float>(c, m, st) : dispatch_grid<double>(c, m, st);
+  int rc = kOk;
   auto fail = [&](int code) {
     cudaStreamSynchronize(st);
     free_model(m);
     delete m;
     return code;
   };
-  if (rc != kOk) return fail(rc);
   cudaError_t e = cudaMalloc((void**)&m->params, kParams * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void**)&m->adamM, kParams * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void**)&m->adamV, kParams * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void**)&m->grad, kParams * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc((void**)&m->pb, kParams * sizeof(__nv_bfloat16));
   if (e != cudaSuccess) return fail(cuda_error(e, "model allocation"));
-  const std::vector<float> p0 = init_params(tp.seed, m->fs.nIn);
-  e = cudaMemcpyAsync(m->params, p0.data(), kParams * sizeof(float), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(m->adamM, 0, kParams * sizeof(float), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(m->adamV, 0, kParams * sizeof(float), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(m->grad, 0, kParams * sizeof(float), st);
-  if (e != cudaSuccess) return fail(cuda_error(e, "model init"));
-  k_to_bf16<<<ceil_div(kParams, 256), 256, 0, st>>>(m->params, m->pb, kParams);
 
   // exact k-th distances of the training queries
   int32_t* idx = nullptr;
   void* d2 = nullptr;
-  float *X = nullptr, *Y = nullptr, *loss = nullptr;
+  float *X = nullptr, *Y = nullptr, *loss = nullptr, *raw = nullptr;
   int32_t* order = nullptr;
+  void* radii = nullptr;
   e = scratch_alloc((void**)&idx, (size_t)nTrain * k * sizeof(int32_t), st);
   if (e == cudaSuccess) e = scratch_alloc(&d2, (size_t)nTrain * k * es, st);
   if (e == cudaSuccess) e = scratch_alloc((void**)&X, (size_t)nTrain * kF * sizeof(float), st);
   if (e == cudaSuccess) e = scratch_alloc((void**)&Y, (size_t)nTrain * sizeof(float), st);
   if (e == cudaSuccess) e = scratch_alloc((void**)&loss, sizeof(float), st);
   if (e == cudaSuccess) e = scratch_alloc((void**)&order, (size_t)nTrain * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&raw, (size_t)nTrain * sizeof(float), st);
+  if (e == cudaSuccess) e = scratch_alloc(&radii, (size_t)nTrain * es, st);
   if (e != cudaSuccess) rc = cuda_error(e, "training buffers");
   if (rc == kOk) {
     KnnArgs a;
@@ -723,10 +779,9 @@ int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nT
     a.maxRadius = maxRadius;
     a.indices = idx;
     a.dists2 = d2;
-    a.traversal = h.traversal;
+    a.traversal = h.traversal == 2 ? 1 : h.traversal;
     rc = search_plain(c, a, st);
   }
-  if (rc == kOk) rc = launch_features(*m, dTrain, nTrain, qStride, X, st);
   std::vector<float> hy;
   if (rc == kOk) {
     double minD2 = 1e-30;
@@ -741,16 +796,21 @@ int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nT
   }
   // standardise the targets; keep samples with a k-th neighbour
   std::vector<int32_t> valid;
+  double medianDk = 0.0;
   if (rc == kOk) {
     double sum = 0.0, sq = 0.0;
+    std::vector<float> logs;
     for (int64_t i = 0; i < nTrain; ++i) {
       if (std::isnan(hy[(size_t)i])) continue;
       valid.push_back((int32_t)i);
+      logs.push_back(hy[(size_t)i]);
       sum += hy[(size_t)i];
       sq += (double)hy[(size_t)i] * hy[(size_t)i];
     }
     if (valid.size() < 16) rc = set_error(kErrArgument, "too few training queries have k neighbours within maxRadius");
     if (rc == kOk) {
+      std::nth_element(logs.begin(), logs.begin() + logs.size() / 2, logs.end());
+      medianDk = std::exp((double)logs[logs.size() / 2]);
       const double mean = sum / valid.size();
       const double var = std::max(sq / valid.size() - mean * mean, 1e-12);
       m->mu = (float)mean;
@@ -760,6 +820,21 @@ int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nT
       e = cudaMemcpyAsync(Y, hy.data(), (size_t)nTrain * sizeof(float), cudaMemcpyHostToDevice, st);
       if (e != cudaSuccess) rc = cuda_error(e, "training targets upload");
     }
+  }
+  // voxel tables (finest voxel = half the median k-th distance), features
+  if (rc == kOk) {
+    const double h0 = std::max(0.5 * medianDk, 1e-12);
+    rc = c.dtype == NABO_CUDA_FLOAT32 ? dispatch_grid<float>(c, m, h0, st) : dispatch_grid<double>(c, m, h0, st);
+  }
+  if (rc == kOk) rc = launch_features(*m, dTrain, nTrain, qStride, X, st);
+  if (rc == kOk) {
+    const std::vector<float> p0 = init_params(tp.seed, m->fs.nIn);
+    e = cudaMemcpyAsync(m->params, p0.data(), kParams * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->adamM, 0, kParams * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->adamV, 0, kParams * sizeof(float), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->grad, 0, kParams * sizeof(float), st);
+    if (e != cudaSuccess) rc = cuda_error(e, "model init");
+    k_to_bf16<<<ceil_div(kParams, 256), 256, 0, st>>>(m->params, m->pb, kParams);
   }
   // Adam with a cosine learning-rate decay
   if (rc == kOk) {
@@ -798,12 +873,35 @@ int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nT
     m->trainLoss = lastLoss / (float)((size_t)stepsPerEpoch * batch);
     m->trainSamples = nValid;
   }
+  // margin: residual quantile so that ~targetMissRate of the training
+  // queries would fall outside their radius
+  m->margin = 0.0f;
+  if (rc == kOk && tp.targetMissRate > 0.0f) {
+    rc = launch_radius(*m, dTrain, nTrain, qStride, 1e300, radii, raw, st);
+    std::vector<float> hraw((size_t)nTrain);
+    if (rc == kOk) {
+      e = cudaMemcpyAsync(hraw.data(), raw, (size_t)nTrain * sizeof(float), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) rc = cuda_error(e, "calibration");
+    }
+    if (rc == kOk) {
+      std::vector<float> res;
+      res.reserve(valid.size());
+      for (int32_t i : valid) res.push_back(hy[(size_t)i] - hraw[(size_t)i]);
+      const size_t qi = std::min(res.size() - 1, (size_t)std::ceil((1.0 - tp.targetMissRate) * (double)res.size()));
+      std::nth_element(res.begin(), res.begin() + qi, res.end());
+      const double need = (double)res[qi] - std::log((double)m->safety) / (double)m->sigma;
+      m->margin = (float)std::max(0.0, need);
+    }
+  }
   if (idx) scratch_free(idx, st);
   if (d2) scratch_free(d2, st);
   if (X) scratch_free(X, st);
   if (Y) scratch_free(Y, st);
   if (loss) scratch_free(loss, st);
   if (order) scratch_free(order, st);
+  if (raw) scratch_free(raw, st);
+  if (radii) scratch_free(radii, st);
   if (rc != kOk) return fail(rc);
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(cuda_error(e, "training"));
@@ -843,6 +941,8 @@ int knn_learned(const nabo_cuda_search* s, const RadiusModel& m, const KnnArgs& 
     KnnArgs a = base;
     a.maxRadii = radii;
     a.found = found;
+    a.evStart = h.evStart;
+    a.evStop = h.evStop;
     rc = search_plain(c, a, st);
   }
   if (rc == kOk) {
@@ -918,7 +1018,7 @@ int radius_model_get(const RadiusModel& m, float* params, float* meta) {
     meta[4] = m.trainLoss;
     meta[5] = (float)m.trainSamples;
     meta[6] = (float)m.fs.nIn;
-    meta[7] = (float)kParams;
+    meta[7] = m.margin;
   }
   return kOk;
 }
@@ -935,6 +1035,7 @@ int radius_model_set(RadiusModel& m, const float* params, const float* meta) {
     m.mu = meta[0];
     m.sigma = meta[1];
     m.safety = meta[2];
+    m.margin = meta[7];
   }
   return kOk;
 }
@@ -977,6 +1078,7 @@ void nabo_cuda_train_params_init(nabo_cuda_train_params* p) {
   p->batch = 4096;
   p->lr = 3e-3f;
   p->safety = 1.2f;
+  p->targetMissRate = 0.03f;
   p->seed = 1234;
 }
 
@@ -999,10 +1101,13 @@ int nabo_cuda_radius_model_train(const nabo_cuda_search* s, const void* trainQue
     tp.batch = params->batch;
     tp.lr = params->lr;
     tp.safety = params->safety;
+    tp.targetMissRate = params->targetMissRate;
     tp.seed = params->seed;
   }
-  if (tp.epochs < 1 || tp.batch < 32 || !(tp.lr > 0.0f) || !(tp.safety >= 1.0f))
-    return set_error(kErrArgument, "training parameters: epochs >= 1, batch >= 32, lr > 0, safety >= 1");
+  if (tp.epochs < 1 || tp.batch < 32 || !(tp.lr > 0.0f) || !(tp.safety >= 1.0f) ||
+      !(tp.targetMissRate >= 0.0f && tp.targetMissRate < 1.0f))
+    return set_error(kErrArgument,
+                     "training parameters: epochs >= 1, batch >= 32, lr > 0, safety >= 1, 0 <= targetMissRate < 1");
   DevGuard g(h.device);
   RadiusModel* m = nullptr;
   rc = radius_model_train(s, trainQueries, n, qStride, k, optionFlags, maxRadius, tp, &m, cudaStreamPerThread);
