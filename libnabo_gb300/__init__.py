@@ -361,14 +361,14 @@ class RadiusModel:
 
     @property
     def meta(self) -> dict:
-        meta = (ctypes.c_float * 8)()
+        meta = (ctypes.c_float * 16)()
         _check(_lib.nabo_cuda_radius_model_get(self._m, None, meta))
         return dict(mu=meta[0], sigma=meta[1], safety=meta[2], k=int(meta[3]), train_loss=meta[4],
-                    train_samples=int(meta[5]), inputs=int(meta[6]), margin=meta[7])
+                    train_samples=int(meta[5]), inputs=int(meta[6]), margin=meta[7], voxel=meta[8])
 
     def get_params(self):
         params = np.zeros(RADIUS_MODEL_PARAMS, np.float32)
-        meta = np.zeros(8, np.float32)
+        meta = np.zeros(16, np.float32)
         _check(_lib.nabo_cuda_radius_model_get(self._m, _ptr(params), _ptr(meta)))
         return params, meta
 

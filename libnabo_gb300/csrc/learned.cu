@@ -541,6 +541,7 @@ struct RadiusModel {
   FeatureSpace fs{};
   void* tables = nullptr;   // all scales' keys and counts
   float margin = 0.0f;      // calibration offset added to the standardised output
+  double h0 = 0.0;          // finest voxel size (3-D features)
   float* params = nullptr;  // FP32 master
   float* adamM = nullptr;
   float* adamV = nullptr;
@@ -583,6 +584,7 @@ int build_grid(const DeviceCloud& c, RadiusModel* m, double h0, cudaStream_t st)
     if (!(ext > 0.0)) ext = 1.0;
     // the finest voxel: at least ext / 2^20 so voxel coordinates fit 21 bits
     h0 = std::max(h0, ext / (double)(1 << 20));
+    m->h0 = h0;
     fs.invH0 = (float)(1.0 / h0);
     fs.invLogN = (float)(1.0 / std::log1p((double)c.n));
     for (int d = 0; d < 3; ++d) fs.lo[d] = (float)c.lo[d];
@@ -1019,11 +1021,22 @@ int radius_model_get(const RadiusModel& m, float* params, float* meta) {
     meta[5] = (float)m.trainSamples;
     meta[6] = (float)m.fs.nIn;
     meta[7] = m.margin;
+    meta[8] = (float)m.h0;
+    for (int i = 9; i < 16; ++i) meta[i] = 0.0f;
   }
   return kOk;
 }
 
 int radius_model_set(RadiusModel& m, const float* params, const float* meta) {
+  if (meta && m.fs.useGrid && meta[8] > 0.0f && (float)m.h0 != meta[8]) {
+    // rebuild the voxel tables at the saved scale
+    const DeviceCloud& c = *handle_view(static_cast<const nabo_cuda_search*>(m.owner)).cloud;
+    if (m.tables) cudaFree(m.tables);
+    m.tables = nullptr;
+    const int rc = c.dtype == NABO_CUDA_FLOAT32 ? dispatch_grid<float>(c, &m, meta[8], cudaStreamPerThread)
+                                                : dispatch_grid<double>(c, &m, meta[8], cudaStreamPerThread);
+    if (rc != kOk) return rc;
+  }
   if (params) {
     cudaError_t e = cudaMemcpy(m.params, params, kParams * sizeof(float), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_error(e, "model write");

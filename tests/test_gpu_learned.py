@@ -47,7 +47,7 @@ def test_inference_matches_float64_forward(lidar, lidar_model):
     raw = raw.cpu().numpy().astype(np.float64)
     err = np.abs(raw - y_cpu)
     assert err.max() < 2e-2 and err.mean() < 2e-3, (err.max(), err.mean())
-    r_cpu = meta[2] * np.exp(meta[0] + meta[1] * raw)
+    r_cpu = meta[2] * np.exp(meta[0] + meta[1] * (raw + meta[7]))
     np.testing.assert_allclose(radii.cpu().numpy(), r_cpu.astype(np.float32), rtol=2e-5)
 
 
