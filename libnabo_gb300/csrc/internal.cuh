@@ -104,6 +104,9 @@ int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream);
 
 template <typename T, int D>
 int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream);
+template <typename T, int D>
+int knn_leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int32_t* order,
+                   cudaStream_t stream);
 
 // Read access to a search object for the allocation-free entry point, and
 // the search-argument checks every entry point applies.

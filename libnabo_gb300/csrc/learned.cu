@@ -518,13 +518,27 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __rest
 }
 
 // Queries whose bounded search found fewer than k neighbours although
-// their learned radius was below the caller's radius.
+// their learned radius was below the caller's radius, listed in the search
+// order (warp-aggregated, so each warp's misses stay contiguous and the
+// repeated search keeps the ordering's coherence).
 template <typename T>
-__global__ void k_collect_misses(const int32_t* __restrict__ found, const T* __restrict__ radii, int64_t nq, int k,
-                                 double maxRadius, int32_t* list, int32_t* count) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nq) return;
-  if (found[i] < k && (double)radii[i] < maxRadius) list[atomicAdd(count, 1)] = (int32_t)i;
+__global__ void k_collect_misses(const int32_t* __restrict__ order, const int32_t* __restrict__ found,
+                                 const T* __restrict__ radii, int64_t nq, int k, double maxRadius, int32_t* list,
+                                 int32_t* count) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int32_t qi = -1;
+  bool miss = false;
+  if (t < nq) {
+    qi = order ? order[t] : (int32_t)t;
+    miss = found[qi] < k && (double)radii[qi] < maxRadius;
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, miss);
+  if (!ball) return;
+  const int lane = threadIdx.x & 31;
+  int32_t base = 0;
+  if (lane == __ffs(ball) - 1) base = atomicAdd(count, __popc(ball));
+  base = __shfl_sync(0xffffffffu, base, __ffs(ball) - 1);
+  if (miss) list[base + __popc(ball & ((1u << lane) - 1u))] = qi;
 }
 
 }  // namespace
@@ -702,6 +716,19 @@ int dispatch_grid(const DeviceCloud& c, RadiusModel* m, double h0, cudaStream_t 
 int search_plain(const DeviceCloud& c, const KnnArgs& a, cudaStream_t st) {
 #define NABO_L_CASE(TT, DD) \
   if (c.dpad == DD) return knn_kdtree<TT, DD>(c, a, st);
+  if (c.dtype == NABO_CUDA_FLOAT32) {
+    NABO_L_CASE(float, 2) NABO_L_CASE(float, 3) NABO_L_CASE(float, 4) NABO_L_CASE(float, 8) NABO_L_CASE(float, 16)
+  } else {
+    NABO_L_CASE(double, 2) NABO_L_CASE(double, 3) NABO_L_CASE(double, 4) NABO_L_CASE(double, 8)
+    NABO_L_CASE(double, 16)
+  }
+#undef NABO_L_CASE
+  return set_error(kErrInternal, "bad dispatch");
+}
+
+int leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int32_t* order, cudaStream_t st) {
+#define NABO_L_CASE(TT, DD) \
+  if (c.dpad == DD) return knn_leaf_order<TT, DD>(c, query, nq, qStride, order, st);
   if (c.dtype == NABO_CUDA_FLOAT32) {
     NABO_L_CASE(float, 2) NABO_L_CASE(float, 3) NABO_L_CASE(float, 4) NABO_L_CASE(float, 8) NABO_L_CASE(float, 16)
   } else {
@@ -931,29 +958,32 @@ int knn_learned(const nabo_cuda_search* s, const RadiusModel& m, const KnnArgs& 
   if (base.nq == 0) return kOk;
   const size_t es = c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
   void* radii = nullptr;
-  int32_t *found = nullptr, *list = nullptr, *count = nullptr;
+  int32_t *found = nullptr, *list = nullptr, *count = nullptr, *order = nullptr;
+  const bool ordered = base.sortQueries && base.nq >= 4096;
   cudaError_t e = scratch_alloc(&radii, (size_t)base.nq * es, st);
   if (e == cudaSuccess) e = scratch_alloc((void**)&found, (size_t)base.nq * sizeof(int32_t), st);
   if (e == cudaSuccess) e = scratch_alloc((void**)&list, (size_t)base.nq * sizeof(int32_t), st);
   if (e == cudaSuccess) e = scratch_alloc((void**)&count, sizeof(int32_t), st);
+  if (e == cudaSuccess && ordered) e = scratch_alloc((void**)&order, (size_t)base.nq * sizeof(int32_t), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(int32_t), st);
   int rc = e == cudaSuccess ? kOk : cuda_error(e, "learned search buffers");
   if (rc == kOk) rc = launch_radius(m, base.query, base.nq, base.qStride, base.maxRadius, radii, nullptr, st);
+  if (rc == kOk && ordered) rc = leaf_order(c, base.query, base.nq, base.qStride, order, st);
   if (rc == kOk) {
     KnnArgs a = base;
     a.maxRadii = radii;
     a.found = found;
     a.evStart = h.evStart;
     a.evStop = h.evStop;
-    rc = search_plain(c, a, st);
+    rc = search_given(c, a, order, st);
   }
   if (rc == kOk) {
     if (c.dtype == NABO_CUDA_FLOAT32)
-      k_collect_misses<float><<<ceil_div(base.nq, 256), 256, 0, st>>>(found, static_cast<const float*>(radii), base.nq,
-                                                                        base.k, base.maxRadius, list, count);
+      k_collect_misses<float><<<ceil_div(base.nq, 256), 256, 0, st>>>(
+          order, found, static_cast<const float*>(radii), base.nq, base.k, base.maxRadius, list, count);
     else
       k_collect_misses<double><<<ceil_div(base.nq, 256), 256, 0, st>>>(
-          found, static_cast<const double*>(radii), base.nq, base.k, base.maxRadius, list, count);
+          order, found, static_cast<const double*>(radii), base.nq, base.k, base.maxRadius, list, count);
     e = cudaGetLastError();
     if (e != cudaSuccess) rc = cuda_error(e, "miss compaction");
   }
@@ -971,6 +1001,7 @@ int knn_learned(const nabo_cuda_search* s, const RadiusModel& m, const KnnArgs& 
   if (found) scratch_free(found, st);
   if (list) scratch_free(list, st);
   if (count) scratch_free(count, st);
+  if (order) scratch_free(order, st);
   return rc;
 }
 

@@ -172,7 +172,34 @@ int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t
   return kOk;
 }
 
+// Leaf order of the queries (the permutation the kd-tree search uses
+// internally), written to `order` (nq entries, device).
+template <typename T, int D>
+int knn_leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int32_t* order,
+                   cudaStream_t stream) {
+  if (nq == 0) return kOk;
+  uint32_t *hist = nullptr, *cell = nullptr, *rank = nullptr;
+  cudaError_t e = scratch_alloc((void**)&hist, (size_t)c.nodeCount * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&cell, (size_t)nq * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&rank, (size_t)nq * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(hist, 0, (size_t)c.nodeCount * sizeof(uint32_t), stream);
+  int rc = kOk;
+  if (e == cudaSuccess) {
+    k_leaf_cells<T, D><<<ceil_div(nq, 256), 256, 0, stream>>>(static_cast<const Node<T>*>(c.nodes),
+                                                              static_cast<const T*>(query), nq, qStride, c.dim, cell,
+                                                              rank, hist);
+    rc = order_by_cells(cell, rank, hist, c.nodeCount, nq, order, stream);
+  } else {
+    rc = cuda_error(e, "query ordering");
+  }
+  if (hist) scratch_free(hist, stream);
+  if (cell) scratch_free(cell, stream);
+  if (rank) scratch_free(rank, stream);
+  return rc;
+}
+
 #define NABO_SEARCH_INSTANTIATE(T, D)                                              \
+  template int knn_leaf_order<T, D>(const DeviceCloud&, const void*, int64_t, int64_t, int32_t*, cudaStream_t); \
   template int knn_kdtree<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
   template int knn_bruteforce<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
   template int knn_kdtree_given_order<T, D>(const DeviceCloud&, const KnnArgs&, const int32_t*, cudaStream_t);
