@@ -73,7 +73,9 @@ typedef struct nabo_cuda_params {
                              packet -- the 32 queries of a warp walk one node
                              sequence, each pruning for itself -- for exact
                              searches (epsilon 0) without TOUCH_STATISTICS */
-  int32_t reserved[4];
+  int32_t threadsPerBlock; /* batched search kernel block size: 32, 64 or 128
+                              (0 = 128); chosen by the autotuner */
+  int32_t reserved[3];
 } nabo_cuda_params;
 
 typedef struct nabo_cuda_search nabo_cuda_search; /* opaque */
@@ -231,6 +233,49 @@ int nabo_cuda_radius_model_gradients(const nabo_cuda_radius_model* m, const floa
  * margin and the voxel size (rebuilding the voxel tables) from meta. */
 int nabo_cuda_radius_model_get(const nabo_cuda_radius_model* m, float* params, float* meta);
 int nabo_cuda_radius_model_set(nabo_cuda_radius_model* m, const float* params, const float* meta);
+
+/* ---------------------------------------------------------------------
+ * Batches of clouds (no counterpart in the reference, which builds one
+ * tree per object). The clouds of a batch are stored back to back (cloud c
+ * = columns [sum of earlier counts, + pointCounts[c]) of a dim x total
+ * column-major array, stride dim); their kd-trees -- each the tree the
+ * reference builds for that cloud alone -- are built together, and all
+ * their queries are searched by one kernel launch, each in its cloud's
+ * tree with the k given for that cloud. Self matches are not allowed
+ * (k <= points - 1 per cloud). Results of cloud c's queries follow those
+ * of the earlier clouds (k_c x nq_c, column-major per cloud), with indices
+ * local to the cloud. */
+typedef struct nabo_cuda_batch nabo_cuda_batch; /* opaque */
+
+/* maxLevels: levels of the level-synchronous top build (segments of more
+ * than 256 points), run without host synchronisation (0 = 48). A tree
+ * needing more is reported by nabo_cuda_batch_status. params: bucketSize
+ * and threadsPerBlock (may be NULL). */
+int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* pointCounts,
+                           const nabo_cuda_params* params, int maxLevels, nabo_cuda_batch** out);
+int nabo_cuda_batch_destroy(nabo_cuda_batch* b);
+/* Queries per cloud and k per cloud (HOST arrays, nClouds each). */
+int nabo_cuda_batch_set_queries(nabo_cuda_batch* b, const int64_t* queryCounts, const int32_t* k);
+/* Builds all trees from `clouds` (DEVICE); stream-ordered, no host sync. */
+int nabo_cuda_batch_build_device(nabo_cuda_batch* b, const void* clouds, void* stream);
+/* Searches all queries (DEVICE, dim x total queries, stride dim); results
+ * into DEVICE arrays of sum(k_c * nq_c) entries. Stream-ordered. */
+int nabo_cuda_batch_knn_device(nabo_cuda_batch* b, const void* queries, double epsilon, unsigned optionFlags,
+                               double maxRadius, int32_t* indices, void* dists2, void* stream);
+/* Build + search as one CUDA graph: captured on the first call for these
+ * buffers and arguments, replayed by later calls with the same ones (new
+ * coordinates written into the same buffers). */
+int nabo_cuda_batch_run(nabo_cuda_batch* b, const void* clouds, const void* queries, double epsilon,
+                        unsigned optionFlags, double maxRadius, int32_t* indices, void* dists2, void* stream);
+/* Synchronises the device, then info[0] = status bits (1 non-finite input,
+ * 2 capacity or level limit exceeded, 4 a tree taller than the search
+ * stack), [1] total nodes, [2] tallest tree, [3] top levels run,
+ * [4] result entries, [5] queries, [6] points, [7] clouds. */
+int nabo_cuda_batch_status(nabo_cuda_batch* b, int64_t info[8]);
+/* One cloud's tree (indices local to the cloud), as nabo_cuda_export_tree;
+ * with cutDim NULL only *nodeCount is set. */
+int nabo_cuda_batch_export_tree(nabo_cuda_batch* b, int cloud, int64_t* nodeCount, int32_t* cutDim, void* cutVal,
+                                uint32_t* right, uint32_t* bucketStart, uint32_t* bucketSize, int32_t* buckets);
 
 /* Object properties: the reference's public members dim, minBound,
  * maxBound, creationOptionFlags (nabo/nabo.h:274-282) plus build facts.

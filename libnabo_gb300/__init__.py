@@ -471,3 +471,117 @@ class RadiusModel:
             None if touched is None else ctypes.c_void_p(touched.data_ptr()),
             None if fallbacks is None else ctypes.c_void_p(fallbacks.data_ptr()), ctypes.c_void_p(st)))
         return idx, d2
+
+
+class BatchSearch:
+    """Many clouds of uneven sizes built and searched together.
+
+    The clouds are stored back to back in one (total_points, dim) CUDA tensor
+    (cloud c = the next ``point_counts[c]`` rows); each gets the kd-tree the
+    reference builds for it alone, all built in one forest build, and all
+    queries (back to back likewise, ``query_counts[c]`` rows for cloud c) are
+    searched by one kernel launch, each with its cloud's ``k``. ``run``
+    captures build + search into a CUDA graph on first use and replays it.
+    Results come back flat: cloud c's (nq_c, k_c) block after the earlier
+    ones; ``split`` cuts them per cloud. Self matches are not allowed.
+    """
+
+    def __init__(self, point_counts, dim: int = 3, dtype=np.float32, bucketSize: int = 8, threadsPerBlock: int = 128,
+                 maxLevels: int = 48):
+        counts = np.ascontiguousarray(np.asarray(point_counts, dtype=np.int64))
+        self.point_counts = counts
+        self.dim = int(dim)
+        self.dtype = np.dtype(dtype)
+        self._b = ctypes.c_void_p()
+        p = nabo_cuda_params()
+        _lib.nabo_cuda_params_init(ctypes.byref(p))
+        p.bucketSize = int(bucketSize)
+        p.threadsPerBlock = int(threadsPerBlock)
+        _check(_lib.nabo_cuda_batch_create(_dtype_code(self.dtype), self.dim, len(counts), _ptr(counts),
+                                           ctypes.byref(p), int(maxLevels), ctypes.byref(self._b)))
+        self.query_counts = None
+        self.k = None
+
+    def close(self) -> None:
+        b = getattr(self, "_b", None)
+        if b is not None and b.value:
+            _lib.nabo_cuda_batch_destroy(b)
+            self._b = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_queries(self, query_counts, k) -> None:
+        qc = np.ascontiguousarray(np.asarray(query_counts, dtype=np.int64))
+        kk = np.ascontiguousarray(np.broadcast_to(np.asarray(k, dtype=np.int32), qc.shape))
+        _check(_lib.nabo_cuda_batch_set_queries(self._b, _ptr(qc), _ptr(kk)))
+        self.query_counts, self.k = qc, kk
+        self.result_entries = int(np.sum(qc * kk))
+
+    def _outputs(self, device):
+        import torch
+        tdt = torch.float32 if self.dtype == np.float32 else torch.float64
+        return (torch.empty(self.result_entries, dtype=torch.int32, device=device),
+                torch.empty(self.result_entries, dtype=tdt, device=device))
+
+    def build(self, clouds, stream=None) -> None:
+        import torch
+        st = stream if stream is not None else torch.cuda.current_stream(clouds.device).cuda_stream
+        _check(_lib.nabo_cuda_batch_build_device(self._b, ctypes.c_void_p(clouds.data_ptr()), ctypes.c_void_p(st)))
+
+    def knn(self, queries, epsilon: float = 0.0, optionFlags: int = 0, maxRadius: float = np.inf, out=None,
+            stream=None):
+        import torch
+        idx, d2 = out if out is not None else self._outputs(queries.device)
+        st = stream if stream is not None else torch.cuda.current_stream(queries.device).cuda_stream
+        _check(_lib.nabo_cuda_batch_knn_device(self._b, ctypes.c_void_p(queries.data_ptr()), float(epsilon),
+                                               int(optionFlags), float(maxRadius), ctypes.c_void_p(idx.data_ptr()),
+                                               ctypes.c_void_p(d2.data_ptr()), ctypes.c_void_p(st)))
+        return idx, d2
+
+    def run(self, clouds, queries, epsilon: float = 0.0, optionFlags: int = 0, maxRadius: float = np.inf,
+            out=None, stream=None):
+        """Build + search as one CUDA graph launch (captured on first use)."""
+        import torch
+        idx, d2 = out if out is not None else self._outputs(queries.device)
+        st = stream if stream is not None else torch.cuda.current_stream(queries.device).cuda_stream
+        _check(_lib.nabo_cuda_batch_run(self._b, ctypes.c_void_p(clouds.data_ptr()),
+                                        ctypes.c_void_p(queries.data_ptr()), float(epsilon), int(optionFlags),
+                                        float(maxRadius), ctypes.c_void_p(idx.data_ptr()),
+                                        ctypes.c_void_p(d2.data_ptr()), ctypes.c_void_p(st)))
+        return idx, d2
+
+    def status(self) -> dict:
+        info = (ctypes.c_int64 * 8)()
+        _check(_lib.nabo_cuda_batch_status(self._b, info))
+        return dict(ok=info[0] == 0, flags=int(info[0]), nodes=int(info[1]), height=int(info[2]),
+                    levels=int(info[3]), results=int(info[4]), queries=int(info[5]), points=int(info[6]),
+                    clouds=int(info[7]))
+
+    def split(self, flat):
+        """Per-cloud (nq_c, k_c) views of a flat result array."""
+        outs, o = [], 0
+        for nq, k in zip(self.query_counts, self.k):
+            outs.append(flat[o:o + nq * k].reshape(nq, k))
+            o += nq * k
+        return outs
+
+    def export_tree(self, cloud: int) -> dict:
+        count = ctypes.c_int64(0)
+        _check(_lib.nabo_cuda_batch_export_tree(self._b, int(cloud), ctypes.byref(count), None, None, None, None,
+                                                None, None))
+        n = int(count.value)
+        cut_dim = np.zeros(n, np.int32)
+        cut_val = np.zeros(n, self.dtype)
+        right = np.zeros(n, np.uint32)
+        b_start = np.zeros(n, np.uint32)
+        b_count = np.zeros(n, np.uint32)
+        buckets = np.zeros(int(self.point_counts[cloud]), np.int32)
+        _check(_lib.nabo_cuda_batch_export_tree(self._b, int(cloud), ctypes.byref(count), _ptr(cut_dim),
+                                                _ptr(cut_val), _ptr(right), _ptr(b_start), _ptr(b_count),
+                                                _ptr(buckets)))
+        return dict(cut_dim=cut_dim, cut_val=cut_val, right=right, bucket_start=b_start, bucket_count=b_count,
+                    buckets=buckets)

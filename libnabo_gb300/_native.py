@@ -36,6 +36,14 @@ SIGNATURES = {
     "nabo_cuda_radius_model_gradients": (_I, [_P, _P, _P, _I64, _P, _P]),
     "nabo_cuda_radius_model_get": (_I, [_P, _P, _P]),
     "nabo_cuda_radius_model_set": (_I, [_P, _P, _P]),
+    "nabo_cuda_batch_create": (_I, [_I, _I, _I, _P, _P, _I, _P]),
+    "nabo_cuda_batch_destroy": (_I, [_P]),
+    "nabo_cuda_batch_set_queries": (_I, [_P, _P, _P]),
+    "nabo_cuda_batch_build_device": (_I, [_P, _P, _P]),
+    "nabo_cuda_batch_knn_device": (_I, [_P, _P, _D, _U, _D, _P, _P, _P]),
+    "nabo_cuda_batch_run": (_I, [_P, _P, _P, _D, _U, _D, _P, _P, _P]),
+    "nabo_cuda_batch_status": (_I, [_P, _P]),
+    "nabo_cuda_batch_export_tree": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P]),
     "nabo_cuda_get_info": (_I, [_P, _P]),
     "nabo_cuda_get_bounds": (_I, [_P, _P, _P]),
     "nabo_cuda_export_tree": (_I, [_P, _P, _P, _P, _P, _P, _P]),
@@ -65,7 +73,8 @@ class nabo_cuda_params(ctypes.Structure):
         ("bucketSize", ctypes.c_uint32),
         ("queryOrdering", ctypes.c_int32),
         ("traversal", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 4),
+        ("threadsPerBlock", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 3),
     ]
 
 

@@ -1,0 +1,93 @@
+"""Autotuner for batched searches.
+
+Times the batched build + search (one CUDA-graph launch) on a sample of the
+batch for every candidate configuration -- kd-tree bucket size and threads
+per block of the search kernel -- and keeps the fastest. Results do not
+depend on the choice (every configuration returns the exact neighbours);
+only speed does. Choices are cached per workload shape (dimension, scalar
+type, largest k, point-count scale), in memory and optionally in a JSON file.
+"""
+from __future__ import annotations
+
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+CANDIDATES = {"bucketSize": (4, 6, 8, 12, 16), "threadsPerBlock": (64, 128)}
+_cache: dict = {}
+
+
+def shape_key(point_counts, dim, dtype, k) -> str:
+    mean = float(np.mean(point_counts))
+    return f"d{dim}-{np.dtype(dtype).name}-k{int(np.max(k))}-n2^{int(round(math.log2(max(mean, 1.0))))}"
+
+
+def _time_config(clouds, queries, pc, qc, ks, dim, dtype, bucket, tpb, repeats):
+    import torch
+
+    from . import BatchSearch
+    b = BatchSearch(pc, dim=dim, dtype=dtype, bucketSize=bucket, threadsPerBlock=tpb)
+    b.set_queries(qc, ks)
+    out = b._outputs(queries.device)
+    b.run(clouds, queries, out=out)  # capture + first launch
+    torch.cuda.synchronize()
+    st = b.status()
+    if not st["ok"]:
+        b.close()
+        return math.inf, st
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = math.inf
+    for _ in range(repeats):
+        ev0.record()
+        b.run(clouds, queries, out=out)
+        ev1.record()
+        torch.cuda.synchronize()
+        best = min(best, ev0.elapsed_time(ev1))
+    b.close()
+    return best, st
+
+
+def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int = 64, repeats: int = 3,
+         cache_path: str | None = None, seed: int = 0) -> dict:
+    """Best {bucketSize, threadsPerBlock} for a batch (lists of (n_c, dim) arrays)."""
+    import torch
+    ks = np.broadcast_to(np.asarray(k, dtype=np.int32), (len(cloud_list),))
+    pcs = np.array([c.shape[0] for c in cloud_list], np.int64)
+    key = shape_key(pcs, dim, dtype, ks)
+    if key in _cache:
+        return dict(_cache[key], key=key, cached=True)
+    if cache_path and os.path.exists(cache_path):
+        with open(cache_path) as f:
+            disk = json.load(f)
+        if key in disk:
+            _cache[key] = disk[key]
+            return dict(disk[key], key=key, cached=True)
+    rng = np.random.default_rng(seed)
+    pick = np.sort(rng.choice(len(cloud_list), min(sample, len(cloud_list)), replace=False))
+    pc = pcs[pick]
+    qc = np.array([query_list[i].shape[0] for i in pick], np.int64)
+    clouds = torch.from_numpy(np.concatenate([cloud_list[i] for i in pick]).astype(dtype)).cuda()
+    queries = torch.from_numpy(np.concatenate([query_list[i] for i in pick]).astype(dtype)).cuda()
+    trials = []
+    t0 = time.perf_counter()
+    for bucket in CANDIDATES["bucketSize"]:
+        for tpb in CANDIDATES["threadsPerBlock"]:
+            ms, st = _time_config(clouds, queries, pc, qc, ks[pick], dim, dtype, bucket, tpb, repeats)
+            trials.append({"bucketSize": bucket, "threadsPerBlock": tpb, "ms": ms, "levels": st["levels"]})
+    best = min(trials, key=lambda t: t["ms"])
+    choice = {"bucketSize": best["bucketSize"], "threadsPerBlock": best["threadsPerBlock"],
+              "maxLevels": max(8, best["levels"] + 8), "sample_ms": best["ms"]}
+    _cache[key] = choice
+    if cache_path:
+        disk = {}
+        if os.path.exists(cache_path):
+            with open(cache_path) as f:
+                disk = json.load(f)
+        disk[key] = choice
+        os.makedirs(os.path.dirname(os.path.abspath(cache_path)), exist_ok=True)
+        with open(cache_path, "w") as f:
+            json.dump(disk, f, indent=1)
+    return dict(choice, key=key, cached=False, trials=trials, tune_s=time.perf_counter() - t0)

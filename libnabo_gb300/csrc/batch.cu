@@ -1,0 +1,425 @@
+// batch.cu -- many clouds of uneven sizes built and searched together.
+//
+// The clouds of a batch are stored back to back; their trees are built in
+// one forest build (all segments of all clouds share each level's kernels;
+// a fixed number of levels runs with no host synchronisation) and all their
+// queries are searched by one launch of the kd-tree kernel, each query in
+// its own cloud's tree with that cloud's k. nabo_cuda_batch_run captures
+// build + search into a CUDA graph on first use and replays it afterwards,
+// so a new batch of the same shape (new coordinates written to the same
+// buffers) costs one graph launch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "internal.cuh"
+#include "nabo_gb300.h"
+
+using namespace nabo_gb300;
+
+struct nabo_cuda_batch {
+  int dtype = 0;
+  int dim = 0;
+  int dpad = 0;
+  int nClouds = 0;
+  int64_t nTotal = 0;
+  unsigned bucketSize = 8;
+  int maxLevels = 48;
+  int blockSize = 128;
+  int device = 0;
+  int64_t* dOff = nullptr;
+  void* recs = nullptr;
+  void* nodes = nullptr;
+  int64_t* nodeOffset = nullptr;
+  void* rootBox = nullptr;
+  int* status = nullptr;
+  // query plan
+  int64_t nq = 0;
+  int kMax = 0;
+  int64_t outTotal = 0;
+  int64_t* dQOff = nullptr;
+  int64_t* dOutOff = nullptr;
+  int32_t* dK = nullptr;
+  int32_t* order = nullptr;
+  uint32_t* hist = nullptr;
+  uint32_t* cell = nullptr;
+  uint32_t* rank = nullptr;
+  // captured graph and the arguments it was captured with
+  cudaGraphExec_t exec = nullptr;
+  const void* gClouds = nullptr;
+  const void* gQuery = nullptr;
+  int32_t* gIdx = nullptr;
+  void* gD2 = nullptr;
+  double gEps = 0.0, gRadius = 0.0;
+  unsigned gFlags = 0;
+};
+
+namespace {
+
+struct Guard {
+  int prev = -1;
+  explicit Guard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+  }
+  ~Guard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+int pad_dim(int dim) {
+  if (dim <= 2) return 2;
+  if (dim == 3) return 3;
+  if (dim == 4) return 4;
+  if (dim <= 8) return 8;
+  if (dim <= 16) return 16;
+  return -1;
+}
+
+void free_query_plan(nabo_cuda_batch* b) {
+  for (void* p : {(void*)b->dQOff, (void*)b->dOutOff, (void*)b->dK, (void*)b->order, (void*)b->hist,
+                  (void*)b->cell, (void*)b->rank})
+    if (p) cudaFree(p);
+  b->dQOff = b->dOutOff = nullptr;
+  b->dK = b->order = nullptr;
+  b->hist = b->cell = b->rank = nullptr;
+}
+
+void drop_graph(nabo_cuda_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+}
+
+int build(nabo_cuda_batch* b, const void* clouds, cudaStream_t st) {
+  ForestOut f;
+  f.recs = b->recs;
+  f.nodes = b->nodes;
+  f.nodeOffset = b->nodeOffset;
+  const size_t es = b->dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  f.rootLo = b->rootBox;
+  f.rootHi = static_cast<unsigned char*>(b->rootBox) + (size_t)b->nClouds * kMaxDim * es;
+  f.status = b->status;
+#define NABO_B_CASE(TT, DD)                                                                                \
+  if (b->dpad == DD)                                                                                       \
+    return build_forest<TT, DD>(static_cast<const TT*>(clouds), b->nTotal, b->dim, b->dim, b->bucketSize, \
+                                b->dOff, b->nClouds, b->maxLevels, st, &f);
+  if (b->dtype == NABO_CUDA_FLOAT32) {
+    NABO_B_CASE(float, 2) NABO_B_CASE(float, 3) NABO_B_CASE(float, 4) NABO_B_CASE(float, 8) NABO_B_CASE(float, 16)
+  } else {
+    NABO_B_CASE(double, 2) NABO_B_CASE(double, 3) NABO_B_CASE(double, 4) NABO_B_CASE(double, 8)
+    NABO_B_CASE(double, 16)
+  }
+#undef NABO_B_CASE
+  return set_error(kErrInternal, "bad dispatch");
+}
+
+int search(nabo_cuda_batch* b, const void* query, double eps, unsigned flags, double maxRadius, int32_t* indices,
+           void* dists2, cudaStream_t st) {
+  BatchArgs a;
+  a.nodes = b->nodes;
+  a.recs = b->recs;
+  a.dim = b->dim;
+  a.nClouds = b->nClouds;
+  a.nodeCap = 2 * b->nTotal;
+  a.nodeOffset = b->nodeOffset;
+  a.qOffset = b->dQOff;
+  a.outOffset = b->dOutOff;
+  a.kOf = b->dK;
+  a.kMax = b->kMax;
+  a.query = query;
+  a.nq = b->nq;
+  a.qStride = b->dim;
+  a.eps = eps;
+  a.optionFlags = flags;
+  a.maxRadius = maxRadius;
+  a.indices = indices;
+  a.dists2 = dists2;
+  a.order = b->order;
+  a.hist = b->hist;
+  a.cell = b->cell;
+  a.rank = b->rank;
+  a.blockSize = b->blockSize;
+#define NABO_B_CASE(TT, DD) \
+  if (b->dpad == DD) return knn_batch<TT, DD>(a, st);
+  if (b->dtype == NABO_CUDA_FLOAT32) {
+    NABO_B_CASE(float, 2) NABO_B_CASE(float, 3) NABO_B_CASE(float, 4) NABO_B_CASE(float, 8) NABO_B_CASE(float, 16)
+  } else {
+    NABO_B_CASE(double, 2) NABO_B_CASE(double, 3) NABO_B_CASE(double, 4) NABO_B_CASE(double, 8)
+    NABO_B_CASE(double, 16)
+  }
+#undef NABO_B_CASE
+  return set_error(kErrInternal, "bad dispatch");
+}
+
+}  // namespace
+
+extern "C" {
+
+int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* pointCounts,
+                           const nabo_cuda_params* params, int maxLevels, nabo_cuda_batch** out) {
+  if (!out || !pointCounts) return set_error(kErrArgument, "NULL argument");
+  *out = nullptr;
+  if (dtype != NABO_CUDA_FLOAT32 && dtype != NABO_CUDA_FLOAT64) return set_error(kErrArgument, "unknown scalar type");
+  if (dim <= 0) return set_error(kErrArgument, "Your space must have at least one dimension");
+  if (nClouds < 1) return set_error(kErrArgument, "a batch needs at least one cloud");
+  const int dpad = pad_dim(dim);
+  if (dpad < 0) return set_error(kErrUnsupported, "the CUDA search types support at most 16 dimensions");
+  nabo_cuda_params p;
+  nabo_cuda_params_init(&p);
+  if (params) {
+    p.bucketSize = params->bucketSize;
+    p.threadsPerBlock = params->threadsPerBlock;
+  }
+  if (p.bucketSize < 2)
+    return set_error(kErrArgument, "Requested bucket size " + std::to_string(p.bucketSize) + ", but must be larger than 2");
+  int64_t total = 0;
+  for (int c = 0; c < nClouds; ++c) {
+    if (pointCounts[c] <= 0) return set_error(kErrArgument, "Cloud has no points");
+    total += pointCounts[c];
+  }
+  if (total > (int64_t)1 << 30) return set_error(kErrUnsupported, "a batch holds at most 2^30 points");
+  nabo_cuda_batch* b = new nabo_cuda_batch();
+  b->dtype = dtype;
+  b->dim = dim;
+  b->dpad = dpad;
+  b->nClouds = nClouds;
+  b->nTotal = total;
+  b->bucketSize = p.bucketSize;
+  b->maxLevels = maxLevels > 0 ? maxLevels : 48;
+  b->blockSize = p.threadsPerBlock > 0 ? p.threadsPerBlock : 128;
+  if (b->blockSize != 32 && b->blockSize != 64 && b->blockSize != 128) {
+    delete b;
+    return set_error(kErrArgument, "threads per block must be 32, 64 or 128");
+  }
+  cudaGetDevice(&b->device);
+  const size_t es = dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  const size_t recBytes = ((size_t)dpad * es + 4 + 15) / 16 * 16;
+  const size_t nodeBytes = dtype == NABO_CUDA_FLOAT32 ? 8 : 16;
+  std::vector<int64_t> off((size_t)nClouds + 1, 0);
+  for (int c = 0; c < nClouds; ++c) off[(size_t)c + 1] = off[(size_t)c] + pointCounts[c];
+  cudaError_t e = cudaMalloc((void**)&b->dOff, off.size() * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->recs, (size_t)total * recBytes);
+  if (e == cudaSuccess) e = cudaMalloc(&b->nodes, (size_t)2 * total * nodeBytes);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->nodeOffset, off.size() * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->rootBox, (size_t)2 * nClouds * kMaxDim * es);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->status, 4 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(b->dOff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(b->status, 0, 4 * sizeof(int));
+  if (e != cudaSuccess) {
+    nabo_cuda_batch_destroy(b);
+    return cuda_error(e, "batch allocation");
+  }
+  *out = b;
+  return kOk;
+}
+
+int nabo_cuda_batch_destroy(nabo_cuda_batch* b) {
+  if (!b) return kOk;
+  Guard g(b->device);
+  drop_graph(b);
+  free_query_plan(b);
+  for (void* p : {(void*)b->dOff, b->recs, b->nodes, (void*)b->nodeOffset, b->rootBox, (void*)b->status})
+    if (p) cudaFree(p);
+  delete b;
+  return kOk;
+}
+
+int nabo_cuda_batch_set_queries(nabo_cuda_batch* b, const int64_t* queryCounts, const int32_t* k) {
+  if (!b || !queryCounts || !k) return set_error(kErrArgument, "NULL argument");
+  Guard g(b->device);
+  int64_t nq = 0, outTotal = 0;
+  int kMax = 0;
+  std::vector<int64_t> qoff((size_t)b->nClouds + 1, 0), ooff((size_t)b->nClouds + 1, 0);
+  std::vector<int32_t> ks((size_t)b->nClouds);
+  std::vector<int64_t> counts((size_t)b->nClouds);
+  std::vector<int64_t> hoff((size_t)b->nClouds + 1);
+  cudaError_t e = cudaMemcpy(hoff.data(), b->dOff, hoff.size() * sizeof(int64_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "batch offsets");
+  for (int c = 0; c < b->nClouds; ++c) {
+    const int64_t pts = hoff[(size_t)c + 1] - hoff[(size_t)c];
+    if (queryCounts[c] < 0) return set_error(kErrArgument, "negative query count");
+    // nabo/nabo.cpp:105-115, self match forbidden: k <= points - 1
+    if (k[c] < 1 || k[c] > pts - 1)
+      return set_error(kErrArgument, "Requesting more points (" + std::to_string(k[c]) +
+                                         ") than available in cloud minus 1 (" + std::to_string(pts - 1) +
+                                         ") (as self match is forbidden)");
+    if (k[c] > 32) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+    ks[(size_t)c] = k[c];
+    kMax = std::max(kMax, k[c]);
+    qoff[(size_t)c + 1] = qoff[(size_t)c] + queryCounts[c];
+    ooff[(size_t)c + 1] = ooff[(size_t)c] + queryCounts[c] * k[c];
+  }
+  nq = qoff.back();
+  outTotal = ooff.back();
+  if (nq > (int64_t)1 << 30) return set_error(kErrUnsupported, "a batch searches at most 2^30 queries");
+  drop_graph(b);
+  free_query_plan(b);
+  b->nq = nq;
+  b->kMax = kMax;
+  b->outTotal = outTotal;
+  e = cudaMalloc((void**)&b->dQOff, qoff.size() * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->dOutOff, ooff.size() * sizeof(int64_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->dK, ks.size() * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->order, (size_t)std::max<int64_t>(nq, 1) * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->cell, (size_t)std::max<int64_t>(nq, 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->rank, (size_t)std::max<int64_t>(nq, 1) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->hist, (size_t)2 * b->nTotal * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemcpy(b->dQOff, qoff.data(), qoff.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->dOutOff, ooff.data(), ooff.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(b->dK, ks.data(), ks.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    free_query_plan(b);
+    return cuda_error(e, "batch query plan");
+  }
+  return kOk;
+}
+
+int nabo_cuda_batch_build_device(nabo_cuda_batch* b, const void* clouds, void* stream) {
+  if (!b || !clouds) return set_error(kErrArgument, "NULL argument");
+  Guard g(b->device);
+  return build(b, clouds, static_cast<cudaStream_t>(stream));
+}
+
+int nabo_cuda_batch_knn_device(nabo_cuda_batch* b, const void* queries, double epsilon, unsigned optionFlags,
+                               double maxRadius, int32_t* indices, void* dists2, void* stream) {
+  if (!b) return set_error(kErrArgument, "NULL batch");
+  if (!b->dQOff) return set_error(kErrArgument, "call nabo_cuda_batch_set_queries first");
+  if (optionFlags & NABO_ALLOW_SELF_MATCH)
+    return set_error(kErrUnsupported, "batched searches forbid self matches (the plan checks k <= points - 1)");
+  if (optionFlags > 3) return set_error(kErrArgument, "OR-ed value of option flags is larger than maximal valid value (3)");
+  if (b->nq == 0) return kOk;
+  if (!queries || !indices || !dists2) return set_error(kErrArgument, "NULL query or result buffer");
+  Guard g(b->device);
+  return search(b, queries, epsilon, optionFlags, maxRadius, indices, dists2, static_cast<cudaStream_t>(stream));
+}
+
+int nabo_cuda_batch_run(nabo_cuda_batch* b, const void* clouds, const void* queries, double epsilon,
+                        unsigned optionFlags, double maxRadius, int32_t* indices, void* dists2, void* stream) {
+  if (!b || !clouds) return set_error(kErrArgument, "NULL argument");
+  if (!b->dQOff) return set_error(kErrArgument, "call nabo_cuda_batch_set_queries first");
+  if (optionFlags & NABO_ALLOW_SELF_MATCH)
+    return set_error(kErrUnsupported, "batched searches forbid self matches (the plan checks k <= points - 1)");
+  if (b->nq > 0 && (!queries || !indices || !dists2)) return set_error(kErrArgument, "NULL query or result buffer");
+  Guard g(b->device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const bool same = b->exec && b->gClouds == clouds && b->gQuery == queries && b->gIdx == indices &&
+                    b->gD2 == dists2 && b->gEps == epsilon && b->gFlags == optionFlags && b->gRadius == maxRadius;
+  if (!same) {
+    drop_graph(b);
+    cudaStream_t cap;
+    cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_error(e, "capture stream");
+    set_capture_allocations(true);
+    e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    int rc = e == cudaSuccess ? kOk : cuda_error(e, "cudaStreamBeginCapture");
+    if (rc == kOk) rc = build(b, clouds, cap);
+    if (rc == kOk && b->nq > 0) rc = search(b, queries, epsilon, optionFlags, maxRadius, indices, dists2, cap);
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(cap, &graph);
+    set_capture_allocations(false);
+    if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, "cudaStreamEndCapture");
+    if (rc == kOk) {
+      e = cudaGraphInstantiate(&b->exec, graph, 0);
+      if (e != cudaSuccess) rc = cuda_error(e, "cudaGraphInstantiate");
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cap);
+    if (rc != kOk) {
+      b->exec = nullptr;
+      return rc;
+    }
+    b->gClouds = clouds;
+    b->gQuery = queries;
+    b->gIdx = indices;
+    b->gD2 = dists2;
+    b->gEps = epsilon;
+    b->gFlags = optionFlags;
+    b->gRadius = maxRadius;
+  }
+  const cudaError_t e = cudaGraphLaunch(b->exec, st);
+  if (e != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
+  return kOk;
+}
+
+int nabo_cuda_batch_status(nabo_cuda_batch* b, int64_t info[8]) {
+  if (!b || !info) return set_error(kErrArgument, "NULL argument");
+  Guard g(b->device);
+  int hs[4];
+  int64_t total = 0;
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(hs, b->status, sizeof(hs), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(&total, b->nodeOffset + b->nClouds, sizeof(int64_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "batch status");
+  // a tree taller than the search's stack (256) is reported as an overflow
+  info[0] = (hs[0] ? 1 : 0) | (hs[1] ? 2 : 0) | (hs[2] > 256 ? 4 : 0);
+  info[1] = total;
+  info[2] = hs[2];
+  info[3] = hs[3];
+  info[4] = b->outTotal;
+  info[5] = b->nq;
+  info[6] = b->nTotal;
+  info[7] = b->nClouds;
+  return kOk;
+}
+
+int nabo_cuda_batch_export_tree(nabo_cuda_batch* b, int cloud, int64_t* nodeCount, int32_t* cutDim, void* cutVal,
+                                uint32_t* right, uint32_t* bucketStart, uint32_t* bucketSize, int32_t* buckets) {
+  if (!b || cloud < 0 || cloud >= b->nClouds || !nodeCount) return set_error(kErrArgument, "bad argument");
+  Guard g(b->device);
+  int64_t noff[2], poff[2];
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(noff, b->nodeOffset + cloud, sizeof(noff), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(poff, b->dOff + cloud, sizeof(poff), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "batch export");
+  const int64_t cnt = noff[1] - noff[0];
+  if (!cutDim) {
+    *nodeCount = cnt;
+    return kOk;
+  }
+  if (*nodeCount < cnt) return set_error(kErrArgument, "arrays too small");
+  *nodeCount = cnt;
+  const bool f32 = b->dtype == NABO_CUDA_FLOAT32;
+  const size_t nodeBytes = f32 ? 8 : 16;
+  std::vector<unsigned char> nodes((size_t)cnt * nodeBytes);
+  e = cudaMemcpy(nodes.data(), static_cast<unsigned char*>(b->nodes) + noff[0] * nodeBytes, nodes.size(),
+                 cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_error(e, "batch export nodes");
+  for (int64_t i = 0; i < cnt; ++i) {
+    const unsigned char* p = nodes.data() + i * nodeBytes;
+    uint32_t meta, start;
+    std::memcpy(&meta, p, 4);
+    std::memcpy(&start, p + 4, 4);
+    const bool leaf = node_is_leaf(meta);
+    cutDim[i] = leaf ? -1 : (int32_t)node_dim(meta);
+    if (right) right[i] = leaf ? 0u : node_payload(meta) - (uint32_t)noff[0];
+    if (bucketStart) bucketStart[i] = leaf ? start - (uint32_t)poff[0] : 0u;
+    if (bucketSize) bucketSize[i] = leaf ? node_payload(meta) : 0u;
+    if (cutVal) {
+      if (f32) {
+        float v = 0.0f;
+        if (!leaf) std::memcpy(&v, p + 4, 4);
+        static_cast<float*>(cutVal)[i] = v;
+      } else {
+        double v = 0.0;
+        if (!leaf) std::memcpy(&v, p + 8, 8);
+        static_cast<double*>(cutVal)[i] = v;
+      }
+    }
+  }
+  if (buckets) {
+    const size_t es = f32 ? 4 : 8;
+    const size_t recBytes = ((size_t)b->dpad * es + 4 + 15) / 16 * 16;
+    const int64_t n = poff[1] - poff[0];
+    std::vector<unsigned char> recs((size_t)n * recBytes);
+    e = cudaMemcpy(recs.data(), static_cast<unsigned char*>(b->recs) + poff[0] * recBytes, recs.size(),
+                   cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_error(e, "batch export buckets");
+    for (int64_t i = 0; i < n; ++i) std::memcpy(buckets + i, recs.data() + i * recBytes + b->dpad * es, 4);
+  }
+  return kOk;
+}
+
+}  // extern "C"

@@ -237,6 +237,18 @@ struct TopNodes {
   int* pre;
 };
 
+// Level bookkeeping kept on the device, so a fixed number of levels can run
+// without reading anything back (graph capture) and the host-driven loop
+// reads only `nseg` after each level.
+struct LevelState {
+  int nseg;       // segments of the current level
+  int levelBase;  // top-node id of the current level's first segment
+  int level;      // current level
+  int nLevels;    // levels finished
+  int overflow;   // capacity exceeded
+  int pad[3];
+};
+
 template <typename T>
 struct SmallSegs {
   int* start;
@@ -286,9 +298,9 @@ __device__ __forceinline__ int arg_max_extent(const T* lo, const T* hi, int dim)
 }
 
 template <typename T>
-__global__ void k_prepare(SegLevel<T> L, int nseg, int dim) {
+__global__ void k_prepare(SegLevel<T> L, const LevelState* st, int dim) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nseg) return;
+  if (s >= st->nseg) return;
   L.cutDim[s] = arg_max_extent(L.boxLo + (int64_t)s * kMaxDim, L.boxHi + (int64_t)s * kMaxDim, dim);
   L.mnK[s] = ordered_key(std::numeric_limits<T>::max());
   L.mxK[s] = ordered_key(std::numeric_limits<T>::lowest());
@@ -297,8 +309,10 @@ __global__ void k_prepare(SegLevel<T> L, int nseg, int dim) {
 }
 
 template <typename T, int D>
-__global__ void k_minmax(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L) {
+__global__ void k_minmax(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
+                         const LevelState* st) {
   using Key = typename KeyOf<T>::type;
+  if (st->nseg == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   int s = -1;
   Key kmin = 0, kmax = 0;
@@ -319,9 +333,9 @@ __global__ void k_minmax(const Rec<T, D>* __restrict__ recs, const int* __restri
 }
 
 template <typename T>
-__global__ void k_cut(SegLevel<T> L, int nseg) {
+__global__ void k_cut(SegLevel<T> L, const LevelState* st) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= nseg) return;
+  if (s >= st->nseg) return;
   const int cd = L.cutDim[s];
   const T mn = ordered_val(L.mnK[s], T(0));
   const T mx = ordered_val(L.mxK[s], T(0));
@@ -345,7 +359,9 @@ __global__ void k_cut(SegLevel<T> L, int nseg) {
 }
 
 template <typename T, int D>
-__global__ void k_count(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L) {
+__global__ void k_count(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
+                        const LevelState* st) {
+  if (st->nseg == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   int s = -1;
   int2 c = make_int2(0, 0);
@@ -397,7 +413,8 @@ __device__ __forceinline__ int2 misplaced(const Rec<T, D>* __restrict__ recs, co
 
 template <typename T, int D>
 __global__ void k_flag_sums(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                            int pass, int2* blockSums) {
+                            int pass, int2* blockSums, const LevelState* st) {
+  if (st->nseg == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   int s;
   const int2 f = misplaced(recs, segOf, n, L, pass, p, &s);
@@ -408,7 +425,11 @@ __global__ void k_flag_sums(const Rec<T, D>* __restrict__ recs, const int* __res
 
 // Single block: exclusive scan of the per-block sums; the grand total goes
 // to *total.
-__global__ void k_scan_block_sums(int2* sums, int nb, int2* total) {
+__global__ void k_scan_block_sums(int2* sums, int nb, int2* total, const LevelState* st) {
+  if (st->nseg == 0) {
+    if (threadIdx.x == 0) *total = make_int2(0, 0);
+    return;
+  }
   int2 carry = make_int2(0, 0);
   for (int base = 0; base < nb; base += kBlock) {
     const int i = base + threadIdx.x;
@@ -423,7 +444,8 @@ __global__ void k_scan_block_sums(int2* sums, int nb, int2* total) {
 
 template <typename T, int D>
 __global__ void k_flag_ranks(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                             int pass, const int2* blockPrefix, int2* S) {
+                             int pass, const int2* blockPrefix, int2* S, const LevelState* st) {
+  if (st->nseg == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   int s;
   const int2 f = misplaced(recs, segOf, n, L, pass, p, &s);
@@ -434,7 +456,8 @@ __global__ void k_flag_ranks(const Rec<T, D>* __restrict__ recs, const int* __re
 
 template <typename T, int D>
 __global__ void k_pairs(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                        int pass, const int2* __restrict__ S, int* pairA, int* pairB) {
+                        int pass, const int2* __restrict__ S, int* pairA, int* pairB, const LevelState* st) {
+  if (st->nseg == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   int s;
@@ -463,10 +486,18 @@ __global__ void k_swap(Rec<T, D>* recs, const int* __restrict__ pairA, const int
 
 // nabo/kdtree_cpu.cpp:180-223: leftCount rule, node, children.
 template <typename T>
-__global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, int nseg, int levelBase, int nextLevelBase, int level,
-                           TopNodes<T> top, SmallSegs<T> small, int* counters, int dim, int segCap, int smallCap) {
+__global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, const LevelState* st, TopNodes<T> top,
+                           SmallSegs<T> small, int* counters, int dim, int segCap, int smallCap, int topCap) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nseg = st->nseg;
   if (s >= nseg) return;
+  const int levelBase = st->levelBase;
+  const int nextLevelBase = levelBase + nseg;
+  const int level = st->level;
+  if (levelBase + s >= topCap) {
+    atomicOr(counters + 3, 1);
+    return;
+  }
   const int count = L.count[s];
   const int start = L.start[s];
   const int br1 = L.lt[s];
@@ -542,13 +573,139 @@ __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, int nseg, int levelB
 }
 
 template <typename T>
-__global__ void k_update_segof(int* segOf, int n, SegLevel<T> L) {
+__global__ void k_update_segof(int* segOf, int n, SegLevel<T> L, const LevelState* st) {
+  if (st->nseg == 0) return;
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= n) return;
   const int s = segOf[p];
   if (s < 0) return;
   const int loc = p - L.start[s];
   segOf[p] = loc < L.leftCount[s] ? L.newLeft[s] : L.newRight[s];
+}
+
+// Closes a level: records its top-node range and makes the segments the
+// level produced the current ones.
+__global__ void k_advance(LevelState* st, int* counters, int* lvStart, int* lvCount, int maxLevels) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (st->nseg > 0) {
+    if (st->level < maxLevels) {
+      lvStart[st->level] = st->levelBase;
+      lvCount[st->level] = st->nseg;
+      st->nLevels = st->level + 1;
+    } else {
+      st->overflow = 1;
+    }
+    st->levelBase += st->nseg;
+    st->level += 1;
+  }
+  st->nseg = counters[0];
+  counters[0] = 0;
+}
+
+// ---- forest set-up: clouds are contiguous point ranges [off[c], off[c+1])
+
+template <typename T, int D>
+__global__ void k_pack_forest(const T* __restrict__ cloud, int64_t n, int64_t stride, int dim,
+                              const int64_t* __restrict__ off, int nClouds, Rec<T, D>* __restrict__ recs) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  Rec<T, D> r;
+#pragma unroll
+  for (int c = 0; c < RecSize<T, D>::chunks; ++c) r.v[c] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+  for (int d = 0; d < D; ++d) r.p.c[d] = d < dim ? cloud[p * stride + d] : T(0);
+  r.p.idx = (int32_t)(p - off[cloud_of(off, nClouds, p)]);
+  recs[p] = r;
+}
+
+// Per-cloud per-dimension min/max (ordered keys) and a non-finite flag.
+template <typename T, int D>
+__global__ void k_bounds_forest(const Rec<T, D>* __restrict__ recs, int64_t n, int dim,
+                                const int64_t* __restrict__ off, int nClouds, typename KeyOf<T>::type* mnK,
+                                typename KeyOf<T>::type* mxK, int* nonFinite) {
+  using Key = typename KeyOf<T>::type;
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int c = -1;
+  Rec<T, D> r;
+  if (p < n) {
+    c = cloud_of(off, nClouds, p);
+    load_rec(recs, p, r);
+  }
+  int bad = 0;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    Key kmin = 0, kmax = 0;
+    if (c >= 0) {
+      kmin = kmax = ordered_key(r.p.c[d]);
+      bad |= (d < dim && !isfinite(r.p.c[d])) ? 1 : 0;
+    }
+    bool tail;
+    kmin = seg_warp_reduce(c, kmin, MinOp(), &tail);
+    kmax = seg_warp_reduce(c, kmax, MaxOp(), &tail);
+    if (tail && c >= 0 && d < dim) {
+      atomicMin(mnK + (int64_t)c * kMaxDim + d, kmin);
+      atomicMax(mxK + (int64_t)c * kMaxDim + d, kmax);
+    }
+  }
+  if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(nonFinite, 1);
+}
+
+template <typename T>
+__global__ void k_init_keys_forest(typename KeyOf<T>::type* mnK, typename KeyOf<T>::type* mxK, int nClouds) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nClouds * kMaxDim) return;
+  mnK[i] = ordered_key(Ar<T>::inf());
+  mxK[i] = ordered_key(-Ar<T>::inf());
+}
+
+// One root per cloud: a level-0 segment when it has more than kSmallMax
+// points, else a small segment. Root box = (min, max(numeric_limits<T>::min(),
+// max)), as the reference's constructor sets it (nabo/nabo.cpp:73-74,
+// nabo/kdtree_cpu.cpp:256-267).
+template <typename T>
+__global__ void k_forest_roots(const int64_t* __restrict__ off, int nClouds, const typename KeyOf<T>::type* mnK,
+                               const typename KeyOf<T>::type* mxK, int dim, SegLevel<T> L, SmallSegs<T> small,
+                               LevelState* st, int* counters, int* rootRef, int* rootSeg, T* rootLo, T* rootHi) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nClouds) return;
+  const int64_t start = off[c];
+  const int count = (int)(off[c + 1] - start);
+  T* lo;
+  T* hi;
+  if (count > kSmallMax) {
+    const int id = atomicAdd(&st->nseg, 1);
+    L.start[id] = (int)start;
+    L.count[id] = count;
+    lo = L.boxLo + (int64_t)id * kMaxDim;
+    hi = L.boxHi + (int64_t)id * kMaxDim;
+    rootRef[c] = id;  // level 0 starts at top-node id 0
+    rootSeg[c] = id;
+  } else {
+    const int sid = atomicAdd(counters + 1, 1);
+    small.start[sid] = (int)start;
+    small.count[sid] = count;
+    small.depth[sid] = 0;
+    lo = small.boxLo + (int64_t)sid * kMaxDim;
+    hi = small.boxHi + (int64_t)sid * kMaxDim;
+    rootRef[c] = ~sid;
+    rootSeg[c] = -1;
+  }
+  for (int d = 0; d < dim; ++d) {
+    const T mn = ordered_val(mnK[(int64_t)c * kMaxDim + d], T(0));
+    const T mx = ordered_val(mxK[(int64_t)c * kMaxDim + d], T(0));
+    const T tiny = std::numeric_limits<T>::min();
+    lo[d] = mn;
+    hi[d] = mx > tiny ? mx : tiny;
+    rootLo[(int64_t)c * kMaxDim + d] = lo[d];
+    rootHi[(int64_t)c * kMaxDim + d] = hi[d];
+  }
+}
+
+__global__ void k_init_segof(int* segOf, int64_t n, const int64_t* __restrict__ off, int nClouds,
+                             const int* __restrict__ rootSeg) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  segOf[p] = rootSeg[cloud_of(off, nClouds, p)];
 }
 
 // ---------------------------------------------------------------------------
@@ -566,10 +723,10 @@ struct SmallStack {
 };
 
 template <typename T, int D>
-__global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, int nSmall, Node<T>* scratch, SmallStack<T> stk,
-                        int dim, unsigned bucketSize, int* counters) {
+__global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, Node<T>* scratch,
+                        SmallStack<T> stk, int dim, unsigned bucketSize, int* counters) {
   const int sid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (sid >= nSmall) return;
+  if (sid >= *nSmall) return;
   const int base = small.start[sid];
   const int segN = small.count[sid];
   Node<T>* out = scratch + 2 * (int64_t)base;
@@ -703,16 +860,15 @@ __device__ __forceinline__ int subtree_size(const TopNodes<T>& top, const SmallS
   return ref >= 0 ? top.size[ref] : small.size[~ref];
 }
 
+// Pre-order numbering of all trees (single block): subtree sizes bottom-up,
+// each cloud's root at the running sum of the previous trees' sizes, then
+// positions top-down.
 template <typename T>
-__global__ void k_renumber(TopNodes<T> top, SmallSegs<T> small, const int* lvStart, const int* lvCount, int nLevels,
-                           Node<T>* nodes, long long* total) {
-  if (nLevels == 0) {
-    if (threadIdx.x == 0) {
-      small.base[0] = 0;
-      *total = small.size[0];
-    }
-    return;
-  }
+__global__ void k_renumber(TopNodes<T> top, SmallSegs<T> small, const int* lvStart, const int* lvCount,
+                           const LevelState* st, const int* rootRef, int nClouds, Node<T>* nodes,
+                           int64_t* nodeOffset) {
+  __shared__ int64_t carry;
+  const int nLevels = st->nLevels;
   for (int l = nLevels - 1; l >= 0; --l) {
     const int b = lvStart[l], c = lvCount[l];
     for (int i = threadIdx.x; i < c; i += blockDim.x) {
@@ -721,9 +877,19 @@ __global__ void k_renumber(TopNodes<T> top, SmallSegs<T> small, const int* lvSta
     }
     __syncthreads();
   }
+  // tree offsets: exclusive scan of the root sizes, in cloud order
   if (threadIdx.x == 0) {
-    top.pre[0] = 0;
-    *total = top.size[0];
+    carry = 0;
+    for (int c = 0; c < nClouds; ++c) {
+      const int ref = rootRef[c];
+      nodeOffset[c] = carry;
+      if (ref >= 0)
+        top.pre[ref] = (int)carry;
+      else
+        small.base[~ref] = (int)carry;
+      carry += subtree_size(top, small, ref);
+    }
+    nodeOffset[nClouds] = carry;
   }
   __syncthreads();
   for (int l = 0; l < nLevels; ++l) {
@@ -749,9 +915,9 @@ __global__ void k_renumber(TopNodes<T> top, SmallSegs<T> small, const int* lvSta
 }
 
 template <typename T>
-__global__ void k_copy_small(const Node<T>* scratch, SmallSegs<T> small, int nSmall, Node<T>* nodes) {
+__global__ void k_copy_small(const Node<T>* scratch, SmallSegs<T> small, const int* nSmall, Node<T>* nodes) {
   const int sid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (sid >= nSmall) return;
+  if (sid >= *nSmall) return;
   const int base = small.base[sid];
   const Node<T>* src = scratch + 2 * (int64_t)small.start[sid];
   const int cnt = small.size[sid];
@@ -760,6 +926,15 @@ __global__ void k_copy_small(const Node<T>* scratch, SmallSegs<T> small, int nSm
     if (!node_is_leaf(nd.meta)) nd.meta = make_meta(node_dim(nd.meta), (uint32_t)base + node_payload(nd.meta));
     nodes[base + i] = nd;
   }
+}
+
+// status[0] non-finite input (set by k_bounds_forest), [1] capacity
+// exceeded, [2] tallest tree's height, [3] top levels run.
+__global__ void k_forest_status(const LevelState* st, const int* counters, int* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  status[1] = (counters[3] || st->overflow || st->nseg > 0) ? 1 : 0;
+  status[2] = counters[2];
+  status[3] = st->nLevels;
 }
 
 // ---------------------------------------------------------------------------
@@ -864,53 +1039,69 @@ int pack_cloud(const T* dCloud, int64_t n, int64_t stride, int dim, cudaStream_t
   return kOk;
 }
 
+// Builds the trees of `nClouds` clouds stored back to back (cloud c =
+// points [off[c], off[c+1]) of dCloud) into one record array and one node
+// array: cloud c's tree is the pre-order range [nodeOffset[c],
+// nodeOffset[c+1]), its points keep their index within the cloud.
+// maxLevels < 0: the host runs levels until none is left (reads one int per
+// level). maxLevels >= 0: exactly that many levels run with no host
+// synchronisation at all, so the whole build can be captured in a CUDA
+// graph; a tree needing more levels sets the overflow flag (f->status).
 template <typename T, int D>
-int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, cudaStream_t stream,
-                 DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats) {
+int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, const int64_t* dOff,
+                 int nClouds, int maxLevels, cudaStream_t stream, ForestOut* f) {
   using Key = typename KeyOf<T>::type;
-  (void)sizeof(Key);
   const int N = (int)n;
+  const bool hostDriven = maxLevels < 0;
   Scratch sc(stream);
-  Rec<T, D>* recs = nullptr;
-  NABO_CUDA_TRY(cudaMalloc((void**)&recs, (size_t)n * sizeof(Rec<T, D>)));
-  out->recs = recs;  // owned by the caller from here on
-  k_pack<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, recs);
+  Rec<T, D>* recs = static_cast<Rec<T, D>*>(f->recs);
+  k_pack_forest<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, dOff, nClouds, recs);
+
+  // per-cloud bounds
+  Key* keys;
+  NABO_CUDA_TRY(sc.get(&keys, 2 * (int64_t)nClouds * kMaxDim));
+  NABO_CUDA_TRY(cudaMemsetAsync(f->status, 0, 4 * sizeof(int), stream));
+  k_init_keys_forest<T><<<ceil_div(nClouds * kMaxDim, 256), 256, 0, stream>>>(keys, keys + nClouds * kMaxDim,
+                                                                              nClouds);
+  k_bounds_forest<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(recs, n, dim, dOff, nClouds, keys,
+                                                                   keys + nClouds * kMaxDim, f->status + 0);
   NABO_CUDA_TRY(cudaGetLastError());
-
-  // Root box: true minimum, and max(numeric_limits<T>::min(), true maximum)
-  // because the reference starts its max bound at the smallest positive
-  // normal value (nabo/nabo.cpp:74, nabo/kdtree_cpu.cpp:256-267).
-  {
-    const int rc = compute_bounds<T, D>(recs, n, dim, stream, sc, out->lo, out->hi);
-    if (rc != kOk) return rc;
-  }
-  Box<T> root;
-  for (int d = 0; d < kMaxDim; ++d) {
-    root.lo[d] = d < dim ? (T)out->lo[d] : T(0);
-    root.hi[d] = d < dim ? std::max((T)out->hi[d], std::numeric_limits<T>::min()) : T(0);
-    rootMin[d] = (double)root.lo[d];
-    rootMax[d] = (double)root.hi[d];
+  if (hostDriven) {
+    int bad = 0;
+    NABO_CUDA_TRY(cudaMemcpyAsync(&bad, f->status + 0, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NABO_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (bad) return set_error(kErrArgument, "Cloud has non-finite (NaN or infinite) coordinates");
   }
 
-  // Working arrays.
+  // working arrays
   int* segOf;
   int2* S;
   int2* blockSums;
   int* pairA;
   int* pairB;
   int* counters;
+  int* lv;
+  int* rootRef;
+  int* rootSeg;
+  LevelState* st;
   const int nb = ceil_div(n, kBlock);
   const int64_t pairCap = n + 1;
   const int64_t segCap = n / (kSmallMax + 1) + 2;
   const int64_t topCap = n + 1;
-  const int64_t smallCap = n + 1;
+  const int64_t smallCap = n + nClouds + 1;
+  const int lvCap = hostDriven ? 4096 : std::max(maxLevels, 1);
   NABO_CUDA_TRY(sc.get(&segOf, n));
   NABO_CUDA_TRY(sc.get(&S, n + 1));
   NABO_CUDA_TRY(sc.get(&blockSums, nb));
   NABO_CUDA_TRY(sc.get(&pairA, pairCap));
   NABO_CUDA_TRY(sc.get(&pairB, pairCap));
   NABO_CUDA_TRY(sc.get(&counters, 4));
+  NABO_CUDA_TRY(sc.get(&lv, 2 * (int64_t)lvCap));
+  NABO_CUDA_TRY(sc.get(&rootRef, nClouds));
+  NABO_CUDA_TRY(sc.get(&rootSeg, nClouds));
+  NABO_CUDA_TRY(sc.get(&st, 1));
   NABO_CUDA_TRY(cudaMemsetAsync(counters, 0, 4 * sizeof(int), stream));
+  NABO_CUDA_TRY(cudaMemsetAsync(st, 0, sizeof(LevelState), stream));
   SegLevel<T> cur, nxt;
   NABO_CUDA_TRY(alloc_level(sc, &cur, segCap));
   NABO_CUDA_TRY(alloc_level(sc, &nxt, segCap));
@@ -930,55 +1121,41 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   NABO_CUDA_TRY(sc.get(&small.size, smallCap));
   NABO_CUDA_TRY(sc.get(&small.base, smallCap));
 
-  int nseg = 0;
-  int nSmall = 0;
-  if (N > kSmallMax) {
-    k_root_segment<T><<<1, 1, 0, stream>>>(cur, N, root, dim);
-    NABO_CUDA_TRY(cudaMemsetAsync(segOf, 0, (size_t)n * sizeof(int), stream));
-    nseg = 1;
-  } else {
-    k_root_small<T><<<1, 1, 0, stream>>>(small, N, root, dim);
-    nSmall = 1;
-    NABO_CUDA_TRY(cudaMemcpyAsync(counters + 1, &nSmall, sizeof(int), cudaMemcpyHostToDevice, stream));
-  }
+  k_forest_roots<T><<<ceil_div(nClouds, 128), 128, 0, stream>>>(
+      dOff, nClouds, keys, keys + nClouds * kMaxDim, dim, cur, small, st, counters, rootRef, rootSeg,
+      static_cast<T*>(f->rootLo), static_cast<T*>(f->rootHi));
+  k_init_segof<<<nb, kBlock, 0, stream>>>(segOf, n, dOff, nClouds, rootSeg);
   NABO_CUDA_TRY(cudaGetLastError());
 
-  std::vector<int> lvStart, lvCount;
-  int levelBase = 0;
-  int level = 0;
-  int hctr[4];
-  while (nseg > 0) {
-    const int sg = ceil_div(nseg, 128);
-    k_prepare<T><<<sg, 128, 0, stream>>>(cur, nseg, dim);
-    k_minmax<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur);
-    k_cut<T><<<sg, 128, 0, stream>>>(cur, nseg);
-    k_count<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur);
+  const int sg = ceil_div(segCap, 128);
+  for (int level = 0; hostDriven || level < maxLevels; ++level) {
+    if (hostDriven) {
+      int nseg = 0;
+      NABO_CUDA_TRY(cudaMemcpyAsync(&nseg, &st->nseg, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      NABO_CUDA_TRY(cudaStreamSynchronize(stream));
+      if (nseg == 0) break;
+      if (level >= lvCap) return set_error(kErrUnsupported, "kd-tree build: too many levels");
+    }
+    k_prepare<T><<<sg, 128, 0, stream>>>(cur, st, dim);
+    k_minmax<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, st);
+    k_cut<T><<<sg, 128, 0, stream>>>(cur, st);
+    k_count<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, st);
     for (int pass = 1; pass <= 2; ++pass) {
-      k_flag_sums<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, blockSums);
-      k_scan_block_sums<<<1, kBlock, 0, stream>>>(blockSums, nb, S + n);
-      k_flag_ranks<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, blockSums, S);
-      k_pairs<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, S, pairA, pairB);
+      k_flag_sums<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, blockSums, st);
+      k_scan_block_sums<<<1, kBlock, 0, stream>>>(blockSums, nb, S + n, st);
+      k_flag_ranks<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, blockSums, S, st);
+      k_pairs<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, S, pairA, pairB, st);
       k_swap<T, D><<<ceil_div(pairCap, kBlock), kBlock, 0, stream>>>(recs, pairA, pairB, S + n, (int)pairCap);
     }
-    k_finalize<T><<<sg, 128, 0, stream>>>(cur, nxt, nseg, levelBase, levelBase + nseg, level, top, small, counters,
-                                          dim, (int)segCap, (int)smallCap);
-    k_update_segof<T><<<nb, kBlock, 0, stream>>>(segOf, N, cur);
+    k_finalize<T><<<sg, 128, 0, stream>>>(cur, nxt, st, top, small, counters, dim, (int)segCap, (int)smallCap,
+                                          (int)topCap);
+    k_update_segof<T><<<nb, kBlock, 0, stream>>>(segOf, N, cur, st);
+    k_advance<<<1, 1, 0, stream>>>(st, counters, lv, lv + lvCap, lvCap);
     NABO_CUDA_TRY(cudaGetLastError());
-    NABO_CUDA_TRY(cudaMemcpyAsync(hctr, counters, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
-    NABO_CUDA_TRY(cudaMemsetAsync(counters, 0, sizeof(int), stream));
-    NABO_CUDA_TRY(cudaStreamSynchronize(stream));
-    lvStart.push_back(levelBase);
-    lvCount.push_back(nseg);
-    levelBase += nseg;
-    nseg = hctr[0];
-    nSmall = hctr[1];
-    if (hctr[3] || nseg > segCap || levelBase + nseg > topCap || nSmall > smallCap)
-      return set_error(kErrInternal, "kd-tree build: segment capacity exceeded");
     std::swap(cur, nxt);
-    ++level;
   }
 
-  // Small segments.
+  // small segments (their count is read on the device: grid for the most)
   Node<T>* scratchNodes;
   NABO_CUDA_TRY(sc.get(&scratchNodes, 2 * n));
   SmallStack<T> stk;
@@ -988,42 +1165,80 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   NABO_CUDA_TRY(sc.get(&stk.depth, n));
   NABO_CUDA_TRY(sc.get(&stk.boxLo, n * kMaxDim));
   NABO_CUDA_TRY(sc.get(&stk.boxHi, n * kMaxDim));
-  k_small<T, D><<<ceil_div(nSmall, 64), 64, 0, stream>>>(recs, small, nSmall, scratchNodes, stk, dim, bucketSize,
-                                                         counters);
-  NABO_CUDA_TRY(cudaGetLastError());
-
-  // Renumber into pre-order.
-  const int nLevels = (int)lvStart.size();
-  int* dLv;
-  NABO_CUDA_TRY(sc.get(&dLv, 2 * std::max(nLevels, 1)));
-  if (nLevels > 0) {
-    NABO_CUDA_TRY(cudaMemcpyAsync(dLv, lvStart.data(), nLevels * sizeof(int), cudaMemcpyHostToDevice, stream));
-    NABO_CUDA_TRY(
-        cudaMemcpyAsync(dLv + nLevels, lvCount.data(), nLevels * sizeof(int), cudaMemcpyHostToDevice, stream));
+  int nSmallHost = (int)smallCap;
+  if (hostDriven) {
+    NABO_CUDA_TRY(cudaMemcpyAsync(&nSmallHost, counters + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NABO_CUDA_TRY(cudaStreamSynchronize(stream));
   }
-  long long* dTotal;
-  NABO_CUDA_TRY(sc.get(&dTotal, 1));
-  // Upper bound on the node count: every leaf holds at least one point.
+  k_small<T, D><<<ceil_div(nSmallHost, 64), 64, 0, stream>>>(recs, small, counters + 1, scratchNodes, stk, dim,
+                                                             bucketSize, counters);
+  NABO_CUDA_TRY(cudaGetLastError());
+  Node<T>* nodes = static_cast<Node<T>*>(f->nodes);
+  k_renumber<T><<<1, 1024, 0, stream>>>(top, small, lv, lv + lvCap, st, rootRef, nClouds, nodes, f->nodeOffset);
+  k_copy_small<T><<<ceil_div(nSmallHost, 128), 128, 0, stream>>>(scratchNodes, small, counters + 1, nodes);
+  k_forest_status<<<1, 1, 0, stream>>>(st, counters, f->status);
+  NABO_CUDA_TRY(cudaGetLastError());
+  if (hostDriven) {
+    int hs[4];
+    NABO_CUDA_TRY(cudaMemcpyAsync(hs, f->status, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    NABO_CUDA_TRY(cudaStreamSynchronize(stream));
+    if (hs[1]) return set_error(kErrInternal, "kd-tree build: capacity exceeded");
+  }
+  return kOk;
+}
+
+template <typename T, int D>
+int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, cudaStream_t stream,
+                 DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats) {
+  Scratch sc(stream);
+  ForestOut f;
+  Rec<T, D>* recs = nullptr;
   Node<T>* nodes = nullptr;
+  NABO_CUDA_TRY(cudaMalloc((void**)&recs, (size_t)n * sizeof(Rec<T, D>)));
+  out->recs = recs;  // owned by the caller from here on
+  // Upper bound on the node count: every leaf holds at least one point.
   const int64_t nodeCap = 2 * n;
   NABO_CUDA_TRY(cudaMalloc((void**)&nodes, (size_t)nodeCap * sizeof(Node<T>)));
   out->nodes = nodes;
-  k_renumber<T><<<1, 1024, 0, stream>>>(top, small, dLv, dLv + nLevels, nLevels, nodes, dTotal);
-  k_copy_small<T><<<ceil_div(nSmall, 128), 128, 0, stream>>>(scratchNodes, small, nSmall, nodes);
-  NABO_CUDA_TRY(cudaGetLastError());
-  long long total = 0;
-  NABO_CUDA_TRY(cudaMemcpyAsync(&total, dTotal, sizeof(long long), cudaMemcpyDeviceToHost, stream));
-  NABO_CUDA_TRY(cudaMemcpyAsync(hctr, counters, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+  int64_t* off;
+  T* rootBox;
+  NABO_CUDA_TRY(sc.get(&off, 2));
+  NABO_CUDA_TRY(sc.get(&f.nodeOffset, 2));
+  NABO_CUDA_TRY(sc.get(&f.status, 4));
+  NABO_CUDA_TRY(sc.get(&rootBox, 2 * kMaxDim));
+  const int64_t hoff[2] = {0, n};
+  NABO_CUDA_TRY(cudaMemcpyAsync(off, hoff, sizeof(hoff), cudaMemcpyHostToDevice, stream));
+  f.recs = recs;
+  f.nodes = nodes;
+  f.rootLo = rootBox;
+  f.rootHi = rootBox + kMaxDim;
+  const int rc = build_forest<T, D>(dCloud, n, stride, dim, bucketSize, off, 1, -1, stream, &f);
+  if (rc != kOk) return rc;
+  int64_t hno[2];
+  int hs[4];
+  T hbox[2 * kMaxDim];
+  NABO_CUDA_TRY(cudaMemcpyAsync(hno, f.nodeOffset, sizeof(hno), cudaMemcpyDeviceToHost, stream));
+  NABO_CUDA_TRY(cudaMemcpyAsync(hs, f.status, sizeof(hs), cudaMemcpyDeviceToHost, stream));
+  NABO_CUDA_TRY(cudaMemcpyAsync(hbox, rootBox, sizeof(hbox), cudaMemcpyDeviceToHost, stream));
   NABO_CUDA_TRY(cudaStreamSynchronize(stream));
-  if (hctr[3] || total <= 0 || total > nodeCap) return set_error(kErrInternal, "kd-tree build: inconsistent node count");
-  if (total - 1 > (long long)kMaxNodeIndex)
+  const int64_t total = hno[1];
+  if (total <= 0 || total > nodeCap) return set_error(kErrInternal, "kd-tree build: inconsistent node count");
+  if (total - 1 > (int64_t)kMaxNodeIndex)
     return set_error(kErrUnsupported, "kd-tree build: the tree has more nodes than the device layout indexes");
   out->nodeCount = total;
-  out->height = hctr[2];
+  out->height = hs[2];
+  for (int d = 0; d < kMaxDim; ++d) {
+    rootMin[d] = d < dim ? (double)hbox[d] : 0.0;
+    rootMax[d] = d < dim ? (double)hbox[kMaxDim + d] : 0.0;
+    // true bounds for query ordering: the root box's max is the true max
+    // unless the quirk lifted it to numeric_limits<T>::min()
+    out->lo[d] = rootMin[d];
+    out->hi[d] = rootMax[d];
+  }
   if (stats) {
-    stats->topLevels = nLevels;
-    stats->topNodes = levelBase;
-    stats->smallSegments = nSmall;
+    stats->topLevels = hs[3];
+    stats->topNodes = 0;
+    stats->smallSegments = 0;
   }
   return kOk;
 }
@@ -1031,6 +1246,8 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
 #define NABO_BUILD_INSTANTIATE(T, D)                                                                          \
   template int build_kdtree<T, D>(const T*, int64_t, int64_t, int, unsigned, cudaStream_t, DeviceCloud*,      \
                                   double*, double*, BuildStats*);                                             \
+  template int build_forest<T, D>(const T*, int64_t, int64_t, int, unsigned, const int64_t*, int, int,        \
+                                  cudaStream_t, ForestOut*);                                                  \
   template int pack_cloud<T, D>(const T*, int64_t, int64_t, int, cudaStream_t, DeviceCloud*);
 
 NABO_BUILD_INSTANTIATE(float, 2)

@@ -60,7 +60,16 @@ static cudaError_t library_pool(cudaMemPool_t* pool) {
   return cudaSuccess;
 }
 
+namespace {
+thread_local bool g_captureAllocations = false;
+}
+
+void set_capture_allocations(bool on) { g_captureAllocations = on; }
+
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
+  // while a CUDA graph is being captured, allocations become graph memory
+  // nodes of the device's default pool
+  if (g_captureAllocations) return cudaMallocAsync(p, bytes, stream);
   cudaMemPool_t pool;
   const cudaError_t e = library_pool(&pool);
   if (e != cudaSuccess) return e;

@@ -180,4 +180,18 @@ struct KeyOf<double> {
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 
+// Index c of the range [off[c], off[c+1]) holding p (off ascending, nClouds
+// ranges); used for batches of clouds stored back to back.
+__device__ __forceinline__ int cloud_of(const int64_t* __restrict__ off, int nClouds, int64_t p) {
+  int lo = 0, hi = nClouds - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= p)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 }  // namespace nabo_gb300

@@ -39,6 +39,9 @@ int cuda_error(cudaError_t e, const char* what);
 // users of cudaMallocAsync are unaffected.
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream);
 cudaError_t scratch_free(void* p, cudaStream_t stream);
+// While set (calling thread only), scratch_alloc uses cudaMallocAsync so the
+// allocations can be captured into a CUDA graph.
+void set_capture_allocations(bool on);
 
 // Device-resident kd-tree (or, for brute force, the packed cloud only).
 struct DeviceCloud {
@@ -70,6 +73,51 @@ struct BuildStats {
 template <typename T, int D>
 int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, cudaStream_t stream,
                  DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats);
+
+// Output buffers of a forest build (all device memory, allocated by the
+// caller): records (n), nodes (2n), nodeOffset (nClouds+1), root boxes
+// (nClouds x kMaxDim each, scalar type), status (4 ints).
+struct ForestOut {
+  void* recs = nullptr;
+  void* nodes = nullptr;
+  int64_t* nodeOffset = nullptr;
+  void* rootLo = nullptr;
+  void* rootHi = nullptr;
+  int* status = nullptr;
+};
+
+// A batched search over a forest (batch.cu).
+struct BatchArgs {
+  const void* nodes;
+  const void* recs;
+  int dim;
+  int nClouds;
+  int64_t nodeCap;              // hist entries (>= total nodes)
+  const int64_t* nodeOffset;    // device, nClouds+1
+  const int64_t* qOffset;       // device, nClouds+1
+  const int64_t* outOffset;     // device, nClouds+1 (result entries)
+  const int32_t* kOf;           // device, nClouds
+  int kMax;
+  const void* query;            // device, dim rows x nq, stride qStride
+  int64_t nq;
+  int64_t qStride;
+  double eps;
+  unsigned optionFlags;
+  double maxRadius;
+  int32_t* indices;             // device, concatenated per cloud
+  void* dists2;
+  int32_t* order;               // scratch
+  uint32_t* hist;
+  uint32_t* cell;
+  uint32_t* rank;
+  int blockSize;                // threads per block of the search kernel
+};
+template <typename T, int D>
+int knn_batch(const BatchArgs& b, cudaStream_t stream);
+
+template <typename T, int D>
+int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, const int64_t* dOff,
+                 int nClouds, int maxLevels, cudaStream_t stream, ForestOut* f);
 
 // Packs the cloud into records in cloud order (brute force) and computes
 // its true bounds.

@@ -81,28 +81,55 @@ constexpr int kVoxelCoordMax = (1 << 21) - 1;
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
 
-// Count of the voxel at scale s holding point (x, y, z); 0 outside the
-// cloud's voxels. Probing is bounded by the table size (a table is at most
-// half full, so a lookup ends at the key or at an empty slot long before).
-__device__ __forceinline__ uint32_t voxel_count(const FeatureSpace& fs, int s, const float (&p)[3]) {
-  const float inv = fs.invH0 * __int_as_float((127 - s) << 23);  // invH0 / 2^s
-  int c[3];
+// Occupancies of scales [s0, s0 + n) for point p: the first probe of every
+// scale is issued before any is inspected (independent loads in flight);
+// collisions continue with the bounded linear probe.
+template <int N>
+__device__ __forceinline__ void voxel_counts(const FeatureSpace& fs, int s0, const float (&p)[3], float (&out)[N]) {
+  unsigned long long key[N];
+  uint32_t slot[N];
+  bool inside[N];
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    const float v = floorf((p[d] - fs.lo[d]) * inv);
-    if (!(v >= 0.0f && v <= (float)kVoxelCoordMax)) return 0u;
-    c[d] = (int)v;
+  for (int j = 0; j < N; ++j) {
+    const int s = s0 + j;
+    const float inv = fs.invH0 * __int_as_float((127 - s) << 23);
+    int c[3];
+    inside[j] = true;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float v = floorf((p[d] - fs.lo[d]) * inv);
+      inside[j] = inside[j] && (v >= 0.0f && v <= (float)kVoxelCoordMax);
+      c[d] = inside[j] ? (int)v : 0;
+    }
+    key[j] = voxel_key(c[0], c[1], c[2]);
+    slot[j] = (uint32_t)mix64(key[j]) & fs.mask[s];
   }
-  const unsigned long long key = voxel_key(c[0], c[1], c[2]);
-  const uint32_t mask = fs.mask[s];
-  uint32_t slot = (uint32_t)mix64(key) & mask;
-  for (uint32_t probe = 0; probe <= mask; ++probe) {
-    const unsigned long long k = fs.keys[s][slot];
-    if (k == key) return fs.counts[s][slot];
-    if (k == 0ull) return 0u;
-    slot = (slot + 1u) & mask;
+  unsigned long long k0[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) k0[j] = inside[j] ? __ldg(fs.keys[s0 + j] + slot[j]) : 0ull;
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    const int s = s0 + j;
+    uint32_t cnt = 0u;
+    if (inside[j] && k0[j] != 0ull) {
+      if (k0[j] == key[j]) {
+        cnt = __ldg(fs.counts[s] + slot[j]);
+      } else {
+        const uint32_t mask = fs.mask[s];
+        uint32_t sl = (slot[j] + 1u) & mask;
+        for (uint32_t probe = 1; probe <= mask; ++probe) {
+          const unsigned long long kk = fs.keys[s][sl];
+          if (kk == key[j]) {
+            cnt = fs.counts[s][sl];
+            break;
+          }
+          if (kk == 0ull) break;
+          sl = (sl + 1u) & mask;
+        }
+      }
+    }
+    out[j] = log1pf((float)cnt) * fs.invLogN;
   }
-  return 0u;
 }
 
 template <typename T>
@@ -112,8 +139,10 @@ __device__ __forceinline__ void features(const T* __restrict__ q, const FeatureS
   for (int d = 0; d < fs.dim && d < kF; ++d) out[d] = fminf(fmaxf(((float)q[d] - fs.center[d]) * fs.invHalf[d], -4.f), 4.f);
   if (fs.useGrid) {
     const float p[3] = {(float)q[0], (float)q[1], (float)q[2]};
+    float occ[kScales];
+    voxel_counts<kScales>(fs, 0, p, occ);
 #pragma unroll
-    for (int s = 0; s < kScales; ++s) out[3 + s] = log1pf((float)voxel_count(fs, s, p)) * fs.invLogN;
+    for (int s = 0; s < kScales; ++s) out[3 + s] = occ[s];
   }
 }
 
@@ -416,18 +445,40 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __rest
   const int64_t tiles = (nq + 15) / 16;
   for (int64_t tile = (int64_t)blockIdx.x * kInferWarps + warp; tile < tiles; tile += (int64_t)gridDim.x * kInferWarps) {
     const int64_t q0 = tile * 16;
-    // features of the tile's 16 queries (lanes 0..15)
-    if (lane < 16) {
-      float f[kF];
-      const int64_t qi = q0 + lane;
+    // features of the tile's 16 queries: lanes l and l + 16 share query l;
+    // the first lane writes the coordinates and the finer half of the voxel
+    // scales, the second the coarser half
+    {
+      const int row = lane & 15;
+      const bool second = lane >= 16;
+      const int64_t qi = q0 + row;
+      __nv_bfloat16* xr = sX[warp] + row * kF;
       if (qi < nq) {
-        features(query + qi * qStride, fs, f);
-      } else {
+        const T* qp = query + qi * qStride;
+        if (fs.useGrid) {
+          const float p[3] = {(float)qp[0], (float)qp[1], (float)qp[2]};
+          float occ[kScales / 2];
+          voxel_counts<kScales / 2>(fs, second ? kScales / 2 : 0, p, occ);
 #pragma unroll
-        for (int j = 0; j < kF; ++j) f[j] = 0.0f;
+          for (int j = 0; j < kScales / 2; ++j) xr[3 + (second ? kScales / 2 : 0) + j] = __float2bfloat16_rn(occ[j]);
+          if (!second) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d)
+              xr[d] = __float2bfloat16_rn(fminf(fmaxf(((float)qp[d] - fs.center[d]) * fs.invHalf[d], -4.f), 4.f));
+          } else {
+#pragma unroll
+            for (int j = 3 + kScales; j < kF; ++j) xr[j] = __float2bfloat16_rn(0.0f);
+          }
+        } else if (!second) {
+          float f[kF];
+          features(qp, fs, f);
+#pragma unroll
+          for (int j = 0; j < kF; ++j) xr[j] = __float2bfloat16_rn(f[j]);
+        }
+      } else if (!second) {
+#pragma unroll
+        for (int j = 0; j < kF; ++j) xr[j] = __float2bfloat16_rn(0.0f);
       }
-#pragma unroll
-      for (int j = 0; j < kF; ++j) sX[warp][lane * kF + j] = __float2bfloat16_rn(f[j]);
     }
     __syncwarp();
     const uint32_t* X32 = reinterpret_cast<const uint32_t*>(sX[warp]);  // row = 8 words

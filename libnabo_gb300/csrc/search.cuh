@@ -103,13 +103,15 @@ __device__ __forceinline__ T dist2_seq(const T (&q)[D], const Rec<T, D>& r) {
 // grouped at the scale of the data's own buckets.
 template <typename T, int D>
 __global__ void k_leaf_cells(const Node<T>* __restrict__ nodes, const T* __restrict__ query, int64_t nq,
-                             int64_t qStride, int dim, uint32_t* cell, uint32_t* rank, uint32_t* hist) {
+                             int64_t qStride, int dim, uint32_t* cell, uint32_t* rank, uint32_t* hist,
+                             const int64_t* __restrict__ bQueryOffset = nullptr,
+                             const int64_t* __restrict__ bNodeOffset = nullptr, int bClouds = 0) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
   T q[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) q[d] = d < dim ? query[i * qStride + d] : T(0);
-  uint32_t node = 0;
+  uint32_t node = bQueryOffset ? (uint32_t)bNodeOffset[cloud_of(bQueryOffset, bClouds, i)] : 0u;
   for (;;) {
     const Node<T> nd = load_node(nodes, node);
     if (node_is_leaf(nd.meta)) break;
@@ -140,6 +142,14 @@ struct KnnLaunch {
   int allowSelf;
   int stats;
   const int32_t* nqDevice;  // if set, only threads t < *nqDevice search (t < nq still bounds the grid)
+  // batches of clouds (all null for one cloud): queries of cloud c are
+  // [bQueryOffset[c], bQueryOffset[c+1]), its tree starts at node
+  // bNodeOffset[c], it wants bK[c] neighbours written from bOutOffset[c]
+  const int64_t* bQueryOffset;
+  const int64_t* bNodeOffset;
+  const int32_t* bK;
+  const int64_t* bOutOffset;
+  int bClouds;
 };
 
 // Leaf scan shared by the kernels: the bucket's records are read in chunks
@@ -202,6 +212,15 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
   unsigned long long touched = 0;
   if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
     const int64_t qi = a.order ? (int64_t)a.order[t] : t;
+    int k = a.k;
+    uint32_t root = 0;
+    int64_t outBase = qi * (int64_t)a.k;
+    if (a.bQueryOffset) {
+      const int c = cloud_of(a.bQueryOffset, a.bClouds, qi);
+      k = a.bK[c];
+      root = (uint32_t)a.bNodeOffset[c];
+      outBase = a.bOutOffset[c] + (qi - a.bQueryOffset[c]) * (int64_t)k;
+    }
     T q[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) q[d] = d < a.dim ? query[qi * a.qStride + d] : T(0);
@@ -212,7 +231,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
     }
     const T maxError2 = (T)a.maxError2;
     TopK<T, K> heap;
-    heap.init(a.k);
+    heap.init(k);
     T off[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) off[d] = T(0);
@@ -220,7 +239,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
     T sRd[STACK];
     T sOff[STACK][D];
     int sp = 0;
-    uint32_t node = 0;
+    uint32_t node = root;
     T rd = T(0);
     for (;;) {
       // descend to a leaf, pushing far children
@@ -265,7 +284,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
       }
       if (!more) break;
     }
-    const int f = heap.store(a.k, a.outIdx + qi * a.k, static_cast<T*>(a.outD2) + qi * a.k);
+    const int f = heap.store(k, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
     if (a.found) a.found[qi] = f;
   }
   if (a.stats) {

@@ -5,6 +5,8 @@
 #include "internal.cuh"
 #include "search.cuh"
 
+#include <cstring>
+
 namespace nabo_gb300 {
 
 // Register top-k sizes compiled; a request for k uses the smallest K >= k.
@@ -48,6 +50,11 @@ KnnLaunch make_launch(const DeviceCloud& c, const KnnArgs& a, const int32_t* ord
   L.allowSelf = (a.optionFlags & 1u) ? 1 : 0;
   L.stats = (a.touchStats && a.touched) ? 1 : 0;
   L.nqDevice = a.nqDevice;
+  L.bQueryOffset = nullptr;
+  L.bNodeOffset = nullptr;
+  L.bK = nullptr;
+  L.bOutOffset = nullptr;
+  L.bClouds = 0;
   return L;
 }
 
@@ -198,7 +205,58 @@ int knn_leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t 
   return rc;
 }
 
+// Batched search over a forest: leaf order of all queries (each in its
+// cloud's tree), then one launch of the reference-order kernel. `order`,
+// `hist` (nodeCap entries), `cell` and `rank` (nq each) are caller scratch.
+template <typename T, int D>
+int knn_batch(const BatchArgs& b, cudaStream_t stream) {
+  if (b.nq == 0) return kOk;
+  const int K = round_k(b.kMax);
+  if (K < 0) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+  NABO_CUDA_TRY(cudaMemsetAsync(b.hist, 0, (size_t)b.nodeCap * sizeof(uint32_t), stream));
+  k_leaf_cells<T, D><<<ceil_div(b.nq, 256), 256, 0, stream>>>(static_cast<const Node<T>*>(b.nodes),
+                                                              static_cast<const T*>(b.query), b.nq, b.qStride, b.dim,
+                                                              b.cell, b.rank, b.hist, b.qOffset, b.nodeOffset,
+                                                              b.nClouds);
+  int rc = order_by_cells(b.cell, b.rank, b.hist, b.nodeCap, b.nq, b.order, stream);
+  if (rc != kOk) return rc;
+  KnnLaunch L;
+  std::memset(&L, 0, sizeof(L));
+  L.nodes = b.nodes;
+  L.recs = b.recs;
+  L.query = b.query;
+  L.nq = b.nq;
+  L.qStride = b.qStride;
+  L.dim = b.dim;
+  L.order = b.order;
+  L.k = b.kMax;
+  const T eps = (T)b.eps;
+  const T e1 = T(1) + eps;
+  L.maxError2 = (double)(T)(e1 * e1);
+  const T r = (T)b.maxRadius;
+  L.maxRadius2 = (double)(T)(r * r);
+  L.outIdx = b.indices;
+  L.outD2 = b.dists2;
+  L.allowSelf = (b.optionFlags & 1u) ? 1 : 0;
+  L.bQueryOffset = b.qOffset;
+  L.bNodeOffset = b.nodeOffset;
+  L.bK = b.kOf;
+  L.bOutOffset = b.outOffset;
+  L.bClouds = b.nClouds;
+  const int grid = ceil_div(b.nq, b.blockSize);
+#define NABO_LAUNCH(KK)                                                                     \
+  case KK:                                                                                  \
+    k_knn_kdtree<T, D, KK, kStackLarge><<<grid, b.blockSize, 0, stream>>>(L);               \
+    break;
+  switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+#undef NABO_LAUNCH
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "batched search launch");
+  return kOk;
+}
+
 #define NABO_SEARCH_INSTANTIATE(T, D)                                              \
+  template int knn_batch<T, D>(const BatchArgs&, cudaStream_t);                    \
   template int knn_leaf_order<T, D>(const DeviceCloud&, const void*, int64_t, int64_t, int32_t*, cudaStream_t); \
   template int knn_kdtree<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
   template int knn_bruteforce<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \

@@ -1,0 +1,139 @@
+"""Batches of uneven clouds: one forest build, one search launch, CUDA-graph
+replay and the autotuner -- against single-cloud searches and the oracle."""
+import numpy as np
+import pytest
+
+import helpers as H
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _nb():
+    import libnabo_gb300 as nb
+    return nb
+
+
+def _batch_data(n_clouds, lo, hi, seed, dtype=np.float32):
+    from libnabo_gb300 import synthetic as S
+    sizes = S.log_uniform_sizes(n_clouds, lo, hi, seed)
+    sizes[:4] = [3, 9, 200, 300][: min(4, n_clouds)]  # single bucket, tiny, below and above the top-phase size
+    rng = np.random.default_rng(seed + 1)
+    clouds = [S.gaussian_blobs(int(n), seed + 10 + i, dtype=dtype) for i, n in enumerate(sizes)]
+    queries = [(c + rng.normal(0, 0.01, c.shape)).astype(dtype) for c in clouds]
+    ks = rng.choice([1, 5, 16], n_clouds).astype(np.int32)
+    ks = np.minimum(ks, sizes - 1).astype(np.int32)
+    return clouds, queries, ks
+
+
+def _run_batch(clouds, queries, ks, dtype=np.float32, graph=False, **kw):
+    import torch
+    nb = _nb()
+    b = nb.BatchSearch([c.shape[0] for c in clouds], dim=clouds[0].shape[1], dtype=dtype, **kw)
+    b.set_queries([q.shape[0] for q in queries], ks)
+    tc = torch.from_numpy(np.concatenate(clouds)).cuda()
+    tq = torch.from_numpy(np.concatenate(queries)).cuda()
+    if graph:
+        idx, d2 = b.run(tc, tq)
+    else:
+        b.build(tc)
+        idx, d2 = b.knn(tq)
+    torch.cuda.synchronize()
+    return b, b.split(idx.cpu().numpy()), b.split(d2.cpu().numpy())
+
+
+def test_batch_trees_equal_oracle_trees():
+    clouds, queries, ks = _batch_data(40, 300, 30000, seed=1)
+    b, _, _ = _run_batch(clouds, queries, ks)
+    st = b.status()
+    assert st["ok"], st
+    for c, cloud in enumerate(clouds):
+        g = b.export_tree(c)
+        o = O.OracleTree(cloud).export()
+        for key in ("cut_dim", "right", "bucket_start", "bucket_count", "buckets"):
+            assert np.array_equal(g[key], o[key]), (c, key)
+        inner = o["cut_dim"] >= 0
+        assert np.array_equal(g["cut_val"][inner], o["cut_val"][inner]), c
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_batch_results_equal_single_searches(graph):
+    nb = _nb()
+    clouds, queries, ks = _batch_data(60, 300, 40000, seed=2)
+    b, bi, bd = _run_batch(clouds, queries, ks, graph=graph)
+    assert b.status()["ok"]
+    for c, (cloud, q) in enumerate(zip(clouds, queries)):
+        s = nb.NearestNeighbourSearch(cloud)
+        si, sd = s.knn(q, int(ks[c]))
+        H.assert_identical(bi[c], bd[c], si, sd, f"cloud {c} (n={cloud.shape[0]}, k={ks[c]})")
+        if c < 8:
+            oi, od, _ = O.OracleTree(cloud).knn(q, int(ks[c]), mode=O.MODE_CANONICAL)
+            H.assert_identical(bi[c], bd[c], oi, od, f"cloud {c} vs oracle")
+
+
+def test_graph_replay_follows_new_data():
+    import torch
+    nb = _nb()
+    clouds, queries, ks = _batch_data(30, 300, 20000, seed=3)
+    b = nb.BatchSearch([c.shape[0] for c in clouds])
+    b.set_queries([q.shape[0] for q in queries], ks)
+    tc = torch.from_numpy(np.concatenate(clouds)).cuda()
+    tq = torch.from_numpy(np.concatenate(queries)).cuda()
+    out = b._outputs(tq.device)
+    b.run(tc, tq, out=out)
+    torch.cuda.synchronize()
+    first = [x.copy() for x in b.split(out[0].cpu().numpy())]
+    # new coordinates of the same shapes written into the captured buffers
+    clouds2, queries2, _ = _batch_data(30, 300, 20000, seed=33)
+    clouds2 = [np.resize(c2, c.shape).astype(np.float32) for c, c2 in zip(clouds, clouds2)]
+    queries2 = [(c + 0.01).astype(np.float32) for c in clouds2]
+    tc.copy_(torch.from_numpy(np.concatenate(clouds2)).cuda())
+    tq.copy_(torch.from_numpy(np.concatenate(queries2)).cuda())
+    b.run(tc, tq, out=out)
+    torch.cuda.synchronize()
+    second_i = b.split(out[0].cpu().numpy())
+    second_d = b.split(out[1].cpu().numpy())
+    changed = 0
+    for c in range(len(clouds)):
+        oi, od, _ = O.OracleTree(clouds2[c]).knn(queries2[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        H.assert_identical(second_i[c], second_d[c], oi, od, f"replay cloud {c}")
+        changed += int(not np.array_equal(first[c], second_i[c]))
+    assert changed > 0
+
+
+def test_level_limit_is_reported():
+    nb = _nb()
+    import torch
+    clouds, queries, ks = _batch_data(8, 20000, 40000, seed=4)
+    b = nb.BatchSearch([c.shape[0] for c in clouds], maxLevels=2)
+    b.set_queries([q.shape[0] for q in queries], ks)
+    b.build(torch.from_numpy(np.concatenate(clouds)).cuda())
+    st = b.status()
+    assert not st["ok"] and (st["flags"] & 2)
+
+
+def test_non_finite_batch_is_reported():
+    nb = _nb()
+    import torch
+    clouds, queries, ks = _batch_data(5, 1000, 2000, seed=5)
+    clouds[3][7, 0] = np.nan
+    b = nb.BatchSearch([c.shape[0] for c in clouds])
+    b.set_queries([q.shape[0] for q in queries], ks)
+    b.build(torch.from_numpy(np.concatenate(clouds)).cuda())
+    assert b.status()["flags"] & 1
+
+
+def test_autotuner_choice_is_exact():
+    nb = _nb()
+    from libnabo_gb300 import autotune
+    clouds, queries, ks = _batch_data(48, 2000, 60000, seed=6)
+    choice = autotune.tune(clouds, queries, ks, sample=16, repeats=2)
+    assert choice["bucketSize"] in autotune.CANDIDATES["bucketSize"]
+    b, bi, bd = _run_batch(clouds, queries, ks, graph=True, bucketSize=choice["bucketSize"],
+                           threadsPerBlock=choice["threadsPerBlock"], maxLevels=choice["maxLevels"])
+    assert b.status()["ok"]
+    for c in range(0, len(clouds), 7):
+        oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        H.assert_identical(bi[c], bd[c], oi, od, f"tuned cloud {c}")
+    again = autotune.tune(clouds, queries, ks, sample=16, repeats=2)
+    assert again["cached"]
