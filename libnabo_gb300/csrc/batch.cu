@@ -96,6 +96,7 @@ int build(nabo_cuda_batch* b, const void* clouds, cudaStream_t st) {
   ForestOut f;
   f.recs = b->recs;
   f.nodes = b->nodes;
+  f.nodeCap = 2 * b->nTotal;
   f.nodeOffset = b->nodeOffset;
   const size_t es = b->dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
   f.rootLo = b->rootBox;

@@ -863,11 +863,26 @@ __device__ __forceinline__ int subtree_size(const TopNodes<T>& top, const SmallS
 // Pre-order numbering of all trees (single block): subtree sizes bottom-up,
 // each cloud's root at the running sum of the previous trees' sizes, then
 // positions top-down.
+//
+// A build that did not finish (status[1]: levels left over after a fixed
+// level count, or a capacity guard hit) has top nodes whose children were
+// never split, so no numbering exists. Every cloud then gets one leaf
+// holding all of its points instead: a well-formed forest that a search
+// (or a captured graph's search) can still traverse, and which gives exact
+// results for finite clouds.
 template <typename T>
 __global__ void k_renumber(TopNodes<T> top, SmallSegs<T> small, const int* lvStart, const int* lvCount,
-                           const LevelState* st, const int* rootRef, int nClouds, Node<T>* nodes,
-                           int64_t* nodeOffset) {
+                           const LevelState* st, const int* rootRef, const int64_t* __restrict__ off, int nClouds,
+                           int* status, Node<T>* nodes, int64_t nodeCap, int64_t* nodeOffset) {
   __shared__ int64_t carry;
+  if (status[1]) {
+    for (int c = threadIdx.x; c <= nClouds; c += blockDim.x) {
+      nodeOffset[c] = c;
+      if (c < nClouds && c < nodeCap) store_leaf(nodes + c, (uint32_t)(off[c + 1] - off[c]), (uint32_t)off[c]);
+    }
+    if (threadIdx.x == 0) status[2] = 0;
+    return;
+  }
   const int nLevels = st->nLevels;
   for (int l = nLevels - 1; l >= 0; --l) {
     const int b = lvStart[l], c = lvCount[l];
@@ -908,19 +923,27 @@ __global__ void k_renumber(TopNodes<T> top, SmallSegs<T> small, const int* lvSta
         top.pre[rref] = rp;
       else
         small.base[~rref] = rp;
-      store_inner(nodes + p, (uint32_t)top.dim[t], (uint32_t)rp, top.cut[t]);
+      if (p >= 0 && p < nodeCap)
+        store_inner(nodes + p, (uint32_t)top.dim[t], (uint32_t)rp, top.cut[t]);
+      else
+        atomicOr(status + 1, 1);  // unreachable for a finished build
     }
     __syncthreads();
   }
 }
 
 template <typename T>
-__global__ void k_copy_small(const Node<T>* scratch, SmallSegs<T> small, const int* nSmall, Node<T>* nodes) {
+__global__ void k_copy_small(const Node<T>* scratch, SmallSegs<T> small, const int* nSmall, int* status,
+                             Node<T>* nodes, int64_t nodeCap) {
   const int sid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (sid >= *nSmall) return;
+  if (status[1] || sid >= *nSmall) return;
   const int base = small.base[sid];
   const Node<T>* src = scratch + 2 * (int64_t)small.start[sid];
   const int cnt = small.size[sid];
+  if (base < 0 || base + (int64_t)cnt > nodeCap) {
+    atomicOr(status + 1, 1);  // unreachable for a finished build
+    return;
+  }
   for (int i = 0; i < cnt; ++i) {
     Node<T> nd = src[i];
     if (!node_is_leaf(nd.meta)) nd.meta = make_meta(node_dim(nd.meta), (uint32_t)base + node_payload(nd.meta));
@@ -928,8 +951,9 @@ __global__ void k_copy_small(const Node<T>* scratch, SmallSegs<T> small, const i
   }
 }
 
-// status[0] non-finite input (set by k_bounds_forest), [1] capacity
-// exceeded, [2] tallest tree's height, [3] top levels run.
+// status[0] non-finite input (set by k_bounds_forest), [1] build did not
+// finish (capacity exceeded or levels left over), [2] tallest tree's height,
+// [3] top levels run. Runs before the numbering, which reads [1].
 __global__ void k_forest_status(const LevelState* st, const int* counters, int* status) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   status[1] = (counters[3] || st->overflow || st->nseg > 0) ? 1 : 0;
@@ -1174,9 +1198,11 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
                                                              bucketSize, counters);
   NABO_CUDA_TRY(cudaGetLastError());
   Node<T>* nodes = static_cast<Node<T>*>(f->nodes);
-  k_renumber<T><<<1, 1024, 0, stream>>>(top, small, lv, lv + lvCap, st, rootRef, nClouds, nodes, f->nodeOffset);
-  k_copy_small<T><<<ceil_div(nSmallHost, 128), 128, 0, stream>>>(scratchNodes, small, counters + 1, nodes);
   k_forest_status<<<1, 1, 0, stream>>>(st, counters, f->status);
+  k_renumber<T><<<1, 1024, 0, stream>>>(top, small, lv, lv + lvCap, st, rootRef, dOff, nClouds, f->status, nodes,
+                                        f->nodeCap, f->nodeOffset);
+  k_copy_small<T><<<ceil_div(nSmallHost, 128), 128, 0, stream>>>(scratchNodes, small, counters + 1, f->status,
+                                                                 nodes, f->nodeCap);
   NABO_CUDA_TRY(cudaGetLastError());
   if (hostDriven) {
     int hs[4];
@@ -1210,6 +1236,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   NABO_CUDA_TRY(cudaMemcpyAsync(off, hoff, sizeof(hoff), cudaMemcpyHostToDevice, stream));
   f.recs = recs;
   f.nodes = nodes;
+  f.nodeCap = nodeCap;
   f.rootLo = rootBox;
   f.rootHi = rootBox + kMaxDim;
   const int rc = build_forest<T, D>(dCloud, n, stride, dim, bucketSize, off, 1, -1, stream, &f);

@@ -80,6 +80,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
 struct ForestOut {
   void* recs = nullptr;
   void* nodes = nullptr;
+  int64_t nodeCap = 0;  // entries of `nodes`
   int64_t* nodeOffset = nullptr;
   void* rootLo = nullptr;
   void* rootHi = nullptr;

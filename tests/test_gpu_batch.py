@@ -101,15 +101,18 @@ def test_graph_replay_follows_new_data():
     assert changed > 0
 
 
-def test_level_limit_is_reported():
-    nb = _nb()
-    import torch
-    clouds, queries, ks = _batch_data(8, 20000, 40000, seed=4)
-    b = nb.BatchSearch([c.shape[0] for c in clouds], maxLevels=2)
-    b.set_queries([q.shape[0] for q in queries], ks)
-    b.build(torch.from_numpy(np.concatenate(clouds)).cuda())
+@pytest.mark.parametrize("graph", [False, True])
+def test_level_limit_is_reported_and_search_stays_exact(graph):
+    """Too few levels for the clouds: the build reports it, and every cloud
+    becomes one leaf, so the same launch still returns exact neighbours."""
+    clouds, queries, ks = _batch_data(8, 2000, 6000, seed=4)
+    b, bi, bd = _run_batch(clouds, queries, ks, graph=graph, maxLevels=2)
     st = b.status()
-    assert not st["ok"] and (st["flags"] & 2)
+    assert not st["ok"] and (st["flags"] & 2), st
+    assert st["nodes"] == len(clouds) and st["height"] == 0, st
+    for c in (0, 3, 7):
+        oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        H.assert_identical(bi[c], bd[c], oi, od, f"level-limited cloud {c}")
 
 
 def test_non_finite_batch_is_reported():
