@@ -201,6 +201,11 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
 int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist, int64_t bins, int64_t nq,
                    int32_t* dOrder, cudaStream_t stream);
 
+// Stable sort of element indices 0..n-1 (or of dVals, when given) by the
+// low `bits` bits of dKeys, written to dOrder; dKeys is clobbered.
+int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaStream_t stream,
+                   const uint32_t* dVals = nullptr);
+
 // Device-wide exclusive scan of uint32 values (in place), returns total via
 // a device pointer. Scratch is stream-ordered.
 int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t stream);

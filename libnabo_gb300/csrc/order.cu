@@ -1,16 +1,21 @@
-// order.cu -- query ordering for warp coherence, and a device-wide scan.
+// order.cu -- query ordering for warp coherence, a stable radix sort and a
+// device-wide scan.
 //
-// A query ordering is a counting sort by cell: every query gets a cell id
-// and a rank inside its cell (an atomic increment of the cell's count), the
-// counts are scanned into offsets and each query is placed at offset+rank.
-// The kd-tree search uses the leaf each query descends to as its cell
-// (k_leaf_cells in search.cuh), which groups queries at the scale of the
-// data's own buckets. order_queries() offers a Morton (Z-order) cell over
-// the bounding box for searches without a tree. The order inside a cell is
-// whatever the atomics produce; results do not depend on it, only timing.
+// The kd-tree search runs one query per thread, so its warps stay coherent
+// only if neighbouring threads get nearby queries. order_queries() sorts the
+// queries by a 30-bit Morton (Z-order) code over the cloud's bounding box
+// with a stable radix sort: ties (queries in one Morton cell) keep input
+// order, which for scanned data keeps the points of one scan line together
+// and makes the warps' result rows adjacent in memory. The kd-tree path for
+// more than 3 dimensions sorts by the leaf each query descends to instead
+// (same stable sort). order_by_cells() is the counting-sort placement the
+// batched search uses (cells = leaves, ranks from atomics, then each
+// cell's queries back in index order). Results never depend on the order,
+// only timing does.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 
 #include "internal.cuh"
@@ -86,8 +91,7 @@ struct CellParams {
 };
 
 template <typename T>
-__global__ void k_cells(const T* __restrict__ q, int64_t nq, int64_t qStride, CellParams p, uint32_t* cell,
-                        uint32_t* rank, uint32_t* hist) {
+__global__ void k_morton_keys(const T* __restrict__ q, int64_t nq, int64_t qStride, CellParams p, uint32_t* key) {
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
   uint32_t c[kMortonDims];
@@ -96,18 +100,85 @@ __global__ void k_cells(const T* __restrict__ q, int64_t nq, int64_t qStride, Ce
   for (int d = 0; d < kMortonDims; ++d) {
     if (d < p.dims) {
       float v = ((float)q[i * qStride + d] - p.lo[d]) * p.scale[d];
-      v = fminf(fmaxf(v, 0.0f), maxc);
+      v = fminf(fmaxf(v, 0.0f), maxc);  // NaN -> 0
       c[d] = (uint32_t)v;
     } else {
       c[d] = 0;
     }
   }
-  uint32_t key = 0;
+  uint32_t k = 0;
   for (int b = p.bits - 1; b >= 0; --b)
-    for (int d = 0; d < p.dims; ++d) key = (key << 1) | ((c[d] >> b) & 1u);
-  const uint32_t cl = key >> p.shift;
-  cell[i] = cl;
-  rank[i] = atomicAdd(hist + cl, 1u);
+    for (int d = 0; d < p.dims; ++d) k = (k << 1) | ((c[d] >> b) & 1u);
+  key[i] = k;
+}
+
+__global__ void k_iota(uint32_t* v, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (uint32_t)i;
+}
+
+// ---- stable LSD radix sort of (key, value) pairs, 10-bit digits.
+// Each warp owns a tile of `rounds` x 32 consecutive elements. Pass p:
+// k_radix_hist counts the tile's digits; the counts, laid out digit-major
+// ([digit][tile]), are scanned into the tile's first output slot per digit;
+// k_radix_scatter walks the tile in element order, 32 at a time, ranking
+// equal digits inside the 32 with __match_any_sync, so equal keys keep their
+// order (stability, which LSD needs across passes).
+constexpr int kRadixBits = 10;
+constexpr int kRadix = 1 << kRadixBits;
+constexpr int kSortWarps = 4;
+
+__global__ void k_radix_hist(const uint32_t* __restrict__ key, int64_t n, int shift, int rounds, int64_t nTiles,
+                             uint32_t* hist) {
+  extern __shared__ uint32_t sh[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tile = (int64_t)blockIdx.x * kSortWarps + warp;
+  if (tile >= nTiles) return;  // warp-uniform
+  uint32_t* h = sh + warp * kRadix;
+  for (int d = lane; d < kRadix; d += 32) h[d] = 0u;
+  __syncwarp();
+  const int64_t base = tile * rounds * 32;
+  for (int r = 0; r < rounds; ++r) {
+    const int64_t i = base + (int64_t)r * 32 + lane;
+    if (i < n) atomicAdd(h + ((key[i] >> shift) & (kRadix - 1)), 1u);
+  }
+  __syncwarp();
+  for (int d = lane; d < kRadix; d += 32) hist[(int64_t)d * nTiles + tile] = h[d];
+}
+
+__global__ void k_radix_scatter(const uint32_t* __restrict__ keyIn, const uint32_t* __restrict__ valIn, int64_t n,
+                                int shift, int rounds, int64_t nTiles, const uint32_t* __restrict__ offs,
+                                uint32_t* keyOut, uint32_t* valOut) {
+  extern __shared__ uint32_t sh[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tile = (int64_t)blockIdx.x * kSortWarps + warp;
+  if (tile >= nTiles) return;  // warp-uniform
+  uint32_t* h = sh + warp * kRadix;
+  for (int d = lane; d < kRadix; d += 32) h[d] = offs[(int64_t)d * nTiles + tile];
+  __syncwarp();
+  const uint32_t below = (1u << lane) - 1u;
+  const int64_t base = tile * rounds * 32;
+  for (int r = 0; r < rounds; ++r) {
+    const int64_t i = base + (int64_t)r * 32 + lane;
+    const bool act = i < n;
+    const unsigned live = __ballot_sync(0xffffffffu, act);
+    if (live == 0u) break;  // warp-uniform: the tile's tail is past n
+    uint32_t k = 0u, v = 0u, d = 0u, peers = 0u, pos = 0u;
+    if (act) {
+      k = keyIn[i];
+      v = valIn[i];
+      d = (k >> shift) & (kRadix - 1);
+      peers = __match_any_sync(live, d);
+      pos = h[d] + __popc(peers & below);
+    }
+    __syncwarp();
+    if (act && lane == 31 - __clz(peers)) h[d] += __popc(peers);
+    __syncwarp();
+    if (act) {
+      keyOut[pos] = k;
+      valOut[pos] = v;
+    }
+  }
 }
 
 __global__ void k_place(const uint32_t* __restrict__ cell, const uint32_t* __restrict__ rank,
@@ -115,6 +186,30 @@ __global__ void k_place(const uint32_t* __restrict__ cell, const uint32_t* __res
   const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= nq) return;
   order[start[cell[i]] + rank[i]] = (int32_t)i;
+}
+
+// Puts the queries of each cell back in index order (the atomic ranks of
+// k_place are in arrival order): queries that are neighbours in the input
+// (points of one scan line, say) then share warps in input order, so the
+// warps' result rows lie side by side and their stores coalesce. Cells with
+// more than kRunSort queries keep arrival order; the order only affects
+// speed, never results.
+constexpr int kRunSort = 64;
+__global__ void k_sort_runs(const uint32_t* __restrict__ start, int64_t bins, int64_t nq, int32_t* order) {
+  const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (b >= bins) return;
+  const int64_t s = start[b];
+  const int64_t e = b + 1 < bins ? (int64_t)start[b + 1] : nq;
+  if (e - s < 2 || e - s > kRunSort) return;
+  for (int64_t i = s + 1; i < e; ++i) {
+    const int32_t v = order[i];
+    int64_t j = i - 1;
+    while (j >= s && order[j] > v) {
+      order[j + 1] = order[j];
+      --j;
+    }
+    order[j + 1] = v;
+  }
 }
 
 }  // namespace
@@ -137,22 +232,69 @@ int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist
   const int rc = scan_exclusive_u32(dHist, bins, nullptr, stream);
   if (rc != kOk) return rc;
   k_place<<<ceil_div(nq, kB), kB, 0, stream>>>(dCell, dRank, dHist, nq, dOrder);
+  k_sort_runs<<<ceil_div(bins, kB), kB, 0, stream>>>(dHist, bins, nq, dOrder);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "order_by_cells");
   return kOk;
 }
 
+int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaStream_t stream, const uint32_t* dVals) {
+  if (n <= 0) return kOk;
+  if (n > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
+  // tiles of at least 32 rounds, few enough that the [digit][tile] counts
+  // stay below 2^26 entries
+  int rounds = 32;
+  while (ceil_div(n, (int64_t)rounds * 32) * kRadix > (int64_t(1) << 26)) rounds *= 2;
+  const int64_t nTiles = ceil_div(n, (int64_t)rounds * 32);
+  const int passes = std::max(1, (bits + kRadixBits - 1) / kRadixBits);
+  uint32_t *k2 = nullptr, *v1 = nullptr, *v2 = nullptr, *hist = nullptr;
+  cudaError_t e = scratch_alloc((void**)&k2, (size_t)n * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&v1, (size_t)n * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&v2, (size_t)n * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&hist, (size_t)(kRadix * nTiles) * sizeof(uint32_t), stream);
+  int rc = e == cudaSuccess ? kOk : cuda_error(e, "sort scratch");
+  if (rc == kOk) {
+    if (dVals)
+      e = cudaMemcpyAsync(v1, dVals, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream);
+    else
+      e = cudaSuccess;
+    if (e != cudaSuccess) rc = cuda_error(e, "sort values");
+  }
+  if (rc == kOk && !dVals) {
+    // identity values: the caller's keys are in element order
+    k_iota<<<ceil_div(n, kB), kB, 0, stream>>>(v1, n);
+  }
+  uint32_t *kin = dKeys, *vin = v1, *kout = k2, *vout = v2;
+  const int blocks = (int)ceil_div(nTiles, (int64_t)kSortWarps);
+  const size_t smem = (size_t)kSortWarps * kRadix * sizeof(uint32_t);
+  for (int p = 0; p < passes && rc == kOk; ++p) {
+    const int shift = p * kRadixBits;
+    k_radix_hist<<<blocks, 32 * kSortWarps, smem, stream>>>(kin, n, shift, rounds, nTiles, hist);
+    rc = scan_exclusive_u32(hist, kRadix * nTiles, nullptr, stream);
+    if (rc != kOk) break;
+    k_radix_scatter<<<blocks, 32 * kSortWarps, smem, stream>>>(kin, vin, n, shift, rounds, nTiles, hist, kout, vout);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_error(e, "radix sort");
+    std::swap(kin, kout);
+    std::swap(vin, vout);
+  }
+  if (rc == kOk) {
+    e = cudaMemcpyAsync(dOrder, vin, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream);
+    if (e != cudaSuccess) rc = cuda_error(e, "sort output");
+  }
+  for (void* ptr : {(void*)k2, (void*)v1, (void*)v2, (void*)hist})
+    if (ptr) scratch_free(ptr, stream);
+  return rc;
+}
+
 template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
                   int32_t* dOrder, cudaStream_t stream) {
+  if (nq <= 0) return kOk;
   CellParams p;
   p.dims = std::min(dim, kMortonDims);
   p.bits = 30 / p.dims;
-  const int keyBits = p.bits * p.dims;
-  int want = 1;
-  while ((int64_t(1) << want) < nq && want < 30) ++want;
-  const int B = std::max(1, std::min({keyBits, want + 1, 22}));
-  p.shift = keyBits - B;
+  p.shift = 0;
   for (int d = 0; d < kMortonDims; ++d) {
     if (d < p.dims) {
       const double ext = hi[d] - lo[d];
@@ -163,22 +305,11 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
       p.scale[d] = 0.0f;
     }
   }
-  const int64_t bins = int64_t(1) << B;
-  uint32_t *hist = nullptr, *cell = nullptr, *rank = nullptr;
-  NABO_CUDA_TRY(scratch_alloc((void**)&hist, (size_t)bins * sizeof(uint32_t), stream));
-  NABO_CUDA_TRY(scratch_alloc((void**)&cell, (size_t)nq * sizeof(uint32_t), stream));
-  NABO_CUDA_TRY(scratch_alloc((void**)&rank, (size_t)nq * sizeof(uint32_t), stream));
-  NABO_CUDA_TRY(cudaMemsetAsync(hist, 0, (size_t)bins * sizeof(uint32_t), stream));
-  k_cells<T><<<ceil_div(nq, kB), kB, 0, stream>>>(dQuery, nq, qStride, p, cell, rank, hist);
-  int rc = scan_exclusive_u32(hist, bins, nullptr, stream);
-  if (rc == kOk) {
-    k_place<<<ceil_div(nq, kB), kB, 0, stream>>>(cell, rank, hist, nq, dOrder);
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) rc = cuda_error(e, "order_queries");
-  }
-  scratch_free(hist, stream);
-  scratch_free(cell, stream);
-  scratch_free(rank, stream);
+  uint32_t* keys = nullptr;
+  NABO_CUDA_TRY(scratch_alloc((void**)&keys, (size_t)nq * sizeof(uint32_t), stream));
+  k_morton_keys<T><<<ceil_div(nq, kB), kB, 0, stream>>>(dQuery, nq, qStride, p, keys);
+  const int rc = sort_order_u32(keys, nq, p.bits * p.dims, dOrder, stream);
+  scratch_free(keys, stream);
   return rc;
 }
 

@@ -11,12 +11,15 @@
 // decision because head never grows. Every +,-,* is separately rounded
 // (no FMA contraction) so distances are bit-identical to the CPU oracle.
 //
-// Top-k: K (dist2, index) pairs in registers, kept in descending order so
-// the head (largest) is slot 0; slots >= k hold -inf so one instantiation
-// serves every k <= K. Pairs are ordered by (dist2, index): among equal
-// distances the lower index is kept, which makes the result independent of
-// visit order (the reference's IndexHeapBruteForceVector keeps the first
-// visited, nabo/index_heap.h:322-334).
+// Top-k: K (dist2, index) entries in registers, kept in descending order so
+// the head (largest) is slot 0; slots >= k hold a value below every entry so
+// one instantiation serves every k <= K. Entries are ordered by (dist2,
+// index): among equal distances the lower index is kept, which makes the
+// result independent of visit order (the reference's
+// IndexHeapBruteForceVector keeps the first visited, nabo/index_heap.h:
+// 322-334). Insertion is branch-free: with g[j] = (slot j > new entry),
+// which is true for a prefix of the slots, slot j takes slot j+1 while
+// g[j+1], the new entry where the prefix ends, and keeps its value after.
 #pragma once
 
 #include "common.cuh"
@@ -28,6 +31,7 @@ __device__ __forceinline__ bool pair_greater(T da, int ia, T db, int ib) {
   return da > db || (da == db && ia > ib);
 }
 
+// Generic form (double): separate distance and index arrays.
 template <typename T, int K>
 struct TopK {
   T d[K];
@@ -42,23 +46,17 @@ struct TopK {
   __device__ __forceinline__ T head() const { return d[0]; }
   __device__ __forceinline__ bool accepts(T dist, int idx) const { return pair_greater(d[0], i[0], dist, idx); }
   // Drops the head and inserts (dist, idx); requires accepts(dist, idx).
-  // Slot j takes its successor while that is still larger than the new
-  // pair, then the new pair, then keeps its own value.
   __device__ __forceinline__ void insert(T dist, int idx) {
+    bool g[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) g[j] = pair_greater(d[j], i[j], dist, idx);
 #pragma unroll
     for (int j = 0; j + 1 < K; ++j) {
-      if (pair_greater(d[j + 1], i[j + 1], dist, idx)) {
-        d[j] = d[j + 1];
-        i[j] = i[j + 1];
-      } else if (pair_greater(d[j], i[j], dist, idx)) {
-        d[j] = dist;
-        i[j] = idx;
-      }
+      d[j] = g[j + 1] ? d[j + 1] : (g[j] ? dist : d[j]);
+      i[j] = g[j + 1] ? i[j + 1] : (g[j] ? idx : i[j]);
     }
-    if (pair_greater(d[K - 1], i[K - 1], dist, idx)) {
-      d[K - 1] = dist;
-      i[K - 1] = idx;
-    }
+    d[K - 1] = g[K - 1] ? dist : d[K - 1];
+    i[K - 1] = g[K - 1] ? idx : i[K - 1];
   }
   // Writes the k entries in ascending order; returns how many are valid.
   __device__ __forceinline__ int store(int k, int32_t* __restrict__ oi, T* __restrict__ od) const {
@@ -69,6 +67,66 @@ struct TopK {
         oi[k - 1 - j] = i[j];
         od[k - 1 - j] = d[j];
         found += i[j] >= 0 ? 1 : 0;
+      }
+    }
+    return found;
+  }
+};
+
+// float: one 64-bit key per entry, (bit pattern of dist2) << 32 | index.
+// Distances are >= 0, where the IEEE bit pattern orders like the value, so
+// one unsigned comparison orders (dist2, index). An empty slot is
+// (+inf, 0): no finite distance compares above it and no infinite one
+// below, as the reference's strict `dist < head` with head = +inf
+// (nabo/kdtree_cpu.cpp:392-396); it is written out as (-1, +inf). Padding
+// slots (>= k) hold 0.
+template <int K>
+struct TopK<float, K> {
+  uint64_t key[K];
+  static __device__ __forceinline__ uint64_t make(float dist, int idx) {
+    return (uint64_t(__float_as_uint(dist)) << 32) | (uint32_t)idx;
+  }
+  __device__ __forceinline__ void init(int k) {
+#pragma unroll
+    for (int j = 0; j < K; ++j) key[j] = j < k ? (uint64_t(0x7f800000u) << 32) : 0ull;
+  }
+  __device__ __forceinline__ float head() const { return __uint_as_float((uint32_t)(key[0] >> 32)); }
+  __device__ __forceinline__ bool accepts(float dist, int idx) const { return make(dist, idx) < key[0]; }
+  __device__ __forceinline__ void insert(float dist, int idx) {
+    const uint64_t x = make(dist, idx);
+    bool g[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) g[j] = key[j] > x;
+#pragma unroll
+    for (int j = 0; j + 1 < K; ++j) key[j] = g[j + 1] ? key[j + 1] : (g[j] ? x : key[j]);
+    key[K - 1] = g[K - 1] ? x : key[K - 1];
+  }
+  __device__ __forceinline__ uint32_t out_idx(int j) const {
+    return (uint32_t)(key[j] >> 32) == 0x7f800000u ? 0xffffffffu : (uint32_t)key[j];
+  }
+  // Writes the k entries in ascending order (slot j goes to position
+  // k-1-j); returns how many are valid. When both rows are 8-byte aligned,
+  // positions (p, p+1) with p even go out as one 64-bit store per row.
+  __device__ __forceinline__ int store(int k, int32_t* __restrict__ oi, float* __restrict__ od) const {
+    int found = 0;
+    const bool pairs = ((reinterpret_cast<uintptr_t>(oi) | reinterpret_cast<uintptr_t>(od)) & 7u) == 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      if (j < k) {
+        const int p = k - 1 - j;
+        found += (uint32_t)(key[j] >> 32) == 0x7f800000u ? 0 : 1;
+        if (!pairs) {
+          oi[p] = (int32_t)out_idx(j);
+          od[p] = __uint_as_float((uint32_t)(key[j] >> 32));
+        } else if ((p & 1) == 0) {
+          if (j >= 1) {  // slot j-1 is position p+1
+            *reinterpret_cast<uint2*>(oi + p) = make_uint2(out_idx(j), out_idx(j - 1));
+            *reinterpret_cast<uint2*>(od + p) = make_uint2((uint32_t)(key[j] >> 32), (uint32_t)(key[j - 1] >> 32));
+          } else {
+            oi[p] = (int32_t)out_idx(j);
+            od[p] = __uint_as_float((uint32_t)(key[j] >> 32));
+          }
+        }
       }
     }
     return found;
@@ -97,10 +155,12 @@ __device__ __forceinline__ T dist2_seq(const T (&q)[D], const Rec<T, D>& r) {
   return dist;
 }
 
-// Query ordering for the kd-tree: each query's cell is the leaf it reaches
+// Leaf cells for query ordering: each query's cell is the leaf it reaches
 // by always taking its near side (new_off > 0 -> right, as the search
 // does). Leaves are numbered in pre-order, so queries sorted by leaf are
-// grouped at the scale of the data's own buckets.
+// grouped at the scale of the data's own buckets. With `hist` set, also
+// counts the queries per leaf and gives each its rank (for a counting
+// sort).
 template <typename T, int D>
 __global__ void k_leaf_cells(const Node<T>* __restrict__ nodes, const T* __restrict__ query, int64_t nq,
                              int64_t qStride, int dim, uint32_t* cell, uint32_t* rank, uint32_t* hist,
@@ -119,7 +179,7 @@ __global__ void k_leaf_cells(const Node<T>* __restrict__ nodes, const T* __restr
     node = newOff > T(0) ? node_payload(nd.meta) : node + 1;
   }
   cell[i] = node;
-  rank[i] = atomicAdd(hist + node, 1u);
+  if (hist) rank[i] = atomicAdd(hist + node, 1u);
 }
 
 struct KnnLaunch {
@@ -153,17 +213,19 @@ struct KnnLaunch {
 };
 
 // Leaf scan shared by the kernels: the bucket's records are read in chunks
-// of 8 (independent loads in flight), candidates that beat the current head
-// are collected in a bit mask and inserted afterwards. The order of
-// insertion inside a leaf does not change the heap after the leaf (the k
-// smallest pairs of the union), so this matches the reference's point-by-
-// point loop (nabo/kdtree_cpu.cpp:378-398); the warp pays for the largest
-// number of insertions of any lane instead of for every point where some
-// lane inserts.
+// of 4 (independent loads in flight; the reference's buckets of at most 8
+// hold 3.8 points on average on lidar scans, so wider chunks mostly compute
+// empty slots), candidates that beat the current head are collected in a
+// bit mask and inserted afterwards. The order of insertion inside a leaf
+// does not change the heap after the leaf (the k smallest pairs of the
+// union), so this matches the reference's point-by-point loop
+// (nabo/kdtree_cpu.cpp:378-398); the warp pays for the largest number of
+// insertions of any lane instead of for every point where some lane
+// inserts.
 template <typename T, int D, int K>
 __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, uint32_t st, uint32_t cnt,
-                                          const T (&q)[D], T maxRadius2, bool selfOk, bool want, TopK<T, K>& heap) {
-  constexpr int kChunk = 8;
+                                          const T (&q)[D], T maxRadius2, T minDist, bool want, TopK<T, K>& heap) {
+  constexpr int kChunk = 4;
   for (uint32_t base = 0; base < cnt; base += kChunk) {
     T dj[kChunk];
     int ij[kChunk];
@@ -178,7 +240,7 @@ __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, ui
         dj[j] = dist2_seq(q, r);
         ij[j] = r.p.idx;
         const bool ok = want && dj[j] <= maxRadius2 && heap.accepts(dj[j], ij[j]) &&
-                        (selfOk || dj[j] > Ar<T>::eps());
+                        dj[j] > minDist;
         mask |= ok ? (1u << j) : 0u;
       }
     }
@@ -199,17 +261,99 @@ __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, ui
   }
 }
 
+// A pushed far child as 32-bit words [rd | off[0..D-1] | node] (a T is one
+// word for float, two for double) in 16-byte chunks: a push is one 128-bit
+// local store per chunk (a lone trailing word is stored alone), a pop reads
+// the first chunk, which holds rd, and the rest only if the child is
+// visited.
+template <typename T, int D>
+struct StackRec {
+  static constexpr int kTW = (int)(sizeof(T) / 4);
+  static constexpr int kWords = kTW * (D + 1) + 1;
+  static constexpr int kChunks = (kWords + 3) / 4;
+  static constexpr int kNode = kTW * (D + 1);
+  uint4 v[kChunks];
+};
+
+__device__ __forceinline__ void put_t(uint32_t* w, int i, float x) { w[i] = __float_as_uint(x); }
+__device__ __forceinline__ void put_t(uint32_t* w, int i, double x) {
+  w[i] = (uint32_t)__double2loint(x);
+  w[i + 1] = (uint32_t)__double2hiint(x);
+}
+template <typename T>
+__device__ __forceinline__ T get_t(const uint32_t* w, int i);
+template <>
+__device__ __forceinline__ float get_t<float>(const uint32_t* w, int i) {
+  return __uint_as_float(w[i]);
+}
+template <>
+__device__ __forceinline__ double get_t<double>(const uint32_t* w, int i) {
+  return __hiloint2double((int)w[i + 1], (int)w[i]);
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void stack_push(StackRec<T, D>* stk, int sp, T rd, const T (&off)[D], int cd, T newOff,
+                                           uint32_t node) {
+  using R = StackRec<T, D>;
+  uint32_t w[R::kChunks * 4];
+#pragma unroll
+  for (int i = 0; i < R::kChunks * 4; ++i) w[i] = 0u;
+  put_t(w, 0, rd);
+#pragma unroll
+  for (int d = 0; d < D; ++d) put_t(w, R::kTW * (1 + d), d == cd ? newOff : off[d]);
+  w[R::kNode] = node;
+#pragma unroll
+  for (int c = 0; c < R::kChunks; ++c) {
+    if (c == R::kChunks - 1 && R::kWords % 4 == 1)
+      stk[sp].v[c].x = w[4 * c];
+    else
+      stk[sp].v[c] = make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+  }
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T stack_rd(const StackRec<T, D>* stk, int sp) {
+  const uint4 c0 = stk[sp].v[0];
+  const uint32_t w[4] = {c0.x, c0.y, c0.z, c0.w};
+  return get_t<T>(w, 0);
+}
+
+template <typename T, int D>
+__device__ __forceinline__ uint32_t stack_take(const StackRec<T, D>* stk, int sp, T (&off)[D]) {
+  using R = StackRec<T, D>;
+  uint32_t w[R::kChunks * 4];
+#pragma unroll
+  for (int c = 0; c < R::kChunks; ++c) {
+    if (c == R::kChunks - 1 && R::kWords % 4 == 1) {
+      w[4 * c] = stk[sp].v[c].x;
+      w[4 * c + 1] = w[4 * c + 2] = w[4 * c + 3] = 0u;
+    } else {
+      const uint4 v = stk[sp].v[c];
+      w[4 * c] = v.x;
+      w[4 * c + 1] = v.y;
+      w[4 * c + 2] = v.z;
+      w[4 * c + 3] = v.w;
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < D; ++d) off[d] = get_t<T>(w, R::kTW * (1 + d));
+  return w[R::kNode];
+}
+
 // Reference-order traversal, structured descend / leaf / pop so the lanes
 // of a warp run each phase together: all lanes descend until every lane
 // stands on a leaf, then all scan their leaves, then all pop.
 template <typename T, int D, int K, int STACK>
 __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
-  const bool selfOk = a.allowSelf != 0;
+  // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396): without
+  // ALLOW_SELF_MATCH a point at distance <= epsilon is skipped; one compare
+  // against -1 (everything passes) or epsilon
+  const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
   const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
   const T* __restrict__ query = static_cast<const T*>(a.query);
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  unsigned long long touched = 0;
+  uint32_t touched = 0;  // a query touches at most the cloud's n < 2^31 points
   if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
     const int64_t qi = a.order ? (int64_t)a.order[t] : t;
     int k = a.k;
@@ -235,9 +379,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
     T off[D];
 #pragma unroll
     for (int d = 0; d < D; ++d) off[d] = T(0);
-    uint32_t sNode[STACK];
-    T sRd[STACK];
-    T sOff[STACK][D];
+    StackRec<T, D> stk[STACK];
     int sp = 0;
     uint32_t node = root;
     T rd = T(0);
@@ -254,30 +396,23 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
         const uint32_t farN = newOff > T(0) ? node + 1 : right;
         // sp <= tree height <= STACK (checked on the host); the test only
         // makes the bound explicit
-        if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < STACK) {
-          sNode[sp] = farN;
-          sRd[sp] = rdFar;
-#pragma unroll
-          for (int d = 0; d < D; ++d) sOff[sp][d] = d == cd ? newOff : off[d];
-          ++sp;
-        }
+        if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < STACK)
+          stack_push(stk, sp++, rdFar, off, cd, newOff, farN);
         node = nearN;
         nd = load_node(nodes, node);
       }
       // leaf
       const uint32_t cnt = node_payload(nd.meta);
-      scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, selfOk, true, heap);
+      scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap);
       touched += cnt;
       // pop the next far child that can still hold a better neighbour
       bool more = false;
       while (sp > 0) {
         --sp;
-        const T e = sRd[sp];
+        const T e = stack_rd(stk, sp);
         if (Ar<T>::mul(e, maxError2) <= heap.head()) {
           rd = e;
-          node = sNode[sp];
-#pragma unroll
-          for (int d = 0; d < D; ++d) off[d] = sOff[sp][d];
+          node = stack_take(stk, sp, off);
           more = true;
           break;
         }
@@ -288,9 +423,10 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
     if (a.found) a.found[qi] = f;
   }
   if (a.stats) {
+    unsigned long long sum = touched;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) touched += __shfl_xor_sync(0xffffffffu, touched, o);
-    if ((threadIdx.x & 31) == 0 && touched) atomicAdd(a.touched, touched);
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if ((threadIdx.x & 31) == 0 && sum) atomicAdd(a.touched, sum);
   }
 }
 
@@ -323,7 +459,10 @@ __device__ __forceinline__ T box_dist2(const T (&off)[D]) {
 template <typename T, int D, int K, int STACK>
 __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
   constexpr unsigned kAll = 0xffffffffu;
-  const bool selfOk = a.allowSelf != 0;
+  // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396): without
+  // ALLOW_SELF_MATCH a point at distance <= epsilon is skipped; one compare
+  // against -1 (everything passes) or epsilon
+  const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
   const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
   const T* __restrict__ query = static_cast<const T*>(a.query);
@@ -382,7 +521,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
         node = first;
         continue;
       }
-      scan_leaf<T, D, K>(recs, node_start(nd), node_payload(nd.meta), q, maxRadius2, selfOk, want, heap);
+      scan_leaf<T, D, K>(recs, node_start(nd), node_payload(nd.meta), q, maxRadius2, minDist, want, heap);
     }
     if (sp == 0) break;
     --sp;
@@ -401,7 +540,10 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
 // query and its top-k. Points are offered in index order.
 template <typename T, int D, int K>
 __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a) {
-  const bool selfOk = a.allowSelf != 0;
+  // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396): without
+  // ALLOW_SELF_MATCH a point at distance <= epsilon is skipped; one compare
+  // against -1 (everything passes) or epsilon
+  const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
   constexpr int kTile = (int)((24 * 1024) / sizeof(Rec<T, D>));
   __shared__ Rec<T, D> tile[kTile];
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
@@ -433,7 +575,7 @@ __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a) {
       for (int j = 0; j < m; ++j) {
         const Rec<T, D>& r = tile[j];
         const T dist = dist2_seq(q, r);
-        if (dist <= maxRadius2 && heap.accepts(dist, r.p.idx) && (selfOk || dist > Ar<T>::eps()))
+        if (dist <= maxRadius2 && heap.accepts(dist, r.p.idx) && dist > minDist)
           heap.insert(dist, r.p.idx);
       }
     }
