@@ -61,17 +61,22 @@ __global__ void k_block_sums(const uint32_t* __restrict__ data, int64_t n, uint3
   if (threadIdx.x == 0) sums[blockIdx.x] = t;
 }
 
+// Single block: each thread scans a contiguous run of the block sums
+// serially, one block-wide scan of the runs' totals joins them.
 __global__ void k_scan_sums(uint32_t* sums, int nb, uint32_t* total) {
-  uint32_t carry = 0;
-  for (int base = 0; base < nb; base += kB) {
-    const int i = base + threadIdx.x;
-    const uint32_t v = i < nb ? sums[i] : 0u;
-    uint32_t t;
-    const uint32_t ex = block_excl_scan_u32(v, &t);
-    if (i < nb) sums[i] = carry + ex;
-    carry += t;
+  const int per = (nb + kB - 1) / kB;
+  const int b0 = threadIdx.x * per;
+  const int b1 = min(b0 + per, nb);
+  uint32_t run = 0;
+  for (int i = b0; i < b1; ++i) run += sums[i];
+  uint32_t t;
+  uint32_t carry = block_excl_scan_u32(run, &t);
+  for (int i = b0; i < b1; ++i) {
+    const uint32_t v = sums[i];
+    sums[i] = carry;
+    carry += v;
   }
-  if (threadIdx.x == 0 && total) *total = carry;
+  if (threadIdx.x == 0 && total) *total = t;
 }
 
 __global__ void k_apply(uint32_t* data, int64_t n, const uint32_t* __restrict__ sums) {
@@ -90,10 +95,37 @@ struct CellParams {
   int shift;
 };
 
+__device__ __forceinline__ uint32_t spread3_10(uint32_t x) {
+  x &= 0x3ffu;
+  x = (x | (x << 16)) & 0x030000ffu;
+  x = (x | (x << 8)) & 0x0300f00fu;
+  x = (x | (x << 4)) & 0x030c30c3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+
+// Morton code of up to 3 coordinates already loaded.
 template <typename T>
-__global__ void k_morton_keys(const T* __restrict__ q, int64_t nq, int64_t qStride, CellParams p, uint32_t* key) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i >= nq) return;
+__device__ __forceinline__ uint32_t morton_key3(const T (&x)[3], const CellParams& p) {
+  uint32_t c[3];
+  const float maxc = (float)((1u << p.bits) - 1u);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    float v = ((float)x[d] - p.lo[d]) * p.scale[d];
+    v = fminf(fmaxf(v, 0.0f), maxc);  // NaN -> 0
+    c[d] = d < p.dims ? (uint32_t)v : 0u;
+  }
+  if (p.dims == 3 && p.bits == 10) return (spread3_10(c[0]) << 2) | (spread3_10(c[1]) << 1) | spread3_10(c[2]);
+  uint32_t k = 0;
+  for (int b = p.bits - 1; b >= 0; --b)
+    for (int d = 0; d < p.dims; ++d) k = (k << 1) | ((c[d] >> b) & 1u);
+  return k;
+}
+
+// Morton code: bit b of dimension d lands at b * dims + (dims - 1 - d).
+template <typename T>
+__device__ __forceinline__ uint32_t morton_key(const T* __restrict__ q, int64_t i, int64_t qStride,
+                                               const CellParams& p) {
   uint32_t c[kMortonDims];
   const float maxc = (float)((1u << p.bits) - 1u);
 #pragma unroll
@@ -106,15 +138,11 @@ __global__ void k_morton_keys(const T* __restrict__ q, int64_t nq, int64_t qStri
       c[d] = 0;
     }
   }
+  if (p.dims == 3 && p.bits == 10) return (spread3_10(c[0]) << 2) | (spread3_10(c[1]) << 1) | spread3_10(c[2]);
   uint32_t k = 0;
   for (int b = p.bits - 1; b >= 0; --b)
     for (int d = 0; d < p.dims; ++d) k = (k << 1) | ((c[d] >> b) & 1u);
-  key[i] = k;
-}
-
-__global__ void k_iota(uint32_t* v, int64_t n) {
-  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) v[i] = (uint32_t)i;
+  return k;
 }
 
 // ---- stable LSD radix sort of (key, value) pairs, 10-bit digits.
@@ -128,6 +156,21 @@ constexpr int kRadixBits = 10;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kSortWarps = 4;
 
+// Adds each distinct digit of the 32 live lanes once (equal digits are
+// common: the keys are spatially sorted after the first pass).
+__device__ __forceinline__ void count_digit(uint32_t* h, bool act, uint32_t d) {
+  const unsigned live = __ballot_sync(0xffffffffu, act);
+  if (act) {
+    const unsigned peers = __match_any_sync(live, d);
+    if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(h + d, (uint32_t)__popc(peers));
+  }
+}
+
+// Loads of kPre rounds are issued before their processing, so a warp
+// keeps that many memory requests in flight (there are few warps: one per
+// tile).
+constexpr int kPre = 8;
+
 __global__ void k_radix_hist(const uint32_t* __restrict__ key, int64_t n, int shift, int rounds, int64_t nTiles,
                              uint32_t* hist) {
   extern __shared__ uint32_t sh[];
@@ -138,45 +181,152 @@ __global__ void k_radix_hist(const uint32_t* __restrict__ key, int64_t n, int sh
   for (int d = lane; d < kRadix; d += 32) h[d] = 0u;
   __syncwarp();
   const int64_t base = tile * rounds * 32;
-  for (int r = 0; r < rounds; ++r) {
-    const int64_t i = base + (int64_t)r * 32 + lane;
-    if (i < n) atomicAdd(h + ((key[i] >> shift) & (kRadix - 1)), 1u);
+  for (int r0 = 0; r0 < rounds; r0 += kPre) {
+    if (base + (int64_t)r0 * 32 >= n) break;  // warp-uniform
+    uint32_t kk[kPre];
+#pragma unroll
+    for (int u = 0; u < kPre; ++u) {
+      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+      kk[u] = i < n ? key[i] : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < kPre; ++u) {
+      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+      count_digit(h, i < n, (kk[u] >> shift) & (kRadix - 1));
+    }
   }
   __syncwarp();
   for (int d = lane; d < kRadix; d += 32) hist[(int64_t)d * nTiles + tile] = h[d];
 }
 
-__global__ void k_radix_scatter(const uint32_t* __restrict__ keyIn, const uint32_t* __restrict__ valIn, int64_t n,
-                                int shift, int rounds, int64_t nTiles, const uint32_t* __restrict__ offs,
-                                uint32_t* keyOut, uint32_t* valOut) {
+// Morton keys of the queries, in the radix sort's tile layout, with the
+// first pass's digit counts.
+template <typename T>
+__global__ void k_morton_tiles(const T* __restrict__ q, int64_t n, int64_t qStride, CellParams p, int rounds,
+                               int64_t nTiles, uint32_t* key, uint32_t* hist) {
   extern __shared__ uint32_t sh[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t tile = (int64_t)blockIdx.x * kSortWarps + warp;
   if (tile >= nTiles) return;  // warp-uniform
   uint32_t* h = sh + warp * kRadix;
-  for (int d = lane; d < kRadix; d += 32) h[d] = offs[(int64_t)d * nTiles + tile];
+  for (int d = lane; d < kRadix; d += 32) h[d] = 0u;
+  __syncwarp();
+  const int64_t base = tile * rounds * 32;
+  for (int r0 = 0; r0 < rounds; r0 += kPre) {
+    if (base + (int64_t)r0 * 32 >= n) break;  // warp-uniform
+    uint32_t kk[kPre];
+    if (p.dims <= 3) {
+      T c[kPre][3];
+#pragma unroll
+      for (int u = 0; u < kPre; ++u) {
+        const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) c[u][d] = (i < n && d < p.dims) ? q[i * qStride + d] : T(0);
+      }
+#pragma unroll
+      for (int u = 0; u < kPre; ++u) kk[u] = morton_key3(c[u], p);
+    } else {
+#pragma unroll
+      for (int u = 0; u < kPre; ++u) {
+        const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+        kk[u] = i < n ? morton_key(q, i, qStride, p) : 0u;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kPre; ++u) {
+      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+      if (i < n) key[i] = kk[u];
+      count_digit(h, i < n, kk[u] & (kRadix - 1));
+    }
+  }
+  __syncwarp();
+  for (int d = lane; d < kRadix; d += 32) hist[(int64_t)d * nTiles + tile] = h[d];
+}
+
+// One block per digit: exclusive scan, in place, of the digit's counts over
+// the tiles (hist[digit][tile]); the digit's total goes to total[digit].
+__global__ void k_digit_scan(uint32_t* hist, int64_t nTiles, uint32_t* total) {
+  uint32_t* row = hist + (int64_t)blockIdx.x * nTiles;
+  const int64_t per = (nTiles + kB - 1) / kB;
+  const int64_t b0 = threadIdx.x * per;
+  const int64_t b1 = b0 + per < nTiles ? b0 + per : nTiles;
+  uint32_t run = 0;
+  for (int64_t i = b0; i < b1; ++i) run += row[i];
+  uint32_t t;
+  uint32_t carry = block_excl_scan_u32(run, &t);
+  for (int64_t i = b0; i < b1; ++i) {
+    const uint32_t v = row[i];
+    row[i] = carry;
+    carry += v;
+  }
+  if (threadIdx.x == 0) total[blockIdx.x] = t;
+}
+
+__global__ void k_radix_scatter(const uint32_t* __restrict__ keyIn, const uint32_t* __restrict__ valIn, int64_t n,
+                                int shift, int rounds, int64_t nTiles, const uint32_t* __restrict__ offs,
+                                const uint32_t* __restrict__ total, uint32_t* keyOut, uint32_t* valOut) {
+  extern __shared__ uint32_t sh[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tile = (int64_t)blockIdx.x * kSortWarps + warp;
+  if (tile >= nTiles) return;  // warp-uniform
+  uint32_t* h = sh + warp * kRadix;
+  // first slot of each digit for this tile: the totals of the smaller
+  // digits (lane l sums digits [32 l, 32 l + 32), a warp scan joins the
+  // lanes) plus the earlier tiles' counts of the digit
+  {
+    constexpr int kPer = kRadix / 32;
+    uint32_t tv[kPer];
+    uint32_t run = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      tv[j] = total[lane * kPer + j];
+      run += tv[j];
+    }
+    uint32_t inc = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += y;
+    }
+    uint32_t carry = inc - run;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) {
+      const int d = lane * kPer + j;
+      h[d] = carry + offs[(int64_t)d * nTiles + tile];
+      carry += tv[j];
+    }
+  }
   __syncwarp();
   const uint32_t below = (1u << lane) - 1u;
   const int64_t base = tile * rounds * 32;
-  for (int r = 0; r < rounds; ++r) {
-    const int64_t i = base + (int64_t)r * 32 + lane;
-    const bool act = i < n;
-    const unsigned live = __ballot_sync(0xffffffffu, act);
-    if (live == 0u) break;  // warp-uniform: the tile's tail is past n
-    uint32_t k = 0u, v = 0u, d = 0u, peers = 0u, pos = 0u;
-    if (act) {
-      k = keyIn[i];
-      v = valIn[i];
-      d = (k >> shift) & (kRadix - 1);
-      peers = __match_any_sync(live, d);
-      pos = h[d] + __popc(peers & below);
+  for (int r0 = 0; r0 < rounds; r0 += kPre) {
+    if (base + (int64_t)r0 * 32 >= n) break;  // warp-uniform
+    uint32_t kk[kPre], vv[kPre];
+#pragma unroll
+    for (int u = 0; u < kPre; ++u) {
+      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+      kk[u] = i < n ? keyIn[i] : 0u;
+      vv[u] = i < n ? (valIn ? valIn[i] : (uint32_t)i) : 0u;
     }
-    __syncwarp();
-    if (act && lane == 31 - __clz(peers)) h[d] += __popc(peers);
-    __syncwarp();
-    if (act) {
-      keyOut[pos] = k;
-      valOut[pos] = v;
+#pragma unroll
+    for (int u = 0; u < kPre; ++u) {
+      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+      const bool act = i < n;
+      const unsigned live = __ballot_sync(0xffffffffu, act);
+      if (live == 0u) break;  // warp-uniform: the tile's tail is past n
+      const uint32_t d = (kk[u] >> shift) & (kRadix - 1);
+      uint32_t peers = 0u, pos = 0u;
+      if (act) {
+        peers = __match_any_sync(live, d);
+        pos = h[d] + __popc(peers & below);
+      }
+      __syncwarp();
+      if (act && lane == 31 - __clz(peers)) h[d] += __popc(peers);
+      __syncwarp();
+      if (act) {
+        if (keyOut) keyOut[pos] = kk[u];
+        valOut[pos] = vv[u];
+      }
     }
   }
 }
@@ -238,52 +388,67 @@ int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist
   return kOk;
 }
 
-int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaStream_t stream, const uint32_t* dVals) {
-  if (n <= 0) return kOk;
-  if (n > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
-  // tiles of at least 32 rounds, few enough that the [digit][tile] counts
-  // stay below 2^26 entries
+namespace {
+
+// Tiles of at least 32 rounds of 32 elements, few enough that the
+// [digit][tile] counts stay below 2^26 entries.
+struct SortPlan {
   int rounds = 32;
-  while (ceil_div(n, (int64_t)rounds * 32) * kRadix > (int64_t(1) << 26)) rounds *= 2;
-  const int64_t nTiles = ceil_div(n, (int64_t)rounds * 32);
+  int64_t nTiles = 0;
+  int blocks = 0;
+  size_t smem = (size_t)kSortWarps * kRadix * sizeof(uint32_t);
+  explicit SortPlan(int64_t n) {
+    while (ceil_div(n, (int64_t)rounds * 32) * (int64_t)kRadix > (int64_t(1) << 26)) rounds *= 2;
+    nTiles = ceil_div(n, (int64_t)rounds * 32);
+    blocks = (int)ceil_div(nTiles, (int64_t)kSortWarps);
+  }
+};
+
+// The radix passes over dKeys (clobbered). Pass 0 takes the values from
+// dVals or, if null, the element indices; its digit counts are already in
+// `hist` when `firstCounted`. The last pass writes the values to dOrder.
+int radix_passes(uint32_t* dKeys, int64_t n, int bits, const uint32_t* dVals, int32_t* dOrder, const SortPlan& P,
+                 uint32_t* hist, bool firstCounted, cudaStream_t stream) {
   const int passes = std::max(1, (bits + kRadixBits - 1) / kRadixBits);
-  uint32_t *k2 = nullptr, *v1 = nullptr, *v2 = nullptr, *hist = nullptr;
-  cudaError_t e = scratch_alloc((void**)&k2, (size_t)n * sizeof(uint32_t), stream);
+  uint32_t *k2 = nullptr, *v1 = nullptr, *v2 = nullptr, *totals = nullptr;
+  cudaError_t e = scratch_alloc((void**)&totals, (size_t)kRadix * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&k2, (size_t)n * sizeof(uint32_t), stream);
   if (e == cudaSuccess) e = scratch_alloc((void**)&v1, (size_t)n * sizeof(uint32_t), stream);
   if (e == cudaSuccess) e = scratch_alloc((void**)&v2, (size_t)n * sizeof(uint32_t), stream);
-  if (e == cudaSuccess) e = scratch_alloc((void**)&hist, (size_t)(kRadix * nTiles) * sizeof(uint32_t), stream);
   int rc = e == cudaSuccess ? kOk : cuda_error(e, "sort scratch");
-  if (rc == kOk) {
-    if (dVals)
-      e = cudaMemcpyAsync(v1, dVals, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream);
-    else
-      e = cudaSuccess;
-    if (e != cudaSuccess) rc = cuda_error(e, "sort values");
-  }
-  if (rc == kOk && !dVals) {
-    // identity values: the caller's keys are in element order
-    k_iota<<<ceil_div(n, kB), kB, 0, stream>>>(v1, n);
-  }
-  uint32_t *kin = dKeys, *vin = v1, *kout = k2, *vout = v2;
-  const int blocks = (int)ceil_div(nTiles, (int64_t)kSortWarps);
-  const size_t smem = (size_t)kSortWarps * kRadix * sizeof(uint32_t);
+  uint32_t* kin = dKeys;
+  uint32_t* kout = k2;
+  const uint32_t* vin = dVals;
+  uint32_t* vbuf[2] = {v1, v2};
   for (int p = 0; p < passes && rc == kOk; ++p) {
     const int shift = p * kRadixBits;
-    k_radix_hist<<<blocks, 32 * kSortWarps, smem, stream>>>(kin, n, shift, rounds, nTiles, hist);
-    rc = scan_exclusive_u32(hist, kRadix * nTiles, nullptr, stream);
-    if (rc != kOk) break;
-    k_radix_scatter<<<blocks, 32 * kSortWarps, smem, stream>>>(kin, vin, n, shift, rounds, nTiles, hist, kout, vout);
+    const bool last = p == passes - 1;
+    if (p > 0 || !firstCounted)
+      k_radix_hist<<<P.blocks, 32 * kSortWarps, P.smem, stream>>>(kin, n, shift, P.rounds, P.nTiles, hist);
+    k_digit_scan<<<kRadix, kB, 0, stream>>>(hist, P.nTiles, totals);
+    uint32_t* vout = last ? reinterpret_cast<uint32_t*>(dOrder) : vbuf[p & 1];
+    k_radix_scatter<<<P.blocks, 32 * kSortWarps, P.smem, stream>>>(kin, vin, n, shift, P.rounds, P.nTiles, hist,
+                                                                    totals, last ? nullptr : kout, vout);
     e = cudaGetLastError();
     if (e != cudaSuccess) rc = cuda_error(e, "radix sort");
     std::swap(kin, kout);
-    std::swap(vin, vout);
+    vin = vout;
   }
-  if (rc == kOk) {
-    e = cudaMemcpyAsync(dOrder, vin, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, stream);
-    if (e != cudaSuccess) rc = cuda_error(e, "sort output");
-  }
-  for (void* ptr : {(void*)k2, (void*)v1, (void*)v2, (void*)hist})
+  for (void* ptr : {(void*)k2, (void*)v1, (void*)v2, (void*)totals})
     if (ptr) scratch_free(ptr, stream);
+  return rc;
+}
+
+}  // namespace
+
+int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaStream_t stream, const uint32_t* dVals) {
+  if (n <= 0) return kOk;
+  if (n > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
+  const SortPlan P(n);
+  uint32_t* hist = nullptr;
+  NABO_CUDA_TRY(scratch_alloc((void**)&hist, (size_t)(kRadix * P.nTiles) * sizeof(uint32_t), stream));
+  const int rc = radix_passes(dKeys, n, bits, dVals, dOrder, P, hist, false, stream);
+  scratch_free(hist, stream);
   return rc;
 }
 
@@ -291,6 +456,7 @@ template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
                   int32_t* dOrder, cudaStream_t stream) {
   if (nq <= 0) return kOk;
+  if (nq > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
   CellParams p;
   p.dims = std::min(dim, kMortonDims);
   p.bits = 30 / p.dims;
@@ -305,11 +471,18 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
       p.scale[d] = 0.0f;
     }
   }
-  uint32_t* keys = nullptr;
-  NABO_CUDA_TRY(scratch_alloc((void**)&keys, (size_t)nq * sizeof(uint32_t), stream));
-  k_morton_keys<T><<<ceil_div(nq, kB), kB, 0, stream>>>(dQuery, nq, qStride, p, keys);
-  const int rc = sort_order_u32(keys, nq, p.bits * p.dims, dOrder, stream);
-  scratch_free(keys, stream);
+  const SortPlan P(nq);
+  uint32_t *keys = nullptr, *hist = nullptr;
+  cudaError_t e = scratch_alloc((void**)&keys, (size_t)nq * sizeof(uint32_t), stream);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&hist, (size_t)(kRadix * P.nTiles) * sizeof(uint32_t), stream);
+  int rc = e == cudaSuccess ? kOk : cuda_error(e, "order scratch");
+  if (rc == kOk) {
+    k_morton_tiles<T><<<P.blocks, 32 * kSortWarps, P.smem, stream>>>(dQuery, nq, qStride, p, P.rounds, P.nTiles,
+                                                                      keys, hist);
+    rc = radix_passes(keys, nq, p.bits * p.dims, nullptr, dOrder, P, hist, true, stream);
+  }
+  if (keys) scratch_free(keys, stream);
+  if (hist) scratch_free(hist, stream);
   return rc;
 }
 
