@@ -364,7 +364,10 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         base = cpu_baseline(cloud, q, k, cfg)
     clocks = clk.summary()
-    launches_per_step = 6 if (nq >= 4096 and not args.no_order) else 1
+    # 3-D query order: Morton keys with the first digit counts, then three
+    # 10-bit radix passes (digit scan + scatter each, counts for the last
+    # two); then the search kernel
+    launches_per_step = 10 if (nq >= 4096 and not args.no_order) else 1
     if use_learned:
         launches_per_step += 3  # radius network, miss compaction, fallback search
     out = {
