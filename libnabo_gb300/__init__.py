@@ -328,7 +328,7 @@ class RadiusModel:
 
     def __init__(self, search: NearestNeighbourSearch, train_queries, k: int, optionFlags: int = 0,
                  maxRadius: float = np.inf, epochs: int = 30, batch: int = 4096, lr: float = 3e-3,
-                 safety: float = 1.2, seed: int = 1234, targetMissRate: float = 0.03):
+                 safety: float = 1.2, seed: int = 1234, targetMissRate: float = 0.01):
         import torch
         self.search = search
         self.k = int(k)

@@ -142,6 +142,11 @@ struct KnnArgs {
   int32_t* found = nullptr;      // optional device output: neighbours found per query
   int traversal = 0;             // 0 auto, 1 reference order, 2 warp packet (exact search only)
   const int32_t* nqDevice = nullptr;  // optional device count: only the first *nqDevice of nq run
+  // With maxRadii: a query whose bounded search found fewer than k
+  // neighbours although its radius was below fallbackRadius searches again
+  // with maxRadius (in the same thread) and is counted in *fallbacks.
+  double fallbackRadius = -1.0;
+  int32_t* fallbacks = nullptr;
   cudaEvent_t evStart = nullptr; // optional: recorded right before / after the search kernel
   cudaEvent_t evStop = nullptr;
 };

@@ -81,6 +81,15 @@ constexpr int kVoxelCoordMax = (1 << 21) - 1;
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 __device__ __forceinline__ float sigm(float z) { return 1.0f / (1.0f + __expf(-z)); }
 
+// Inference SiLU: sigma(z) = (1 + tanh(z / 2)) / 2 with the hardware tanh
+// approximation (PTX tanh.approx.f32, one special-function op; relative
+// error about 2^-11, below the BF16 rounding the first layer's output gets).
+__device__ __forceinline__ float silu_fast(float z) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(0.5f * z));
+  return z * fmaf(0.5f, t, 0.5f);
+}
+
 // Occupancies of scales [s0, s0 + n) for point p: the first probe of every
 // scale is issued before any is inspected (independent loads in flight);
 // collisions continue with the bounded linear probe.
@@ -508,7 +517,7 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __rest
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const float z = z1[j][e] + sb1[c + (e & 1)];
-          v[e] = z * sigm(z);
+          v[e] = silu_fast(z);
         }
         a1[s][2 * h + 0] = pack2(v[0], v[1]);
         a1[s][2 * h + 1] = pack2(v[2], v[3]);
@@ -541,7 +550,7 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __rest
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const float z = z2[j][e] + sb2[c + (e & 1)];
-        const float act = z * sigm(z) * sw3[c + (e & 1)];
+        const float act = silu_fast(z) * sw3[c + (e & 1)];
         if (e < 2)
           y0 += act;
         else
@@ -559,37 +568,15 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __rest
         if (qi < nq) {
           const float yn = (h == 0 ? y0 : y1) + b3;
           if (rawOut) rawOut[qi] = yn;
-          const double r = (double)ro.safety * exp((double)ro.mu + (double)ro.sigma * ((double)yn + ro.margin));
-          radii[qi] = (T)(r < ro.maxRadius ? r : ro.maxRadius);
+          // single precision: the radius only steers the search, the
+          // results are exact whatever it is
+          const float r = ro.safety * expf(ro.mu + ro.sigma * (yn + ro.margin));
+          radii[qi] = (double)r < ro.maxRadius ? (T)r : (T)ro.maxRadius;
         }
       }
     }
     __syncwarp();
   }
-}
-
-// Queries whose bounded search found fewer than k neighbours although
-// their learned radius was below the caller's radius, listed in the search
-// order (warp-aggregated, so each warp's misses stay contiguous and the
-// repeated search keeps the ordering's coherence).
-template <typename T>
-__global__ void k_collect_misses(const int32_t* __restrict__ order, const int32_t* __restrict__ found,
-                                 const T* __restrict__ radii, int64_t nq, int k, double maxRadius, int32_t* list,
-                                 int32_t* count) {
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int32_t qi = -1;
-  bool miss = false;
-  if (t < nq) {
-    qi = order ? order[t] : (int32_t)t;
-    miss = found[qi] < k && (double)radii[qi] < maxRadius;
-  }
-  const unsigned ball = __ballot_sync(0xffffffffu, miss);
-  if (!ball) return;
-  const int lane = threadIdx.x & 31;
-  int32_t base = 0;
-  if (lane == __ffs(ball) - 1) base = atomicAdd(count, __popc(ball));
-  base = __shfl_sync(0xffffffffu, base, __ffs(ball) - 1);
-  if (miss) list[base + __popc(ball & ((1u << lane) - 1u))] = qi;
 }
 
 }  // namespace
@@ -1000,8 +987,10 @@ int radius_model_predict(const RadiusModel& m, const void* query, int64_t nq, in
   return launch_radius(m, query, nq, qStride, maxRadius, radii, raw, st);
 }
 
-// Bounded search with the learned radii, then the exact search again for
-// the queries that found fewer than k neighbours inside their radius.
+// Bounded search with the learned radii; a query that finds fewer than k
+// neighbours inside a radius below the caller's maxRadius searches again
+// without the bound, in the same thread of the same launch (so the repeats
+// spread over the whole grid instead of forming a small second launch).
 int knn_learned(const nabo_cuda_search* s, const RadiusModel& m, const KnnArgs& base, int32_t* dFallbacks,
                 cudaStream_t st) {
   const HandleView h = handle_view(s);
@@ -1009,11 +998,9 @@ int knn_learned(const nabo_cuda_search* s, const RadiusModel& m, const KnnArgs& 
   if (base.nq == 0) return kOk;
   const size_t es = c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
   void* radii = nullptr;
-  int32_t *found = nullptr, *list = nullptr, *count = nullptr, *order = nullptr;
+  int32_t *count = nullptr, *order = nullptr;
   const bool ordered = base.sortQueries && base.nq >= 4096;
   cudaError_t e = scratch_alloc(&radii, (size_t)base.nq * es, st);
-  if (e == cudaSuccess) e = scratch_alloc((void**)&found, (size_t)base.nq * sizeof(int32_t), st);
-  if (e == cudaSuccess) e = scratch_alloc((void**)&list, (size_t)base.nq * sizeof(int32_t), st);
   if (e == cudaSuccess) e = scratch_alloc((void**)&count, sizeof(int32_t), st);
   if (e == cudaSuccess && ordered) e = scratch_alloc((void**)&order, (size_t)base.nq * sizeof(int32_t), st);
   if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(int32_t), st);
@@ -1023,34 +1010,17 @@ int knn_learned(const nabo_cuda_search* s, const RadiusModel& m, const KnnArgs& 
   if (rc == kOk) {
     KnnArgs a = base;
     a.maxRadii = radii;
-    a.found = found;
+    a.fallbackRadius = base.maxRadius;
+    a.fallbacks = count;
     a.evStart = h.evStart;
     a.evStop = h.evStop;
     rc = search_given(c, a, order, st);
-  }
-  if (rc == kOk) {
-    if (c.dtype == NABO_CUDA_FLOAT32)
-      k_collect_misses<float><<<ceil_div(base.nq, 256), 256, 0, st>>>(
-          order, found, static_cast<const float*>(radii), base.nq, base.k, base.maxRadius, list, count);
-    else
-      k_collect_misses<double><<<ceil_div(base.nq, 256), 256, 0, st>>>(
-          order, found, static_cast<const double*>(radii), base.nq, base.k, base.maxRadius, list, count);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) rc = cuda_error(e, "miss compaction");
-  }
-  if (rc == kOk) {
-    KnnArgs a = base;
-    a.maxRadii = nullptr;
-    a.nqDevice = count;
-    rc = search_given(c, a, list, st);
   }
   if (rc == kOk && dFallbacks) {
     e = cudaMemcpyAsync(dFallbacks, count, sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
     if (e != cudaSuccess) rc = cuda_error(e, "fallback count");
   }
   if (radii) scratch_free(radii, st);
-  if (found) scratch_free(found, st);
-  if (list) scratch_free(list, st);
   if (count) scratch_free(count, st);
   if (order) scratch_free(order, st);
   return rc;
@@ -1173,7 +1143,7 @@ void nabo_cuda_train_params_init(nabo_cuda_train_params* p) {
   p->batch = 4096;
   p->lr = 3e-3f;
   p->safety = 1.2f;
-  p->targetMissRate = 0.03f;
+  p->targetMissRate = 0.01f;
   p->seed = 1234;
 }
 

@@ -58,6 +58,12 @@ struct TopK {
     d[K - 1] = g[K - 1] ? dist : d[K - 1];
     i[K - 1] = g[K - 1] ? idx : i[K - 1];
   }
+  __device__ __forceinline__ int count(int k) const {
+    int c = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) c += (j < k && i[j] >= 0) ? 1 : 0;
+    return c;
+  }
   // Writes the k entries in ascending order; returns how many are valid.
   __device__ __forceinline__ int store(int k, int32_t* __restrict__ oi, T* __restrict__ od) const {
     int found = 0;
@@ -100,6 +106,12 @@ struct TopK<float, K> {
 #pragma unroll
     for (int j = 0; j + 1 < K; ++j) key[j] = g[j + 1] ? key[j + 1] : (g[j] ? x : key[j]);
     key[K - 1] = g[K - 1] ? x : key[K - 1];
+  }
+  __device__ __forceinline__ int count(int k) const {
+    int c = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) c += (j < k && (uint32_t)(key[j] >> 32) != 0x7f800000u) ? 1 : 0;
+    return c;
   }
   __device__ __forceinline__ uint32_t out_idx(int j) const {
     return (uint32_t)(key[j] >> 32) == 0x7f800000u ? 0xffffffffu : (uint32_t)key[j];
@@ -202,6 +214,8 @@ struct KnnLaunch {
   int allowSelf;
   int stats;
   const int32_t* nqDevice;  // if set, only threads t < *nqDevice search (t < nq still bounds the grid)
+  double fallbackRadius;    // >= 0: bounded searches that miss rerun with maxRadius2 (see KnnArgs)
+  int32_t* fallbacks;
   // batches of clouds (all null for one cloud): queries of cloud c are
   // [bQueryOffset[c], bQueryOffset[c+1]), its tree starts at node
   // bNodeOffset[c], it wants bK[c] neighbours written from bOutOffset[c]
@@ -369,55 +383,66 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
 #pragma unroll
     for (int d = 0; d < D; ++d) q[d] = d < a.dim ? query[qi * a.qStride + d] : T(0);
     T maxRadius2 = (T)a.maxRadius2;
+    // a bounded search (per-query radius) that misses may run once more
+    // without its bound (the learned-radius form's fallback)
+    bool mayFall = false;
     if (a.maxRadii) {
       const T r = static_cast<const T*>(a.maxRadii)[qi];
       maxRadius2 = Ar<T>::mul(r, r);
+      mayFall = a.fallbackRadius >= 0.0 && (double)r < a.fallbackRadius;
     }
     const T maxError2 = (T)a.maxError2;
     TopK<T, K> heap;
     heap.init(k);
     T off[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) off[d] = T(0);
     StackRec<T, D> stk[STACK];
-    int sp = 0;
-    uint32_t node = root;
-    T rd = T(0);
-    for (;;) {
-      // descend to a leaf, pushing far children
-      Node<T> nd = load_node(nodes, node);
-      while (!node_is_leaf(nd.meta)) {
-        const int cd = (int)node_dim(nd.meta);
-        const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
-        const T oldOff = pick(off, cd);
-        const T rdFar = Ar<T>::add(rd, Ar<T>::add(-Ar<T>::mul(oldOff, oldOff), Ar<T>::mul(newOff, newOff)));
-        const uint32_t right = node_payload(nd.meta);
-        const uint32_t nearN = newOff > T(0) ? right : node + 1;
-        const uint32_t farN = newOff > T(0) ? node + 1 : right;
-        // sp <= tree height <= STACK (checked on the host); the test only
-        // makes the bound explicit
-        if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < STACK)
-          stack_push(stk, sp++, rdFar, off, cd, newOff, farN);
-        node = nearN;
-        nd = load_node(nodes, node);
-      }
-      // leaf
-      const uint32_t cnt = node_payload(nd.meta);
-      scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap);
-      touched += cnt;
-      // pop the next far child that can still hold a better neighbour
-      bool more = false;
-      while (sp > 0) {
-        --sp;
-        const T e = stack_rd(stk, sp);
-        if (Ar<T>::mul(e, maxError2) <= heap.head()) {
-          rd = e;
-          node = stack_take(stk, sp, off);
-          more = true;
-          break;
+    for (;;) {  // the search, and at most once more without the bound
+#pragma unroll
+      for (int d = 0; d < D; ++d) off[d] = T(0);
+      int sp = 0;
+      uint32_t node = root;
+      T rd = T(0);
+      for (;;) {
+        // descend to a leaf, pushing far children
+        Node<T> nd = load_node(nodes, node);
+        while (!node_is_leaf(nd.meta)) {
+          const int cd = (int)node_dim(nd.meta);
+          const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
+          const T oldOff = pick(off, cd);
+          const T rdFar = Ar<T>::add(rd, Ar<T>::add(-Ar<T>::mul(oldOff, oldOff), Ar<T>::mul(newOff, newOff)));
+          const uint32_t right = node_payload(nd.meta);
+          const uint32_t nearN = newOff > T(0) ? right : node + 1;
+          const uint32_t farN = newOff > T(0) ? node + 1 : right;
+          // sp <= tree height <= STACK (checked on the host); the test only
+          // makes the bound explicit
+          if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < STACK)
+            stack_push(stk, sp++, rdFar, off, cd, newOff, farN);
+          node = nearN;
+          nd = load_node(nodes, node);
         }
+        // leaf
+        const uint32_t cnt = node_payload(nd.meta);
+        scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap);
+        touched += cnt;
+        // pop the next far child that can still hold a better neighbour
+        bool more = false;
+        while (sp > 0) {
+          --sp;
+          const T e = stack_rd(stk, sp);
+          if (Ar<T>::mul(e, maxError2) <= heap.head()) {
+            rd = e;
+            node = stack_take(stk, sp, off);
+            more = true;
+            break;
+          }
+        }
+        if (!more) break;
       }
-      if (!more) break;
+      if (!mayFall || heap.count(k) == k) break;
+      mayFall = false;
+      maxRadius2 = (T)a.maxRadius2;
+      heap.init(k);
+      if (a.fallbacks) atomicAdd(a.fallbacks, 1);
     }
     const int f = heap.store(k, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
     if (a.found) a.found[qi] = f;

@@ -50,6 +50,8 @@ KnnLaunch make_launch(const DeviceCloud& c, const KnnArgs& a, const int32_t* ord
   L.allowSelf = (a.optionFlags & 1u) ? 1 : 0;
   L.stats = (a.touchStats && a.touched) ? 1 : 0;
   L.nqDevice = a.nqDevice;
+  L.fallbackRadius = a.maxRadii ? a.fallbackRadius : -1.0;
+  L.fallbacks = a.fallbacks;
   L.bQueryOffset = nullptr;
   L.bNodeOffset = nullptr;
   L.bK = nullptr;
@@ -141,6 +143,7 @@ int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t
   const bool packet = a.traversal == 2;
   if (packet && (a.eps != 0.0 || L.stats))
     return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
+  if (a.evStart) cudaEventRecord(a.evStart, stream);
 #define NABO_LAUNCH(KK)                                                            \
   case KK:                                                                         \
     if (packet) {                                                                  \
@@ -157,6 +160,7 @@ int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t
     break;
   switch (K) { NABO_K_LIST(NABO_LAUNCH) }
 #undef NABO_LAUNCH
+  if (a.evStop) cudaEventRecord(a.evStop, stream);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree launch");
   return kOk;
