@@ -47,7 +47,8 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["lidar", "uniform"], default="lidar")
+    p.add_argument("--workload", choices=["lidar", "uniform", "batched"], default="lidar",
+                   help="batched: 512 uneven 3-D clouds built and searched per step (one CUDA graph)")
     p.add_argument("--k", type=int, default=10)
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -393,7 +394,7 @@ def run_ours(args):
                    "k": k, "maxRadius": cfg["maxRadius"], "selfMatch": False, "bucketSize": 8,
                    "form": "learned radius (MLP) + kd-tree" if use_learned else "plain GPU kd-tree",
                    "traversal": "warp packet" if args.traversal == 2 else "reference order",
-                   "query_order": "given" if args.no_order else "kd-tree leaf",
+                   "query_order": "given" if args.no_order else "30-bit Morton code, stable radix sort",
                    "l2": "flushed between steps (256 MiB write)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
@@ -419,9 +420,230 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# Batched workload: 512 independent 3-D float32 clouds, sizes log-uniform in
+# [2,000; 200,000], each a mixture of 8 anisotropic Gaussian blobs (sigma
+# 0.05-2.0); each cloud is queried by a copy of itself with per-point noise
+# sigma 0.01; k per cloud from {1, 5, 16}. One step = every tree built and
+# every query searched, as one CUDA-graph launch (forest build + one search
+# kernel), with bucket size and threads per block from the autotuner.
+
+BATCH_METRIC = "batched kNN queries/s (512 uneven 3-D clouds, build + search per step)"
+
+
+def batched_workload(rank: int, n_clouds: int = 512):
+    from libnabo_gb300 import synthetic as S
+    seed = S.SEED_BASE + 300 + 7919 * rank
+    sizes = S.log_uniform_sizes(n_clouds, 2000, 200000, seed)
+    rng = np.random.default_rng(seed + 1)
+    clouds = [S.gaussian_blobs(int(n), seed + 10 + i) for i, n in enumerate(sizes)]
+    queries = [(c + rng.normal(0, 0.01, c.shape)).astype(np.float32) for c in clouds]
+    ks = rng.choice([1, 5, 16], n_clouds).astype(np.int32)
+    return clouds, queries, ks
+
+
+def batched_cpu(clouds, queries, ks, sample: int = 16, seed: int = 0):
+    """Oracle (the reference's OpenMP KDTREE_LINEAR_HEAP restated) on a
+    sample of the clouds: build + search time, queries/s, touched/query."""
+    from oracle import oracle as O
+    rng = np.random.default_rng(seed)
+    pick = np.sort(rng.choice(len(clouds), min(sample, len(clouds)), replace=False))
+    nq, t_build, t_search, touched = 0, 0.0, 0.0, 0
+    for c in pick:
+        t0 = time.perf_counter()
+        tree = O.OracleTree(clouds[c], bucket_size=8, creation_flags=O.TOUCH_STATISTICS)
+        t_build += time.perf_counter() - t0
+        t0 = time.perf_counter()
+        _, _, tc = tree.knn(queries[c], int(ks[c]), mode=O.MODE_REFERENCE)
+        t_search += time.perf_counter() - t0
+        nq += queries[c].shape[0]
+        touched += int(tc)
+    return {"value": nq / (t_build + t_search), "unit": "queries/s", "cores": O.num_threads(), "kind": "port",
+            "sample": f"{len(pick)} of {len(clouds)} clouds ({nq} queries), tree build + search each",
+            "search_only_queries_per_s": nq / t_search, "touched_per_query": touched / nq, "clouds": pick.tolist()}
+
+
+def run_batched(args):
+    import torch
+    import torch.distributed as dist
+
+    import libnabo_gb300 as nb
+    from libnabo_gb300 import autotune
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    clouds, queries, ks = batched_workload(rank)
+    pc = np.array([c.shape[0] for c in clouds], np.int64)
+    qc = np.array([q.shape[0] for q in queries], np.int64)
+    t0 = time.perf_counter()
+    choice = autotune.tune(clouds, queries, ks, sample=64, repeats=3)
+    tune_s = time.perf_counter() - t0
+    b = nb.BatchSearch(pc, bucketSize=choice["bucketSize"], threadsPerBlock=choice["threadsPerBlock"],
+                       maxLevels=choice["maxLevels"])
+    b.set_queries(qc, ks)
+    hc = np.concatenate(clouds)
+    hq = np.concatenate(queries)
+    tc = torch.from_numpy(hc).to(dev)
+    tq = torch.from_numpy(hq).to(dev)
+    out = b._outputs(dev)
+    nq_total = int(qc.sum())
+
+    def step():
+        b.run(tc, tq, out=out)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    st = b.status()
+    if world > 1:
+        dist.barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with ClockSampler(local) as clk:
+        for e0, e1 in ev:
+            e0.record()
+            step()
+            e1.record()
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    step_ms = max_ranks(sum(e0.elapsed_time(e1) for e0, e1 in ev) / args.steps, world)
+    # phases outside the graph (same kernels): forest build, then search
+    b.build(tc)
+    torch.cuda.synchronize()
+    tb = []
+    ts = []
+    for _ in range(3):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record()
+        b.build(tc)
+        e1.record()
+        b.knn(tq, out=out)
+        e2.record()
+        torch.cuda.synchronize()
+        tb.append(e0.elapsed_time(e1))
+        ts.append(e1.elapsed_time(e2))
+    build_ms, search_ms = min(tb), min(ts)
+    # exactness on a few clouds against the oracle
+    from oracle import oracle as O
+    gi = b.split(out[0].cpu().numpy())
+    gd = b.split(out[1].cpu().numpy())
+    checked, same = 0, True
+    for c in range(0, len(clouds), max(1, len(clouds) // 8)):
+        oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        same = same and np.array_equal(gi[c], oi) and np.array_equal(gd[c].view(np.uint32), od.view(np.uint32))
+        checked += 1
+    # end to end: clouds and queries from pinned host memory, results back
+    pin_c = torch.from_numpy(hc).pin_memory()
+    pin_q = torch.from_numpy(hq).pin_memory()
+    h_idx = torch.empty(out[0].shape, dtype=out[0].dtype).pin_memory()
+    h_d2 = torch.empty(out[1].shape, dtype=out[1].dtype).pin_memory()
+    e2e_steps = args.e2e_steps or 3
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        tc.copy_(pin_c, non_blocking=True)
+        tq.copy_(pin_q, non_blocking=True)
+        step()
+        h_idx.copy_(out[0], non_blocking=True)
+        h_d2.copy_(out[1], non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = max_ranks((time.perf_counter() - t0) / e2e_steps, world)
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    base = None if args.no_cpu_baseline else batched_cpu(clouds, queries, ks)
+    peak, peak_kind = measured_peaks()
+    p_bar = base["touched_per_query"] if base else None
+    achieved, b_q = None, None
+    if p_bar is not None:
+        s = 4
+        mean_k = float(np.sum(qc * ks) / nq_total)
+        b_q = 3 * s + mean_k * (4 + s) + p_bar * (3 * s + 4)
+        achieved = nq_total * b_q / (search_ms * 1e-3) / 1e9
+    res = {
+        "metric": BATCH_METRIC, "value": world * nq_total / (step_ms / 1e3), "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "batched512_3d", "clouds": len(clouds), "points": int(pc.sum()),
+                   "queries": nq_total, "k": "per cloud from {1, 5, 16}", "selfMatch": False,
+                   "bucketSize": choice["bucketSize"], "threadsPerBlock": choice["threadsPerBlock"],
+                   "maxLevels": choice["maxLevels"], "autotune_s": tune_s,
+                   "step": "forest build + search, one CUDA graph launch",
+                   "l2": "inputs larger than L2 (clouds + queries %.0f MB)" % ((hc.nbytes + hq.nbytes) / 1e6),
+                   "parallelism": f"replicas x{world}"},
+        "phases_ms": {"build": build_ms, "search": search_ms},
+        "status": st, "exact_vs_oracle": {"clouds_checked": checked, "identical": bool(same)},
+        "e2e": {"value": world * nq_total / e2e_s, "unit": "queries/s",
+                "h2d_bytes_per_step": int(hc.nbytes + hq.nbytes),
+                "d2h_bytes_per_step": int(h_idx.numel() * 4 + h_d2.numel() * 4)},
+        "roofline": None if achieved is None else {
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None, "peak_source": peak_kind,
+            "kernel": "batched search call (query ordering + k_knn_kdtree), event-timed",
+            "kernel_ms": search_ms, "bytes_per_query": b_q, "touched_per_query": p_bar},
+        "cpu_baseline": None if base is None else {kk: base[kk] for kk in ("value", "unit", "cores", "kind",
+                                                                           "sample", "search_only_queries_per_s")},
+        "clocks": clk.summary(),
+        # per graph launch: forest set-up 6 + 17 per level + small/status/
+        # renumber/copy 4; search: leaf cells, 3 scan kernels, placement,
+        # run sort, search 7
+        "gpu_launches": args.steps * (6 + 17 * choice["maxLevels"] + 4 + 7),
+    }
+    print(json.dumps(res))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def run_batched_reference(args):
+    """The reference algorithm (oracle restatement, all host threads) on a
+    sample of the batched workload's clouds; rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    clouds, queries, ks = batched_workload(0)
+    for _ in range(args.warmup):
+        batched_cpu(clouds, queries, ks, sample=4, seed=99)
+    vals = [batched_cpu(clouds, queries, ks) for _ in range(args.steps)]
+    v = statistics.mean(x["value"] for x in vals)
+    base = vals[0]
+    nq = sum(queries[c].shape[0] for c in base["clouds"])
+    out = {
+        "metric": BATCH_METRIC, "value": v, "unit": "queries/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": nq / v * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "batched512_3d", "search": "KDTREE_LINEAR_HEAP restated in C++/OpenMP "
+                   "(oracle/nabo_oracle.cpp), tree build + search per cloud"},
+        "cpu_baseline": {"value": v, "unit": "queries/s", "cores": base["cores"], "kind": "port",
+                         "sample": base["sample"]},
+        "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def max_ranks(x, world):
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+    return x
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.workload == "batched":
+        if args.impl == "reference":
+            run_batched_reference(args)
+        else:
+            run_batched(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

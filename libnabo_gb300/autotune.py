@@ -50,6 +50,20 @@ def _time_config(clouds, queries, pc, qc, ks, dim, dtype, bucket, tpb, repeats):
     return best, st
 
 
+def _levels_of(cloud, queries, k, dim, dtype, bucket) -> int:
+    """Top-phase levels the forest build needs for one cloud."""
+    import torch
+
+    from . import BatchSearch
+    b = BatchSearch([cloud.shape[0]], dim=dim, dtype=dtype, bucketSize=bucket, maxLevels=256)
+    b.set_queries([0], [k])
+    b.build(torch.from_numpy(np.ascontiguousarray(cloud, dtype=dtype)).cuda())
+    torch.cuda.synchronize()
+    levels = b.status()["levels"]
+    b.close()
+    return int(levels)
+
+
 def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int = 64, repeats: int = 3,
          cache_path: str | None = None, seed: int = 0) -> dict:
     """Best {bucketSize, threadsPerBlock} for a batch (lists of (n_c, dim) arrays)."""
@@ -78,8 +92,14 @@ def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int 
             ms, st = _time_config(clouds, queries, pc, qc, ks[pick], dim, dtype, bucket, tpb, repeats)
             trials.append({"bucketSize": bucket, "threadsPerBlock": tpb, "ms": ms, "levels": st["levels"]})
     best = min(trials, key=lambda t: t["ms"])
+    # the fixed level count must cover the batch's largest cloud, sampled or not
+    levels = best["levels"]
+    big = int(np.argmax(pcs))
+    if big not in set(pick.tolist()):
+        levels = max(levels, _levels_of(cloud_list[big], query_list[big], int(ks[big]), dim, dtype,
+                                        best["bucketSize"]))
     choice = {"bucketSize": best["bucketSize"], "threadsPerBlock": best["threadsPerBlock"],
-              "maxLevels": max(8, best["levels"] + 8), "sample_ms": best["ms"]}
+              "maxLevels": max(8, levels + 8), "sample_ms": best["ms"]}
     _cache[key] = choice
     if cache_path:
         disk = {}
