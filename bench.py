@@ -47,8 +47,10 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["lidar", "uniform", "batched"], default="lidar",
-                   help="batched: 512 uneven 3-D clouds built and searched per step (one CUDA graph)")
+    p.add_argument("--workload", choices=["lidar", "uniform", "batched", "c4"], default="lidar",
+                   help="batched: 512 uneven 3-D clouds built and searched per step (one CUDA graph); "
+                        "c4: 128 8-D clouds (half f32, half f64), k=32, epsilon 0 and 0.5")
+    p.add_argument("--c4-clouds", type=int, default=128, help="clouds of the c4 workload (a prefix of the 128)")
     p.add_argument("--k", type=int, default=10)
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -600,6 +602,153 @@ def run_batched(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# 8-D workload: 128 clouds, sizes log-uniform in [50,000; 2,000,000], half
+# float32 and half float64, each a mixture of 32 isotropic Gaussian clusters
+# with sigma log-uniform in [0.01, 1]; 100,000 queries per cloud from the
+# same mixture; k = 32; epsilon 0 (exact) and 0.5 (approximate, within the
+# reference's (1+eps) bound). One BatchSearch per scalar type; trees built
+# once, a step searches every query of both batches.
+
+C4_METRIC = "batched 8-D kNN queries/s (128 clouds, half f32 / half f64, k=32)"
+
+
+def c4_workload(n_clouds: int = 128):
+    from libnabo_gb300 import synthetic as S
+    seed = S.SEED_BASE + 400
+    sizes = S.log_uniform_sizes(128, 50000, 2000000, seed)[:n_clouds]
+    out = {np.float32: ([], []), np.float64: ([], [])}
+    for i, n in enumerate(sizes):
+        dt = np.float32 if i % 2 == 0 else np.float64
+        cloud, centres, sig = S.clusters(int(n), 8, seed + 10 + i, dtype=dt)
+        qs, _, _ = S.clusters(100000, 8, seed + 10000 + i, dtype=dt, centres=centres, sigmas=sig)
+        out[dt][0].append(cloud)
+        out[dt][1].append(qs)
+    return out
+
+
+def run_c4(args):
+    import torch
+
+    import libnabo_gb300 as nb
+    from oracle import oracle as O
+
+    dev = torch.device("cuda", 0)
+    data = c4_workload(args.c4_clouds)
+    k = 32
+    batches = []
+    t_gen = time.perf_counter()
+    for dt, (clouds, queries) in data.items():
+        if not clouds:
+            continue
+        pc = np.array([c.shape[0] for c in clouds], np.int64)
+        qc = np.array([q.shape[0] for q in queries], np.int64)
+        b = nb.BatchSearch(pc, dim=8, dtype=dt, bucketSize=8, maxLevels=64)
+        b.set_queries(qc, np.full(len(clouds), k, np.int32))
+        tc = torch.from_numpy(np.concatenate(clouds)).to(dev)
+        tq = torch.from_numpy(np.concatenate(queries)).to(dev)
+        batches.append(dict(dt=dt, b=b, tc=tc, tq=tq, out=b._outputs(dev), clouds=clouds, queries=queries,
+                            points=int(pc.sum()), nq=int(qc.sum())))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for x in batches:
+        x["b"].build(x["tc"])
+    e1.record()
+    torch.cuda.synchronize()
+    build_ms = e0.elapsed_time(e1)
+    for x in batches:  # a tree deeper than 64 top levels: rebuild with room for it
+        if x["b"].status()["flags"] & 2:
+            x["b"] = nb.BatchSearch([c.shape[0] for c in x["clouds"]], dim=8, dtype=x["dt"], bucketSize=8,
+                                    maxLevels=256)
+            x["b"].set_queries([q.shape[0] for q in x["queries"]], np.full(len(x["clouds"]), k, np.int32))
+            x["b"].build(x["tc"])
+    status = {np.dtype(x["dt"]).name: x["b"].status() for x in batches}
+    nq_total = sum(x["nq"] for x in batches)
+
+    def step(eps, outs=None):
+        for j, x in enumerate(batches):
+            x["b"].knn(x["tq"], epsilon=eps, out=outs[j] if outs else x["out"])
+
+    forms = {}
+    exact_out = None
+    with ClockSampler(0) as clk:
+        for eps in (0.0, 0.5):
+            outs = [x["b"]._outputs(dev) for x in batches]
+            for _ in range(args.warmup):
+                step(eps, outs)
+            torch.cuda.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+            for a0, a1 in ev:
+                a0.record()
+                step(eps, outs)
+                a1.record()
+            torch.cuda.synchronize()
+            ms = sum(a0.elapsed_time(a1) for a0, a1 in ev) / args.steps
+            forms[f"eps{eps}"] = {"ms_per_step": ms, "queries_per_s": nq_total / (ms / 1e3)}
+            if eps == 0.0:
+                exact_out = outs
+            else:
+                approx_out = outs
+    # per scalar type, exact search
+    per_type = {}
+    for j, x in enumerate(batches):
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        x["b"].knn(x["tq"], epsilon=0.0, out=exact_out[j])
+        a1.record()
+        torch.cuda.synchronize()
+        ms = a0.elapsed_time(a1)
+        per_type[np.dtype(x["dt"]).name] = {"ms": ms, "queries_per_s": x["nq"] / (ms / 1e3)}
+    forms["eps0.0"]["per_type"] = per_type
+    # CPU baseline: the oracle (reference algorithm, all host threads) on the
+    # two smallest clouds of each type, 5,000 queries each
+    base = None
+    if not args.no_cpu_baseline:
+        nqb, tb, touched = 0, 0.0, 0
+        for x in batches:
+            for c in np.argsort([cl.shape[0] for cl in x["clouds"]])[:2]:
+                qs = x["queries"][c][:5000]
+                tree = O.OracleTree(x["clouds"][c], creation_flags=O.TOUCH_STATISTICS)
+                t0 = time.perf_counter()
+                _, _, tcount = tree.knn(qs, k, mode=O.MODE_REFERENCE)
+                tb += time.perf_counter() - t0
+                nqb += qs.shape[0]
+                touched += int(tcount)
+        base = {"value": nqb / tb, "unit": "queries/s", "cores": O.num_threads(), "kind": "port",
+                "sample": f"search only, 2 smallest clouds of each type, 5000 queries each ({nqb} queries, eps 0)",
+                "touched_per_query": touched / nqb}
+    # checks on the smallest cloud of each type: exact at eps 0 (oracle,
+    # canonical ties), the (1+eps)^2 bound on squared distances at eps 0.5
+    checks = {}
+    for j, x in enumerate(batches):
+        c = int(np.argmin([cl.shape[0] for cl in x["clouds"]]))
+        sub = slice(0, 2000)
+        gi = x["b"].split(exact_out[j][0].cpu().numpy())[c][sub]
+        gd = x["b"].split(exact_out[j][1].cpu().numpy())[c][sub]
+        ad = x["b"].split(approx_out[j][1].cpu().numpy())[c][sub]
+        oi, od, _ = O.OracleTree(x["clouds"][c]).knn(x["queries"][c][sub], k, mode=O.MODE_CANONICAL)
+        checks[np.dtype(x["dt"]).name] = {
+            "cloud": c, "points": int(x["clouds"][c].shape[0]), "queries_checked": 2000,
+            "exact_identical": bool(np.array_equal(gi, oi) and np.array_equal(gd, od)),
+            "eps0.5_within_bound": bool((ad <= (1.5 ** 2) * od * (1 + 1e-6)).all())}
+    res = {
+        "metric": C4_METRIC, "value": forms["eps0.0"]["queries_per_s"], "unit": "queries/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": forms["eps0.0"]["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": "c4_8d", "clouds": sum(len(x["clouds"]) for x in batches),
+                   "points": sum(x["points"] for x in batches), "queries": nq_total, "k": k, "dims": 8,
+                   "per_type": {np.dtype(x["dt"]).name: {"clouds": len(x["clouds"]), "points": x["points"],
+                                                          "queries": x["nq"]} for x in batches},
+                   "step": "search of every query of both batches (trees built once)",
+                   "l2": "inputs larger than L2"},
+        "forms": forms, "build_ms": build_ms, "status": status, "checks": checks, "cpu_baseline": base,
+        "clocks": clk.summary(), "data_s": time.perf_counter() - t_gen,
+    }
+    print(json.dumps(res, default=str))
+
+
 def run_batched_reference(args):
     """The reference algorithm (oracle restatement, all host threads) on a
     sample of the batched workload's clouds; rank 0 only."""
@@ -638,6 +787,9 @@ def max_ranks(x, world):
 
 def main():
     args = parse()
+    if args.workload == "c4":
+        run_c4(args)
+        return
     if args.workload == "batched":
         if args.impl == "reference":
             run_batched_reference(args)
