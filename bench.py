@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["lidar", "uniform", "batched", "c4"], default="lidar",
+    p.add_argument("--workload", choices=["lidar", "uniform", "c0", "batched", "c4"], default="lidar",
                    help="batched: 512 uneven 3-D clouds built and searched per step (one CUDA graph); "
                         "c4: 128 8-D clouds (half f32, half f64), k=32, epsilon 0 and 0.5")
     p.add_argument("--c4-clouds", type=int, default=128, help="clouds of the c4 workload (a prefix of the 128)")
@@ -68,6 +68,10 @@ def workload(name: str, rank: int):
         cloud = S.lidar_scan()
         q = S.lidar_queries(cloud, seed=S.SEED_BASE + 1 + 7919 * rank)
         return cloud, q, dict(maxRadius=1.0, flags=0, label="lidar64_1.15M")
+    if name == "c0":  # the reference's small CPU-runnable case: 10,000 uniform points and queries
+        cloud = S.uniform(10_000, 3, seed=S.SEED_BASE + 7)
+        q = S.uniform(10_000, 3, seed=S.SEED_BASE + 8 + 7919 * rank)
+        return cloud, q, dict(maxRadius=float("inf"), flags=0, label="uniform_10k")
     cloud = S.uniform(1_000_000, 3, seed=S.SEED_BASE + 5)
     q = S.uniform(1_000_000, 3, seed=S.SEED_BASE + 6 + 7919 * rank)
     return cloud, q, dict(maxRadius=float("inf"), flags=0, label="uniform_1M")
