@@ -1,0 +1,128 @@
+// Exercises include/nabo_cuda.hpp the way a libnabo user would.
+//   frontend_check errors                -- argument errors raised before any GPU work
+//   frontend_check search <in> <out>     -- searches (float and double) and knn() size checks
+// <in>: int32 n, nq, k, dim; float cloud[dim*n]; float query[dim*nq]; float radii[nq]
+// <out>: per type (float, double): int32 idx[k*nq], T d2[k*nq] (plain), int32 idx, T d2 (radii),
+//        uint64 touched
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "nabo_cuda.hpp"
+
+template <typename S>
+using M = nabo_cuda::DenseMatrix<S>;
+
+static int expect_error(const char* what, const std::string& needle, void (*fn)()) {
+  try {
+    fn();
+  } catch (const nabo_cuda::runtime_error& e) {
+    if (std::string(e.what()).find(needle) != std::string::npos) {
+      std::printf("ok %s: %s\n", what, e.what());
+      return 0;
+    }
+    std::printf("FAIL %s: wrong message: %s\n", what, e.what());
+    return 1;
+  } catch (const std::exception& e) {
+    std::printf("FAIL %s: unexpected exception type: %s\n", what, e.what());
+    return 1;
+  }
+  std::printf("FAIL %s: no exception\n", what);
+  return 1;
+}
+
+static M<float> g_cloud(3, 50), g_empty(3, 0);
+
+static int errors() {
+  for (long i = 0; i < g_cloud.size(); ++i) g_cloud(i) = (float)(i % 7) * 0.1f;
+  int bad = 0;
+  bad += expect_error("dim 0", "Your space must have at least one dimension",
+                      [] { delete nabo_cuda::NNSearchF::create(g_cloud, 0); });
+  bad += expect_error("bucket size", "Requested bucket size 1, but must be larger than 2", [] {
+    nabo_cuda::NNSearchF::Parameters p;
+    p.bucketSize = 1;
+    delete nabo_cuda::NNSearchF::create(g_cloud, 3, nabo_cuda::NNSearchF::KDTREE_CUDA, 0, p);
+  });
+  bad += expect_error("empty cloud", "Cloud has no points",
+                      [] { delete nabo_cuda::NNSearchF::createKDTreeLinearHeap(g_empty); });
+  bad += expect_error("cpu type", "only the CUDA search types",
+                      [] { delete nabo_cuda::NNSearchF::create(g_cloud, 3, nabo_cuda::NNSearchF::KDTREE_TREE_HEAP); });
+  return bad;
+}
+
+template <typename T>
+static int search_type(const std::vector<float>& c, const std::vector<float>& q, const std::vector<float>& r, int n,
+                       int nq, int k, int dim, FILE* out) {
+  using NNS = nabo_cuda::NearestNeighbourSearch<T>;
+  M<T> cloud(dim, n), query(dim, nq), radii(nq, 1);
+  for (long i = 0; i < cloud.size(); ++i) cloud(i) = (T)c[(size_t)i];
+  for (long i = 0; i < query.size(); ++i) query(i) = (T)q[(size_t)i];
+  for (long i = 0; i < nq; ++i) radii(i) = (T)r[(size_t)i];
+  NNS* s = NNS::createKDTreeLinearHeap(cloud, dim, NNS::TOUCH_STATISTICS);
+  M<int> idx(k, nq), idx2(k, nq);
+  M<T> d2(k, nq), d22(k, nq);
+  const unsigned long touched = s->knn(query, idx, d2, k, 0, NNS::SORT_RESULTS, (T)1.0);
+  s->knn(query, idx2, d22, radii, k, 0, 0);
+  std::fwrite(idx.data(), 4, (size_t)idx.size(), out);
+  std::fwrite(d2.data(), sizeof(T), (size_t)d2.size(), out);
+  std::fwrite(idx2.data(), 4, (size_t)idx2.size(), out);
+  std::fwrite(d22.data(), sizeof(T), (size_t)d22.size(), out);
+  const uint64_t t64 = touched;
+  std::fwrite(&t64, 8, 1, out);
+  // knn() argument checks on a live object, in the reference's order
+  int bad = 0;
+  auto must = [&](const char* what, const std::string& needle, auto fn) {
+    try {
+      fn();
+      std::printf("FAIL %s: no exception\n", what);
+      ++bad;
+    } catch (const nabo_cuda::runtime_error& e) {
+      const bool ok = std::string(e.what()).find(needle) != std::string::npos;
+      std::printf("%s %s: %s\n", ok ? "ok" : "FAIL", what, e.what());
+      bad += ok ? 0 : 1;
+    }
+  };
+  M<int> wrongRows(k + 1, nq);
+  M<T> wrongCols(k, nq + 1), shortRadii(nq - 1, 1), fewDims(dim - 1, nq);
+  must("k too large", "than available in cloud minus 1", [&] { s->knn(query, idx, d2, (long)n, 0, 0); });
+  must("query dims", "Query has less dimensions", [&] { s->knn(fewDims, idx, d2, k); });
+  must("index rows", "Index matrix has a different number of rows", [&] { s->knn(query, wrongRows, d2, k); });
+  must("dist cols", "Distance matrix has a different number of columns", [&] { s->knn(query, idx, wrongCols, k); });
+  must("radii", "Maximum radii vector has not the same length", [&] { s->knn(query, idx, d2, shortRadii, k); });
+  must("flags", "OR-ed value of option flags (4)", [&] { s->knn(query, idx, d2, k, 0, 4); });
+  std::printf("%s bounds %g..%g dim %ld\n", sizeof(T) == 4 ? "float" : "double", (double)s->minBound[0],
+              (double)s->maxBound[0], (long)s->dim);
+  delete s;
+  return bad;
+}
+
+int main(int argc, char** argv) {
+  if (argc >= 2 && std::strcmp(argv[1], "errors") == 0) return errors();
+  if (argc < 4 || std::strcmp(argv[1], "search") != 0) {
+    std::fprintf(stderr, "usage: frontend_check errors | search <in> <out>\n");
+    return 2;
+  }
+  FILE* in = std::fopen(argv[2], "rb");
+  if (!in) return 2;
+  int hdr[4];
+  if (std::fread(hdr, 4, 4, in) != 4) return 2;
+  const int n = hdr[0], nq = hdr[1], k = hdr[2], dim = hdr[3];
+  std::vector<float> c((size_t)dim * n), q((size_t)dim * nq), r((size_t)nq);
+  if (std::fread(c.data(), 4, c.size(), in) != c.size() || std::fread(q.data(), 4, q.size(), in) != q.size() ||
+      std::fread(r.data(), 4, r.size(), in) != r.size())
+    return 2;
+  std::fclose(in);
+  FILE* out = std::fopen(argv[3], "wb");
+  if (!out) return 2;
+  int bad = 0;
+  try {
+    bad += search_type<float>(c, q, r, n, nq, k, dim, out);
+    bad += search_type<double>(c, q, r, n, nq, k, dim, out);
+  } catch (const std::exception& e) {
+    std::printf("FAIL search: %s\n", e.what());
+    bad += 1;
+  }
+  std::fclose(out);
+  return bad;
+}
