@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["lidar", "uniform", "c0", "batched", "c4"], default="lidar",
+    p.add_argument("--workload", choices=["lidar", "uniform", "c0", "batched", "c4", "bf"], default="lidar",
                    help="batched: 512 uneven 3-D clouds built and searched per step (one CUDA graph); "
                         "c4: 128 8-D clouds (half f32, half f64), k=32, epsilon 0 and 0.5")
     p.add_argument("--c4-clouds", type=int, default=128, help="clouds of the c4 workload (a prefix of the 128)")
@@ -753,6 +753,81 @@ def run_c4(args):
     print(json.dumps(res, default=str))
 
 
+# ---------------------------------------------------------------------------
+# Brute force: 100,000 uniform 3-D float32 points against 100,000 queries,
+# k = 5 (the reference's small case scaled up so one launch is measurable).
+# Bound by the FP32 pipe: flops = Q * N * 3D (D subtractions and D
+# multiply-adds counted as two), against the FMA peak measured live.
+
+BF_METRIC = "brute-force kNN queries/s (100k uniform 3-D points, k=5)"
+
+
+def run_bf(args):
+    import torch
+
+    import libnabo_gb300 as nb
+    from libnabo_gb300 import synthetic as S
+    from oracle import oracle as O
+
+    dev = torch.device("cuda", 0)
+    n, nq, k, d = 100_000, 100_000, 5, 3
+    cloud = S.uniform(n, d, seed=S.SEED_BASE + 9)
+    q = S.uniform(nq, d, seed=S.SEED_BASE + 10)
+    s = nb.NearestNeighbourSearch(cloud, nb.SearchType.BRUTE_FORCE_CUDA)
+    tq = torch.from_numpy(q).to(dev)
+    idx = torch.empty((nq, k), dtype=torch.int32, device=dev)
+    d2 = torch.empty((nq, k), dtype=torch.float32, device=dev)
+    s.profile(True)
+    for _ in range(args.warmup):
+        s.knn_device(tq, k, out=(idx, d2))
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    kms = []
+    with ClockSampler(0) as clk:
+        for e0, e1 in ev:
+            e0.record()
+            s.knn_device(tq, k, out=(idx, d2))
+            e1.record()
+            kms.append(s.last_kernel_ms())
+        torch.cuda.synchronize()
+    step_ms = sum(e0.elapsed_time(e1) for e0, e1 in ev) / args.steps
+    kernel_ms = statistics.mean(kms)
+    peak = nb.measure_fma_peak(np.float32)
+    flops = float(nq) * n * 3 * d
+    achieved = flops / (kernel_ms * 1e-3)
+    # exactness and CPU baseline on a sample of the queries
+    sample = 2000
+    t0 = time.perf_counter()
+    oi, od, _ = O.bf_knn(cloud, q[:sample], k, mode=O.MODE_CANONICAL)
+    cpu_s = time.perf_counter() - t0
+    gi = idx[:sample].cpu().numpy()
+    gd = d2[:sample].cpu().numpy()
+    hi, hd = s.knn(q, k)  # host API, for e2e
+    t0 = time.perf_counter()
+    for _ in range(3):
+        s.knn(q, k)
+    e2e_s = (time.perf_counter() - t0) / 3
+    res = {
+        "metric": BF_METRIC, "value": nq / (step_ms / 1e3), "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "bruteforce_uniform_100k_k5", "points": n, "queries": nq, "k": k,
+                   "l2": "cloud (1.6 MB) is reread from L2 by design; the bound is the FP32 pipe"},
+        "e2e": {"value": nq / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
+                "d2h_bytes_per_step": int(nq * k * 8)},
+        "roofline": {"bound": "fp32 pipe", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": "FMA chains measured in this run",
+                     "kernel": "k_knn_bruteforce", "kernel_ms": kernel_ms, "flops_per_launch": flops},
+        "exact_vs_oracle": {"queries_checked": sample,
+                            "identical": bool(np.array_equal(gi, oi) and np.array_equal(gd, od))},
+        "cpu_baseline": {"value": sample / cpu_s, "unit": "queries/s", "cores": O.num_threads(), "kind": "port",
+                         "sample": f"{sample} queries against all {n} points (oracle brute force)"},
+        "clocks": clk.summary(), "gpu_launches": args.steps,
+        "fp64_fma_peak_tflops": nb.measure_fma_peak(np.float64) / 1e12,
+    }
+    print(json.dumps(res))
+
+
 def run_batched_reference(args):
     """The reference algorithm (oracle restatement, all host threads) on a
     sample of the batched workload's clouds; rank 0 only."""
@@ -793,6 +868,9 @@ def main():
     args = parse()
     if args.workload == "c4":
         run_c4(args)
+        return
+    if args.workload == "bf":
+        run_bf(args)
         return
     if args.workload == "batched":
         if args.impl == "reference":

@@ -312,6 +312,12 @@ const char* nabo_cuda_last_error(void);
 /* Library version string. */
 const char* nabo_cuda_version(void);
 
+/* Measured fused-multiply-add throughput of the current GPU in flop/s (two
+ * flops per FMA) for NABO_CUDA_FLOAT32 or NABO_CUDA_FLOAT64: the denominator
+ * of the brute-force search's roofline, which is bound by the arithmetic
+ * pipes rather than by memory. Runs a short kernel (a few milliseconds). */
+int nabo_cuda_measure_fma_peak(int dtype, double* flops);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,6 +89,14 @@ def version() -> str:
     return _lib.nabo_cuda_version().decode()
 
 
+def measure_fma_peak(dtype=np.float32) -> float:
+    """Measured FMA throughput of the current GPU in flop/s (the brute-force
+    search's roofline denominator)."""
+    out = ctypes.c_double(0.0)
+    _check(_lib.nabo_cuda_measure_fma_peak(_dtype_code(np.dtype(dtype)), ctypes.byref(out)))
+    return float(out.value)
+
+
 def _dtype_code(dt) -> int:
     dt = np.dtype(dt)
     if dt == np.float32:

@@ -51,6 +51,7 @@ SIGNATURES = {
     "nabo_cuda_last_kernel_ms": (_I, [_P, _P]),
     "nabo_cuda_last_error": (ctypes.c_char_p, []),
     "nabo_cuda_version": (ctypes.c_char_p, []),
+    "nabo_cuda_measure_fma_peak": (_I, [_I, _P]),
 }
 
 
