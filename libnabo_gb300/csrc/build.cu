@@ -308,27 +308,33 @@ __global__ void k_prepare(SegLevel<T> L, const LevelState* st, int dim) {
   L.eq[s] = 0;
 }
 
+// Also keeps each position's coordinate along its segment's cut dimension in
+// `val` for the rest of the level (4 or 8 bytes instead of a whole record;
+// the swaps move it with the records).
 template <typename T, int D>
 __global__ void k_minmax(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                         const LevelState* st) {
+                         const LevelState* st, T* __restrict__ val) {
   using Key = typename KeyOf<T>::type;
   if (st->nseg == 0) return;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  int s = -1;
-  Key kmin = 0, kmax = 0;
-  if (p < n) {
-    s = segOf[p];
-    if (s >= 0) {
-      const T v = recs[p].p.c[L.cutDim[s]];
-      kmin = kmax = ordered_key(v);
+  for (int64_t tile = blockIdx.x; tile * kBlock < n; tile += gridDim.x) {
+    const int64_t p = tile * kBlock + threadIdx.x;
+    int s = -1;
+    Key kmin = 0, kmax = 0;
+    if (p < n) {
+      s = segOf[p];
+      if (s >= 0) {
+        const T v = recs[p].p.c[L.cutDim[s]];
+        val[p] = v;
+        kmin = kmax = ordered_key(v);
+      }
     }
-  }
-  bool tail;
-  kmin = seg_warp_reduce(s, kmin, MinOp(), &tail);
-  kmax = seg_warp_reduce(s, kmax, MaxOp(), &tail);
-  if (tail && s >= 0) {
-    atomicMin(L.mnK + s, kmin);
-    atomicMax(L.mxK + s, kmax);
+    bool tail;
+    kmin = seg_warp_reduce(s, kmin, MinOp(), &tail);
+    kmax = seg_warp_reduce(s, kmax, MaxOp(), &tail);
+    if (tail && s >= 0) {
+      atomicMin(L.mnK + s, kmin);
+      atomicMax(L.mxK + s, kmax);
+    }
   }
 }
 
@@ -358,26 +364,28 @@ __global__ void k_cut(SegLevel<T> L, const LevelState* st) {
   L.mode[s] = mode;
 }
 
-template <typename T, int D>
-__global__ void k_count(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
+template <typename T>
+__global__ void k_count(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
                         const LevelState* st) {
   if (st->nseg == 0) return;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  int s = -1;
-  int2 c = make_int2(0, 0);
-  if (p < n) {
-    s = segOf[p];
-    if (s >= 0) {
-      const T v = recs[p].p.c[L.cutDim[s]];
-      const T cut = L.cut[s];
-      c = make_int2(v < cut ? 1 : 0, v == cut ? 1 : 0);
+  for (int64_t tile = blockIdx.x; tile * kBlock < n; tile += gridDim.x) {
+    const int64_t p = tile * kBlock + threadIdx.x;
+    int s = -1;
+    int2 c = make_int2(0, 0);
+    if (p < n) {
+      s = segOf[p];
+      if (s >= 0) {
+        const T v = val[p];
+        const T cut = L.cut[s];
+        c = make_int2(v < cut ? 1 : 0, v == cut ? 1 : 0);
+      }
     }
-  }
-  bool tail;
-  c = seg_warp_reduce(s, c, AddOp(), &tail);
-  if (tail && s >= 0) {
-    if (c.x) atomicAdd(L.lt + s, c.x);
-    if (c.y) atomicAdd(L.eq + s, c.y);
+    bool tail;
+    c = seg_warp_reduce(s, c, AddOp(), &tail);
+    if (tail && s >= 0) {
+      if (c.x) atomicAdd(L.lt + s, c.x);
+      if (c.y) atomicAdd(L.eq + s, c.y);
+    }
   }
 }
 
@@ -385,15 +393,17 @@ __global__ void k_count(const Rec<T, D>* __restrict__ recs, const int* __restric
 // :149-177). Pass 1 scans the whole segment for `< cut`: a left element
 // that is not `< cut` inside the first L positions trades with a right
 // element that is not `>= cut`. Pass 2 scans from br1 = L for `<= cut`.
-template <typename T, int D>
-__device__ __forceinline__ int2 misplaced(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n,
+// (A segment without points equal to its cut has nothing to move in pass 2:
+// after pass 1 everything < cut is left of lt and everything else right.)
+template <typename T>
+__device__ __forceinline__ int2 misplaced(const T* __restrict__ val, const int* __restrict__ segOf, int n,
                                           const SegLevel<T>& L, int pass, int p, int* segOut) {
   int2 f = make_int2(0, 0);
   int s = -1;
   if (p < n) {
     s = segOf[p];
-    if (s >= 0) {
-      const T v = recs[p].p.c[L.cutDim[s]];
+    if (s >= 0 && (pass == 1 || L.eq[s] != 0)) {
+      const T v = val[p];
       const T cut = L.cut[s];
       const int loc = p - L.start[s];
       const int lt = L.lt[s];
@@ -411,77 +421,94 @@ __device__ __forceinline__ int2 misplaced(const Rec<T, D>* __restrict__ recs, co
   return f;
 }
 
-template <typename T, int D>
-__global__ void k_flag_sums(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                            int pass, int2* blockSums, const LevelState* st) {
+// Block b owns tiles [b * tiles, (b + 1) * tiles) of kBlock positions.
+template <typename T>
+__global__ void k_flag_sums(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
+                            int pass, int tiles, int2* blockSums, const LevelState* st) {
   if (st->nseg == 0) return;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  int s;
-  const int2 f = misplaced(recs, segOf, n, L, pass, p, &s);
+  int2 acc = make_int2(0, 0);
+  for (int t = 0; t < tiles; ++t) {
+    const int64_t p = ((int64_t)blockIdx.x * tiles + t) * kBlock + threadIdx.x;
+    int s;
+    acc = add2(acc, misplaced(val, segOf, n, L, pass, p < n ? (int)p : n, &s));
+  }
   int2 total;
-  block_excl_scan(f, &total);
+  block_excl_scan(acc, &total);
   if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
 }
 
 // Single block: exclusive scan of the per-block sums; the grand total goes
-// to *total.
+// to *total. Each thread scans a contiguous run serially and one block-wide
+// scan joins the runs (a loop of block-wide scans over the sums would
+// serialise on its barriers: 0.2 ms per call at 22 M points).
 __global__ void k_scan_block_sums(int2* sums, int nb, int2* total, const LevelState* st) {
   if (st->nseg == 0) {
     if (threadIdx.x == 0) *total = make_int2(0, 0);
     return;
   }
-  int2 carry = make_int2(0, 0);
-  for (int base = 0; base < nb; base += kBlock) {
-    const int i = base + threadIdx.x;
-    const int2 v = i < nb ? sums[i] : make_int2(0, 0);
-    int2 t;
-    const int2 ex = block_excl_scan(v, &t);
-    if (i < nb) sums[i] = add2(carry, ex);
-    carry = add2(carry, t);
+  const int per = (nb + kBlock - 1) / kBlock;
+  const int b0 = threadIdx.x * per;
+  const int b1 = min(b0 + per, nb);
+  int2 run = make_int2(0, 0);
+  for (int i = b0; i < b1; ++i) run = add2(run, sums[i]);
+  int2 t;
+  int2 carry = block_excl_scan(run, &t);
+  for (int i = b0; i < b1; ++i) {
+    const int2 v = sums[i];
+    sums[i] = carry;
+    carry = add2(carry, v);
   }
-  if (threadIdx.x == 0) *total = carry;
+  if (threadIdx.x == 0) *total = t;
 }
 
-template <typename T, int D>
-__global__ void k_flag_ranks(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                             int pass, const int2* blockPrefix, int2* S, const LevelState* st) {
+template <typename T>
+__global__ void k_flag_ranks(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
+                             int pass, int tiles, const int2* blockPrefix, int2* S, const LevelState* st) {
   if (st->nseg == 0) return;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  int s;
-  const int2 f = misplaced(recs, segOf, n, L, pass, p, &s);
-  int2 total;
-  const int2 ex = block_excl_scan(f, &total);
-  if (p < n) S[p] = add2(ex, blockPrefix[blockIdx.x]);
+  int2 carry = blockPrefix[blockIdx.x];
+  for (int t = 0; t < tiles; ++t) {
+    const int64_t p = ((int64_t)blockIdx.x * tiles + t) * kBlock + threadIdx.x;
+    int s;
+    const int2 f = misplaced(val, segOf, n, L, pass, p < n ? (int)p : n, &s);
+    int2 total;
+    const int2 ex = block_excl_scan(f, &total);
+    if (p < n) S[p] = add2(ex, carry);
+    carry = add2(carry, total);
+  }
 }
 
-template <typename T, int D>
-__global__ void k_pairs(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
+template <typename T>
+__global__ void k_pairs(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
                         int pass, const int2* __restrict__ S, int* pairA, int* pairB, const LevelState* st) {
   if (st->nseg == 0) return;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  int s;
-  const int2 f = misplaced(recs, segOf, n, L, pass, p, &s);
-  if (f.x) pairA[S[p].x] = p;
-  if (f.y) {
-    const int st = L.start[s];
-    const int base = S[st].y;
-    const int m = S[st + L.count[s]].y - base;
-    const int j = S[p].y - base;
-    const int slot = base + m - 1 - j;
-    if (slot >= 0 && slot < n) pairB[slot] = p;
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    int s;
+    const int2 f = misplaced(val, segOf, n, L, pass, p, &s);
+    if (f.x) pairA[S[p].x] = p;
+    if (f.y) {
+      const int st = L.start[s];
+      const int base = S[st].y;
+      const int m = S[st + L.count[s]].y - base;
+      const int j = S[p].y - base;
+      const int slot = base + m - 1 - j;
+      if (slot >= 0 && slot < n) pairB[slot] = p;
+    }
   }
 }
 
 template <typename T, int D>
-__global__ void k_swap(Rec<T, D>* recs, const int* __restrict__ pairA, const int* __restrict__ pairB,
+__global__ void k_swap(Rec<T, D>* recs, T* val, const int* __restrict__ pairA, const int* __restrict__ pairB,
                        const int2* __restrict__ total, int cap) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= cap || t >= total->x || t >= total->y) return;
-  const int a = pairA[t], b = pairB[t];
-  const Rec<T, D> ra = recs[a];
-  recs[a] = recs[b];
-  recs[b] = ra;
+  const int m = min(cap, min(total->x, total->y));
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
+    const int a = pairA[t], b = pairB[t];
+    const Rec<T, D> ra = recs[a];
+    recs[a] = recs[b];
+    recs[b] = ra;
+    const T va = val[a];
+    val[a] = val[b];
+    val[b] = va;
+  }
 }
 
 // nabo/kdtree_cpu.cpp:180-223: leftCount rule, node, children.
@@ -575,12 +602,12 @@ __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, const LevelState* st
 template <typename T>
 __global__ void k_update_segof(int* segOf, int n, SegLevel<T> L, const LevelState* st) {
   if (st->nseg == 0) return;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  const int s = segOf[p];
-  if (s < 0) return;
-  const int loc = p - L.start[s];
-  segOf[p] = loc < L.leftCount[s] ? L.newLeft[s] : L.newRight[s];
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    const int s = segOf[p];
+    if (s < 0) continue;
+    const int loc = p - L.start[s];
+    segOf[p] = loc < L.leftCount[s] ? L.newLeft[s] : L.newRight[s];
+  }
 }
 
 // Closes a level: records its top-node range and makes the segments the
@@ -1114,7 +1141,9 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   const int64_t topCap = n + 1;
   const int64_t smallCap = n + nClouds + 1;
   const int lvCap = hostDriven ? 4096 : std::max(maxLevels, 1);
+  T* val;
   NABO_CUDA_TRY(sc.get(&segOf, n));
+  NABO_CUDA_TRY(sc.get(&val, n));
   NABO_CUDA_TRY(sc.get(&S, n + 1));
   NABO_CUDA_TRY(sc.get(&blockSums, nb));
   NABO_CUDA_TRY(sc.get(&pairA, pairCap));
@@ -1152,6 +1181,15 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   NABO_CUDA_TRY(cudaGetLastError());
 
   const int sg = ceil_div(segCap, 128);
+  // per-position passes: a fixed grid of 8 blocks per SM looping over tiles
+  // of kBlock positions; the two scan passes give each block a contiguous
+  // run of `tiles` tiles
+  int device = 0, sms = 0;
+  NABO_CUDA_TRY(cudaGetDevice(&device));
+  NABO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int grid = std::max(1, std::min(nb, 8 * std::max(sms, 1)));
+  const int tiles = ceil_div(nb, grid);
+  const int scanBlocks = ceil_div(nb, tiles);
   for (int level = 0; hostDriven || level < maxLevels; ++level) {
     if (hostDriven) {
       int nseg = 0;
@@ -1161,19 +1199,19 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
       if (level >= lvCap) return set_error(kErrUnsupported, "kd-tree build: too many levels");
     }
     k_prepare<T><<<sg, 128, 0, stream>>>(cur, st, dim);
-    k_minmax<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, st);
+    k_minmax<T, D><<<grid, kBlock, 0, stream>>>(recs, segOf, N, cur, st, val);
     k_cut<T><<<sg, 128, 0, stream>>>(cur, st);
-    k_count<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, st);
+    k_count<T><<<grid, kBlock, 0, stream>>>(val, segOf, N, cur, st);
     for (int pass = 1; pass <= 2; ++pass) {
-      k_flag_sums<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, blockSums, st);
-      k_scan_block_sums<<<1, kBlock, 0, stream>>>(blockSums, nb, S + n, st);
-      k_flag_ranks<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, blockSums, S, st);
-      k_pairs<T, D><<<nb, kBlock, 0, stream>>>(recs, segOf, N, cur, pass, S, pairA, pairB, st);
-      k_swap<T, D><<<ceil_div(pairCap, kBlock), kBlock, 0, stream>>>(recs, pairA, pairB, S + n, (int)pairCap);
+      k_flag_sums<T><<<scanBlocks, kBlock, 0, stream>>>(val, segOf, N, cur, pass, tiles, blockSums, st);
+      k_scan_block_sums<<<1, kBlock, 0, stream>>>(blockSums, scanBlocks, S + n, st);
+      k_flag_ranks<T><<<scanBlocks, kBlock, 0, stream>>>(val, segOf, N, cur, pass, tiles, blockSums, S, st);
+      k_pairs<T><<<grid, kBlock, 0, stream>>>(val, segOf, N, cur, pass, S, pairA, pairB, st);
+      k_swap<T, D><<<grid, kBlock, 0, stream>>>(recs, val, pairA, pairB, S + n, (int)pairCap);
     }
     k_finalize<T><<<sg, 128, 0, stream>>>(cur, nxt, st, top, small, counters, dim, (int)segCap, (int)smallCap,
                                           (int)topCap);
-    k_update_segof<T><<<nb, kBlock, 0, stream>>>(segOf, N, cur, st);
+    k_update_segof<T><<<grid, kBlock, 0, stream>>>(segOf, N, cur, st);
     k_advance<<<1, 1, 0, stream>>>(st, counters, lv, lv + lvCap, lvCap);
     NABO_CUDA_TRY(cudaGetLastError());
     std::swap(cur, nxt);
