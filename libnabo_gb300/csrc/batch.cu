@@ -35,6 +35,8 @@ struct nabo_cuda_batch {
   int64_t* nodeOffset = nullptr;
   void* rootBox = nullptr;
   int* status = nullptr;
+  void* recs32 = nullptr;    // f64: float copies of recs for the search's pre-filter
+  float* coordMax = nullptr;
   // query plan
   int64_t nq = 0;
   int kMax = 0;
@@ -103,9 +105,12 @@ int build(nabo_cuda_batch* b, const void* clouds, cudaStream_t st) {
   f.rootHi = static_cast<unsigned char*>(b->rootBox) + (size_t)b->nClouds * kMaxDim * es;
   f.status = b->status;
 #define NABO_B_CASE(TT, DD)                                                                                \
-  if (b->dpad == DD)                                                                                       \
-    return build_forest<TT, DD>(static_cast<const TT*>(clouds), b->nTotal, b->dim, b->dim, b->bucketSize, \
-                                b->dOff, b->nClouds, b->maxLevels, st, &f);
+  if (b->dpad == DD) {                                                                                     \
+    const int rc = build_forest<TT, DD>(static_cast<const TT*>(clouds), b->nTotal, b->dim, b->dim,        \
+                                        b->bucketSize, b->dOff, b->nClouds, b->maxLevels, st, &f);         \
+    if (rc != kOk || !b->recs32) return rc;                                                                \
+    return narrow_records<DD>(b->recs, b->nTotal, b->dim, b->recs32, b->coordMax, st);                   \
+  }
   if (b->dtype == NABO_CUDA_FLOAT32) {
     NABO_B_CASE(float, 2) NABO_B_CASE(float, 3) NABO_B_CASE(float, 4) NABO_B_CASE(float, 8) NABO_B_CASE(float, 16)
   } else {
@@ -142,6 +147,8 @@ int search(nabo_cuda_batch* b, const void* query, double eps, unsigned flags, do
   a.cell = b->cell;
   a.rank = b->rank;
   a.blockSize = b->blockSize;
+  a.recs32 = b->recs32;
+  a.coordMax = b->coordMax;
 #define NABO_B_CASE(TT, DD) \
   if (b->dpad == DD) return knn_batch<TT, DD>(a, st);
   if (b->dtype == NABO_CUDA_FLOAT32) {
@@ -206,6 +213,11 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->nodeOffset, off.size() * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->rootBox, (size_t)2 * nClouds * kMaxDim * es);
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->status, 4 * sizeof(int));
+  if (e == cudaSuccess && dtype == NABO_CUDA_FLOAT64) {
+    const size_t rec32 = ((size_t)dpad * 4 + 4 + 15) / 16 * 16;  // sizeof(Rec<float, dpad>)
+    e = cudaMalloc(&b->recs32, (size_t)total * rec32);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->coordMax, sizeof(float));
+  }
   if (e == cudaSuccess) e = cudaMemcpy(b->dOff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(b->status, 0, 4 * sizeof(int));
   if (e != cudaSuccess) {
@@ -221,7 +233,8 @@ int nabo_cuda_batch_destroy(nabo_cuda_batch* b) {
   Guard g(b->device);
   drop_graph(b);
   free_query_plan(b);
-  for (void* p : {(void*)b->dOff, b->recs, b->nodes, (void*)b->nodeOffset, b->rootBox, (void*)b->status})
+  for (void* p : {(void*)b->dOff, b->recs, b->nodes, (void*)b->nodeOffset, b->rootBox, (void*)b->status, b->recs32,
+                  (void*)b->coordMax})
     if (p) cudaFree(p);
   delete b;
   return kOk;

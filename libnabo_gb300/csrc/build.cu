@@ -1308,6 +1308,55 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   return kOk;
 }
 
+namespace {
+
+// Float copies of double records (same order), for the search's float
+// pre-filter of leaf points, and the largest coordinate magnitude over the
+// searched dimensions (as float bits, atomicMax: non-negative floats order
+// like their bit patterns). Coordinates beyond the float range become inf,
+// which switches the pre-filter off.
+template <int D>
+__global__ void k_narrow(const Rec<double, D>* __restrict__ recs, int64_t n, int dim, Rec<float, D>* out,
+                         unsigned* coordMaxBits) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  float m = 0.0f;
+  if (p < n) {
+    Rec<double, D> r;
+    load_rec(recs, p, r);
+    Rec<float, D> f;
+#pragma unroll
+    for (int c = 0; c < RecSize<float, D>::chunks; ++c) f.v[c] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      f.p.c[d] = (float)r.p.c[d];
+      if (d < dim) m = fmaxf(m, fabsf(f.p.c[d]));
+    }
+    f.p.idx = r.p.idx;
+    out[p] = f;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(kFull, m, o));
+  if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(coordMaxBits, __float_as_uint(m));
+}
+
+}  // namespace
+
+template <int D>
+int narrow_records(const void* recs, int64_t n, int dim, void* recs32, float* coordMax, cudaStream_t stream) {
+  NABO_CUDA_TRY(cudaMemsetAsync(coordMax, 0, sizeof(float), stream));
+  if (n > 0)
+    k_narrow<D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(static_cast<const Rec<double, D>*>(recs), n, dim,
+                                                            static_cast<Rec<float, D>*>(recs32),
+                                                            reinterpret_cast<unsigned*>(coordMax));
+  NABO_CUDA_TRY(cudaGetLastError());
+  return kOk;
+}
+template int narrow_records<2>(const void*, int64_t, int, void*, float*, cudaStream_t);
+template int narrow_records<3>(const void*, int64_t, int, void*, float*, cudaStream_t);
+template int narrow_records<4>(const void*, int64_t, int, void*, float*, cudaStream_t);
+template int narrow_records<8>(const void*, int64_t, int, void*, float*, cudaStream_t);
+template int narrow_records<16>(const void*, int64_t, int, void*, float*, cudaStream_t);
+
 #define NABO_BUILD_INSTANTIATE(T, D)                                                                          \
   template int build_kdtree<T, D>(const T*, int64_t, int64_t, int, unsigned, cudaStream_t, DeviceCloud*,      \
                                   double*, double*, BuildStats*);                                             \

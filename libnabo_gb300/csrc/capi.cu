@@ -153,6 +153,34 @@ int pad_dim(int dim) {
     return set_error(kErrInternal, "bad dispatch");              \
   } while (0)
 
+// The same dispatch, storing the result in `rc` instead of returning it.
+#define NABO_DISPATCH_RC(rc, dtype, dpad, CALL)                  \
+  do {                                                           \
+    bool hit_ = true;                                            \
+    if ((dtype) == NABO_CUDA_FLOAT32) {                          \
+      using T = float;                                           \
+      switch (dpad) {                                            \
+        case 2: { constexpr int D = 2; rc = CALL; break; }       \
+        case 3: { constexpr int D = 3; rc = CALL; break; }       \
+        case 4: { constexpr int D = 4; rc = CALL; break; }       \
+        case 8: { constexpr int D = 8; rc = CALL; break; }       \
+        case 16: { constexpr int D = 16; rc = CALL; break; }     \
+        default: hit_ = false;                                   \
+      }                                                          \
+    } else {                                                     \
+      using T = double;                                          \
+      switch (dpad) {                                            \
+        case 2: { constexpr int D = 2; rc = CALL; break; }       \
+        case 3: { constexpr int D = 3; rc = CALL; break; }       \
+        case 4: { constexpr int D = 4; rc = CALL; break; }       \
+        case 8: { constexpr int D = 8; rc = CALL; break; }       \
+        case 16: { constexpr int D = 16; rc = CALL; break; }     \
+        default: hit_ = false;                                   \
+      }                                                          \
+    }                                                            \
+    if (!hit_) rc = set_error(kErrInternal, "bad dispatch");     \
+  } while (0)
+
 uint32_t storage_bit_count(uint32_t v) {
   for (uint32_t i = 0; i < 64; ++i) {
     if (v == 0) return i;
@@ -161,12 +189,33 @@ uint32_t storage_bit_count(uint32_t v) {
   return 64;
 }
 
+// Float copies of a double kd-tree's records for the search's pre-filter.
+template <int D>
+int narrow_cloud_d(DeviceCloud& c, cudaStream_t st) {
+  NABO_CUDA_TRY(cudaMalloc(&c.recs32, (size_t)c.n * sizeof(Rec<float, D>)));
+  NABO_CUDA_TRY(cudaMalloc((void**)&c.coordMax, sizeof(float)));
+  return narrow_records<D>(c.recs, c.n, c.dim, c.recs32, c.coordMax, st);
+}
+
+int narrow_cloud(DeviceCloud& c, cudaStream_t st) {
+  switch (c.dpad) {
+    case 2: return narrow_cloud_d<2>(c, st);
+    case 3: return narrow_cloud_d<3>(c, st);
+    case 4: return narrow_cloud_d<4>(c, st);
+    case 8: return narrow_cloud_d<8>(c, st);
+    default: return narrow_cloud_d<16>(c, st);
+  }
+}
+
 int build_any(nabo_cuda_search* h, const void* dCloud, int64_t stride, cudaStream_t st) {
   double rootMin[kMaxDim], rootMax[kMaxDim];
   if (h->searchType == NABO_SEARCH_KDTREE_CUDA) {
-    NABO_DISPATCH(h->c.dtype, h->c.dpad,
-                  (build_kdtree<T, D>(static_cast<const T*>(dCloud), h->c.n, stride, h->c.dim, h->c.bucketSize, st,
-                                      &h->c, rootMin, rootMax, nullptr)));
+    int rc = kOk;
+    NABO_DISPATCH_RC(rc, h->c.dtype, h->c.dpad,
+                     (build_kdtree<T, D>(static_cast<const T*>(dCloud), h->c.n, stride, h->c.dim, h->c.bucketSize,
+                                         st, &h->c, rootMin, rootMax, nullptr)));
+    if (rc == kOk && h->c.dtype == NABO_CUDA_FLOAT64) rc = narrow_cloud(h->c, st);
+    return rc;
   }
   NABO_DISPATCH(h->c.dtype, h->c.dpad, (pack_cloud<T, D>(static_cast<const T*>(dCloud), h->c.n, stride, h->c.dim, st, &h->c)));
 }
@@ -187,8 +236,12 @@ void free_events(nabo_cuda_search* s) {
 void free_cloud(DeviceCloud& c) {
   if (c.recs) cudaFree(c.recs);
   if (c.nodes) cudaFree(c.nodes);
+  if (c.recs32) cudaFree(c.recs32);
+  if (c.coordMax) cudaFree(c.coordMax);
   c.recs = nullptr;
   c.nodes = nullptr;
+  c.recs32 = nullptr;
+  c.coordMax = nullptr;
 }
 
 int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int64_t n, int64_t colStride, int dimIn,

@@ -56,6 +56,10 @@ struct DeviceCloud {
   int height = 0;         // max inner nodes on a root-to-leaf path
   double lo[kMaxDim];     // true per-dimension bounds of the points (for query ordering)
   double hi[kMaxDim];
+  // f64 kd-trees: float copies of recs (same order) and the largest
+  // coordinate magnitude (device float), for the search's float pre-filter
+  void* recs32 = nullptr;
+  float* coordMax = nullptr;
 };
 
 struct BuildStats {
@@ -112,9 +116,16 @@ struct BatchArgs {
   uint32_t* cell;
   uint32_t* rank;
   int blockSize;                // threads per block of the search kernel
+  const void* recs32;           // f64: float copies of recs, or null
+  const float* coordMax;        // f64: device float, largest coordinate magnitude
 };
 template <typename T, int D>
 int knn_batch(const BatchArgs& b, cudaStream_t stream);
+
+// Float copies of double records and their largest coordinate magnitude
+// (recs32 holds n Rec<float, D>; coordMax one device float).
+template <int D>
+int narrow_records(const void* recs, int64_t n, int dim, void* recs32, float* coordMax, cudaStream_t stream);
 
 template <typename T, int D>
 int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, const int64_t* dOff,

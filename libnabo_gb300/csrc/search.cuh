@@ -216,6 +216,8 @@ struct KnnLaunch {
   const int32_t* nqDevice;  // if set, only threads t < *nqDevice search (t < nq still bounds the grid)
   double fallbackRadius;    // >= 0: bounded searches that miss rerun with maxRadius2 (see KnnArgs)
   int32_t* fallbacks;
+  const void* recs32;       // double clouds: float copies of recs for the leaf pre-filter, or null
+  const float* coordMax;    // largest coordinate magnitude of the cloud (device float)
   // batches of clouds (all null for one cloud): queries of cloud c are
   // [bQueryOffset[c], bQueryOffset[c+1]), its tree starts at node
   // bNodeOffset[c], it wants bK[c] neighbours written from bOutOffset[c]
@@ -236,19 +238,77 @@ struct KnnLaunch {
 // (nabo/kdtree_cpu.cpp:378-398); the warp pays for the largest number of
 // insertions of any lane instead of for every point where some lane
 // inserts.
+// Float pre-filter of leaf points for double clouds (the GB300 runs FP64 at
+// 1/64 of its FP32 rate, and the leaf distances are most of a double
+// search's arithmetic). With q~ and p~ the float roundings of the query and
+// point coordinates and e = (max|q~| + max|p~|) * 2^-22, every coordinate
+// difference satisfies |q - p| >= |q~ - p~|_float - e (conversion and
+// subtraction errors are at most 2.1 * 2^-24 * (|q| + |p|) each), so
+//     LB = sum_d max(0, |q~_d - p~_d| - e)^2,  taken * (1 - 2^-17)
+// is below the exact squared distance, float roundings of LB itself and the
+// double sum's own rounding included. A point with LB above a float at or
+// above min(head, maxRadius^2) cannot enter the heap, and only the others
+// get the exact double distance: results are unchanged. Coordinates beyond
+// the float range make e infinite, which rejects nothing.
+template <typename T, int D>
+struct LeafFilter {
+  __device__ __forceinline__ void init(const void*, const float*, const T (&)[D]) {}
+  __device__ __forceinline__ bool on() const { return false; }
+  __device__ __forceinline__ float threshold(T, T) const { return 0.0f; }
+  __device__ __forceinline__ bool rejects(int64_t, float) const { return false; }
+};
+
+template <int D>
+struct LeafFilter<double, D> {
+  const Rec<float, D>* recs32;
+  float qf[D];
+  float e;
+  __device__ __forceinline__ void init(const void* r32, const float* coordMax, const double (&q)[D]) {
+    recs32 = static_cast<const Rec<float, D>*>(r32);
+    e = Ar<float>::inf();
+    if (recs32) {
+      float mq = 0.0f;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        qf[d] = (float)q[d];
+        mq = fmaxf(mq, fabsf(qf[d]));
+      }
+      e = (mq + *coordMax) * 0x1p-22f;
+    }
+  }
+  __device__ __forceinline__ bool on() const { return recs32 != nullptr; }
+  // a float at or above min(head, maxRadius2)
+  __device__ __forceinline__ float threshold(double head, double maxRadius2) const {
+    return __double2float_ru(fmin(head, maxRadius2));
+  }
+  __device__ __forceinline__ bool rejects(int64_t i, float thr) const {
+    Rec<float, D> f;
+    load_rec(recs32, i, f);
+    float lb = 0.0f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const float a = fmaxf(fabsf(qf[d] - f.p.c[d]) - e, 0.0f);
+      lb += a * a;
+    }
+    return lb * (1.0f - 0x1p-17f) > thr;
+  }
+};
+
 template <typename T, int D, int K>
 __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, uint32_t st, uint32_t cnt,
-                                          const T (&q)[D], T maxRadius2, T minDist, bool want, TopK<T, K>& heap) {
+                                          const T (&q)[D], T maxRadius2, T minDist, bool want, TopK<T, K>& heap,
+                                          const LeafFilter<T, D>& flt) {
   constexpr int kChunk = 4;
   for (uint32_t base = 0; base < cnt; base += kChunk) {
     T dj[kChunk];
     int ij[kChunk];
     unsigned mask = 0;
+    const float thr = flt.on() ? flt.threshold(heap.head(), maxRadius2) : 0.0f;
 #pragma unroll
     for (int j = 0; j < kChunk; ++j) {
       dj[j] = Ar<T>::inf();
       ij[j] = -1;
-      if (base + j < cnt) {
+      if (base + j < cnt && !(flt.on() && flt.rejects((int64_t)st + base + j, thr))) {
         Rec<T, D> r;
         load_rec(recs, (int64_t)st + base + j, r);
         dj[j] = dist2_seq(q, r);
@@ -394,6 +454,8 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
     const T maxError2 = (T)a.maxError2;
     TopK<T, K> heap;
     heap.init(k);
+    LeafFilter<T, D> flt;
+    flt.init(a.recs32, a.coordMax, q);
     T off[D];
     StackRec<T, D> stk[STACK];
     for (;;) {  // the search, and at most once more without the bound
@@ -422,7 +484,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
         }
         // leaf
         const uint32_t cnt = node_payload(nd.meta);
-        scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap);
+        scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap, flt);
         touched += cnt;
         // pop the next far child that can still hold a better neighbour
         bool more = false;
@@ -505,6 +567,8 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
   if (!active) maxRadius2 = -Ar<T>::inf();  // wants nothing
   TopK<T, K> heap;
   heap.init(a.k);
+  LeafFilter<T, D> flt;
+  flt.init(nullptr, nullptr, q);
   T off[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) off[d] = T(0);
@@ -546,7 +610,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
         node = first;
         continue;
       }
-      scan_leaf<T, D, K>(recs, node_start(nd), node_payload(nd.meta), q, maxRadius2, minDist, want, heap);
+      scan_leaf<T, D, K>(recs, node_start(nd), node_payload(nd.meta), q, maxRadius2, minDist, want, heap, flt);
     }
     if (sp == 0) break;
     --sp;

@@ -52,6 +52,8 @@ KnnLaunch make_launch(const DeviceCloud& c, const KnnArgs& a, const int32_t* ord
   L.nqDevice = a.nqDevice;
   L.fallbackRadius = a.maxRadii ? a.fallbackRadius : -1.0;
   L.fallbacks = a.fallbacks;
+  L.recs32 = c.recs32;
+  L.coordMax = c.coordMax;
   L.bQueryOffset = nullptr;
   L.bNodeOffset = nullptr;
   L.bK = nullptr;
@@ -229,6 +231,8 @@ int knn_batch(const BatchArgs& b, cudaStream_t stream) {
   L.bK = b.kOf;
   L.bOutOffset = b.outOffset;
   L.bClouds = b.nClouds;
+  L.recs32 = b.recs32;
+  L.coordMax = b.coordMax;
   const int grid = ceil_div(b.nq, b.blockSize);
 #define NABO_LAUNCH(KK)                                                                     \
   case KK:                                                                                  \
