@@ -31,31 +31,43 @@ __device__ __forceinline__ bool pair_greater(T da, int ia, T db, int ib) {
   return da > db || (da == db && ia > ib);
 }
 
-// Generic form (double): separate distance and index arrays.
+// double: the distance's 64-bit pattern and the index in separate arrays.
+// Distances are >= 0, where the pattern orders like the value, so the
+// (dist2, index) order is decided by integer compares on the ALU, keeping
+// the scarce FP64 pipe for distances. An empty slot is (+inf, -1): no finite
+// distance compares above it, as the reference's strict `dist < head` with
+// head = +inf; padding slots (>= k) hold (+0, -1), below every entry.
 template <typename T, int K>
 struct TopK {
-  T d[K];
+  unsigned long long d[K];
   int i[K];
+  static __device__ __forceinline__ bool greater(unsigned long long da, int ia, unsigned long long db, int ib) {
+    return da > db || (da == db && ia > ib);
+  }
+  static __device__ __forceinline__ unsigned long long bits(T x) {
+    return (unsigned long long)__double_as_longlong((double)x);
+  }
   __device__ __forceinline__ void init(int k) {
 #pragma unroll
     for (int j = 0; j < K; ++j) {
-      d[j] = j < k ? Ar<T>::inf() : -Ar<T>::inf();
+      d[j] = j < k ? bits(Ar<T>::inf()) : 0ull;
       i[j] = -1;
     }
   }
-  __device__ __forceinline__ T head() const { return d[0]; }
-  __device__ __forceinline__ bool accepts(T dist, int idx) const { return pair_greater(d[0], i[0], dist, idx); }
+  __device__ __forceinline__ T head() const { return (T)__longlong_as_double((long long)d[0]); }
+  __device__ __forceinline__ bool accepts(T dist, int idx) const { return greater(d[0], i[0], bits(dist), idx); }
   // Drops the head and inserts (dist, idx); requires accepts(dist, idx).
   __device__ __forceinline__ void insert(T dist, int idx) {
+    const unsigned long long x = bits(dist);
     bool g[K];
 #pragma unroll
-    for (int j = 0; j < K; ++j) g[j] = pair_greater(d[j], i[j], dist, idx);
+    for (int j = 0; j < K; ++j) g[j] = greater(d[j], i[j], x, idx);
 #pragma unroll
     for (int j = 0; j + 1 < K; ++j) {
-      d[j] = g[j + 1] ? d[j + 1] : (g[j] ? dist : d[j]);
+      d[j] = g[j + 1] ? d[j + 1] : (g[j] ? x : d[j]);
       i[j] = g[j + 1] ? i[j + 1] : (g[j] ? idx : i[j]);
     }
-    d[K - 1] = g[K - 1] ? dist : d[K - 1];
+    d[K - 1] = g[K - 1] ? x : d[K - 1];
     i[K - 1] = g[K - 1] ? idx : i[K - 1];
   }
   __device__ __forceinline__ int count(int k) const {
@@ -71,7 +83,7 @@ struct TopK {
     for (int j = 0; j < K; ++j) {
       if (j < k) {
         oi[k - 1 - j] = i[j];
-        od[k - 1 - j] = d[j];
+        od[k - 1 - j] = (T)__longlong_as_double((long long)d[j]);
         found += i[j] >= 0 ? 1 : 0;
       }
     }
