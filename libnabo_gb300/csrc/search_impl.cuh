@@ -96,9 +96,9 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
         k_knn_kdtree_packet<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);   \
     } else {                                                                       \
       if (small)                                                                   \
-        k_knn_kdtree<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);          \
+        launch_kdtree<T, D, KK, kStackSmall>(grid, 128, stream, L);          \
       else                                                                         \
-        k_knn_kdtree<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);          \
+        launch_kdtree<T, D, KK, kStackLarge>(grid, 128, stream, L);          \
     }                                                                              \
     break;
   switch (K) { NABO_K_LIST(NABO_LAUNCH) }
@@ -155,9 +155,9 @@ int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t
         k_knn_kdtree_packet<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);   \
     } else {                                                                       \
       if (small)                                                                   \
-        k_knn_kdtree<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);          \
+        launch_kdtree<T, D, KK, kStackSmall>(grid, 128, stream, L);          \
       else                                                                         \
-        k_knn_kdtree<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);          \
+        launch_kdtree<T, D, KK, kStackLarge>(grid, 128, stream, L);          \
     }                                                                              \
     break;
   switch (K) { NABO_K_LIST(NABO_LAUNCH) }
@@ -236,7 +236,7 @@ int knn_batch(const BatchArgs& b, cudaStream_t stream) {
   const int grid = ceil_div(b.nq, b.blockSize);
 #define NABO_LAUNCH(KK)                                                                     \
   case KK:                                                                                  \
-    k_knn_kdtree<T, D, KK, kStackLarge><<<grid, b.blockSize, 0, stream>>>(L);               \
+    launch_kdtree<T, D, KK, kStackLarge>(grid, b.blockSize, stream, L);               \
     break;
   switch (K) { NABO_K_LIST(NABO_LAUNCH) }
 #undef NABO_LAUNCH
