@@ -24,13 +24,7 @@
 
 #include "common.cuh"
 
-
 namespace nabo_gb300 {
-
-template <typename T>
-__device__ __forceinline__ bool pair_greater(T da, int ia, T db, int ib) {
-  return da > db || (da == db && ia > ib);
-}
 
 // double: the distance's 64-bit pattern and the index in separate arrays.
 // Distances are >= 0, where the pattern orders like the value, so the
