@@ -307,3 +307,31 @@ def test_non_finite_cloud_is_rejected():
     c = np.concatenate([cloud, np.full((500, 1), np.nan, np.float32)], axis=1)
     s = nb.NearestNeighbourSearch(c, dim=3)
     assert s.dim == 3
+
+
+@pytest.mark.parametrize("case", ["huge", "tiny", "offset", "far_queries", "mixed_scale"])
+def test_double_prefilter_edge_cases(case):
+    """Double clouds are searched with a float pre-filter of leaf points (a
+    float lower bound of each squared distance with a proven margin). Its
+    edge cases must still give the oracle's exact answer: coordinates beyond
+    the float range (the margin becomes infinite), values that are subnormal
+    or zero in float, a large common offset with tiny separations (float
+    cancellation), queries far from the cloud, and mixed scales."""
+    rng = np.random.default_rng(["huge", "tiny", "offset", "far_queries", "mixed_scale"].index(case) + 500)
+    if case == "huge":
+        cloud = rng.random((3000, 3)) * 1e40
+        q = rng.random((800, 3)) * 1e40
+    elif case == "tiny":
+        cloud = rng.random((3000, 3)) * 1e-40
+        q = rng.random((800, 3)) * 1e-40
+    elif case == "offset":
+        cloud = 1e6 + rng.random((3000, 3)) * 1e-3
+        q = 1e6 + rng.random((800, 3)) * 1e-3
+    elif case == "far_queries":
+        cloud = rng.random((3000, 3))
+        q = rng.random((800, 3)) * 1e3 + 1e5
+    else:
+        cloud = np.concatenate([rng.random((1500, 3)) * 1e-6, rng.random((1500, 3)) * 1e6])
+        q = np.concatenate([rng.random((400, 3)) * 1e-6, rng.random((400, 3)) * 1e6])
+    for k in (1, 10, 32):
+        _check_against_oracle(cloud.astype(np.float64), q.astype(np.float64), k)
