@@ -22,6 +22,8 @@
 // g[j+1], the new entry where the prefix ends, and keeps its value after.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace nabo_gb300 {
@@ -105,8 +107,9 @@ struct TopK<float, K> {
   }
   __device__ __forceinline__ float head() const { return __uint_as_float((uint32_t)(key[0] >> 32)); }
   __device__ __forceinline__ bool accepts(float dist, int idx) const { return make(dist, idx) < key[0]; }
-  __device__ __forceinline__ void insert(float dist, int idx) {
-    const uint64_t x = make(dist, idx);
+  __device__ __forceinline__ void insert(float dist, int idx) { insert_key(make(dist, idx)); }
+  // requires x < key[0]
+  __device__ __forceinline__ void insert_key(uint64_t x) {
     bool g[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) g[j] = key[j] > x;
@@ -307,37 +310,63 @@ __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, ui
                                           const LeafFilter<T, D>& flt) {
   constexpr int kChunk = 4;
   for (uint32_t base = 0; base < cnt; base += kChunk) {
-    T dj[kChunk];
-    int ij[kChunk];
     unsigned mask = 0;
-    const float thr = flt.on() ? flt.threshold(heap.head(), maxRadius2) : 0.0f;
+    if constexpr (std::is_same<T, float>::value) {
+      // float: candidates as packed (dist2 bits, index) keys, one 64-bit
+      // compare against the head and one 64-bit select per insertion
+      uint64_t kj[kChunk];
 #pragma unroll
-    for (int j = 0; j < kChunk; ++j) {
-      dj[j] = Ar<T>::inf();
-      ij[j] = -1;
-      if (base + j < cnt && !(flt.on() && flt.rejects((int64_t)st + base + j, thr))) {
-        Rec<T, D> r;
-        load_rec(recs, (int64_t)st + base + j, r);
-        dj[j] = dist2_seq(q, r);
-        ij[j] = r.p.idx;
-        const bool ok = want && dj[j] <= maxRadius2 && heap.accepts(dj[j], ij[j]) &&
-                        dj[j] > minDist;
-        mask |= ok ? (1u << j) : 0u;
-      }
-    }
-    while (mask) {
-      const int j = __ffs(mask) - 1;
-      mask &= mask - 1;
-      T dv = dj[0];
-      int iv = ij[0];
-#pragma unroll
-      for (int m = 1; m < kChunk; ++m) {
-        if (j == m) {
-          dv = dj[m];
-          iv = ij[m];
+      for (int j = 0; j < kChunk; ++j) {
+        kj[j] = ~0ull;
+        if (base + j < cnt) {
+          Rec<T, D> r;
+          load_rec(recs, (int64_t)st + base + j, r);
+          const float d = dist2_seq(q, r);
+          kj[j] = TopK<float, K>::make(d, r.p.idx);
+          const bool ok = want && d <= maxRadius2 && kj[j] < heap.key[0] && d > minDist;
+          mask |= ok ? (1u << j) : 0u;
         }
       }
-      if (heap.accepts(dv, iv)) heap.insert(dv, iv);
+      while (mask) {
+        const int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        uint64_t v = kj[0];
+#pragma unroll
+        for (int m = 1; m < kChunk; ++m)
+          if (j == m) v = kj[m];
+        if (v < heap.key[0]) heap.insert_key(v);
+      }
+    } else {
+      T dj[kChunk];
+      int ij[kChunk];
+      const float thr = flt.on() ? flt.threshold(heap.head(), maxRadius2) : 0.0f;
+#pragma unroll
+      for (int j = 0; j < kChunk; ++j) {
+        dj[j] = Ar<T>::inf();
+        ij[j] = -1;
+        if (base + j < cnt && !(flt.on() && flt.rejects((int64_t)st + base + j, thr))) {
+          Rec<T, D> r;
+          load_rec(recs, (int64_t)st + base + j, r);
+          dj[j] = dist2_seq(q, r);
+          ij[j] = r.p.idx;
+          const bool ok = want && dj[j] <= maxRadius2 && heap.accepts(dj[j], ij[j]) && dj[j] > minDist;
+          mask |= ok ? (1u << j) : 0u;
+        }
+      }
+      while (mask) {
+        const int j = __ffs(mask) - 1;
+        mask &= mask - 1;
+        T dv = dj[0];
+        int iv = ij[0];
+#pragma unroll
+        for (int m = 1; m < kChunk; ++m) {
+          if (j == m) {
+            dv = dj[m];
+            iv = ij[m];
+          }
+        }
+        if (heap.accepts(dv, iv)) heap.insert(dv, iv);
+      }
     }
   }
 }
