@@ -72,7 +72,8 @@ typedef struct nabo_cuda_params {
                              367-447), one query per thread; 2: the warp
                              packet -- the 32 queries of a warp walk one node
                              sequence, each pruning for itself -- for exact
-                             searches (epsilon 0) without TOUCH_STATISTICS */
+                             searches (epsilon 0) without TOUCH_STATISTICS
+                             and k <= 32 (larger k use the reference order) */
   int32_t threadsPerBlock; /* batched search kernel block size: 32, 64 or 128
                               (0 = 128); chosen by the autotuner */
   int32_t reserved[3];
@@ -112,7 +113,9 @@ int nabo_cuda_destroy(nabo_cuda_search* s);
  * touched (may be NULL): receives the reference's TOUCH_STATISTICS count
  * (points examined in visited leaves; nq*n for brute force) when the
  * object was created with NABO_TOUCH_STATISTICS, else 0.
- * Results are always sorted ascending (SORT_RESULTS is accepted). */
+ * Results are always sorted ascending (SORT_RESULTS is accepted).
+ * k up to 32 runs one query per thread, k from 33 to 1024 one query per
+ * warp (same results); larger k returns NABO_CUDA_ERR_UNSUPPORTED. */
 int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride, int k,
                   double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii, int32_t* indices,
                   void* dists2, uint64_t* touched);

@@ -259,7 +259,8 @@ int nabo_cuda_batch_set_queries(nabo_cuda_batch* b, const int64_t* queryCounts, 
       return set_error(kErrArgument, "Requesting more points (" + std::to_string(k[c]) +
                                          ") than available in cloud minus 1 (" + std::to_string(pts - 1) +
                                          ") (as self match is forbidden)");
-    if (k[c] > 32) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+    if (k[c] > 1024)
+      return set_error(kErrUnsupported, "k larger than 1024 is not supported by the CUDA search types");
     ks[(size_t)c] = k[c];
     kMax = std::max(kMax, k[c]);
     qoff[(size_t)c + 1] = qoff[(size_t)c] + queryCounts[c];

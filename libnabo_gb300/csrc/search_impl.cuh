@@ -4,6 +4,7 @@
 
 #include "internal.cuh"
 #include "search.cuh"
+#include "search_wide.cuh"
 
 #include <cstring>
 
@@ -22,6 +23,62 @@ inline int round_k(int k) {
   NABO_K_LIST(NABO_ROUND)
 #undef NABO_ROUND
   return -1;
+}
+
+// k above kMaxK: one warp per query holding 32*M slots (M compiled below).
+#define NABO_WIDE_LIST(X) X(2) X(4) X(8) X(16) X(32)
+constexpr int kMaxWideK = 1024;
+constexpr int kWideWarps = 4;  // queries per block of the kd-tree kernel
+constexpr int kWideBfWarps = 8;  // queries per block of the brute force
+
+inline int wide_m(int k) {
+#define NABO_ROUND(MM) \
+  if (k <= 32 * MM) return MM;
+  NABO_WIDE_LIST(NABO_ROUND)
+#undef NABO_ROUND
+  return -1;
+}
+
+inline int k_unsupported() {
+  return set_error(kErrUnsupported, "k larger than 1024 is not supported by the CUDA search types");
+}
+
+// Launches the one-warp-per-query kd-tree search for L.k (or the batch's
+// largest k) above kMaxK; `height` bounds the traversal stack.
+template <typename T, int D>
+int launch_wide_kdtree(const KnnLaunch& L, int kMax, int height, cudaStream_t stream) {
+  const int M = wide_m(kMax);
+  if (M < 0) return k_unsupported();
+  const int cap = height + 1;
+  const size_t smem = wide_stack_bytes<T, D>(kWideWarps, cap);
+  const int grid = ceil_div(L.nq, kWideWarps);
+  cudaError_t e = cudaSuccess;
+#define NABO_WIDE(MM)                                                                                 \
+  case MM: {                                                                                          \
+    if (smem > 48 * 1024)                                                                             \
+      e = cudaFuncSetAttribute(k_knn_kdtree_wide<T, D, MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                               (int)smem);                                                            \
+    if (e == cudaSuccess) k_knn_kdtree_wide<T, D, MM><<<grid, 32 * kWideWarps, smem, stream>>>(L, cap); \
+    break;                                                                                            \
+  }
+  switch (M) { NABO_WIDE_LIST(NABO_WIDE) }
+#undef NABO_WIDE
+  if (e != cudaSuccess) return cuda_error(e, "wide kd-tree search shared memory");
+  return kOk;
+}
+
+template <typename T, int D>
+int launch_wide_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
+  const int M = wide_m(L.k);
+  if (M < 0) return k_unsupported();
+  const int grid = ceil_div(L.nq, kWideBfWarps);
+#define NABO_WIDE(MM)                                                                    \
+  case MM:                                                                               \
+    k_knn_bruteforce_wide<T, D, MM><<<grid, 32 * kWideBfWarps, 0, stream>>>(L);          \
+    break;
+  switch (M) { NABO_WIDE_LIST(NABO_WIDE) }
+#undef NABO_WIDE
+  return kOk;
 }
 
 template <typename T, int D>
@@ -66,7 +123,7 @@ template <typename T, int D>
 int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
   if (a.nq == 0) return kOk;
   const int K = round_k(a.k);
-  if (K < 0) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+  if (K < 0 && a.k > kMaxWideK) return k_unsupported();
   if (c.height > kStackLarge)
     return set_error(kErrUnsupported, "kd-tree height exceeds the traversal stack of the CUDA search");
   int32_t* order = nullptr;
@@ -82,11 +139,23 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
   const int grid = ceil_div(a.nq, 128);
   const bool small = c.height <= kStackSmall;
   // Default: the reference visit order (it is also the faster one on the
-  // measured workloads); the warp packet is opt-in for exact searches.
-  const bool packet = a.traversal == 2;
-  if (packet && (a.eps != 0.0 || L.stats))
+  // measured workloads); the warp packet is opt-in for exact searches with
+  // k <= kMaxK.
+  const bool packet = a.traversal == 2 && K > 0;
+  if (packet && (a.eps != 0.0 || L.stats)) {
+    if (order) scratch_free(order, stream);
     return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
+  }
   if (a.evStart) cudaEventRecord(a.evStart, stream);
+  if (K < 0) {
+    const int rc = launch_wide_kdtree<T, D>(L, a.k, c.height, stream);
+    if (a.evStop) cudaEventRecord(a.evStop, stream);
+    const cudaError_t e = cudaGetLastError();
+    if (order) scratch_free(order, stream);
+    if (rc != kOk) return rc;
+    if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree_wide launch");
+    return kOk;
+  }
 #define NABO_LAUNCH(KK)                                                            \
   case KK:                                                                         \
     if (packet) {                                                                  \
@@ -114,15 +183,19 @@ template <typename T, int D>
 int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
   if (a.nq == 0) return kOk;
   const int K = round_k(a.k);
-  if (K < 0) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+  if (K < 0 && a.k > kMaxWideK) return k_unsupported();
   const KnnLaunch L = make_launch<T, D>(c, a, nullptr);
   const int grid = ceil_div(a.nq, 128);
   if (a.evStart) cudaEventRecord(a.evStart, stream);
+  if (K < 0) {
+    const int rc = launch_wide_bruteforce<T, D>(L, stream);
+    if (rc != kOk) return rc;
+  }
 #define NABO_LAUNCH(KK)                                              \
   case KK:                                                           \
     k_knn_bruteforce<T, D, KK><<<grid, 128, 0, stream>>>(L);         \
     break;
-  switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+  if (K > 0) switch (K) { NABO_K_LIST(NABO_LAUNCH) }
 #undef NABO_LAUNCH
   if (a.evStop) cudaEventRecord(a.evStop, stream);
   const cudaError_t e = cudaGetLastError();
@@ -136,16 +209,24 @@ template <typename T, int D>
 int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream) {
   if (a.nq == 0) return kOk;
   const int K = round_k(a.k);
-  if (K < 0) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+  if (K < 0 && a.k > kMaxWideK) return k_unsupported();
   if (c.height > kStackLarge)
     return set_error(kErrUnsupported, "kd-tree height exceeds the traversal stack of the CUDA search");
   const KnnLaunch L = make_launch<T, D>(c, a, order);
   const int grid = ceil_div(a.nq, 128);
   const bool small = c.height <= kStackSmall;
-  const bool packet = a.traversal == 2;
+  const bool packet = a.traversal == 2 && K > 0;
   if (packet && (a.eps != 0.0 || L.stats))
     return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
   if (a.evStart) cudaEventRecord(a.evStart, stream);
+  if (K < 0) {
+    const int rc = launch_wide_kdtree<T, D>(L, a.k, c.height, stream);
+    if (a.evStop) cudaEventRecord(a.evStop, stream);
+    if (rc != kOk) return rc;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree_wide launch");
+    return kOk;
+  }
 #define NABO_LAUNCH(KK)                                                            \
   case KK:                                                                         \
     if (packet) {                                                                  \
@@ -200,7 +281,7 @@ template <typename T, int D>
 int knn_batch(const BatchArgs& b, cudaStream_t stream) {
   if (b.nq == 0) return kOk;
   const int K = round_k(b.kMax);
-  if (K < 0) return set_error(kErrUnsupported, "k larger than 32 is not supported by the CUDA search types");
+  if (K < 0 && b.kMax > kMaxWideK) return k_unsupported();
   NABO_CUDA_TRY(cudaMemsetAsync(b.hist, 0, (size_t)b.nodeCap * sizeof(uint32_t), stream));
   k_leaf_cells<T, D><<<ceil_div(b.nq, 256), 256, 0, stream>>>(static_cast<const Node<T>*>(b.nodes),
                                                               static_cast<const T*>(b.query), b.nq, b.qStride, b.dim,
@@ -234,11 +315,15 @@ int knn_batch(const BatchArgs& b, cudaStream_t stream) {
   L.recs32 = b.recs32;
   L.coordMax = b.coordMax;
   const int grid = ceil_div(b.nq, b.blockSize);
+  if (K < 0) {  // some cloud wants more than kMaxK: the whole batch runs one warp per query
+    rc = launch_wide_kdtree<T, D>(L, b.kMax, kStackLarge, stream);  // taller trees are flagged by the build
+    if (rc != kOk) return rc;
+  }
 #define NABO_LAUNCH(KK)                                                                     \
   case KK:                                                                                  \
     launch_kdtree<T, D, KK, kStackLarge>(grid, b.blockSize, stream, L);               \
     break;
-  switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+  if (K > 0) switch (K) { NABO_K_LIST(NABO_LAUNCH) }
 #undef NABO_LAUNCH
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "batched search launch");

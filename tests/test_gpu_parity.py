@@ -211,8 +211,8 @@ def test_search_errors_match_reference_messages():
         assert str(eg.value) == str(eo.value)
     with pytest.raises(nb.NaboError, match="Query has less dimensions"):
         s.knn(cloud[:, :2], 2)
-    with pytest.raises(nb.NaboError, match="k larger than 32"):
-        nb.NearestNeighbourSearch(rng.random((100, 3)).astype(np.float32)).knn(cloud, 33)
+    with pytest.raises(nb.NaboError, match="k larger than 1024"):
+        nb.NearestNeighbourSearch(rng.random((2000, 3)).astype(np.float32)).knn(cloud, 1025)
 
 
 def test_device_api_matches_host_api():
