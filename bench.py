@@ -47,7 +47,7 @@ def parse():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=["lidar", "uniform", "c0", "batched", "c4", "bf"], default="lidar",
+    p.add_argument("--workload", choices=["lidar", "uniform", "c0", "batched", "c4", "bf", "latency"], default="lidar",
                    help="batched: 512 uneven 3-D clouds built and searched per step (one CUDA graph); "
                         "c4: 128 8-D clouds (half f32, half f64), k=32, epsilon 0 and 0.5")
     p.add_argument("--c4-clouds", type=int, default=128, help="clouds of the c4 workload (a prefix of the 128)")
@@ -828,6 +828,71 @@ def run_bf(args):
     print(json.dumps(res))
 
 
+def run_latency(args):
+    """Per-call latency of the host-buffer API (the reference's knn on host
+    matrices, nabo/nabo.h:338, and its single-point form, nabo/nabo.h:325)
+    for batches of 1 to 65,536 lidar queries, k=10, r = 1 m; the oracle
+    (the reference algorithm, all host threads) timed the same way."""
+    import libnabo_gb300 as nb
+    from libnabo_gb300 import synthetic as S
+    from oracle import oracle as O
+
+    cloud = S.lidar_scan()
+    q = S.lidar_queries(cloud)
+    k, r = 10, 1.0
+    import torch
+    s = nb.NearestNeighbourSearch(cloud)
+    sp = nb.NearestNeighbourSearch(cloud)  # device API with the kernel bracketed by events
+    sp.profile(True)
+    orc = O.OracleTree(cloud)
+    sizes = [1, 16, 256, 4096, 65536]
+    rows = {}
+    with ClockSampler(0) as clk:
+        for n in sizes:
+            qq = np.ascontiguousarray(q[:n])
+            tq = torch.from_numpy(qq).cuda()
+            kms = []
+            for i in range(25):
+                sp.knn_device(tq, k, 0.0, 0, r)
+                if i >= 5:
+                    kms.append(sp.last_kernel_ms())
+            reps = max(20, min(2000, 400_000 // n))
+            for _ in range(max(args.warmup, 5)):
+                gi, gd = s.knn(qq, k, 0.0, 0, r)
+            t = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                s.knn(qq, k, 0.0, 0, r)
+                t.append(time.perf_counter() - t0)
+            oi, od, _ = orc.knn(qq, k, 0.0, 0, r, mode=O.MODE_CANONICAL)
+            tc = []
+            for _ in range(min(reps, 200)):
+                t0 = time.perf_counter()
+                orc.knn(qq, k, 0.0, 0, r, mode=O.MODE_CANONICAL)
+                tc.append(time.perf_counter() - t0)
+            g_us = statistics.median(t) * 1e6
+            c_us = statistics.median(tc) * 1e6
+            rows[str(n)] = {"gpu_us_per_call": g_us, "gpu_queries_per_s": n / (g_us * 1e-6),
+                            "search_kernel_us": statistics.median(kms) * 1e3,
+                            "cpu_us_per_call": c_us, "cpu_queries_per_s": n / (c_us * 1e-6),
+                            "calls_timed": reps,
+                            "identical": bool(np.array_equal(gi, oi) and np.array_equal(gd, od))}
+    one = rows["1"]
+    res = {
+        "metric": "host-API kNN call latency, one query (lidar 1.15M points, k=10)", "value": one["gpu_us_per_call"],
+        "unit": "us", "n_gpus": 1, "steps": None, "warmup": max(args.warmup, 5), "ms_per_step": one["gpu_us_per_call"] / 1e3,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "latency_lidar64_k10", "points": int(cloud.shape[0]), "k": k, "maxRadius": r,
+                   "timing": "median wall time of the Python call (ctypes) from host arrays to host arrays, "
+                             "both arms; the GPU arm includes the copies and the stream synchronisation"},
+        "sizes": rows,
+        "cpu_baseline": {"value": one["cpu_us_per_call"], "unit": "us", "cores": O.num_threads(), "kind": "port",
+                         "sample": "the same calls on the oracle"},
+        "clocks": clk.summary(), "gpu_launches": 1,
+    }
+    print(json.dumps(res))
+
+
 def run_batched_reference(args):
     """The reference algorithm (oracle restatement, all host threads) on a
     sample of the batched workload's clouds; rank 0 only."""
@@ -871,6 +936,9 @@ def main():
         return
     if args.workload == "bf":
         run_bf(args)
+        return
+    if args.workload == "latency":
+        run_latency(args)
         return
     if args.workload == "batched":
         if args.impl == "reference":

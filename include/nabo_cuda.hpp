@@ -10,9 +10,9 @@
 // Nabo::runtime_error (nabo/nabo.cpp:50-66).
 //
 // Matrices are column-major, one point per column, as the reference's Eigen
-// matrices: any type with rows(), cols() and data() works, so Eigen::MatrixXf
-// / MatrixXi / VectorXf instantiate it directly; DenseMatrix below serves
-// callers without Eigen. The cloud is copied to the GPU at creation; the
+// matrices: any type with rows(), cols() and data() works (vectors also need
+// resize()), so Eigen::MatrixXf / MatrixXi / VectorXf / VectorXi instantiate
+// it directly; DenseMatrix and DenseVector below serve callers without Eigen. The cloud is copied to the GPU at creation; the
 // object keeps a reference to the caller's cloud for the `cloud` member, as
 // the reference does (nabo/nabo.h:273-274).
 #pragma once
@@ -54,6 +54,27 @@ class DenseMatrix {
   std::vector<S> v_;
 };
 
+// Column vector for callers without Eigen (the reference's Vector and
+// IndexVector, nabo/nabo.h:263-269).
+template <typename S>
+class DenseVector {
+ public:
+  using Scalar = S;
+  DenseVector() = default;
+  explicit DenseVector(long n) : v_((size_t)n) {}
+  long rows() const { return (long)v_.size(); }
+  long cols() const { return 1; }
+  long size() const { return (long)v_.size(); }
+  void resize(long n) { v_.resize((size_t)n); }
+  S* data() { return v_.data(); }
+  const S* data() const { return v_.data(); }
+  S& operator()(long i) { return v_[(size_t)i]; }
+  const S& operator()(long i) const { return v_[(size_t)i]; }
+
+ private:
+  std::vector<S> v_;
+};
+
 namespace detail {
 template <typename T>
 constexpr int dtype() {
@@ -66,12 +87,13 @@ inline void check(int rc) {
 }  // namespace detail
 
 template <typename T, typename CloudType = DenseMatrix<T>, typename IndexMatrixType = DenseMatrix<int>,
-          typename VectorType = DenseMatrix<T>>
+          typename VectorType = DenseVector<T>, typename IndexVectorType = DenseVector<int>>
 class NearestNeighbourSearch {
  public:
   using Matrix = CloudType;
   using IndexMatrix = IndexMatrixType;
   using Vector = VectorType;
+  using IndexVector = IndexVectorType;
   using Index = long;
 
   // Values of the reference's enums (nabo/nabo.h:290-312), extended by the
@@ -132,6 +154,19 @@ class NearestNeighbourSearch {
                     T maxRadius = std::numeric_limits<T>::infinity()) const {
     return run(query, indices, dists2, nullptr, 0, k, epsilon, optionFlags, maxRadius);
   }
+  // nabo/nabo.h:325 (nabo/nabo.cpp:82-100): one query point; the first dim
+  // entries of `query` are used, indices and dists2 are resized to k.
+  unsigned long knn(const Vector& query, IndexVector& indices, Vector& dists2, Index k = 1, T epsilon = 0,
+                    unsigned optionFlags = 0, T maxRadius = std::numeric_limits<T>::infinity()) const {
+    if ((Index)(query.rows() * query.cols()) < dim)
+      throw runtime_error("Query has less dimensions (" + std::to_string((long)(query.rows() * query.cols())) +
+                          ") than requested for cloud (" + std::to_string(dim) + ")");
+    if (k < 0) throw runtime_error("k must be at least 1");
+    indices.resize(k);
+    dists2.resize(k);
+    return run_raw(query.data(), (long)dim, 1, (long)dim, indices.data(), (long)k, 1, dists2.data(), (long)k, 1,
+                   nullptr, 0, k, epsilon, optionFlags, maxRadius);
+  }
   // nabo/nabo.h:351: one radius per query column.
   unsigned long knn(const Matrix& query, IndexMatrix& indices, Matrix& dists2, const Vector& maxRadii,
                     Index k = 1, T epsilon = 0, unsigned optionFlags = 0) const {
@@ -155,9 +190,17 @@ class NearestNeighbourSearch {
 
   unsigned long run(const Matrix& query, IndexMatrix& indices, Matrix& dists2, const T* radii, long nRadii,
                     Index k, T epsilon, unsigned optionFlags, T maxRadius) const {
-    // the reference's checkSizesKnn (nabo/nabo.cpp:102-131), in its order
-    // and with its messages (which print rows() in the column messages and k
-    // in the radii message); the library repeats the checks it can make
+    return run_raw(query.data(), (long)query.rows(), (long)query.cols(), (long)query.rows(), indices.data(),
+                   (long)indices.rows(), (long)indices.cols(), dists2.data(), (long)dists2.rows(),
+                   (long)dists2.cols(), radii, nRadii, k, epsilon, optionFlags, maxRadius);
+  }
+
+  // the reference's checkSizesKnn (nabo/nabo.cpp:102-131), in its order and
+  // with its messages (which print rows() in the column messages and k in
+  // the radii message); the library repeats the checks it can make
+  unsigned long run_raw(const T* qData, long qRows, long qCols, long qStride, int* iData, long iRows, long iCols,
+                        T* dData, long dRows, long dCols, const T* radii, long nRadii, Index k, T epsilon,
+                        unsigned optionFlags, T maxRadius) const {
     using std::to_string;
     const long n = (long)cloud.cols();
     if (optionFlags & ALLOW_SELF_MATCH) {
@@ -168,22 +211,22 @@ class NearestNeighbourSearch {
       throw runtime_error("Requesting more points (" + to_string(k) + ") than available in cloud minus 1 (" +
                           to_string(n - 1) + ") (as self match is forbidden)");
     }
-    if ((Index)query.rows() < dim)
-      throw runtime_error("Query has less dimensions (" + to_string((long)query.rows()) +
-                          ") than requested for cloud (" + to_string(dim) + ")");
-    if ((Index)indices.rows() != k)
-      throw runtime_error("Index matrix has a different number of rows (" + to_string((long)indices.rows()) +
-                          ") than k (" + to_string(k) + ")");
-    if (indices.cols() != query.cols())
-      throw runtime_error("Index matrix has a different number of columns (" + to_string((long)indices.rows()) +
-                          ") than query (" + to_string((long)query.cols()) + ")");
-    if ((Index)dists2.rows() != k)
-      throw runtime_error("Distance matrix has a different number of rows (" + to_string((long)dists2.rows()) +
-                          ") than k (" + to_string(k) + ")");
-    if (dists2.cols() != query.cols())
-      throw runtime_error("Distance matrix has a different number of columns (" +
-                          to_string((long)dists2.rows()) + ") than query (" + to_string((long)query.cols()) + ")");
-    if (radii && nRadii != (long)query.cols())
+    if ((Index)qRows < dim)
+      throw runtime_error("Query has less dimensions (" + to_string(qRows) + ") than requested for cloud (" +
+                          to_string(dim) + ")");
+    if ((Index)iRows != k)
+      throw runtime_error("Index matrix has a different number of rows (" + to_string(iRows) + ") than k (" +
+                          to_string(k) + ")");
+    if (iCols != qCols)
+      throw runtime_error("Index matrix has a different number of columns (" + to_string(iRows) +
+                          ") than query (" + to_string(qCols) + ")");
+    if ((Index)dRows != k)
+      throw runtime_error("Distance matrix has a different number of rows (" + to_string(dRows) + ") than k (" +
+                          to_string(k) + ")");
+    if (dCols != qCols)
+      throw runtime_error("Distance matrix has a different number of columns (" + to_string(dRows) +
+                          ") than query (" + to_string(qCols) + ")");
+    if (radii && nRadii != qCols)
       throw runtime_error("Maximum radii vector has not the same length (" + to_string(nRadii) +
                           ") than query has columns (" + to_string(k) + ")");
     const unsigned maxFlags = ALLOW_SELF_MATCH | SORT_RESULTS;
@@ -191,9 +234,8 @@ class NearestNeighbourSearch {
       throw runtime_error("OR-ed value of option flags (" + to_string(optionFlags) +
                           ") is larger than maximal valid value (" + to_string(maxFlags) + ")");
     uint64_t touched = 0;
-    detail::check(nabo_cuda_knn(h_, query.data(), (int)query.rows(), (int64_t)query.cols(),
-                                (int64_t)query.rows(), (int)k, (double)epsilon, optionFlags, (double)maxRadius,
-                                radii, indices.data(), dists2.data(), &touched));
+    detail::check(nabo_cuda_knn(h_, qData, (int)qRows, (int64_t)qCols, (int64_t)qStride, (int)k, (double)epsilon,
+                                optionFlags, (double)maxRadius, radii, iData, dData, &touched));
     return (creationOptionFlags & TOUCH_STATISTICS) ? (unsigned long)touched : 0ul;
   }
 

@@ -99,6 +99,13 @@ struct nabo_cuda_search {
   double maxBound[kMaxDim];
   cudaEvent_t evStart = nullptr;  // profiling: bracket the search kernel
   cudaEvent_t evStop = nullptr;
+  // Staging for small host-buffer calls: one pinned host block and one
+  // device block with the same layout, so a call is one upload, the search
+  // and one download. Taken with try_lock; a concurrent call on the same
+  // object uses the general path instead.
+  mutable std::mutex stageLock;
+  mutable void* stageHost = nullptr;
+  mutable void* stageDev = nullptr;
 };
 
 namespace {
@@ -231,6 +238,12 @@ void free_events(nabo_cuda_search* s) {
   if (s->evStart) cudaEventDestroy(s->evStart);
   if (s->evStop) cudaEventDestroy(s->evStop);
   s->evStart = s->evStop = nullptr;
+}
+
+void free_stage(nabo_cuda_search* s) {
+  if (s->stageHost) cudaFreeHost(s->stageHost);
+  if (s->stageDev) cudaFree(s->stageDev);
+  s->stageHost = s->stageDev = nullptr;
 }
 
 void free_cloud(DeviceCloud& c) {
@@ -444,10 +457,107 @@ int nabo_cuda_destroy(nabo_cuda_search* s) {
   if (!s) return kOk;
   DeviceGuard g(s->device);
   free_events(s);
+  free_stage(s);
   free_cloud(s->c);
   delete s;
   return kOk;
 }
+
+}  // extern "C"
+
+namespace {
+
+constexpr size_t kStageBytes = size_t(4) << 20;
+
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+void knn_args_common(const nabo_cuda_search* s, KnnArgs& a, int64_t nq, int k, double epsilon, unsigned optionFlags,
+                     double maxRadius) {
+  a.nq = nq;
+  a.k = k;
+  a.eps = epsilon;
+  a.optionFlags = optionFlags;
+  a.touchStats = (s->creationFlags & NABO_TOUCH_STATISTICS) != 0;
+  a.maxRadius = maxRadius;
+  a.sortQueries = s->queryOrdering != 0;
+  a.traversal = s->traversal;
+}
+
+uint64_t touched_result(const nabo_cuda_search* s, int64_t nq, unsigned long long counted) {
+  if (!(s->creationFlags & NABO_TOUCH_STATISTICS)) return 0;
+  if (s->searchType == NABO_SEARCH_BRUTE_FORCE_CUDA) return (uint64_t)nq * (uint64_t)s->c.n;  // nabo/brute_force_cpu.cpp:99-100
+  return counted;
+}
+
+// The host-buffer search through the object's staging blocks, laid out as
+// [query (packed columns) | radii | touched | indices | dists2]: the upload
+// covers query..touched (touched uploaded as 0), the download
+// touched..dists2. Returns -1 when the call does not fit or the staging is
+// in use by another thread.
+int knn_staged(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride, int k,
+               double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii, int32_t* indices,
+               void* dists2, uint64_t* touched) {
+  const size_t es = s->c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  const size_t outN = (size_t)nq * (size_t)k;
+  const size_t rowBytes = (size_t)qRows * es;
+  const size_t offRadii = align16((size_t)nq * rowBytes);
+  const size_t offTouched = align16(offRadii + (maxRadii ? (size_t)nq * es : 0));
+  const size_t offIdx = offTouched + 16;
+  const size_t offD2 = align16(offIdx + outN * sizeof(int32_t));
+  const size_t total = align16(offD2 + outN * es);
+  if (total > kStageBytes) return -1;
+  std::unique_lock<std::mutex> lock(s->stageLock, std::try_to_lock);
+  if (!lock.owns_lock()) return -1;
+  cudaError_t e = cudaSuccess;
+  if (!s->stageHost) {
+    e = cudaMallocHost(&s->stageHost, kStageBytes);
+    if (e == cudaSuccess) e = cudaMalloc(&s->stageDev, kStageBytes);
+    if (e != cudaSuccess) {
+      free_stage(const_cast<nabo_cuda_search*>(s));
+      return cuda_error(e, "knn staging buffers");
+    }
+  }
+  unsigned char* h = static_cast<unsigned char*>(s->stageHost);
+  unsigned char* d = static_cast<unsigned char*>(s->stageDev);
+  const unsigned char* q = static_cast<const unsigned char*>(query);
+  if (qStride == qRows)
+    std::memcpy(h, q, (size_t)nq * rowBytes);
+  else
+    for (int64_t i = 0; i < nq; ++i) std::memcpy(h + (size_t)i * rowBytes, q + (size_t)i * qStride * es, rowBytes);
+  if (maxRadii) std::memcpy(h + offRadii, maxRadii, (size_t)nq * es);
+  std::memset(h + offTouched, 0, 16);
+  cudaStream_t st = cudaStreamPerThread;
+  e = cudaMemcpyAsync(d, h, offTouched + 16, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return cuda_error(e, "knn upload");
+  KnnArgs a;
+  knn_args_common(s, a, nq, k, epsilon, optionFlags, maxRadius);
+  a.query = d;
+  a.qStride = qRows;
+  a.maxRadii = maxRadii ? d + offRadii : nullptr;
+  a.indices = reinterpret_cast<int32_t*>(d + offIdx);
+  a.dists2 = d + offD2;
+  a.touched = reinterpret_cast<unsigned long long*>(d + offTouched);
+  int rc = knn_any(s, a, st);
+  if (rc == kOk) {
+    e = cudaMemcpyAsync(h + offTouched, d + offTouched, total - offTouched, cudaMemcpyDeviceToHost, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "knn download");
+  }
+  e = cudaStreamSynchronize(st);
+  if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, "knn");
+  if (rc != kOk) return rc;
+  std::memcpy(indices, h + offIdx, outN * sizeof(int32_t));
+  std::memcpy(dists2, h + offD2, outN * es);
+  if (touched) {
+    unsigned long long ht;
+    std::memcpy(&ht, h + offTouched, sizeof(ht));
+    *touched = touched_result(s, nq, ht);
+  }
+  return kOk;
+}
+
+}  // namespace
+
+extern "C" {
 
 int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride, int k,
                   double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii, int32_t* indices,
@@ -460,6 +570,10 @@ int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64
   if (!query || !indices || !dists2) return set_error(kErrArgument, "NULL query or result buffer");
   DeviceGuard g(s->device);
   if (!g.ok) return cuda_error(cudaGetLastError(), "cudaSetDevice");
+  rc = knn_staged(s, query, qRows, nq, qStride, k, epsilon, optionFlags, maxRadius, maxRadii, indices, dists2,
+                  touched);
+  if (rc != -1) return rc;
+  rc = kOk;
   cudaStream_t st = cudaStreamPerThread;
   const size_t es = s->c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
   const size_t qBytes = (size_t)((nq - 1) * qStride + qRows) * es;
@@ -478,20 +592,13 @@ int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64
   if (e != cudaSuccess) rc = cuda_error(e, "knn setup");
   if (rc == kOk) {
     KnnArgs a;
+    knn_args_common(s, a, nq, k, epsilon, optionFlags, maxRadius);
     a.query = dq;
-    a.nq = nq;
     a.qStride = qStride;
-    a.k = k;
-    a.eps = epsilon;
-    a.optionFlags = optionFlags;
-    a.touchStats = (s->creationFlags & NABO_TOUCH_STATISTICS) != 0;
-    a.maxRadius = maxRadius;
     a.maxRadii = dr;
     a.indices = di;
     a.dists2 = dd;
     a.touched = dt;
-    a.sortQueries = s->queryOrdering != 0;
-    a.traversal = s->traversal;
     rc = knn_any(s, a, st);
   }
   unsigned long long ht = 0;
@@ -508,14 +615,7 @@ int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64
   if (dt) scratch_free(dt, st);
   e = cudaStreamSynchronize(st);
   if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, "knn");
-  if (rc == kOk && touched) {
-    if (!(s->creationFlags & NABO_TOUCH_STATISTICS))
-      *touched = 0;
-    else if (s->searchType == NABO_SEARCH_BRUTE_FORCE_CUDA)
-      *touched = (uint64_t)nq * (uint64_t)s->c.n;  // nabo/brute_force_cpu.cpp:99-100
-    else
-      *touched = ht;
-  }
+  if (rc == kOk && touched) *touched = touched_result(s, nq, ht);
   return rc;
 }
 

@@ -55,7 +55,8 @@ template <typename T>
 static int search_type(const std::vector<float>& c, const std::vector<float>& q, const std::vector<float>& r, int n,
                        int nq, int k, int dim, FILE* out) {
   using NNS = nabo_cuda::NearestNeighbourSearch<T>;
-  M<T> cloud(dim, n), query(dim, nq), radii(nq, 1);
+  M<T> cloud(dim, n), query(dim, nq);
+  nabo_cuda::DenseVector<T> radii(nq);
   for (long i = 0; i < cloud.size(); ++i) cloud(i) = (T)c[(size_t)i];
   for (long i = 0; i < query.size(); ++i) query(i) = (T)q[(size_t)i];
   for (long i = 0; i < nq; ++i) radii(i) = (T)r[(size_t)i];
@@ -70,8 +71,23 @@ static int search_type(const std::vector<float>& c, const std::vector<float>& q,
   std::fwrite(d22.data(), sizeof(T), (size_t)d22.size(), out);
   const uint64_t t64 = touched;
   std::fwrite(&t64, 8, 1, out);
-  // knn() argument checks on a live object, in the reference's order
+  // the single-point overload (nabo/nabo.h:325) against the matrix call's columns
   int bad = 0;
+  {
+    nabo_cuda::DenseVector<T> qv(dim + 1), dv;  // a longer vector: only the first dim entries count
+    nabo_cuda::DenseVector<int> iv;
+    int diff = 0;
+    for (int j = 0; j < nq && j < 40; ++j) {
+      for (int d = 0; d < dim; ++d) qv(d) = query(d, j);
+      qv(dim) = (T)1e30;
+      s->knn(qv, iv, dv, k, 0, 0, (T)1.0);
+      if (iv.size() != k || dv.size() != k) ++diff;
+      for (int r = 0; r < k && r < iv.size(); ++r) diff += (iv(r) != idx(r, j) || dv(r) != d2(r, j)) ? 1 : 0;
+    }
+    std::printf("%s single-vector knn: %d differences\n", diff ? "FAIL" : "ok", diff);
+    bad += diff ? 1 : 0;
+  }
+  // knn() argument checks on a live object, in the reference's order
   auto must = [&](const char* what, const std::string& needle, auto fn) {
     try {
       fn();
@@ -84,7 +100,8 @@ static int search_type(const std::vector<float>& c, const std::vector<float>& q,
     }
   };
   M<int> wrongRows(k + 1, nq);
-  M<T> wrongCols(k, nq + 1), shortRadii(nq - 1, 1), fewDims(dim - 1, nq);
+  M<T> wrongCols(k, nq + 1), fewDims(dim - 1, nq);
+  nabo_cuda::DenseVector<T> shortRadii(nq - 1);
   must("k too large", "than available in cloud minus 1", [&] { s->knn(query, idx, d2, (long)n, 0, 0); });
   must("query dims", "Query has less dimensions", [&] { s->knn(fewDims, idx, d2, k); });
   must("index rows", "Index matrix has a different number of rows", [&] { s->knn(query, wrongRows, d2, k); });
