@@ -76,7 +76,12 @@ typedef struct nabo_cuda_params {
                              and k <= 32 (larger k use the reference order) */
   int32_t threadsPerBlock; /* batched search kernel block size: 32, 64 or 128
                               (0 = 128); chosen by the autotuner */
-  int32_t reserved[3];
+  int32_t pipelineChunks;  /* host-buffer searches of 2^18 queries or more
+                              with page-locked result buffers: searched in
+                              this many chunks whose downloads overlap the
+                              next chunk's search (0 = default, 1 = one
+                              search then one download; at most 64) */
+  int32_t reserved[2];
 } nabo_cuda_params;
 
 typedef struct nabo_cuda_search nabo_cuda_search; /* opaque */

@@ -139,6 +139,8 @@ class NearestNeighbourSearch:
                 p.queryOrdering = int(val)
             elif key == "traversal":
                 p.traversal = int(val)
+            elif key == "pipelineChunks":
+                p.pipelineChunks = int(val)
             else:
                 raise NaboError(1, f"unknown parameter {key!r}")
         self.searchType = int(searchType)

@@ -75,7 +75,8 @@ class nabo_cuda_params(ctypes.Structure):
         ("queryOrdering", ctypes.c_int32),
         ("traversal", ctypes.c_int32),
         ("threadsPerBlock", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 3),
+        ("pipelineChunks", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
 

@@ -87,6 +87,10 @@ int cuda_error(cudaError_t e, const char* what) {
 
 using namespace nabo_gb300;
 
+namespace nabo_gb300 {
+constexpr int kPipelineMaxChunks = 64;  // nabo_cuda_params::pipelineChunks
+}  // namespace nabo_gb300
+
 struct nabo_cuda_search {
   DeviceCloud c;
   int searchType = 0;
@@ -95,6 +99,7 @@ struct nabo_cuda_search {
   int device = 0;
   int queryOrdering = 1;
   int traversal = 0;
+  int pipelineChunks = 0;
   double minBound[kMaxDim];
   double maxBound[kMaxDim];
   cudaEvent_t evStart = nullptr;  // profiling: bracket the search kernel
@@ -234,6 +239,15 @@ int knn_any(const nabo_cuda_search* h, const KnnArgs& a, cudaStream_t st) {
   NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_bruteforce<T, D>(h->c, a, st)));
 }
 
+int knn_given_order_any(const nabo_cuda_search* h, const KnnArgs& a, const int32_t* order, cudaStream_t st) {
+  NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_kdtree_given_order<T, D>(h->c, a, order, st)));
+}
+
+int chunk_order_any(const nabo_cuda_search* h, const void* query, int64_t nq, int64_t qStride, int64_t chunk,
+                    int32_t* order, cudaStream_t st) {
+  NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_chunk_order<T, D>(h->c, query, nq, qStride, chunk, order, st)));
+}
+
 void free_events(nabo_cuda_search* s) {
   if (s->evStart) cudaEventDestroy(s->evStart);
   if (s->evStop) cudaEventDestroy(s->evStop);
@@ -268,7 +282,10 @@ int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int6
     p.bucketSize = params->bucketSize;
     p.queryOrdering = params->queryOrdering;
     p.traversal = params->traversal;
+    p.pipelineChunks = params->pipelineChunks;
   }
+  if (p.pipelineChunks < 0 || p.pipelineChunks > kPipelineMaxChunks)
+    return set_error(kErrArgument, "pipelineChunks must be between 0 and 64");
   // NearestNeighbourSearch::create (nabo/nabo.cpp:137-138)
   if (dimIn <= 0) return set_error(kErrArgument, "Your space must have at least one dimension");
   if (searchType < 0 || searchType >= NABO_SEARCH_TYPE_COUNT) return set_error(kErrArgument, "Unknown search type");
@@ -313,6 +330,7 @@ int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int6
   h->rows = rows;
   h->queryOrdering = p.queryOrdering;
   h->traversal = p.traversal;
+  h->pipelineChunks = p.pipelineChunks;
   if (p.traversal < 0 || p.traversal > 2) {
     delete h;
     return set_error(kErrArgument, "traversal must be 0, 1 or 2");
@@ -555,6 +573,131 @@ int knn_staged(const nabo_cuda_search* s, const void* query, int qRows, int64_t 
   return kOk;
 }
 
+bool is_pinned(const void* p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeHost;
+}
+
+// Large host-buffer searches whose result buffers are pinned: the queries
+// are uploaded and ordered once, then searched in pipelineChunks
+// consecutive chunks, one launch each on alternating streams, and a copy
+// stream downloads each chunk's result rows as soon as its search is done,
+// while the next chunk searches. With query ordering the order is
+// chunk-major (each chunk's queries along the Morton curve), so a chunk's
+// launch covers a contiguous part of one order. Results are those of one
+// call: each query's result goes to its own column and the touched counter
+// sums over the chunks. Returns -1 when the call is too small, a result
+// buffer is not pinned, or the cloud has more than 3 dimensions with
+// query ordering on.
+constexpr int64_t kPipelineMin = int64_t(1) << 18;
+constexpr int kPipelineChunks = 4;  // default
+
+int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride, int k,
+                  double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii, int32_t* indices,
+                  void* dists2, uint64_t* touched) {
+  const int nChunks = s->pipelineChunks > 0 ? s->pipelineChunks : kPipelineChunks;
+  if (nq < kPipelineMin || nChunks < 2) return -1;
+  if (!is_pinned(indices) || !is_pinned(dists2)) return -1;
+  const bool ordered = s->searchType == NABO_SEARCH_KDTREE_CUDA && s->queryOrdering != 0;
+  if (ordered && s->c.dim > 3) return -1;
+  const size_t es = s->c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  const size_t qBytes = (size_t)((nq - 1) * qStride + qRows) * es;
+  const size_t outN = (size_t)nq * (size_t)k;
+  const int64_t chunk = (nq + nChunks - 1) / nChunks;
+  cudaStream_t main = cudaStreamPerThread;
+  cudaStream_t comp[2] = {}, copy = nullptr;
+  cudaEvent_t ready = nullptr, copied = nullptr, searched[kPipelineMaxChunks] = {}, compDone[2] = {};
+  unsigned char *dq = nullptr, *dr = nullptr, *dd = nullptr;
+  int32_t *di = nullptr, *order = nullptr;
+  unsigned long long* dt = nullptr;
+  int rc = kOk;
+  cudaError_t e = cudaStreamCreateWithFlags(&copy, cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&comp[i], cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&compDone[i], cudaEventDisableTiming);
+  for (int i = 0; i < nChunks && e == cudaSuccess; ++i)
+    e = cudaEventCreateWithFlags(&searched[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&dq, qBytes, main);
+  if (e == cudaSuccess && maxRadii) e = scratch_alloc((void**)&dr, (size_t)nq * es, main);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&di, outN * sizeof(int32_t), main);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&dd, outN * es, main);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&dt, sizeof(unsigned long long), main);
+  if (e == cudaSuccess && ordered) e = scratch_alloc((void**)&order, (size_t)nq * sizeof(int32_t), main);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dq, query, qBytes, cudaMemcpyHostToDevice, main);
+  if (e == cudaSuccess && maxRadii) e = cudaMemcpyAsync(dr, maxRadii, (size_t)nq * es, cudaMemcpyHostToDevice, main);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dt, 0, sizeof(unsigned long long), main);
+  if (e != cudaSuccess) rc = cuda_error(e, "knn pipeline setup");
+  if (rc == kOk && ordered) rc = chunk_order_any(s, dq, nq, qStride, chunk, order, main);
+  if (rc == kOk && cudaEventRecord(ready, main) != cudaSuccess) rc = cuda_error(cudaGetLastError(), "knn pipeline");
+  for (int c = 0; c < nChunks && rc == kOk; ++c) {
+    const int64_t c0 = std::min<int64_t>(nq, chunk * c), c1 = std::min<int64_t>(nq, chunk * (c + 1));
+    const int64_t m = c1 - c0;
+    if (m <= 0) break;
+    cudaStream_t cs = comp[c & 1];
+    e = cudaStreamWaitEvent(cs, ready, 0);
+    if (e != cudaSuccess) {
+      rc = cuda_error(e, "knn pipeline");
+      break;
+    }
+    KnnArgs a;
+    knn_args_common(s, a, m, k, epsilon, optionFlags, maxRadius);
+    a.touched = dt;
+    a.qStride = qStride;
+    if (ordered) {  // the chunk's part of the order holds global query indices
+      a.query = dq;
+      a.maxRadii = dr;
+      a.indices = di;
+      a.dists2 = dd;
+      rc = knn_given_order_any(s, a, order + c0, cs);
+    } else {
+      a.query = dq + (size_t)c0 * qStride * es;
+      a.maxRadii = maxRadii ? dr + (size_t)c0 * es : nullptr;
+      a.indices = di + (size_t)c0 * k;
+      a.dists2 = dd + (size_t)c0 * k * es;
+      rc = knn_any(s, a, cs);
+    }
+    if (rc != kOk) break;
+    e = cudaEventRecord(searched[c], cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(copy, searched[c], 0);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(indices + (size_t)c0 * k, di + (size_t)c0 * k, (size_t)m * k * sizeof(int32_t),
+                          cudaMemcpyDeviceToHost, copy);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(static_cast<unsigned char*>(dists2) + (size_t)c0 * k * es, dd + (size_t)c0 * k * es,
+                          (size_t)m * k * es, cudaMemcpyDeviceToHost, copy);
+    if (e != cudaSuccess) rc = cuda_error(e, "knn chunk download");
+  }
+  // the main stream waits for the compute and copy streams before the frees
+  for (int i = 0; i < 2; ++i)
+    if (comp[i] && cudaEventRecord(compDone[i], comp[i]) == cudaSuccess) cudaStreamWaitEvent(main, compDone[i], 0);
+  if (copy && cudaEventRecord(copied, copy) == cudaSuccess) cudaStreamWaitEvent(main, copied, 0);
+  unsigned long long ht = 0;
+  if (rc == kOk) {
+    e = cudaMemcpyAsync(&ht, dt, sizeof(ht), cudaMemcpyDeviceToHost, main);
+    if (e != cudaSuccess) rc = cuda_error(e, "knn touched count");
+  }
+  for (void* p : {(void*)dq, (void*)dr, (void*)di, (void*)dd, (void*)dt, (void*)order})
+    if (p) scratch_free(p, main);
+  e = cudaStreamSynchronize(main);
+  if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, "knn");
+  for (int i = 0; i < 2; ++i) {
+    if (comp[i]) cudaStreamDestroy(comp[i]);
+    if (compDone[i]) cudaEventDestroy(compDone[i]);
+  }
+  for (int i = 0; i < nChunks; ++i)
+    if (searched[i]) cudaEventDestroy(searched[i]);
+  if (copy) cudaStreamDestroy(copy);
+  if (ready) cudaEventDestroy(ready);
+  if (copied) cudaEventDestroy(copied);
+  if (rc == kOk && touched) *touched = touched_result(s, nq, ht);
+  return rc;
+}
+
 }  // namespace
 
 extern "C" {
@@ -572,6 +715,9 @@ int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64
   if (!g.ok) return cuda_error(cudaGetLastError(), "cudaSetDevice");
   rc = knn_staged(s, query, qRows, nq, qStride, k, epsilon, optionFlags, maxRadius, maxRadii, indices, dists2,
                   touched);
+  if (rc != -1) return rc;
+  rc = knn_pipelined(s, query, qRows, nq, qStride, k, epsilon, optionFlags, maxRadius, maxRadii, indices, dists2,
+                     touched);
   if (rc != -1) return rc;
   rc = kOk;
   cudaStream_t st = cudaStreamPerThread;

@@ -170,6 +170,9 @@ int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream);
 template <typename T, int D>
 int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream);
 template <typename T, int D>
+int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int64_t chunk,
+                    int32_t* order, cudaStream_t stream);
+template <typename T, int D>
 int knn_leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int32_t* order,
                    cudaStream_t stream);
 
@@ -207,10 +210,14 @@ int radius_model_set(RadiusModel& m, const float* params, const float* meta);
 const void* radius_model_owner(const RadiusModel& m);
 int radius_model_k(const RadiusModel& m);
 
-// Query ordering: writes a permutation of [0, nq) grouping nearby queries.
+// Query ordering: writes a permutation of [0, nq) grouping nearby queries
+// (a stable sort by Morton code). With chunk > 0 the permutation is
+// chunk-major: the queries [c*chunk, (c+1)*chunk) come before those of
+// chunk c+1, in Morton order among themselves (the chunk number takes the
+// top bits of a 32-bit key, so more chunks leave a coarser curve).
 template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
-                  int32_t* dOrder, cudaStream_t stream);
+                  int32_t* dOrder, cudaStream_t stream, int64_t chunk = 0);
 
 // Counting-sort placement: dHist holds per-cell counts (turned into offsets
 // in place), dCell/dRank each query's cell and rank inside it.

@@ -93,6 +93,7 @@ struct CellParams {
   int dims;
   int bits;
   int shift;
+  int64_t chunk;  // > 0: element i's key carries i / chunk above its dims*bits Morton bits
 };
 
 __device__ __forceinline__ uint32_t spread3_10(uint32_t x) {
@@ -235,6 +236,7 @@ __global__ void k_morton_tiles(const T* __restrict__ q, int64_t n, int64_t qStri
 #pragma unroll
     for (int u = 0; u < kPre; ++u) {
       const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+      if (p.chunk > 0) kk[u] |= (uint32_t)(i / p.chunk) << (p.bits * p.dims);
       if (i < n) key[i] = kk[u];
       count_digit(h, i < n, kk[u] & (kRadix - 1));
     }
@@ -454,13 +456,21 @@ int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaSt
 
 template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
-                  int32_t* dOrder, cudaStream_t stream) {
+                  int32_t* dOrder, cudaStream_t stream, int64_t chunk) {
   if (nq <= 0) return kOk;
   if (nq > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
   CellParams p;
   p.dims = std::min(dim, kMortonDims);
   p.bits = 30 / p.dims;
   p.shift = 0;
+  p.chunk = chunk > 0 && chunk < nq ? chunk : 0;
+  int chunkBits = 0;
+  if (p.chunk > 0) {
+    while ((int64_t(1) << chunkBits) < ceil_div(nq, p.chunk)) ++chunkBits;
+    // the chunk number above the Morton code, within 32 bits
+    p.bits = std::min(p.bits, (32 - chunkBits) / p.dims);
+  }
+  if (p.bits < 1 || p.bits * p.dims + chunkBits > 32) return set_error(kErrInternal, "sort: too many query chunks");
   for (int d = 0; d < kMortonDims; ++d) {
     if (d < p.dims) {
       const double ext = hi[d] - lo[d];
@@ -479,7 +489,7 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
   if (rc == kOk) {
     k_morton_tiles<T><<<P.blocks, 32 * kSortWarps, P.smem, stream>>>(dQuery, nq, qStride, p, P.rounds, P.nTiles,
                                                                       keys, hist);
-    rc = radix_passes(keys, nq, p.bits * p.dims, nullptr, dOrder, P, hist, true, stream);
+    rc = radix_passes(keys, nq, p.bits * p.dims + chunkBits, nullptr, dOrder, P, hist, true, stream);
   }
   if (keys) scratch_free(keys, stream);
   if (hist) scratch_free(hist, stream);
@@ -487,8 +497,8 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
 }
 
 template int order_queries<float>(const float*, int64_t, int64_t, int, const double*, const double*, int32_t*,
-                                  cudaStream_t);
+                                  cudaStream_t, int64_t);
 template int order_queries<double>(const double*, int64_t, int64_t, int, const double*, const double*, int32_t*,
-                                   cudaStream_t);
+                                   cudaStream_t, int64_t);
 
 }  // namespace nabo_gb300

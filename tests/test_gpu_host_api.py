@@ -20,14 +20,28 @@ def _nb():
     return nb
 
 
-def _knn_strided(s, q, k, pad, radii=None):
-    """nabo_cuda_knn on columns of q.shape[1] rows stored pad values apart."""
+def _host(shape, dtype, pinned):
+    if not pinned:
+        return np.zeros(shape, dtype)
+    import torch
+    tdt = {np.dtype(np.float32): torch.float32, np.dtype(np.float64): torch.float64,
+           np.dtype(np.int32): torch.int32}[np.dtype(dtype)]
+    return torch.zeros(shape, dtype=tdt).pin_memory().numpy()
+
+
+def _knn_strided(s, q, k, pad, radii=None, pinned=False):
+    """nabo_cuda_knn on columns of q.shape[1] rows stored pad values apart
+    (page-locked host buffers with pinned=True)."""
     from libnabo_gb300 import _native
     nq, rows = q.shape
-    buf = np.zeros((nq, rows + pad), q.dtype)
+    buf = _host((nq, rows + pad), q.dtype, pinned)
     buf[:, :rows] = q
-    idx = np.empty((nq, k), np.int32)
-    d2 = np.empty((nq, k), q.dtype)
+    idx = _host((nq, k), np.int32, pinned)
+    d2 = _host((nq, k), q.dtype, pinned)
+    if radii is not None and pinned:
+        r = _host(radii.shape, radii.dtype, True)
+        r[:] = radii
+        radii = r
     touched = ctypes.c_uint64(0)
     rptr = None if radii is None else radii.ctypes.data_as(ctypes.c_void_p)
     rc = _native.lib.nabo_cuda_knn(s._h, buf.ctypes.data_as(ctypes.c_void_p), rows, nq, rows + pad, k, 0.0, 0,
@@ -54,6 +68,54 @@ def test_strided_queries_match_oracle(nq):
     oi, od, ot = orc.knn(q, 10, max_radii=radii, mode=O.MODE_CANONICAL)
     H.assert_identical(gi, gd, oi, od, f"strided radii nq={nq}")
     assert gt == ot
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_pinned_large_call_is_pipelined_and_exact(dtype):
+    """Page-locked buffers and 2^18 or more queries: chunks on several
+    streams, copies overlapping searches; same results and touched count."""
+    nb = _nb()
+    rng = np.random.default_rng(11)
+    cloud = rng.random((200_000, 3)).astype(dtype)
+    nq = 700_001
+    q = rng.random((nq, 3)).astype(dtype)
+    radii = rng.uniform(0.002, 0.02, nq).astype(dtype)
+    s = nb.NearestNeighbourSearch(cloud, creationOptionFlags=nb.TOUCH_STATISTICS)
+    orc = O.OracleTree(cloud, creation_flags=H.TOUCH_STATISTICS)
+    gi, gd, gt = _knn_strided(s, q, 7, pad=2, pinned=True)
+    oi, od, ot = orc.knn(q, 7, mode=O.MODE_CANONICAL)
+    H.assert_identical(gi, gd, oi, od, "pipelined")
+    assert gt == ot
+    gi, gd, gt = _knn_strided(s, q, 7, pad=0, radii=radii, pinned=True)
+    oi, od, ot = orc.knn(q, 7, max_radii=radii, mode=O.MODE_CANONICAL)
+    H.assert_identical(gi, gd, oi, od, "pipelined radii")
+    assert gt == ot
+    hq = _host(q.shape, dtype, True)
+    hq[:] = q
+    out = (_host((nq, 40), np.int32, True), _host((nq, 40), dtype, True))
+    gi, gd = s.knn(hq, 40, out=out)  # k > 32 through the same path
+    oi, od, _ = orc.knn(q, 40, mode=O.MODE_CANONICAL)
+    H.assert_identical(gi, gd, oi, od, "pipelined k=40")
+
+
+@pytest.mark.parametrize("variant", ["bruteforce", "unordered"])
+def test_pinned_large_call_unordered_chunks(variant):
+    """The pipelined path without a query order: brute force, and the
+    kd-tree with query ordering off, searched in plain consecutive chunks."""
+    nb = _nb()
+    rng = np.random.default_rng(12)
+    cloud = rng.random((4000, 3)).astype(np.float32)
+    nq = 300_000
+    q = rng.random((nq, 3)).astype(np.float32)
+    if variant == "bruteforce":
+        s = nb.NearestNeighbourSearch(cloud, nb.SearchType.BRUTE_FORCE_CUDA, creationOptionFlags=nb.TOUCH_STATISTICS)
+    else:
+        s = nb.NearestNeighbourSearch(cloud, params={"queryOrdering": 0}, creationOptionFlags=nb.TOUCH_STATISTICS)
+    orc = O.OracleTree(cloud, creation_flags=H.TOUCH_STATISTICS)
+    gi, gd, gt = _knn_strided(s, q, 6, pad=1, pinned=True)
+    oi, od, ot = orc.knn(q, 6, mode=O.MODE_CANONICAL)
+    H.assert_identical(gi, gd, oi, od, variant)
+    assert gt == (nq * cloud.shape[0] if variant == "bruteforce" else ot)
 
 
 def test_concurrent_calls_on_one_object():
