@@ -32,6 +32,7 @@ def test_params_defaults():
     p = _native.nabo_cuda_params()
     _native.lib.nabo_cuda_params_init(ctypes.byref(p))
     assert p.bucketSize == 8 and p.queryOrdering == 1 and p.struct_size == ctypes.sizeof(p)
+    assert p.pipelineChunks == 0 and ctypes.sizeof(p) == 32
 
 
 def test_version():
@@ -45,6 +46,8 @@ def test_version():
     (dict(params={"bucketSize": 0}), "Requested bucket size 0, but must be larger than 2", 1),
     (dict(searchType=1), "only the CUDA search types", 3),
     (dict(searchType=99), "Unknown search type", 1),
+    (dict(params={"pipelineChunks": 65}), "pipelineChunks must be between 0 and 64", 1),
+    (dict(params={"pipelineChunks": -1}), "pipelineChunks must be between 0 and 64", 1),
 ])
 def test_create_argument_errors(kwargs, msg, code):
     import libnabo_gb300 as nb
