@@ -749,134 +749,194 @@ struct SmallStack {
   T* boxHi;
 };
 
+// One of the reference's two partition passes (nabo/kdtree_cpu.cpp:149-177)
+// over the node's points pts[0, count), by a warp. Scanning from both ends,
+// the reference swaps the i-th element from the left that fails the test
+// with the i-th element from the right that passes it, while the first
+// stays left of the second. Those are exactly the failing elements inside
+// [lo, mid) and the passing elements inside [mid, hi) (mid = lo + the
+// number of passing elements of [lo, hi)), paired in order from the left
+// and from the right: `less` is the test `v < cut` of pass 1 over
+// [0, count) and `v <= cut` of pass 2 over [lt, count).
+template <typename T, int D>
+__device__ __forceinline__ void warp_partition_pass(Rec<T, D>* pts, int lo, int mid, int hi, int cd, T cut,
+                                                    bool lessEq, int* posL, int* posR, int lane) {
+  const unsigned below = (1u << lane) - 1u;
+  int nl = 0, nr = 0;
+  for (int c0 = lo; c0 < hi; c0 += 32) {
+    const int i = c0 + lane;
+    bool fl = false, fr = false;
+    if (i < hi) {
+      const T v = pts[i].p.c[cd];
+      const bool pass = lessEq ? (v <= cut) : (v < cut);
+      fl = i < mid && !pass;
+      fr = i >= mid && pass;
+    }
+    const unsigned bl = __ballot_sync(0xffffffffu, fl);
+    const unsigned br = __ballot_sync(0xffffffffu, fr);
+    // at most half of the node's points are misplaced on either side
+    const int jl = nl + __popc(bl & below), jr = nr + __popc(br & below);
+    if (fl && jl < kSmallMax / 2) posL[jl] = i;
+    if (fr && jr < kSmallMax / 2) posR[jr] = i;
+    nl += __popc(bl);
+    nr += __popc(br);
+  }
+  __syncwarp();
+  int m = nl < nr ? nl : nr;  // equal for a consistent mid
+  m = m < kSmallMax / 2 ? m : kSmallMax / 2;
+  for (int j = lane; j < m; j += 32) {
+    const int a = posL[j], b = posR[m - 1 - j];
+    const Rec<T, D> t = pts[a];
+    pts[a] = pts[b];
+    pts[b] = t;
+  }
+  __syncwarp();
+}
+
+// Small segments (at most kSmallMax points), one warp each over a fixed
+// grid: the segment's records are staged in shared memory and its subtree is
+// built by the reference recursion (nabo/kdtree_cpu.cpp:110-225) in
+// pre-order with an explicit stack (global scratch, written by lane 0). Each
+// split's min/max, counts and partition passes run across the lanes; node
+// records and bucket order come out as the reference's.
 template <typename T, int D>
 __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, Node<T>* scratch,
                         SmallStack<T> stk, int dim, unsigned bucketSize, int* counters) {
-  const int sid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (sid >= *nSmall) return;
-  const int base = small.start[sid];
-  const int segN = small.count[sid];
-  Node<T>* out = scratch + 2 * (int64_t)base;
-  int sp = 0;
-  {
-    const int e = base;
-    stk.start[e] = base;
-    stk.count[e] = small.count[sid];
-    stk.parent[e] = -1;
-    stk.depth[e] = small.depth[sid];
-    for (int d = 0; d < dim; ++d) {
-      stk.boxLo[(int64_t)e * kMaxDim + d] = small.boxLo[(int64_t)sid * kMaxDim + d];
-      stk.boxHi[(int64_t)e * kMaxDim + d] = small.boxHi[(int64_t)sid * kMaxDim + d];
-    }
-    sp = 1;
-  }
-  int emitted = 0;
+  extern __shared__ __align__(16) unsigned char smallSmem[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int warps = blockDim.x >> 5;
+  Rec<T, D>* pts = reinterpret_cast<Rec<T, D>*>(smallSmem) + (size_t)warp * kSmallMax;
+  int* posL = reinterpret_cast<int*>(reinterpret_cast<Rec<T, D>*>(smallSmem) + (size_t)warps * kSmallMax) +
+              (size_t)warp * kSmallMax;
+  int* posR = posL + kSmallMax / 2;
+  const int nS = *nSmall;
   int hmax = 0;
-  T lo[kMaxDim], hi[kMaxDim];
-  while (sp > 0) {
-    --sp;
-    const int e = base + sp;
-    const int st = stk.start[e];
-    const int count = stk.count[e];
-    const int parent = stk.parent[e];
-    const int depth = stk.depth[e];
-    const int local = emitted++;
-    if (parent >= 0) out[parent].meta = make_meta(node_dim(out[parent].meta), (uint32_t)local);
-    if (count <= (int)bucketSize) {
-      store_leaf(out + local, (uint32_t)count, (uint32_t)st);
-      hmax = depth > hmax ? depth : hmax;
-      continue;
-    }
-    for (int d = 0; d < dim; ++d) {
-      lo[d] = stk.boxLo[(int64_t)e * kMaxDim + d];
-      hi[d] = stk.boxHi[(int64_t)e * kMaxDim + d];
-    }
-    const int cd = arg_max_extent(lo, hi, dim);
-    const T ideal = Ar<T>::mul(Ar<T>::add(hi[cd], lo[cd]), T(0.5));
-    T mn = std::numeric_limits<T>::max(), mx = std::numeric_limits<T>::lowest();
-    for (int i = 0; i < count; ++i) {
-      const T v = recs[st + i].p.c[cd];
-      mn = (mn < v) ? mn : v;
-      mx = (v < mx) ? mx : v;
-    }
-    T cut;
-    if (ideal < mn)
-      cut = mn;
-    else if (ideal > mx)
-      cut = mx;
-    else
-      cut = ideal;
-    // two-pass partition, nabo/kdtree_cpu.cpp:149-177
-    Rec<T, D>* pts = recs + st;
-    int l = 0, r = count - 1;
-    for (;;) {
-      while (l < count && pts[l].p.c[cd] < cut) ++l;
-      while (r >= 0 && pts[r].p.c[cd] >= cut) --r;
-      if (l > r) break;
-      const Rec<T, D> tmp = pts[l];
-      pts[l] = pts[r];
-      pts[r] = tmp;
-      ++l;
-      --r;
-    }
-    const int br1 = l;
-    r = count - 1;
-    for (;;) {
-      while (l < count && pts[l].p.c[cd] <= cut) ++l;
-      while (r >= br1 && pts[r].p.c[cd] > cut) --r;
-      if (l > r) break;
-      const Rec<T, D> tmp = pts[l];
-      pts[l] = pts[r];
-      pts[r] = tmp;
-      ++l;
-      --r;
-    }
-    const int br2 = l;
-    int leftCount;
-    if (ideal < mn)
-      leftCount = 1;
-    else if (ideal > mx)
-      leftCount = count - 1;
-    else if (br1 > count / 2)
-      leftCount = br1;
-    else if (br2 < count / 2)
-      leftCount = br2;
-    else
-      leftCount = count / 2;
-    leftCount = leftCount < 1 ? 1 : (leftCount > count - 1 ? count - 1 : leftCount);
-    if (sp + 2 > segN || local + 2 >= 2 * segN) {  // cannot happen for a valid split; never overrun
-      atomicOr(counters + 3, 2);
-      break;
-    }
-    store_inner(out + local, (uint32_t)cd, 0u, cut);
-    // push right (processed after the whole left subtree), then left
-    {
-      const int f = base + sp;
-      stk.start[f] = st + leftCount;
-      stk.count[f] = count - leftCount;
-      stk.parent[f] = local;
-      stk.depth[f] = depth + 1;
+  for (int sid = blockIdx.x * warps + warp; sid < nS; sid += gridDim.x * warps) {
+    const int base = small.start[sid];
+    const int segN = small.count[sid];
+    for (int i = lane; i < segN; i += 32) pts[i] = recs[base + i];
+    Node<T>* out = scratch + 2 * (int64_t)base;
+    if (lane == 0) {
+      stk.start[base] = 0;
+      stk.count[base] = segN;
+      stk.parent[base] = -1;
+      stk.depth[base] = small.depth[sid];
       for (int d = 0; d < dim; ++d) {
-        stk.boxLo[(int64_t)f * kMaxDim + d] = d == cd ? cut : lo[d];
-        stk.boxHi[(int64_t)f * kMaxDim + d] = hi[d];
+        stk.boxLo[(int64_t)base * kMaxDim + d] = small.boxLo[(int64_t)sid * kMaxDim + d];
+        stk.boxHi[(int64_t)base * kMaxDim + d] = small.boxHi[(int64_t)sid * kMaxDim + d];
       }
-      ++sp;
     }
-    {
-      const int f = base + sp;
-      stk.start[f] = st;
-      stk.count[f] = leftCount;
-      stk.parent[f] = -1;
-      stk.depth[f] = depth + 1;
+    __syncwarp();
+    int sp = 1;
+    int emitted = 0;
+    T lo[kMaxDim], hi[kMaxDim];
+    while (sp > 0) {
+      --sp;
+      const int e = base + sp;
+      const int st = stk.start[e];  // local to the segment
+      const int count = stk.count[e];
+      const int parent = stk.parent[e];
+      const int depth = stk.depth[e];
+      const int local = emitted++;
+      if (lane == 0 && parent >= 0) out[parent].meta = make_meta(node_dim(out[parent].meta), (uint32_t)local);
+      if (count <= (int)bucketSize) {
+        if (lane == 0) store_leaf(out + local, (uint32_t)count, (uint32_t)(base + st));
+        hmax = depth > hmax ? depth : hmax;
+        __syncwarp();
+        continue;
+      }
       for (int d = 0; d < dim; ++d) {
-        stk.boxLo[(int64_t)f * kMaxDim + d] = lo[d];
-        stk.boxHi[(int64_t)f * kMaxDim + d] = d == cd ? cut : hi[d];
+        lo[d] = stk.boxLo[(int64_t)e * kMaxDim + d];
+        hi[d] = stk.boxHi[(int64_t)e * kMaxDim + d];
       }
-      ++sp;
+      const int cd = arg_max_extent(lo, hi, dim);
+      const T ideal = Ar<T>::mul(Ar<T>::add(hi[cd], lo[cd]), T(0.5));
+      Rec<T, D>* node = pts + st;
+      T mn = std::numeric_limits<T>::max(), mx = std::numeric_limits<T>::lowest();
+      for (int i = lane; i < count; i += 32) {
+        const T v = node[i].p.c[cd];
+        mn = (mn < v) ? mn : v;
+        mx = (v < mx) ? mx : v;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const T a = __shfl_xor_sync(0xffffffffu, mn, o);
+        const T b = __shfl_xor_sync(0xffffffffu, mx, o);
+        mn = (mn < a) ? mn : a;
+        mx = (b < mx) ? mx : b;
+      }
+      T cut;
+      if (ideal < mn)
+        cut = mn;
+      else if (ideal > mx)
+        cut = mx;
+      else
+        cut = ideal;
+      int lt = 0, eq = 0;
+      for (int c0 = 0; c0 < count; c0 += 32) {
+        const int i = c0 + lane;
+        const T v = i < count ? node[i].p.c[cd] : T(0);
+        lt += __popc(__ballot_sync(0xffffffffu, i < count && v < cut));
+        eq += __popc(__ballot_sync(0xffffffffu, i < count && v == cut));
+      }
+      warp_partition_pass<T, D>(node, 0, lt, count, cd, cut, false, posL, posR, lane);
+      if (eq > 0) warp_partition_pass<T, D>(node, lt, lt + eq, count, cd, cut, true, posL, posR, lane);
+      const int br1 = lt, br2 = lt + eq;
+      int leftCount;
+      if (ideal < mn)
+        leftCount = 1;
+      else if (ideal > mx)
+        leftCount = count - 1;
+      else if (br1 > count / 2)
+        leftCount = br1;
+      else if (br2 < count / 2)
+        leftCount = br2;
+      else
+        leftCount = count / 2;
+      leftCount = leftCount < 1 ? 1 : (leftCount > count - 1 ? count - 1 : leftCount);
+      if (sp + 2 > segN || local + 2 >= 2 * segN) {  // cannot happen for a valid split; never overrun
+        if (lane == 0) atomicOr(counters + 3, 2);
+        break;
+      }
+      if (lane == 0) {
+        store_inner(out + local, (uint32_t)cd, 0u, cut);
+        // push right (processed after the whole left subtree), then left
+        int f = base + sp;
+        stk.start[f] = st + leftCount;
+        stk.count[f] = count - leftCount;
+        stk.parent[f] = local;
+        stk.depth[f] = depth + 1;
+        for (int d = 0; d < dim; ++d) {
+          stk.boxLo[(int64_t)f * kMaxDim + d] = d == cd ? cut : lo[d];
+          stk.boxHi[(int64_t)f * kMaxDim + d] = hi[d];
+        }
+        f = base + sp + 1;
+        stk.start[f] = st;
+        stk.count[f] = leftCount;
+        stk.parent[f] = -1;
+        stk.depth[f] = depth + 1;
+        for (int d = 0; d < dim; ++d) {
+          stk.boxLo[(int64_t)f * kMaxDim + d] = lo[d];
+          stk.boxHi[(int64_t)f * kMaxDim + d] = d == cd ? cut : hi[d];
+        }
+      }
+      sp += 2;
+      __syncwarp();
     }
+    __syncwarp();
+    for (int i = lane; i < segN; i += 32) recs[base + i] = pts[i];
+    if (lane == 0) small.size[sid] = emitted;
+    __syncwarp();
   }
-  small.size[sid] = emitted;
-  atomicMax(counters + 2, hmax);
+  if (lane == 0) atomicMax(counters + 2, hmax);
+}
+
+template <typename T, int D>
+inline int small_warps_per_block() {
+  const size_t perWarp = (size_t)kSmallMax * (sizeof(Rec<T, D>) + sizeof(int));
+  const size_t w = (48 * 1024) / perWarp;
+  return (int)(w < 1 ? 1 : (w > 4 ? 4 : w));
 }
 
 // ---------------------------------------------------------------------------
@@ -1232,8 +1292,13 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
     NABO_CUDA_TRY(cudaMemcpyAsync(&nSmallHost, counters + 1, sizeof(int), cudaMemcpyDeviceToHost, stream));
     NABO_CUDA_TRY(cudaStreamSynchronize(stream));
   }
-  k_small<T, D><<<ceil_div(nSmallHost, 64), 64, 0, stream>>>(recs, small, counters + 1, scratchNodes, stk, dim,
-                                                             bucketSize, counters);
+  {
+    const int wpb = small_warps_per_block<T, D>();
+    const size_t smem = (size_t)wpb * kSmallMax * (sizeof(Rec<T, D>) + sizeof(int));
+    const int smallGrid = std::max(1, std::min(ceil_div(std::max(nSmallHost, 1), wpb), 16 * std::max(sms, 1)));
+    k_small<T, D><<<smallGrid, 32 * wpb, smem, stream>>>(recs, small, counters + 1, scratchNodes, stk, dim,
+                                                         bucketSize, counters);
+  }
   NABO_CUDA_TRY(cudaGetLastError());
   Node<T>* nodes = static_cast<Node<T>*>(f->nodes);
   k_forest_status<<<1, 1, 0, stream>>>(st, counters, f->status);
