@@ -453,7 +453,10 @@ __device__ __forceinline__ uint32_t stack_take(const StackRec<T, D>* stk, int sp
 // Reference-order traversal, structured descend / leaf / pop so the lanes
 // of a warp run each phase together: all lanes descend until every lane
 // stands on a leaf, then all scan their leaves, then all pop.
-template <typename T, int D, int K, int STACK>
+// EXACT (epsilon 0, so maxError2 = 1 and rd * maxError2 = rd exactly): the
+// push test rd <= maxRadius2 && rd <= head is one compare against
+// min(maxRadius2, head), refreshed after each leaf; decisions are the same.
+template <typename T, int D, int K, int STACK, bool EXACT>
 __device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
   // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396): without
   // ALLOW_SELF_MATCH a point at distance <= epsilon is skipped; one compare
@@ -502,6 +505,8 @@ __device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
       T rd = T(0);
       for (;;) {
         // descend to a leaf, pushing far children
+        // min(maxRadius2, head), where a NaN radius (which passes nothing) wins
+        const T bound = EXACT ? (heap.head() < maxRadius2 ? heap.head() : maxRadius2) : T(0);
         Node<T> nd = load_node(nodes, node);
         while (!node_is_leaf(nd.meta)) {
           const int cd = (int)node_dim(nd.meta);
@@ -513,8 +518,9 @@ __device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
           const uint32_t farN = newOff > T(0) ? node + 1 : right;
           // sp <= tree height <= STACK (checked on the host); the test only
           // makes the bound explicit
-          if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < STACK)
-            stack_push(stk, sp++, rdFar, off, cd, newOff, farN);
+          const bool far = EXACT ? rdFar <= bound
+                                 : (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head());
+          if (far && sp < STACK) stack_push(stk, sp++, rdFar, off, cd, newOff, farN);
           node = nearN;
           nd = load_node(nodes, node);
         }
@@ -527,7 +533,7 @@ __device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
         while (sp > 0) {
           --sp;
           const T e = stack_rd(stk, sp);
-          if (Ar<T>::mul(e, maxError2) <= heap.head()) {
+          if ((EXACT ? e : Ar<T>::mul(e, maxError2)) <= heap.head()) {
             rd = e;
             node = stack_take(stk, sp, off);
             more = true;
@@ -553,26 +559,34 @@ __device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
   }
 }
 
-template <typename T, int D, int K, int STACK>
+template <typename T, int D, int K, int STACK, bool EXACT>
 __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
-  knn_kdtree_body<T, D, K, STACK>(a);
+  knn_kdtree_body<T, D, K, STACK, EXACT>(a);
 }
 
 // Double searches with a long top-k hold ~100 registers of heap alone;
 // limited to 128 registers a thread, 4 blocks share an SM, and the FP64 pipe
 // gets the extra warps it needs to hide its latency (12 % faster on 8-D
 // clouds, k = 32).
-template <typename T, int D, int K, int STACK>
+template <typename T, int D, int K, int STACK, bool EXACT>
 __global__ void __launch_bounds__(128, 4) k_knn_kdtree_lean(KnnLaunch a) {
-  knn_kdtree_body<T, D, K, STACK>(a);
+  knn_kdtree_body<T, D, K, STACK, EXACT>(a);
+}
+
+template <typename T, int D, int K, int STACK, bool EXACT>
+void launch_kdtree_as(int grid, int block, cudaStream_t stream, const KnnLaunch& L) {
+  if constexpr (sizeof(T) == 8 && K >= 16)
+    k_knn_kdtree_lean<T, D, K, STACK, EXACT><<<grid, block, 0, stream>>>(L);
+  else
+    k_knn_kdtree<T, D, K, STACK, EXACT><<<grid, block, 0, stream>>>(L);
 }
 
 template <typename T, int D, int K, int STACK>
 void launch_kdtree(int grid, int block, cudaStream_t stream, const KnnLaunch& L) {
-  if constexpr (sizeof(T) == 8 && K >= 16)
-    k_knn_kdtree_lean<T, D, K, STACK><<<grid, block, 0, stream>>>(L);
+  if (L.maxError2 == 1.0)
+    launch_kdtree_as<T, D, K, STACK, true>(grid, block, stream, L);
   else
-    k_knn_kdtree<T, D, K, STACK><<<grid, block, 0, stream>>>(L);
+    launch_kdtree_as<T, D, K, STACK, false>(grid, block, stream, L);
 }
 
 // Warp-packet traversal for exact search (epsilon = 0).
