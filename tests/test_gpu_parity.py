@@ -196,6 +196,26 @@ def test_empty_query_and_far_queries():
     _check_against_oracle(cloud, far, 4)
 
 
+def test_double_far_queries_ties_and_nan_radii():
+    """Double clouds: exact searches decide the reference's traversal on
+    float bounds and fall back to the double traversal when a decision is not
+    certain. Queries 1e16 away from a unit cloud make every squared distance
+    round to a few double values (ties at the head, cells whose rounded box
+    distance sits on the head), and NaN radii pass nothing: results and
+    touched counts must still be the oracle kd-tree's."""
+    rng = np.random.default_rng(31)
+    cloud = rng.random((2000, 3))
+    far = rng.random((300, 3)) * 1e15 + 1e16
+    _check_against_oracle(cloud, far, 4)
+    _check_against_oracle(cloud, far, 16)
+    q = rng.random((400, 3))
+    radii = rng.uniform(0.01, 0.2, 400)
+    radii[::7] = np.nan
+    _check_against_oracle(cloud, q, 6, radii=radii)
+    grid = np.stack(np.meshgrid(*[np.arange(7.0)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    _check_against_oracle(grid, grid[::5] + 0.5, 8)
+
+
 def test_search_errors_match_reference_messages():
     nb = _nb()
     rng = np.random.default_rng(14)
