@@ -121,8 +121,8 @@ class NearestNeighbourSearch:
     ``Nabo::NearestNeighbourSearch<T>::create`` (nabo/nabo.h:360). ``cloud``
     is a numpy array (host) or a CUDA torch tensor (device) of shape
     (n, rows); it is copied into the search object. ``params`` accepts the
-    reference's ``bucketSize`` key, ``queryOrdering`` (1 = sort queries
-    along a Morton curve inside each search, the default) and ``traversal``
+    reference's ``bucketSize`` key, ``queryOrdering`` (1 = sort the queries
+    of searches of 2^18 or more along a Morton curve, the default) and ``traversal``
     (0 or 1 the reference's visit order, 2 the warp packet for exact
     searches without touch statistics).
     """
