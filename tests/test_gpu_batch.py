@@ -57,6 +57,26 @@ def test_batch_trees_equal_oracle_trees():
 
 
 @pytest.mark.parametrize("graph", [False, True])
+def test_large_batch_trees_equal_oracle_trees(graph):
+    """A forest of 4.8 M points (about 37 k small segments, one warp each,
+    many more than the warps resident at once)."""
+    from libnabo_gb300 import synthetic as S
+    sizes = [120_000] * 40
+    clouds = [S.gaussian_blobs(n, 900 + i) for i, n in enumerate(sizes)]
+    queries = [c[:100] for c in clouds]
+    ks = np.full(len(clouds), 4, np.int32)
+    b, gi, gd = _run_batch(clouds, queries, ks, graph=graph, maxLevels=64)
+    assert b.status()["ok"], b.status()
+    for c in (0, 17, 39):
+        g = b.export_tree(c)
+        o = O.OracleTree(clouds[c]).export()
+        for key in ("cut_dim", "right", "bucket_start", "bucket_count", "buckets"):
+            assert np.array_equal(g[key], o[key]), (c, key)
+        oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], 4, mode=O.MODE_CANONICAL)
+        H.assert_identical(gi[c], gd[c], oi, od, f"cloud {c}")
+
+
+@pytest.mark.parametrize("graph", [False, True])
 def test_batch_results_equal_single_searches(graph):
     nb = _nb()
     clouds, queries, ks = _batch_data(60, 300, 40000, seed=2)

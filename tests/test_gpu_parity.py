@@ -58,6 +58,14 @@ def test_tree_identical_to_oracle(bucket):
         assert np.array_equal(gpu.minBound, o["min_bound"]) and np.array_equal(gpu.maxBound, o["max_bound"])
 
 
+def test_tree_identical_to_oracle_many_small_segments():
+    """A cloud of 8 M points: about 40 k small segments, each built by one
+    warp, many more than the warps resident at once."""
+    nb = _nb()
+    cloud = np.random.default_rng(77).random((8_000_000, 3)).astype(np.float32)
+    _tree_equal(nb.NearestNeighbourSearch(cloud), O.OracleTree(cloud), "uniform 8M")
+
+
 @pytest.mark.parametrize("case", H.KNNVALIDATE_CASES, ids=lambda c: f"{c[0]}-m{c[3]}-r{c[4]}")
 def test_knnvalidate_cases_gpu(ref_scans, case):
     """tests/knnvalidate.cpp on the reference clouds, with the CUDA types."""
