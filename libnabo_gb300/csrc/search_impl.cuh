@@ -31,15 +31,24 @@ inline int round_k(int k) {
   return -1;
 }
 
-// k above kMaxK: one warp per query holding 32*M slots (M compiled below).
-#define NABO_WIDE_LIST(X) X(2) X(4) X(8) X(16) X(32)
+// k above kMaxK: a group of lanes per query holding K slots (K compiled
+// below): 8 lanes for K = 64 and 16 for K = 128 (several queries share a
+// warp's traversal instructions), a whole warp beyond; 8 slots per lane up
+// to K = 256.
+#define NABO_WIDE_LIST(X) X(64) X(128) X(256) X(512) X(1024)
 constexpr int kMaxWideK = 1024;
-constexpr int kWideWarps = 4;  // queries per block of the kd-tree kernel
-constexpr int kWideBfWarps = 8;  // queries per block of the brute force
+constexpr int kWideThreads = 128;  // threads per block of the kd-tree kernel
+constexpr int kWideBfWarps = 8;    // queries per block of the brute force
 
-inline int wide_m(int k) {
-#define NABO_ROUND(MM) \
-  if (k <= 32 * MM) return MM;
+template <int KK>
+struct WideShape {
+  static constexpr int G = KK <= 64 ? 8 : (KK <= 128 ? 16 : 32);
+  static constexpr int M = KK / G;
+};
+
+inline int wide_k(int k) {
+#define NABO_ROUND(KK) \
+  if (k <= KK) return KK;
   NABO_WIDE_LIST(NABO_ROUND)
 #undef NABO_ROUND
   return -1;
@@ -49,42 +58,49 @@ inline int k_unsupported() {
   return set_error(kErrUnsupported, "k larger than 1024 is not supported by the CUDA search types");
 }
 
-// Launches the one-warp-per-query kd-tree search for L.k (or the batch's
+template <typename T, int D, int M, int G>
+int launch_wide_kdtree_as(const KnnLaunch& L, int height, cudaStream_t stream) {
+  const int cap = height + 1;
+  // the groups' stacks in shared memory: smaller blocks for tall trees of
+  // long records
+  int threads = kWideThreads;
+  while (threads > 32 && wide_stack_bytes<T, D>(threads / G, cap) > (size_t)160 * 1024) threads /= 2;
+  const size_t smem = wide_stack_bytes<T, D>(threads / G, cap);
+  cudaError_t e = cudaSuccess;
+  if (smem > 48 * 1024)
+    e = cudaFuncSetAttribute(k_knn_kdtree_wide<T, D, M, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return cuda_error(e, "wide kd-tree search shared memory");
+  const int grid = ceil_div(L.nq, threads / G);
+  k_knn_kdtree_wide<T, D, M, G><<<grid, threads, smem, stream>>>(L, cap);
+  return kOk;
+}
+
+// Launches the group-per-query kd-tree search for L.k (or the batch's
 // largest k) above kMaxK; `height` bounds the traversal stack.
 template <typename T, int D>
 int launch_wide_kdtree(const KnnLaunch& L, int kMax, int height, cudaStream_t stream) {
-  const int M = wide_m(kMax);
-  if (M < 0) return k_unsupported();
-  const int cap = height + 1;
-  const size_t smem = wide_stack_bytes<T, D>(kWideWarps, cap);
-  const int grid = ceil_div(L.nq, kWideWarps);
-  cudaError_t e = cudaSuccess;
-#define NABO_WIDE(MM)                                                                                 \
-  case MM: {                                                                                          \
-    if (smem > 48 * 1024)                                                                             \
-      e = cudaFuncSetAttribute(k_knn_kdtree_wide<T, D, MM>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                               (int)smem);                                                            \
-    if (e == cudaSuccess) k_knn_kdtree_wide<T, D, MM><<<grid, 32 * kWideWarps, smem, stream>>>(L, cap); \
-    break;                                                                                            \
-  }
-  switch (M) { NABO_WIDE_LIST(NABO_WIDE) }
+  switch (wide_k(kMax)) {
+#define NABO_WIDE(KK) \
+  case KK:            \
+    return launch_wide_kdtree_as<T, D, WideShape<KK>::M, WideShape<KK>::G>(L, height, stream);
+    NABO_WIDE_LIST(NABO_WIDE)
 #undef NABO_WIDE
-  if (e != cudaSuccess) return cuda_error(e, "wide kd-tree search shared memory");
-  return kOk;
+  }
+  return k_unsupported();
 }
 
 template <typename T, int D>
 int launch_wide_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
-  const int M = wide_m(L.k);
-  if (M < 0) return k_unsupported();
   const int grid = ceil_div(L.nq, kWideBfWarps);
-#define NABO_WIDE(MM)                                                                    \
-  case MM:                                                                               \
-    k_knn_bruteforce_wide<T, D, MM><<<grid, 32 * kWideBfWarps, 0, stream>>>(L);          \
-    break;
-  switch (M) { NABO_WIDE_LIST(NABO_WIDE) }
+  switch (wide_k(L.k)) {
+#define NABO_WIDE(KK)                                                                    \
+  case KK:                                                                               \
+    k_knn_bruteforce_wide<T, D, KK / 32><<<grid, 32 * kWideBfWarps, 0, stream>>>(L);     \
+    return kOk;
+    NABO_WIDE_LIST(NABO_WIDE)
 #undef NABO_WIDE
-  return kOk;
+  }
+  return k_unsupported();
 }
 
 template <typename T, int D>

@@ -1,86 +1,96 @@
-// search_wide.cuh -- kNN for k above 32: one warp per query.
+// search_wide.cuh -- kNN for k above 32: a group of G lanes per query.
 //
 // The reference's heaps have no cap on k (nabo/index_heap.h:51-165 grows an
 // STL heap to k entries, nabo/index_heap.h:263-369 keeps a sorted vector of
 // k). One thread's registers hold at most 32 (dist2, index) pairs, so for
-// larger k a whole warp serves one query: the top-k is spread over the 32
-// lanes' registers, the traversal runs once for the warp (every lane holds
-// the same query state, so the warp never diverges), a leaf's points are
-// taken one per lane, and an insertion costs each lane a few compares and
-// selects on its own slots plus one shuffle. Visit order, pruning tests,
-// self-match rule, tie rule and TOUCH_STATISTICS are the one-thread kernels'
-// (the reference's recurseKnn, nabo/kdtree_cpu.cpp:367-447), so results are
-// identical to theirs and to the reference's for any k.
+// larger k a group of G lanes (8, 16 or 32; 32 / G queries per warp) serves
+// one query: the top-k is spread over the group's registers, the traversal
+// runs once per group (every lane of a group holds the same query state, so
+// a group never diverges), a leaf's points are taken one per lane, and an
+// insertion costs each lane a few compares and selects on its own slots
+// plus one shuffle. Visit order, pruning tests, self-match rule, tie rule
+// and TOUCH_STATISTICS are the one-thread kernels' (the reference's
+// recurseKnn, nabo/kdtree_cpu.cpp:367-447), so results are identical to
+// theirs and to the reference's for any k.
 #pragma once
 
 #include "search.cuh"
 
 namespace nabo_gb300 {
 
-constexpr unsigned kWarpAll = 0xffffffffu;
+// The lanes of the G-lane group holding `lane` (G divides 32).
+template <int G>
+__device__ __forceinline__ unsigned group_mask(int lane) {
+  if constexpr (G == 32)
+    return 0xffffffffu;
+  else
+    return ((1u << G) - 1u) << (lane & ~(G - 1));
+}
 
-// A warp's top-k with K = 32*M slots in ascending order; lane L holds slots
-// [L*M, L*M + M) in registers. The live entries are the last k slots, so the
-// head (the k-th smallest pair) is always lane 31's last register; the K-k
-// slots before them hold padding that orders below every pair. Inserting a
-// pair below the head drops the head and moves every slot above the
-// insertion point up by one: each lane compares and selects its own M slots
-// and takes the slot below its first one from the previous lane.
-template <typename T, int M>
-struct WarpTopK;
+// A group's top-k with K = G*M slots in ascending order; group lane g holds
+// slots [g*M, g*M + M) in registers. The live entries are the last k slots,
+// so the head (the k-th smallest pair) is always the group's last lane's
+// last register; the K-k slots before them hold padding that orders below
+// every pair. Inserting a pair below the head drops the head and moves every
+// slot above the insertion point up by one: each lane compares and selects
+// its own M slots and takes the slot below its first one from the previous
+// lane. Called by all lanes of the group with the same arguments.
+template <typename T, int M, int G>
+struct GroupTopK;
 
 // float: packed (dist2 bits << 32 | index) keys, as the one-thread TopK;
 // an empty slot is (+inf, 0) and is written out as (-1, +inf); padding is 0.
-template <int M>
-struct WarpTopK<float, M> {
-  static constexpr int K = 32 * M;
+template <int M, int G>
+struct GroupTopK<float, M, G> {
+  static constexpr int K = G * M;
   static constexpr uint64_t kEmpty = uint64_t(0x7f800000u) << 32;
   uint64_t a[M];
-  uint64_t h;  // the head key, the same in every lane
-  __device__ __forceinline__ void init(int k, int lane) {
+  uint64_t h;  // the head key, the same in every lane of the group
+  __device__ __forceinline__ void init(int k, int g) {
 #pragma unroll
-    for (int r = 0; r < M; ++r) a[r] = lane * M + r >= K - k ? kEmpty : 0ull;
+    for (int r = 0; r < M; ++r) a[r] = g * M + r >= K - k ? kEmpty : 0ull;
     h = kEmpty;
   }
   __device__ __forceinline__ float head() const { return __uint_as_float((uint32_t)(h >> 32)); }
-  // x < h; called by all lanes with the same x
-  __device__ __forceinline__ void insert_key(uint64_t x, int lane) {
-    uint64_t prev = __shfl_up_sync(kWarpAll, a[M - 1], 1);
-    if (lane == 0) prev = 0ull;
-    bool g[M];
+  // x < h
+  __device__ __forceinline__ void insert_key(uint64_t x, int g, unsigned gm) {
+    uint64_t prev = __shfl_up_sync(gm, a[M - 1], 1, G);
+    if (g == 0) prev = 0ull;
+    bool gt[M];
 #pragma unroll
-    for (int r = 0; r < M; ++r) g[r] = a[r] > x;
+    for (int r = 0; r < M; ++r) gt[r] = a[r] > x;
 #pragma unroll
-    for (int r = M - 1; r >= 1; --r) a[r] = g[r] ? (g[r - 1] ? a[r - 1] : x) : a[r];
-    a[0] = g[0] ? (prev > x ? prev : x) : a[0];
-    h = __shfl_sync(kWarpAll, a[M - 1], 31);
+    for (int r = M - 1; r >= 1; --r) a[r] = gt[r] ? (gt[r - 1] ? a[r - 1] : x) : a[r];
+    a[0] = gt[0] ? (prev > x ? prev : x) : a[0];
+    h = __shfl_sync(gm, a[M - 1], G - 1, G);
   }
-  __device__ __forceinline__ int count(int k, int lane) const {
+  __device__ __forceinline__ int count(int k, int g, unsigned gm) const {
     int c = 0;
 #pragma unroll
-    for (int r = 0; r < M; ++r) c += (lane * M + r >= K - k && (uint32_t)(a[r] >> 32) != 0x7f800000u) ? 1 : 0;
-    return __reduce_add_sync(kWarpAll, c);
+    for (int r = 0; r < M; ++r) c += (g * M + r >= K - k && (uint32_t)(a[r] >> 32) != 0x7f800000u) ? 1 : 0;
+    return __reduce_add_sync(gm, c);
   }
   // The k entries in ascending order; returns how many are valid.
-  __device__ __forceinline__ int store(int k, int lane, int32_t* __restrict__ oi, float* __restrict__ od) const {
+  __device__ __forceinline__ int store(int k, int g, unsigned gm, int32_t* __restrict__ oi,
+                                       float* __restrict__ od) const {
 #pragma unroll
     for (int r = 0; r < M; ++r) {
-      const int s = lane * M + r;
+      const int s = g * M + r;
       if (s >= K - k) {
         const uint32_t db = (uint32_t)(a[r] >> 32);
         oi[s - (K - k)] = db == 0x7f800000u ? -1 : (int32_t)(uint32_t)a[r];
         od[s - (K - k)] = __uint_as_float(db);
       }
     }
-    return count(k, lane);
+    return count(k, g, gm);
   }
 };
 
 // double: (bit pattern of dist2, index) pairs compared as integers, as the
 // one-thread TopK; an empty slot is (+inf, -1), padding (0, -1).
-template <int M>
-struct WarpTopK<double, M> {
-  static constexpr int K = 32 * M;
+template <int M, int G>
+struct GroupTopK<double, M, G> {
+  static constexpr int K = G * M;
   unsigned long long d[M];
   int i[M];
   unsigned long long hd;
@@ -91,11 +101,11 @@ struct WarpTopK<double, M> {
   static __device__ __forceinline__ unsigned long long bits(double x) {
     return (unsigned long long)__double_as_longlong(x);
   }
-  __device__ __forceinline__ void init(int k, int lane) {
+  __device__ __forceinline__ void init(int k, int g) {
     const unsigned long long inf = bits(Ar<double>::inf());
 #pragma unroll
     for (int r = 0; r < M; ++r) {
-      d[r] = lane * M + r >= K - k ? inf : 0ull;
+      d[r] = g * M + r >= K - k ? inf : 0ull;
       i[r] = -1;
     }
     hd = inf;
@@ -103,132 +113,137 @@ struct WarpTopK<double, M> {
   }
   __device__ __forceinline__ double head() const { return __longlong_as_double((long long)hd); }
   __device__ __forceinline__ bool accepts(double dist, int idx) const { return greater(hd, hi, bits(dist), idx); }
-  // accepts(dist, idx); called by all lanes with the same pair
-  __device__ __forceinline__ void insert(double dist, int idx, int lane) {
+  // accepts(dist, idx)
+  __device__ __forceinline__ void insert(double dist, int idx, int g, unsigned gm) {
     const unsigned long long x = bits(dist);
-    unsigned long long pd = __shfl_up_sync(kWarpAll, d[M - 1], 1);
-    int pi = __shfl_up_sync(kWarpAll, i[M - 1], 1);
-    if (lane == 0) {
+    unsigned long long pd = __shfl_up_sync(gm, d[M - 1], 1, G);
+    int pi = __shfl_up_sync(gm, i[M - 1], 1, G);
+    if (g == 0) {
       pd = 0ull;
       pi = -1;
     }
-    bool g[M];
+    bool gt[M];
 #pragma unroll
-    for (int r = 0; r < M; ++r) g[r] = greater(d[r], i[r], x, idx);
+    for (int r = 0; r < M; ++r) gt[r] = greater(d[r], i[r], x, idx);
 #pragma unroll
     for (int r = M - 1; r >= 1; --r) {
-      d[r] = g[r] ? (g[r - 1] ? d[r - 1] : x) : d[r];
-      i[r] = g[r] ? (g[r - 1] ? i[r - 1] : idx) : i[r];
+      d[r] = gt[r] ? (gt[r - 1] ? d[r - 1] : x) : d[r];
+      i[r] = gt[r] ? (gt[r - 1] ? i[r - 1] : idx) : i[r];
     }
     const bool gp = greater(pd, pi, x, idx);
-    d[0] = g[0] ? (gp ? pd : x) : d[0];
-    i[0] = g[0] ? (gp ? pi : idx) : i[0];
-    hd = __shfl_sync(kWarpAll, d[M - 1], 31);
-    hi = __shfl_sync(kWarpAll, i[M - 1], 31);
+    d[0] = gt[0] ? (gp ? pd : x) : d[0];
+    i[0] = gt[0] ? (gp ? pi : idx) : i[0];
+    hd = __shfl_sync(gm, d[M - 1], G - 1, G);
+    hi = __shfl_sync(gm, i[M - 1], G - 1, G);
   }
-  __device__ __forceinline__ int count(int k, int lane) const {
+  __device__ __forceinline__ int count(int k, int g, unsigned gm) const {
     int c = 0;
 #pragma unroll
-    for (int r = 0; r < M; ++r) c += (lane * M + r >= K - k && i[r] >= 0) ? 1 : 0;
-    return __reduce_add_sync(kWarpAll, c);
+    for (int r = 0; r < M; ++r) c += (g * M + r >= K - k && i[r] >= 0) ? 1 : 0;
+    return __reduce_add_sync(gm, c);
   }
-  __device__ __forceinline__ int store(int k, int lane, int32_t* __restrict__ oi, double* __restrict__ od) const {
+  __device__ __forceinline__ int store(int k, int g, unsigned gm, int32_t* __restrict__ oi,
+                                       double* __restrict__ od) const {
 #pragma unroll
     for (int r = 0; r < M; ++r) {
-      const int s = lane * M + r;
+      const int s = g * M + r;
       if (s >= K - k) {
         oi[s - (K - k)] = i[r];
         od[s - (K - k)] = __longlong_as_double((long long)d[r]);
       }
     }
-    return count(k, lane);
+    return count(k, g, gm);
   }
 };
 
-// Offers the leaf records [st + base, st + base + 32) (those below cnt), one
-// per lane, to the warp's top-k: each lane tests its point against the head
-// as it was when the batch started, and the candidates are inserted one by
-// one in lane order, each re-tested against the current head. The k
-// smallest pairs after the batch do not depend on that order. kShared: the
-// records sit in shared memory (read with plain loads, not the read-only
-// global path).
-template <typename T, int D, int M, bool kShared>
+// Offers the records [first, first + G) (those below avail), one per group
+// lane, to the group's top-k: each lane tests its point against the head as
+// it was when the batch started, and the candidates are inserted one by one
+// in lane order, each re-tested against the current head. The k smallest
+// pairs after the batch do not depend on that order. kShared: the records
+// sit in shared memory (read with plain loads, not the read-only global
+// path).
+template <typename T, int D, int M, int G, bool kShared>
 __device__ __forceinline__ void wide_offer(const Rec<T, D>* __restrict__ recs, int64_t first, int avail,
-                                           const T (&q)[D], T maxRadius2, T minDist, WarpTopK<T, M>& heap,
-                                           const LeafFilter<T, D>& flt, int lane) {
+                                           const T (&q)[D], T maxRadius2, T minDist, GroupTopK<T, M, G>& heap,
+                                           const LeafFilter<T, D>& flt, int g, unsigned gm) {
+  const int shift = __ffs(gm) - 1;  // the group's first lane in the warp
   if constexpr (std::is_same<T, float>::value) {
     uint64_t key = ~0ull;
     bool ok = false;
-    if (lane < avail) {
+    if (g < avail) {
       Rec<T, D> r;
       if constexpr (kShared)
-        r = recs[first + lane];
+        r = recs[first + g];
       else
-        load_rec(recs, first + lane, r);
+        load_rec(recs, first + g, r);
       const float dist = dist2_seq(q, r);
       key = TopK<float, 1>::make(dist, r.p.idx);
       ok = dist <= maxRadius2 && key < heap.h && dist > minDist;
     }
-    unsigned mask = __ballot_sync(kWarpAll, ok);
+    unsigned mask = (__ballot_sync(gm, ok) & gm) >> shift;
     while (mask) {
       const int src = __ffs(mask) - 1;
       mask &= mask - 1;
-      const uint64_t x = __shfl_sync(kWarpAll, key, src);
-      if (x < heap.h) heap.insert_key(x, lane);
+      const uint64_t x = __shfl_sync(gm, key, src, G);
+      if (x < heap.h) heap.insert_key(x, g, gm);
     }
   } else {
     T dist = Ar<T>::inf();
     int idx = -1;
     bool ok = false;
     const float thr = flt.on() ? flt.threshold(heap.head(), maxRadius2) : 0.0f;
-    if (lane < avail && !(flt.on() && flt.rejects(first + lane, thr))) {
+    if (g < avail && !(flt.on() && flt.rejects(first + g, thr))) {
       Rec<T, D> r;
       if constexpr (kShared)
-        r = recs[first + lane];
+        r = recs[first + g];
       else
-        load_rec(recs, first + lane, r);
+        load_rec(recs, first + g, r);
       dist = dist2_seq(q, r);
       idx = r.p.idx;
       ok = dist <= maxRadius2 && heap.accepts(dist, idx) && dist > minDist;
     }
-    unsigned mask = __ballot_sync(kWarpAll, ok);
+    unsigned mask = (__ballot_sync(gm, ok) & gm) >> shift;
     while (mask) {
       const int src = __ffs(mask) - 1;
       mask &= mask - 1;
-      const T dv = __shfl_sync(kWarpAll, dist, src);
-      const int iv = __shfl_sync(kWarpAll, idx, src);
-      if (heap.accepts(dv, iv)) heap.insert(dv, iv, lane);
+      const T dv = __shfl_sync(gm, dist, src, G);
+      const int iv = __shfl_sync(gm, idx, src, G);
+      if (heap.accepts(dv, iv)) heap.insert(dv, iv, g, gm);
     }
   }
 }
 
-// Shared memory of one warp's traversal stack: cap entries of rd, off[D]
-// (T each) and the node (uint32), laid out per block as all warps' T parts
-// followed by all warps' node parts.
+// Shared memory of one group's traversal stack: cap entries of rd, off[D]
+// (T each) and the node (uint32), laid out per block as all groups' T parts
+// followed by all groups' node parts.
 template <typename T, int D>
-inline size_t wide_stack_bytes(int warps, int cap) {
-  return (size_t)warps * (size_t)cap * ((D + 1) * sizeof(T) + sizeof(uint32_t));
+inline size_t wide_stack_bytes(int groups, int cap) {
+  return (size_t)groups * (size_t)cap * ((D + 1) * sizeof(T) + sizeof(uint32_t));
 }
 
-// Reference-order kd-tree search, one warp per query (blockDim.x / 32
+// Reference-order kd-tree search, one G-lane group per query (blockDim.x / G
 // queries per block). The traversal stack sits in shared memory, written by
-// lane 0 and read by all lanes; `cap` >= the tree height bounds it.
-template <typename T, int D, int M>
+// the group's first lane and read by all its lanes; `cap` >= the tree height
+// bounds it.
+template <typename T, int D, int M, int G>
 __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
   extern __shared__ __align__(16) unsigned char wideSmem[];
   const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const int warps = blockDim.x >> 5;
-  T* const sRd = reinterpret_cast<T*>(wideSmem) + (size_t)warp * cap * (D + 1);
+  const int g = lane & (G - 1);  // lane within the group
+  const unsigned gm = group_mask<G>(lane);
+  const int group = threadIdx.x / G;
+  const int groups = blockDim.x / G;
+  T* const sRd = reinterpret_cast<T*>(wideSmem) + (size_t)group * cap * (D + 1);
   T* const sOff = sRd + cap;
-  uint32_t* const sNode =
-      reinterpret_cast<uint32_t*>(reinterpret_cast<T*>(wideSmem) + (size_t)warps * cap * (D + 1)) + (size_t)warp * cap;
+  uint32_t* const sNode = reinterpret_cast<uint32_t*>(reinterpret_cast<T*>(wideSmem) + (size_t)groups * cap * (D + 1)) +
+                          (size_t)group * cap;
   // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396)
   const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
   const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
   const T* __restrict__ query = static_cast<const T*>(a.query);
-  const int64_t t = (int64_t)blockIdx.x * warps + warp;
+  const int64_t t = (int64_t)blockIdx.x * groups + group;
   uint32_t touched = 0;
   if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
     const int64_t qi = a.order ? (int64_t)a.order[t] : t;
@@ -252,8 +267,8 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
       mayFall = a.fallbackRadius >= 0.0 && (double)r < a.fallbackRadius;
     }
     const T maxError2 = (T)a.maxError2;
-    WarpTopK<T, M> heap;
-    heap.init(k, lane);
+    GroupTopK<T, M, G> heap;
+    heap.init(k, g);
     LeafFilter<T, D> flt;
     flt.init(a.recs32, a.coordMax, q);
     T off[D];
@@ -264,7 +279,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
       uint32_t node = root;
       T rd = T(0);
       for (;;) {
-        __syncwarp();  // the last pop's reads come before the next pushes
+        __syncwarp(gm);  // the last pop's reads come before the next pushes
         Node<T> nd = load_node(nodes, node);
         while (!node_is_leaf(nd.meta)) {
           const int cd = (int)node_dim(nd.meta);
@@ -275,7 +290,7 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
           const uint32_t nearN = newOff > T(0) ? right : node + 1;
           const uint32_t farN = newOff > T(0) ? node + 1 : right;
           if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < cap) {
-            if (lane == 0) {
+            if (g == 0) {
               sRd[sp] = rdFar;
 #pragma unroll
               for (int d = 0; d < D; ++d) sOff[(size_t)sp * D + d] = d == cd ? newOff : off[d];
@@ -288,10 +303,11 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
         }
         const uint32_t cnt = node_payload(nd.meta);
         const uint32_t st = node_start(nd);
-        for (uint32_t base = 0; base < cnt; base += 32)
-          wide_offer<T, D, M, false>(recs, (int64_t)st + base, (int)(cnt - base), q, maxRadius2, minDist, heap, flt, lane);
+        for (uint32_t base = 0; base < cnt; base += G)
+          wide_offer<T, D, M, G, false>(recs, (int64_t)st + base, (int)(cnt - base), q, maxRadius2, minDist, heap,
+                                        flt, g, gm);
         touched += cnt;
-        __syncwarp();  // lane 0's pushes are visible to every lane
+        __syncwarp(gm);  // the first lane's pushes are visible to the group
         bool more = false;
         while (sp > 0) {
           --sp;
@@ -307,16 +323,16 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
         }
         if (!more) break;
       }
-      if (!mayFall || heap.count(k, lane) == k) break;
+      if (!mayFall || heap.count(k, g, gm) == k) break;
       mayFall = false;
       maxRadius2 = (T)a.maxRadius2;
-      heap.init(k, lane);
-      if (a.fallbacks && lane == 0) atomicAdd(a.fallbacks, 1);
+      heap.init(k, g);
+      if (a.fallbacks && g == 0) atomicAdd(a.fallbacks, 1);
     }
-    const int f = heap.store(k, lane, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
-    if (a.found && lane == 0) a.found[qi] = f;
+    const int f = heap.store(k, g, gm, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
+    if (a.found && g == 0) a.found[qi] = f;
   }
-  if (a.stats && lane == 0 && touched) atomicAdd(a.touched, (unsigned long long)touched);
+  if (a.stats && g == 0 && touched) atomicAdd(a.touched, (unsigned long long)touched);
 }
 
 // Brute force (nabo/brute_force_cpu.cpp:63-103) for k above 32: one warp per
@@ -342,7 +358,7 @@ __global__ void __launch_bounds__(256) k_knn_bruteforce_wide(KnnLaunch a) {
     const T r = static_cast<const T*>(a.maxRadii)[qi];
     maxRadius2 = Ar<T>::mul(r, r);
   }
-  WarpTopK<T, M> heap;
+  GroupTopK<T, M, 32> heap;
   heap.init(a.k, lane);
   LeafFilter<T, D> flt;
   flt.init(nullptr, nullptr, q);
@@ -357,10 +373,11 @@ __global__ void __launch_bounds__(256) k_knn_bruteforce_wide(KnnLaunch a) {
     }
     __syncthreads();
     if (active)
-      for (int j = 0; j < m; j += 32) wide_offer<T, D, M, true>(tile, j, m - j, q, maxRadius2, minDist, heap, flt, lane);
+      for (int j = 0; j < m; j += 32)
+        wide_offer<T, D, M, 32, true>(tile, j, m - j, q, maxRadius2, minDist, heap, flt, lane, 0xffffffffu);
   }
   if (active) {
-    const int f = heap.store(a.k, lane, a.outIdx + qi * a.k, static_cast<T*>(a.outD2) + qi * a.k);
+    const int f = heap.store(a.k, lane, 0xffffffffu, a.outIdx + qi * a.k, static_cast<T*>(a.outD2) + qi * a.k);
     if (a.found && lane == 0) a.found[qi] = f;
   }
 }
