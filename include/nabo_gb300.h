@@ -65,11 +65,13 @@ extern "C" {
 typedef struct nabo_cuda_params {
   uint32_t struct_size;   /* sizeof(nabo_cuda_params) */
   uint32_t bucketSize;    /* "bucketSize", default 8 (nabo/kdtree_cpu.cpp:230) */
-  int32_t queryOrdering;  /* 1 (default): reorder the queries of searches of
-                             2^18 queries or more along a Morton curve
-                             (smaller searches keep the given order: the
-                             sort costs more than it saves there); 0: keep
-                             the given order */
+  int32_t queryOrdering;  /* 1 (default): reorder the queries of large
+                             searches along a Morton curve (by leaf for more
+                             than 3 dimensions): from about 2^18 queries at
+                             k = 10 in 3-D, fewer for larger k or more
+                             dimensions; smaller searches keep the given
+                             order, the sort costing more than it saves
+                             there; 0: keep the given order */
   int32_t traversal;      /* kd-tree search order. 0 (default) or 1: the
                              reference's visit order (nabo/kdtree_cpu.cpp:
                              367-447), one query per thread; 2: the warp

@@ -122,7 +122,7 @@ class NearestNeighbourSearch:
     is a numpy array (host) or a CUDA torch tensor (device) of shape
     (n, rows); it is copied into the search object. ``params`` accepts the
     reference's ``bucketSize`` key, ``queryOrdering`` (1 = sort the queries
-    of searches of 2^18 or more along a Morton curve, the default) and ``traversal``
+    of large searches along a Morton curve, the default) and ``traversal``
     (0 or 1 the reference's visit order, 2 the warp packet for exact
     searches without touch statistics).
     """
