@@ -111,6 +111,7 @@ struct nabo_cuda_search {
   mutable std::mutex stageLock;
   mutable void* stageHost = nullptr;
   mutable void* stageDev = nullptr;
+  mutable size_t stageBytes = 0;  // size of each block, grown by powers of two
 };
 
 namespace {
@@ -258,6 +259,7 @@ void free_stage(nabo_cuda_search* s) {
   if (s->stageHost) cudaFreeHost(s->stageHost);
   if (s->stageDev) cudaFree(s->stageDev);
   s->stageHost = s->stageDev = nullptr;
+  s->stageBytes = 0;
 }
 
 void free_cloud(DeviceCloud& c) {
@@ -485,7 +487,8 @@ int nabo_cuda_destroy(nabo_cuda_search* s) {
 
 namespace {
 
-constexpr size_t kStageBytes = size_t(4) << 20;
+constexpr size_t kStageBytes = size_t(4) << 20;  // largest call staged
+constexpr size_t kStageMinBytes = size_t(64) << 10;
 
 size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
@@ -527,9 +530,13 @@ int knn_staged(const nabo_cuda_search* s, const void* query, int qRows, int64_t 
   std::unique_lock<std::mutex> lock(s->stageLock, std::try_to_lock);
   if (!lock.owns_lock()) return -1;
   cudaError_t e = cudaSuccess;
-  if (!s->stageHost) {
-    e = cudaMallocHost(&s->stageHost, kStageBytes);
-    if (e == cudaSuccess) e = cudaMalloc(&s->stageDev, kStageBytes);
+  if (s->stageBytes < total) {  // the blocks fit the calls seen so far: page-locked memory is scarce
+    size_t bytes = std::max(kStageMinBytes, s->stageBytes);
+    while (bytes < total) bytes *= 2;
+    free_stage(const_cast<nabo_cuda_search*>(s));
+    e = cudaMallocHost(&s->stageHost, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&s->stageDev, bytes);
+    if (e == cudaSuccess) s->stageBytes = bytes;
     if (e != cudaSuccess) {
       free_stage(const_cast<nabo_cuda_search*>(s));
       return cuda_error(e, "knn staging buffers");
