@@ -609,7 +609,8 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
   const int nChunks = s->pipelineChunks > 0 ? s->pipelineChunks : kPipelineChunks;
   if (nq < kPipelineMin || nChunks < 2) return -1;
   if (!is_pinned(indices) || !is_pinned(dists2)) return -1;
-  const bool ordered = s->searchType == NABO_SEARCH_KDTREE_CUDA && s->queryOrdering != 0;
+  const bool ordered =
+      s->searchType == NABO_SEARCH_KDTREE_CUDA && s->queryOrdering != 0 && worth_sorting(nq, k, s->c.dim);
   if (ordered && s->c.dim > 3) return -1;
   const size_t es = s->c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
   const size_t qBytes = (size_t)((nq - 1) * qStride + qRows) * es;

@@ -13,16 +13,6 @@ namespace nabo_gb300 {
 // Register top-k sizes compiled; a request for k uses the smallest K >= k.
 #define NABO_K_LIST(X) X(1) X(2) X(5) X(8) X(10) X(16) X(32)
 constexpr int kMaxK = 32;
-// Whether a search runs its queries in a sorted order. The sort costs about
-// 130 us almost whatever the size, so it pays only for enough work: measured
-// on GB300, 3-D lidar scans at k = 10 gained from 2^18 queries (440 vs
-// 470 us) and lost below (131 k: 346 vs 260 us), while 8-D clustered clouds
-// at k = 32 gained 30 % at 200 k queries (16.7 vs 23.9 ms). The rule weighs
-// the queries by k and by the dimension.
-inline bool worth_sorting(int64_t nq, int k, int dim) {
-  const double work = (double)nq * (k + 10) / 20.0 * (dim > 3 ? 8.0 : 1.0);
-  return work >= (double)(int64_t(1) << 18);
-}
 // Traversal stack depths compiled; the tree's height selects one.
 constexpr int kStackSmall = 64;
 constexpr int kStackLarge = 256;
