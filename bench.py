@@ -386,10 +386,12 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         base = cpu_baseline(cloud, q, k, cfg)
     clocks = clk.summary()
-    # 3-D query order: Morton keys with the first digit counts, then three
-    # 10-bit radix passes (digit scan + scatter each, counts for the last
-    # two); then the search kernel
-    launches_per_step = 10 if (nq >= 4096 and not args.no_order) else 1
+    # the library sorts the queries when the work outweighs the sort (its
+    # worth_sorting rule, csrc/internal.cuh). A 3-D sort is Morton keys with
+    # the first digit counts, then three 10-bit radix passes (digit scan +
+    # scatter each, counts for the last two); then the search kernel.
+    sorts = not args.no_order and nq * (k + 10) / 20 * (8 if cloud.shape[1] > 3 else 1) >= 2 ** 18
+    launches_per_step = 10 if sorts else 1
     if use_learned:
         launches_per_step += 1  # radius network (misses rerun inside the search kernel)
     out = {
