@@ -89,6 +89,44 @@ using namespace nabo_gb300;
 
 namespace nabo_gb300 {
 constexpr int kPipelineMaxChunks = 64;  // nabo_cuda_params::pipelineChunks
+
+// Two compute streams, a copy stream and the events that order them.
+struct PipeRes {
+  cudaStream_t comp[2] = {};
+  cudaStream_t copy = nullptr;
+  cudaEvent_t ready = nullptr, copied = nullptr;
+  cudaEvent_t compDone[2] = {};
+  cudaEvent_t searched[kPipelineMaxChunks] = {};
+  bool made = false;
+};
+
+inline void destroy_pipe(PipeRes& p) {
+  for (int i = 0; i < 2; ++i) {
+    if (p.comp[i]) cudaStreamDestroy(p.comp[i]);
+    if (p.compDone[i]) cudaEventDestroy(p.compDone[i]);
+  }
+  for (int i = 0; i < kPipelineMaxChunks; ++i)
+    if (p.searched[i]) cudaEventDestroy(p.searched[i]);
+  if (p.copy) cudaStreamDestroy(p.copy);
+  if (p.ready) cudaEventDestroy(p.ready);
+  if (p.copied) cudaEventDestroy(p.copied);
+  p = PipeRes();
+}
+
+inline cudaError_t make_pipe(PipeRes& p) {
+  cudaError_t e = cudaStreamCreateWithFlags(&p.copy, cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&p.comp[i], cudaStreamNonBlocking);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&p.compDone[i], cudaEventDisableTiming);
+  for (int i = 0; i < kPipelineMaxChunks && e == cudaSuccess; ++i)
+    e = cudaEventCreateWithFlags(&p.searched[i], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p.ready, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p.copied, cudaEventDisableTiming);
+  if (e != cudaSuccess)
+    destroy_pipe(p);
+  else
+    p.made = true;
+  return e;
+}
 }  // namespace nabo_gb300
 
 struct nabo_cuda_search {
@@ -112,6 +150,10 @@ struct nabo_cuda_search {
   mutable void* stageHost = nullptr;
   mutable void* stageDev = nullptr;
   mutable size_t stageBytes = 0;  // size of each block, grown by powers of two
+  // Streams and events of the pipelined large-call path, made on first use
+  // and kept (a call made while another holds them makes its own).
+  mutable std::mutex pipeLock;
+  mutable PipeRes pipe;
 };
 
 namespace {
@@ -478,6 +520,7 @@ int nabo_cuda_destroy(nabo_cuda_search* s) {
   DeviceGuard g(s->device);
   free_events(s);
   free_stage(s);
+  destroy_pipe(s->pipe);
   free_cloud(s->c);
   delete s;
   return kOk;
@@ -617,19 +660,21 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
   const size_t outN = (size_t)nq * (size_t)k;
   const int64_t chunk = (nq + nChunks - 1) / nChunks;
   cudaStream_t main = cudaStreamPerThread;
-  cudaStream_t comp[2] = {}, copy = nullptr;
-  cudaEvent_t ready = nullptr, copied = nullptr, searched[kPipelineMaxChunks] = {}, compDone[2] = {};
+  // the object's streams and events, or this call's own while another call holds them
+  PipeRes own;
+  PipeRes* pr = &own;
+  std::unique_lock<std::mutex> lock(s->pipeLock, std::try_to_lock);
+  if (lock.owns_lock() && (s->pipe.made || make_pipe(s->pipe) == cudaSuccess)) pr = &s->pipe;
   unsigned char *dq = nullptr, *dr = nullptr, *dd = nullptr;
   int32_t *di = nullptr, *order = nullptr;
   unsigned long long* dt = nullptr;
   int rc = kOk;
-  cudaError_t e = cudaStreamCreateWithFlags(&copy, cudaStreamNonBlocking);
-  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaStreamCreateWithFlags(&comp[i], cudaStreamNonBlocking);
-  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreateWithFlags(&compDone[i], cudaEventDisableTiming);
-  for (int i = 0; i < nChunks && e == cudaSuccess; ++i)
-    e = cudaEventCreateWithFlags(&searched[i], cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&copied, cudaEventDisableTiming);
+  cudaError_t e = pr == &own ? make_pipe(own) : cudaSuccess;
+  cudaStream_t* const comp = pr->comp;
+  cudaStream_t copy = pr->copy;
+  cudaEvent_t ready = pr->ready, copied = pr->copied;
+  cudaEvent_t* const searched = pr->searched;
+  cudaEvent_t* const compDone = pr->compDone;
   if (e == cudaSuccess) e = scratch_alloc((void**)&dq, qBytes, main);
   if (e == cudaSuccess && maxRadii) e = scratch_alloc((void**)&dr, (size_t)nq * es, main);
   if (e == cudaSuccess) e = scratch_alloc((void**)&di, outN * sizeof(int32_t), main);
@@ -693,15 +738,7 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
     if (p) scratch_free(p, main);
   e = cudaStreamSynchronize(main);
   if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, "knn");
-  for (int i = 0; i < 2; ++i) {
-    if (comp[i]) cudaStreamDestroy(comp[i]);
-    if (compDone[i]) cudaEventDestroy(compDone[i]);
-  }
-  for (int i = 0; i < nChunks; ++i)
-    if (searched[i]) cudaEventDestroy(searched[i]);
-  if (copy) cudaStreamDestroy(copy);
-  if (ready) cudaEventDestroy(ready);
-  if (copied) cudaEventDestroy(copied);
+  if (pr == &own) destroy_pipe(own);
   if (rc == kOk && touched) *touched = touched_result(s, nq, ht);
   return rc;
 }
