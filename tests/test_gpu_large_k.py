@@ -137,3 +137,39 @@ def test_learned_radius_large_k():
     pi, pd = s.knn(q, 40)
     li, ld = m.knn(q, 40)
     H.assert_identical(li, ld, pi, pd, "learned k=40")
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+@pytest.mark.parametrize("dim,bucket", [(16, 8), (3, 17), (8, 33)])
+def test_large_k_wide_records_and_big_buckets(dtype, dim, bucket):
+    """16-dimensional records (the groups' stacks outgrow the default shared
+    memory) and buckets larger than a lane group (a leaf takes several
+    passes of the group)."""
+    nb = _nb()
+    cloud, q = _data(8000, 600, dim, dtype, seed=dim * 100 + bucket)
+    s = nb.NearestNeighbourSearch(cloud, creationOptionFlags=nb.TOUCH_STATISTICS, params={"bucketSize": bucket})
+    orc = O.OracleTree(cloud, bucket_size=bucket, creation_flags=H.TOUCH_STATISTICS)
+    for k in (40, 128, 300):
+        idx, d2 = s.knn(q, k)
+        oi, od, ot = orc.knn(q, k, mode=O.MODE_CANONICAL)
+        H.assert_identical(idx, d2, oi, od, f"dim={dim} bucket={bucket} k={k}")
+        assert s.touched == ot
+
+
+def test_large_k_tall_tree_smaller_blocks():
+    """A double 16-D tree about 110 levels tall: the lane groups' stacks
+    need more shared memory than a block may have, so blocks shrink."""
+    nb = _nb()
+    rng = np.random.default_rng(3)
+    n = 800
+    cloud = rng.random((n, 16)) * 1e-30
+    cloud[:, 0] = 0.5 ** (np.arange(n) / 2)  # crowded along one axis: a deep chain of splits
+    q = cloud[rng.choice(n, 300, replace=False)] * (1 + rng.normal(0, 1e-3, (300, 16)))
+    s = nb.NearestNeighbourSearch(cloud, creationOptionFlags=nb.TOUCH_STATISTICS)
+    orc = O.OracleTree(cloud, creation_flags=H.TOUCH_STATISTICS)
+    assert orc.height > 100 and s.height == orc.height
+    for k in (64, 200):
+        idx, d2 = s.knn(q, k)
+        oi, od, ot = orc.knn(q, k, mode=O.MODE_CANONICAL)
+        H.assert_identical(idx, d2, oi, od, f"tall tree k={k}")
+        assert s.touched == ot
