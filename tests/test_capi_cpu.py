@@ -76,3 +76,32 @@ def test_create_messages_match_oracle():
         with pytest.raises(nb.NaboError) as eg:
             nb.NearestNeighbourSearch(cloud, params={"bucketSize": bs})
         assert str(eo.value) == str(eg.value)
+
+
+def test_c_header_compiles_links_and_runs_as_c99(tmp_path):
+    """include/nabo_gb300.h is a C header: a C99 program includes it with
+    every warning on, links the library and calls what needs no GPU."""
+    import os
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lib = os.path.join(root, "libnabo_gb300", "lib")
+    src = tmp_path / "c_check.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "nabo_gb300.h"\n'
+        "int main(void) {\n"
+        "  nabo_cuda_params p;\n  nabo_cuda_search* s = 0;\n"
+        "  nabo_cuda_params_init(&p);\n"
+        "  if (p.bucketSize != 8 || p.struct_size != sizeof p) return 1;\n"
+        "  if (nabo_cuda_create(NABO_CUDA_FLOAT32, 0, 3, 0, 3, 0, 6, 0, &p, &s) == 0) return 2;\n"
+        '  printf("%s|%s\\n", nabo_cuda_version(), nabo_cuda_last_error());\n'
+        "  return 0;\n}\n")
+    exe = tmp_path / "c_check"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Wpedantic", "-Werror", "-I", os.path.join(root, "include"),
+                    str(src), "-L", lib, "-lnabo_gb300", f"-Wl,-rpath,{lib}", "-o", str(exe)], check=True,
+                   capture_output=True, text=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("0.1.0|") and "Your space must have at least one dimension" in r.stdout
