@@ -933,6 +933,13 @@ def max_ranks(x, world):
 
 def main():
     args = parse()
+    if args.impl == "reference" and args.workload in ("c4", "bf", "latency"):
+        # these workloads time the reference algorithm on the host cores
+        # themselves (the cpu_baseline field of their line)
+        print(json.dumps({"impl": "reference", "workload": args.workload,
+                          "unavailable": "no separate reference arm for this workload: its own line reports the "
+                                         "reference algorithm on the host cores in cpu_baseline"}))
+        return
     if args.workload == "c4":
         run_c4(args)
         return
