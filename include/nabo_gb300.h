@@ -85,7 +85,9 @@ typedef struct nabo_cuda_params {
                               with page-locked result buffers: searched in
                               this many chunks whose downloads overlap the
                               next chunk's search (0 = default, 1 = one
-                              search then one download; at most 64) */
+                              search then one download; at most 64); for a
+                              batch, the cloud groups of
+                              nabo_cuda_batch_run_host */
   int32_t reserved[2];
 } nabo_cuda_params;
 
@@ -282,6 +284,18 @@ int nabo_cuda_batch_knn_device(nabo_cuda_batch* b, const void* queries, double e
  * coordinates written into the same buffers). */
 int nabo_cuda_batch_run(nabo_cuda_batch* b, const void* clouds, const void* queries, double epsilon,
                         unsigned optionFlags, double maxRadius, int32_t* indices, void* dists2, void* stream);
+/* Build + search from HOST buffers (clouds, queries) into HOST result
+ * arrays; returns when the results are there. The device copies are the
+ * batch's own, allocated on first use. When all four buffers are
+ * page-locked, one CUDA graph (captured as for nabo_cuda_batch_run) uploads
+ * the queries during the build and searches the clouds in
+ * params.pipelineChunks groups (0 = 8) of about equal result size, each
+ * group's results downloaded while the next group is searched; otherwise
+ * plain copies surround the device run. Results equal
+ * nabo_cuda_batch_run's. Device calls on this batch still running on
+ * other streams must have finished. */
+int nabo_cuda_batch_run_host(nabo_cuda_batch* b, const void* clouds, const void* queries, double epsilon,
+                             unsigned optionFlags, double maxRadius, int32_t* indices, void* dists2);
 /* Synchronises the device, then info[0] = status bits (1 non-finite input,
  * 2 capacity or level limit exceeded, 4 a tree taller than the search
  * stack), [1] total nodes, [2] tallest tree, [3] top levels run,

@@ -497,7 +497,7 @@ class BatchSearch:
     """
 
     def __init__(self, point_counts, dim: int = 3, dtype=np.float32, bucketSize: int = 8, threadsPerBlock: int = 128,
-                 maxLevels: int = 48):
+                 maxLevels: int = 48, pipelineChunks: int = 0):
         counts = np.ascontiguousarray(np.asarray(point_counts, dtype=np.int64))
         self.point_counts = counts
         self.dim = int(dim)
@@ -507,6 +507,7 @@ class BatchSearch:
         _lib.nabo_cuda_params_init(ctypes.byref(p))
         p.bucketSize = int(bucketSize)
         p.threadsPerBlock = int(threadsPerBlock)
+        p.pipelineChunks = int(pipelineChunks)
         _check(_lib.nabo_cuda_batch_create(_dtype_code(self.dtype), self.dim, len(counts), _ptr(counts),
                                            ctypes.byref(p), int(maxLevels), ctypes.byref(self._b)))
         self.query_counts = None
@@ -562,6 +563,31 @@ class BatchSearch:
                                         ctypes.c_void_p(queries.data_ptr()), float(epsilon), int(optionFlags),
                                         float(maxRadius), ctypes.c_void_p(idx.data_ptr()),
                                         ctypes.c_void_p(d2.data_ptr()), ctypes.c_void_p(st)))
+        return idx, d2
+
+    def run_host(self, clouds, queries, epsilon: float = 0.0, optionFlags: int = 0, maxRadius: float = np.inf,
+                 out=None):
+        """Build + search from host arrays ((total_points, dim) and
+        (total_queries, dim), C order) into host result arrays; returns when
+        they are filled. With page-locked arrays (e.g. pinned torch tensors'
+        ``.numpy()``) the copies overlap the build and search inside one CUDA
+        graph (``pipelineChunks`` cloud groups, 0 = 8)."""
+        if self.query_counts is None:
+            raise NaboError(1, "call set_queries first")
+        c = np.ascontiguousarray(clouds, dtype=self.dtype)
+        q = np.ascontiguousarray(queries, dtype=self.dtype)
+        if c.shape != (int(self.point_counts.sum()), self.dim):
+            raise NaboError(1, f"clouds must be ({int(self.point_counts.sum())}, {self.dim})")
+        if q.shape != (int(self.query_counts.sum()), self.dim):
+            raise NaboError(1, f"queries must be ({int(self.query_counts.sum())}, {self.dim})")
+        if out is None:
+            out = (np.empty(self.result_entries, np.int32), np.empty(self.result_entries, self.dtype))
+        idx, d2 = out
+        if (idx.dtype != np.int32 or d2.dtype != self.dtype or idx.size != self.result_entries
+                or d2.size != self.result_entries or not idx.flags.c_contiguous or not d2.flags.c_contiguous):
+            raise NaboError(1, f"out must be contiguous int32 and {self.dtype} arrays of {self.result_entries} entries")
+        _check(_lib.nabo_cuda_batch_run_host(self._b, _ptr(c), _ptr(q), float(epsilon), int(optionFlags),
+                                             float(maxRadius), _ptr(idx), _ptr(d2)))
         return idx, d2
 
     def status(self) -> dict:

@@ -42,6 +42,7 @@ SIGNATURES = {
     "nabo_cuda_batch_build_device": (_I, [_P, _P, _P]),
     "nabo_cuda_batch_knn_device": (_I, [_P, _P, _D, _U, _D, _P, _P, _P]),
     "nabo_cuda_batch_run": (_I, [_P, _P, _P, _D, _U, _D, _P, _P, _P]),
+    "nabo_cuda_batch_run_host": (_I, [_P, _P, _P, _D, _U, _D, _P, _P]),
     "nabo_cuda_batch_status": (_I, [_P, _P]),
     "nabo_cuda_batch_export_tree": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P]),
     "nabo_cuda_get_info": (_I, [_P, _P]),

@@ -7,11 +7,14 @@
 // its own cloud's tree with that cloud's k. nabo_cuda_batch_run captures
 // build + search into a CUDA graph on first use and replays it afterwards,
 // so a new batch of the same shape (new coordinates written to the same
-// buffers) costs one graph launch.
+// buffers) costs one graph launch. nabo_cuda_batch_run_host does the same
+// from host buffers; page-locked ones are copied inside the graph, on a
+// branch that overlaps the copies with the work (see capture_host).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "internal.cuh"
@@ -56,6 +59,23 @@ struct nabo_cuda_batch {
   void* gD2 = nullptr;
   double gEps = 0.0, gRadius = 0.0;
   unsigned gFlags = 0;
+  // host-buffer runs: the plan's offsets on the host, device copies of the
+  // inputs and results, two streams and the graph of the last page-locked call
+  std::vector<int64_t> hQOff, hOutOff;
+  int groups = 8;
+  void* devClouds = nullptr;
+  void* devQueries = nullptr;
+  int32_t* devIdx = nullptr;
+  void* devD2 = nullptr;
+  cudaStream_t hostStream = nullptr;
+  cudaStream_t copyStream = nullptr;
+  cudaGraphExec_t hostExec = nullptr;
+  const void* hClouds = nullptr;
+  const void* hQuery = nullptr;
+  int32_t* hIdx = nullptr;
+  void* hD2 = nullptr;
+  double hEps = 0.0, hRadius = 0.0;
+  unsigned hFlags = 0;
 };
 
 namespace {
@@ -80,18 +100,49 @@ int pad_dim(int dim) {
   return -1;
 }
 
+void drop_graph(nabo_cuda_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->hostExec) cudaGraphExecDestroy(b->hostExec);
+  b->exec = nullptr;
+  b->hostExec = nullptr;
+}
+
 void free_query_plan(nabo_cuda_batch* b) {
   for (void* p : {(void*)b->dQOff, (void*)b->dOutOff, (void*)b->dK, (void*)b->order, (void*)b->hist,
-                  (void*)b->cell, (void*)b->rank})
+                  (void*)b->cell, (void*)b->rank, b->devQueries, (void*)b->devIdx, b->devD2})
     if (p) cudaFree(p);
   b->dQOff = b->dOutOff = nullptr;
   b->dK = b->order = nullptr;
   b->hist = b->cell = b->rank = nullptr;
+  b->devQueries = b->devD2 = nullptr;
+  b->devIdx = nullptr;
+  b->hQOff.clear();
+  b->hOutOff.clear();
 }
 
-void drop_graph(nabo_cuda_batch* b) {
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  b->exec = nullptr;
+// f(T(), std::integral_constant<int, D>()) for the batch's scalar type and
+// compiled record dimension.
+template <typename F>
+int dispatch(const nabo_cuda_batch* b, F&& f) {
+  using std::integral_constant;
+  if (b->dtype == NABO_CUDA_FLOAT32) {
+    switch (b->dpad) {
+      case 2: return f(float(), integral_constant<int, 2>());
+      case 3: return f(float(), integral_constant<int, 3>());
+      case 4: return f(float(), integral_constant<int, 4>());
+      case 8: return f(float(), integral_constant<int, 8>());
+      case 16: return f(float(), integral_constant<int, 16>());
+    }
+  } else {
+    switch (b->dpad) {
+      case 2: return f(double(), integral_constant<int, 2>());
+      case 3: return f(double(), integral_constant<int, 3>());
+      case 4: return f(double(), integral_constant<int, 4>());
+      case 8: return f(double(), integral_constant<int, 8>());
+      case 16: return f(double(), integral_constant<int, 16>());
+    }
+  }
+  return set_error(kErrInternal, "bad dispatch");
 }
 
 int build(nabo_cuda_batch* b, const void* clouds, cudaStream_t st) {
@@ -121,8 +172,8 @@ int build(nabo_cuda_batch* b, const void* clouds, cudaStream_t st) {
   return set_error(kErrInternal, "bad dispatch");
 }
 
-int search(nabo_cuda_batch* b, const void* query, double eps, unsigned flags, double maxRadius, int32_t* indices,
-           void* dists2, cudaStream_t st) {
+BatchArgs batch_args(const nabo_cuda_batch* b, const void* query, double eps, unsigned flags, double maxRadius,
+                     int32_t* indices, void* dists2) {
   BatchArgs a;
   a.nodes = b->nodes;
   a.recs = b->recs;
@@ -149,16 +200,131 @@ int search(nabo_cuda_batch* b, const void* query, double eps, unsigned flags, do
   a.blockSize = b->blockSize;
   a.recs32 = b->recs32;
   a.coordMax = b->coordMax;
-#define NABO_B_CASE(TT, DD) \
-  if (b->dpad == DD) return knn_batch<TT, DD>(a, st);
-  if (b->dtype == NABO_CUDA_FLOAT32) {
-    NABO_B_CASE(float, 2) NABO_B_CASE(float, 3) NABO_B_CASE(float, 4) NABO_B_CASE(float, 8) NABO_B_CASE(float, 16)
-  } else {
-    NABO_B_CASE(double, 2) NABO_B_CASE(double, 3) NABO_B_CASE(double, 4) NABO_B_CASE(double, 8)
-    NABO_B_CASE(double, 16)
+  return a;
+}
+
+int search(nabo_cuda_batch* b, const void* query, double eps, unsigned flags, double maxRadius, int32_t* indices,
+           void* dists2, cudaStream_t st) {
+  const BatchArgs a = batch_args(b, query, eps, flags, maxRadius, indices, dists2);
+  return dispatch(b, [&](auto t, auto d) { return knn_batch<decltype(t), decltype(d)::value>(a, st); });
+}
+
+size_t elem_bytes(const nabo_cuda_batch* b) { return b->dtype == NABO_CUDA_FLOAT32 ? 4 : 8; }
+
+// Device copies of a host run's inputs and results, streams; made on first use.
+int host_buffers(nabo_cuda_batch* b) {
+  const size_t es = elem_bytes(b);
+  cudaError_t e = cudaSuccess;
+  if (!b->hostStream) e = cudaStreamCreateWithFlags(&b->hostStream, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !b->copyStream) e = cudaStreamCreateWithFlags(&b->copyStream, cudaStreamNonBlocking);
+  if (e == cudaSuccess && !b->devClouds) e = cudaMalloc(&b->devClouds, (size_t)b->nTotal * b->dim * es);
+  if (e == cudaSuccess && !b->devQueries) e = cudaMalloc(&b->devQueries, (size_t)std::max<int64_t>(b->nq, 1) * b->dim * es);
+  if (e == cudaSuccess && !b->devIdx) e = cudaMalloc((void**)&b->devIdx, (size_t)std::max<int64_t>(b->outTotal, 1) * 4);
+  if (e == cudaSuccess && !b->devD2) e = cudaMalloc(&b->devD2, (size_t)std::max<int64_t>(b->outTotal, 1) * es);
+  return e == cudaSuccess ? kOk : cuda_error(e, "batch host-run buffers");
+}
+
+// True if [p, p + bytes) starts and ends in page-locked host memory.
+bool pinned_range(const void* p, size_t bytes) {
+  if (bytes == 0) return true;
+  for (const void* q : {p, (const void*)(static_cast<const unsigned char*>(p) + bytes - 1)}) {
+    cudaPointerAttributes attr;
+    if (cudaPointerGetAttributes(&attr, q) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (attr.type != cudaMemoryTypeHost) return false;
   }
-#undef NABO_B_CASE
-  return set_error(kErrInternal, "bad dispatch");
+  return true;
+}
+
+// Download groups: runs of whole clouds [cuts[i], cuts[i+1]) of about
+// outTotal / groups result entries each (a cloud's results are contiguous
+// only as a whole; see order_batch).
+std::vector<int> group_cuts(const nabo_cuda_batch* b) {
+  std::vector<int> cuts{0};
+  for (int g = 1; g < b->groups; ++g) {
+    const int64_t target = b->outTotal * g / b->groups;
+    int c = cuts.back();
+    while (c < b->nClouds && b->hOutOff[(size_t)c] < target) ++c;
+    if (c > cuts.back() && c < b->nClouds) cuts.push_back(c);
+  }
+  cuts.push_back(b->nClouds);
+  return cuts;
+}
+
+// The page-locked host run as one graph with two branches. Copy branch:
+// clouds up, queries up (during the build), then each group's results down
+// as soon as its search is done. Work branch: forest build once the clouds
+// are in, query order once the queries are in, then one search launch per
+// group of clouds, so downloads overlap the remaining searches.
+int capture_host(nabo_cuda_batch* b, const void* clouds, const void* queries, double eps, unsigned flags,
+                 double maxRadius, int32_t* indices, void* dists2) {
+  const size_t es = elem_bytes(b);
+  cudaStream_t st = b->hostStream, cp = b->copyStream;
+  int rc = kOk;
+  auto check = [&](cudaError_t e, const char* what) {
+    if (rc == kOk && e != cudaSuccess) rc = cuda_error(e, what);
+    return rc == kOk;
+  };
+  // events for the links between the branches, made before the capture
+  std::vector<cudaEvent_t> events((size_t)b->groups + 4, nullptr);
+  for (cudaEvent_t& ev : events) check(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "cudaEventCreate");
+  size_t used = 0;
+  // `to` waits for the work enqueued so far on `from` (tried even after an
+  // error, so that the copy branch is always joined before the capture ends)
+  auto link = [&](cudaStream_t from, cudaStream_t to) {
+    if (used >= events.size() || !events[used]) return;
+    cudaEvent_t ev = events[used++];
+    cudaError_t e = cudaEventRecord(ev, from);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(to, ev, 0);
+    check(e, "stream link");
+  };
+  const BatchArgs a = batch_args(b, b->devQueries, eps, flags, maxRadius, b->devIdx, b->devD2);
+  set_capture_allocations(true);
+  if (rc == kOk && check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture")) {
+    link(st, cp);
+    if (rc == kOk)
+      check(cudaMemcpyAsync(b->devClouds, clouds, (size_t)b->nTotal * b->dim * es, cudaMemcpyHostToDevice, cp),
+            "cloud upload");
+    link(cp, st);
+    if (rc == kOk) rc = build(b, b->devClouds, st);
+    if (rc == kOk && b->nq > 0) {
+      check(cudaMemcpyAsync(b->devQueries, queries, (size_t)b->nq * b->dim * es, cudaMemcpyHostToDevice, cp),
+            "query upload");
+      link(cp, st);
+      if (rc == kOk)
+        rc = dispatch(b, [&](auto t, auto d) { return order_batch<decltype(t), decltype(d)::value>(a, st); });
+      const std::vector<int> cuts = group_cuts(b);
+      for (size_t g = 0; rc == kOk && g + 1 < cuts.size(); ++g) {
+        const int64_t q0 = b->hQOff[(size_t)cuts[g]], q1 = b->hQOff[(size_t)cuts[g + 1]];
+        const int64_t o0 = b->hOutOff[(size_t)cuts[g]], o1 = b->hOutOff[(size_t)cuts[g + 1]];
+        rc = dispatch(b, [&](auto t, auto d) {
+          return search_batch<decltype(t), decltype(d)::value>(a, q0, q1, st);
+        });
+        link(st, cp);
+        if (rc == kOk && o1 > o0) {
+          check(cudaMemcpyAsync(indices + o0, b->devIdx + o0, (size_t)(o1 - o0) * 4, cudaMemcpyDeviceToHost, cp),
+                "index download");
+          check(cudaMemcpyAsync(static_cast<unsigned char*>(dists2) + o0 * es,
+                                static_cast<unsigned char*>(b->devD2) + o0 * es, (size_t)(o1 - o0) * es,
+                                cudaMemcpyDeviceToHost, cp),
+                "distance download");
+        }
+      }
+    }
+    link(cp, st);  // join the copy branch
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(st, &graph);
+    check(e, "cudaStreamEndCapture");
+    if (rc == kOk) check(cudaGraphInstantiate(&b->hostExec, graph, 0), "cudaGraphInstantiate");
+    if (graph) cudaGraphDestroy(graph);
+  }
+  set_capture_allocations(false);
+  for (cudaEvent_t ev : events)
+    if (ev) cudaEventDestroy(ev);
+  if (rc != kOk) b->hostExec = nullptr;
+  return rc;
 }
 
 }  // namespace
@@ -179,7 +345,10 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
   if (params) {
     p.bucketSize = params->bucketSize;
     p.threadsPerBlock = params->threadsPerBlock;
+    p.pipelineChunks = params->pipelineChunks;
   }
+  if (p.pipelineChunks < 0 || p.pipelineChunks > 64)
+    return set_error(kErrArgument, "pipelineChunks must be between 0 and 64");
   if (p.bucketSize < 2)
     return set_error(kErrArgument, "Requested bucket size " + std::to_string(p.bucketSize) + ", but must be larger than 2");
   int64_t total = 0;
@@ -197,6 +366,7 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
   b->bucketSize = p.bucketSize;
   b->maxLevels = maxLevels > 0 ? maxLevels : 48;
   b->blockSize = p.threadsPerBlock > 0 ? p.threadsPerBlock : 128;
+  b->groups = p.pipelineChunks > 0 ? p.pipelineChunks : 8;
   if (b->blockSize != 32 && b->blockSize != 64 && b->blockSize != 128) {
     delete b;
     return set_error(kErrArgument, "threads per block must be 32, 64 or 128");
@@ -234,8 +404,10 @@ int nabo_cuda_batch_destroy(nabo_cuda_batch* b) {
   drop_graph(b);
   free_query_plan(b);
   for (void* p : {(void*)b->dOff, b->recs, b->nodes, (void*)b->nodeOffset, b->rootBox, (void*)b->status, b->recs32,
-                  (void*)b->coordMax})
+                  (void*)b->coordMax, b->devClouds})
     if (p) cudaFree(p);
+  for (cudaStream_t st : {b->hostStream, b->copyStream})
+    if (st) cudaStreamDestroy(st);
   delete b;
   return kOk;
 }
@@ -288,6 +460,8 @@ int nabo_cuda_batch_set_queries(nabo_cuda_batch* b, const int64_t* queryCounts, 
     free_query_plan(b);
     return cuda_error(e, "batch query plan");
   }
+  b->hQOff = std::move(qoff);
+  b->hOutOff = std::move(ooff);
   return kOk;
 }
 
@@ -322,7 +496,8 @@ int nabo_cuda_batch_run(nabo_cuda_batch* b, const void* clouds, const void* quer
   const bool same = b->exec && b->gClouds == clouds && b->gQuery == queries && b->gIdx == indices &&
                     b->gD2 == dists2 && b->gEps == epsilon && b->gFlags == optionFlags && b->gRadius == maxRadius;
   if (!same) {
-    drop_graph(b);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
     cudaStream_t cap;
     cudaError_t e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
     if (e != cudaSuccess) return cuda_error(e, "capture stream");
@@ -355,6 +530,59 @@ int nabo_cuda_batch_run(nabo_cuda_batch* b, const void* clouds, const void* quer
   }
   const cudaError_t e = cudaGraphLaunch(b->exec, st);
   if (e != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
+  return kOk;
+}
+
+int nabo_cuda_batch_run_host(nabo_cuda_batch* b, const void* clouds, const void* queries, double epsilon,
+                             unsigned optionFlags, double maxRadius, int32_t* indices, void* dists2) {
+  if (!b || !clouds) return set_error(kErrArgument, "NULL argument");
+  if (!b->dQOff) return set_error(kErrArgument, "call nabo_cuda_batch_set_queries first");
+  if (optionFlags & NABO_ALLOW_SELF_MATCH)
+    return set_error(kErrUnsupported, "batched searches forbid self matches (the plan checks k <= points - 1)");
+  if (optionFlags > 3) return set_error(kErrArgument, "OR-ed value of option flags is larger than maximal valid value (3)");
+  if (b->nq > 0 && (!queries || !indices || !dists2)) return set_error(kErrArgument, "NULL query or result buffer");
+  Guard g(b->device);
+  int rc = host_buffers(b);
+  if (rc != kOk) return rc;
+  const size_t es = elem_bytes(b);
+  const size_t cBytes = (size_t)b->nTotal * b->dim * es, qBytes = (size_t)b->nq * b->dim * es;
+  const size_t oEntries = (size_t)b->outTotal;
+  cudaStream_t st = b->hostStream;
+  cudaError_t e;
+  if (pinned_range(clouds, cBytes) && pinned_range(queries, qBytes) && pinned_range(indices, oEntries * 4) &&
+      pinned_range(dists2, oEntries * es)) {
+    const bool same = b->hostExec && b->hClouds == clouds && b->hQuery == queries && b->hIdx == indices &&
+                      b->hD2 == dists2 && b->hEps == epsilon && b->hFlags == optionFlags && b->hRadius == maxRadius;
+    if (!same) {
+      if (b->hostExec) cudaGraphExecDestroy(b->hostExec);
+      b->hostExec = nullptr;
+      rc = capture_host(b, clouds, queries, epsilon, optionFlags, maxRadius, indices, dists2);
+      if (rc != kOk) return rc;
+      b->hClouds = clouds;
+      b->hQuery = queries;
+      b->hIdx = indices;
+      b->hD2 = dists2;
+      b->hEps = epsilon;
+      b->hFlags = optionFlags;
+      b->hRadius = maxRadius;
+    }
+    e = cudaGraphLaunch(b->hostExec, st);
+    if (e != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
+  } else {
+    // pageable buffers: plain copies around the device run
+    e = cudaMemcpyAsync(b->devClouds, clouds, cBytes, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && qBytes) e = cudaMemcpyAsync(b->devQueries, queries, qBytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_error(e, "batch upload");
+    rc = nabo_cuda_batch_run(b, b->devClouds, b->devQueries, epsilon, optionFlags, maxRadius, b->devIdx, b->devD2, st);
+    if (rc != kOk) return rc;
+    if (oEntries) {
+      e = cudaMemcpyAsync(indices, b->devIdx, oEntries * 4, cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(dists2, b->devD2, oEntries * es, cudaMemcpyDeviceToHost, st);
+      if (e != cudaSuccess) return cuda_error(e, "batch download");
+    }
+  }
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_error(e, "batch host run");
   return kOk;
 }
 

@@ -121,6 +121,12 @@ struct BatchArgs {
 };
 template <typename T, int D>
 int knn_batch(const BatchArgs& b, cudaStream_t stream);
+// knn_batch in two steps: the leaf order of all queries, then the search
+// of order positions [begin, end).
+template <typename T, int D>
+int order_batch(const BatchArgs& b, cudaStream_t stream);
+template <typename T, int D>
+int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t stream);
 
 // Float copies of double records and their largest coordinate magnitude
 // (recs32 holds n Rec<float, D>; coordMax one device float).

@@ -303,29 +303,37 @@ int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t
 }
 
 // Batched search over a forest: leaf order of all queries (each in its
-// cloud's tree), then one launch of the reference-order kernel. `order`,
+// cloud's tree), then the reference-order kernel over that order. `order`,
 // `hist` (nodeCap entries), `cell` and `rank` (nq each) are caller scratch.
+// The leaves are numbered cloud by cloud, so the order is too: positions
+// [qOffset[c0], qOffset[c1]) hold exactly the queries of clouds c0..c1-1,
+// and search_batch over that range writes exactly their results.
 template <typename T, int D>
-int knn_batch(const BatchArgs& b, cudaStream_t stream) {
+int order_batch(const BatchArgs& b, cudaStream_t stream) {
   if (b.nq == 0) return kOk;
-  const int K = round_k(b.kMax);
-  if (K < 0 && b.kMax > kMaxWideK) return k_unsupported();
   NABO_CUDA_TRY(cudaMemsetAsync(b.hist, 0, (size_t)b.nodeCap * sizeof(uint32_t), stream));
   k_leaf_cells<T, D><<<ceil_div(b.nq, 256), 256, 0, stream>>>(static_cast<const Node<T>*>(b.nodes),
                                                               static_cast<const T*>(b.query), b.nq, b.qStride, b.dim,
                                                               b.cell, b.rank, b.hist, b.qOffset, b.nodeOffset,
                                                               b.nClouds);
-  int rc = order_by_cells(b.cell, b.rank, b.hist, b.nodeCap, b.nq, b.order, stream);
-  if (rc != kOk) return rc;
+  return order_by_cells(b.cell, b.rank, b.hist, b.nodeCap, b.nq, b.order, stream);
+}
+
+template <typename T, int D>
+int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t stream) {
+  if (end <= begin) return kOk;
+  const int K = round_k(b.kMax);
+  if (K < 0 && b.kMax > kMaxWideK) return k_unsupported();
+  int rc = kOk;
   KnnLaunch L;
   std::memset(&L, 0, sizeof(L));
   L.nodes = b.nodes;
   L.recs = b.recs;
   L.query = b.query;
-  L.nq = b.nq;
+  L.nq = end - begin;
   L.qStride = b.qStride;
   L.dim = b.dim;
-  L.order = b.order;
+  L.order = b.order + begin;
   L.k = b.kMax;
   const T eps = (T)b.eps;
   const T e1 = T(1) + eps;
@@ -342,7 +350,7 @@ int knn_batch(const BatchArgs& b, cudaStream_t stream) {
   L.bClouds = b.nClouds;
   L.recs32 = b.recs32;
   L.coordMax = b.coordMax;
-  const int grid = ceil_div(b.nq, b.blockSize);
+  const int grid = ceil_div(L.nq, b.blockSize);
   if (K < 0) {  // some cloud wants more than kMaxK: the whole batch runs one warp per query
     rc = launch_wide_kdtree<T, D>(L, b.kMax, kStackLarge, stream);  // taller trees are flagged by the build
     if (rc != kOk) return rc;
@@ -358,8 +366,17 @@ int knn_batch(const BatchArgs& b, cudaStream_t stream) {
   return kOk;
 }
 
+template <typename T, int D>
+int knn_batch(const BatchArgs& b, cudaStream_t stream) {
+  if (b.nq == 0) return kOk;
+  const int rc = order_batch<T, D>(b, stream);
+  return rc != kOk ? rc : search_batch<T, D>(b, 0, b.nq, stream);
+}
+
 #define NABO_SEARCH_INSTANTIATE(T, D)                                              \
   template int knn_batch<T, D>(const BatchArgs&, cudaStream_t);                    \
+  template int order_batch<T, D>(const BatchArgs&, cudaStream_t);                  \
+  template int search_batch<T, D>(const BatchArgs&, int64_t, int64_t, cudaStream_t); \
   template int knn_leaf_order<T, D>(const DeviceCloud&, const void*, int64_t, int64_t, int32_t*, cudaStream_t); \
   template int knn_kdtree<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
   template int knn_bruteforce<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \

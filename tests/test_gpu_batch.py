@@ -160,3 +160,104 @@ def test_autotuner_choice_is_exact():
         H.assert_identical(bi[c], bd[c], oi, od, f"tuned cloud {c}")
     again = autotune.tune(clouds, queries, ks, sample=16, repeats=2)
     assert again["cached"]
+
+
+def _host_buffers(pinned):
+    """Copies of arrays in page-locked (pinned=True) or ordinary host memory;
+    the pinned tensors stay referenced by the returned list."""
+    import torch
+    hold = []
+
+    def host(a):
+        a = np.ascontiguousarray(a)
+        if not pinned:
+            return a.copy()
+        t = torch.from_numpy(a).pin_memory()
+        hold.append(t)
+        return t.numpy()
+    return host, hold
+
+
+def _device_flat(b, clouds, queries, **kw):
+    """The device-buffer run (graph) of batch b: flat host copies of its results."""
+    import torch
+    tc = torch.from_numpy(np.concatenate(clouds)).cuda()
+    tq = torch.from_numpy(np.concatenate(queries)).cuda()
+    idx, d2 = b.run(tc, tq, **kw)
+    torch.cuda.synchronize()
+    return idx.cpu().numpy(), d2.cpu().numpy()
+
+
+@pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
+@pytest.mark.parametrize("dtype", [np.float32, np.float64], ids=["f32", "f64"])
+def test_host_run_equals_device_run(pinned, dtype):
+    """nabo_cuda_batch_run_host: same results as the device run, replays on
+    new data written into the same host buffers, recaptures on new
+    arguments; one cloud without queries."""
+    nb = _nb()
+    clouds, queries, ks = _batch_data(50, 300, 30000, seed=5, dtype=dtype)
+    queries[7] = queries[7][:0]
+    b = nb.BatchSearch([c.shape[0] for c in clouds], dtype=dtype)
+    b.set_queries([q.shape[0] for q in queries], ks)
+    host, hold = _host_buffers(pinned)
+    hc, hq = host(np.concatenate(clouds)), host(np.concatenate(queries))
+    out = (host(np.full(b.result_entries, -7, np.int32)), host(np.full(b.result_entries, -1, dtype)))
+    gi, gd = b.run_host(hc, hq, out=out)
+    assert gi is out[0] and gd is out[1]
+    di, dd = _device_flat(b, clouds, queries)
+    H.assert_identical(gi[:, None], gd[:, None], di[:, None], dd[:, None], "host run vs device run")
+    for c in (0, 1, 7, 20, 49):
+        oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        H.assert_identical(b.split(gi)[c], b.split(gd)[c], oi, od, f"cloud {c}")
+    # new coordinates in the same buffers: the captured graph reads them
+    clouds2 = [(c * 1.5 + 0.25).astype(dtype) for c in clouds]
+    queries2 = [(q * 1.5 + 0.25).astype(dtype) for q in queries]
+    hc[:] = np.concatenate(clouds2)
+    hq[:] = np.concatenate(queries2)
+    gi, gd = b.run_host(hc, hq, out=out)
+    for c in (0, 3, 33):
+        oi, od, _ = O.OracleTree(clouds2[c]).knn(queries2[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        H.assert_identical(b.split(gi)[c], b.split(gd)[c], oi, od, f"replay cloud {c}")
+    # another radius: a new capture, same results as the device run
+    gi, gd = b.run_host(hc, hq, maxRadius=0.02, out=out)
+    di, dd = _device_flat(b, clouds2, queries2, maxRadius=0.02)
+    H.assert_identical(gi[:, None], gd[:, None], di[:, None], dd[:, None], "host run with a radius")
+    assert (gi == -1).any() and (gi >= 0).any()
+    del hold
+
+
+@pytest.mark.parametrize("chunks", [1, 3, 64])
+def test_host_run_groups_and_wide_k(chunks):
+    """Cloud groups of the pinned host run (one, three, more groups than
+    clouds), with a cloud whose k sends the batch to the warp-per-query
+    kernel."""
+    nb = _nb()
+    clouds, queries, _ = _batch_data(12, 300, 5000, seed=6)
+    rng = np.random.default_rng(6)
+    ks = np.minimum(rng.choice([1, 5, 40], len(clouds)), [c.shape[0] - 1 for c in clouds]).astype(np.int32)
+    ks[5] = min(40, clouds[5].shape[0] - 1)
+    b = nb.BatchSearch([c.shape[0] for c in clouds], pipelineChunks=chunks)
+    b.set_queries([q.shape[0] for q in queries], ks)
+    host, hold = _host_buffers(True)
+    hc, hq = host(np.concatenate(clouds)), host(np.concatenate(queries))
+    out = (host(np.zeros(b.result_entries, np.int32)), host(np.zeros(b.result_entries, np.float32)))
+    gi, gd = b.run_host(hc, hq, out=out)
+    for c in range(len(clouds)):
+        oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        H.assert_identical(b.split(gi)[c], b.split(gd)[c], oi, od, f"cloud {c} k={ks[c]}")
+    del hold
+
+
+def test_host_run_argument_errors():
+    nb = _nb()
+    clouds, queries, ks = _batch_data(6, 300, 2000, seed=7)
+    b = nb.BatchSearch([c.shape[0] for c in clouds])
+    with pytest.raises(nb.NaboError, match="set_queries"):
+        b.run_host(np.concatenate(clouds), np.concatenate(queries))
+    b.set_queries([q.shape[0] for q in queries], ks)
+    with pytest.raises(nb.NaboError, match="clouds must be"):
+        b.run_host(np.concatenate(clouds)[1:], np.concatenate(queries))
+    with pytest.raises(nb.NaboError, match="self match"):
+        b.run_host(np.concatenate(clouds), np.concatenate(queries), optionFlags=nb.ALLOW_SELF_MATCH)
+    with pytest.raises(nb.NaboError, match="pipelineChunks"):
+        nb.BatchSearch([c.shape[0] for c in clouds], pipelineChunks=65)
