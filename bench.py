@@ -556,7 +556,7 @@ def run_batched(args):
     b.run_host(*host_in, out=host_out)  # first call captures its graph
     e2e_same = bool(np.array_equal(host_out[0], out[0].cpu().numpy())
                     and np.array_equal(host_out[1].view(np.uint32), out[1].cpu().numpy().view(np.uint32)))
-    e2e_steps = args.e2e_steps or 3
+    e2e_steps = args.e2e_steps or max(10, args.steps)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         b.run_host(*host_in, out=host_out)

@@ -19,8 +19,10 @@
 //        pass 1/2 the reference's two Hoare-style passes: the i-th misplaced
 //                 element from the left trades places with the i-th
 //                 misplaced element from the right. Ranks come from a
-//                 device-wide exclusive scan of the misplaced flags, the
-//                 pairs are written to two slot tables and swapped.
+//                 device-wide exclusive scan of the misplaced flags (block
+//                 sums, their scan, then the block scans again writing each
+//                 element straight to its pair slot), and the pairs in the
+//                 two slot tables are swapped.
 //        finalize leftCount, node, children
 //   3. small segments: one thread each runs the reference's sequential
 //      recursion (as an explicit stack in global scratch) on its points,
@@ -421,20 +423,32 @@ __device__ __forceinline__ int2 misplaced(const T* __restrict__ val, const int* 
   return f;
 }
 
-// Block b owns tiles [b * tiles, (b + 1) * tiles) of kBlock positions.
+// Block b owns tiles [b * tiles, (b + 1) * tiles) of kBlock positions and
+// scans their misplaced flags in position order. Besides its total it
+// records, for each segment, the block's running count at the segment's
+// first position (exclusive) and last position (inclusive): with the block
+// prefixes these give the segment's global range of ranks, so the pairing
+// pass needs no per-position rank array.
 template <typename T>
 __global__ void k_flag_sums(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                            int pass, int tiles, int2* blockSums, const LevelState* st) {
+                            int pass, int tiles, int2* blockSums, int2* segFirst, int2* segLast,
+                            const LevelState* st) {
   if (st->nseg == 0) return;
-  int2 acc = make_int2(0, 0);
+  int2 carry = make_int2(0, 0);
   for (int t = 0; t < tiles; ++t) {
     const int64_t p = ((int64_t)blockIdx.x * tiles + t) * kBlock + threadIdx.x;
     int s;
-    acc = add2(acc, misplaced(val, segOf, n, L, pass, p < n ? (int)p : n, &s));
+    const int2 f = misplaced(val, segOf, n, L, pass, p < n ? (int)p : n, &s);
+    int2 total;
+    const int2 ex = add2(block_excl_scan(f, &total), carry);
+    if (s >= 0) {
+      const int first = L.start[s];
+      if (p == first) segFirst[s] = ex;
+      if (p == first + L.count[s] - 1) segLast[s] = add2(ex, f);
+    }
+    carry = add2(carry, total);
   }
-  int2 total;
-  block_excl_scan(acc, &total);
-  if (threadIdx.x == 0) blockSums[blockIdx.x] = total;
+  if (threadIdx.x == 0) blockSums[blockIdx.x] = carry;
 }
 
 // Single block: exclusive scan of the per-block sums; the grand total goes
@@ -461,47 +475,51 @@ __global__ void k_scan_block_sums(int2* sums, int nb, int2* total, const LevelSt
   if (threadIdx.x == 0) *total = t;
 }
 
+// The pairs of both passes: the i-th misplaced element from the left of a
+// segment trades with its i-th misplaced element from the right. A left
+// element's slot is its global rank among the left-misplaced; a right
+// element of rank j among its segment's m goes to slot base + m - 1 - j,
+// base being the segment's first global rank (so both tables list the
+// segment's pairs in the same slots).
 template <typename T>
-__global__ void k_flag_ranks(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                             int pass, int tiles, const int2* blockPrefix, int2* S, const LevelState* st) {
+__global__ void k_flag_pairs(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
+                             int pass, int tiles, const int2* __restrict__ blockPrefix,
+                             const int2* __restrict__ segFirst, const int2* __restrict__ segLast, int* pairA,
+                             int* pairB, int cap, const LevelState* st) {
   if (st->nseg == 0) return;
+  const int perBlock = tiles * kBlock;
   int2 carry = blockPrefix[blockIdx.x];
   for (int t = 0; t < tiles; ++t) {
     const int64_t p = ((int64_t)blockIdx.x * tiles + t) * kBlock + threadIdx.x;
     int s;
     const int2 f = misplaced(val, segOf, n, L, pass, p < n ? (int)p : n, &s);
     int2 total;
-    const int2 ex = block_excl_scan(f, &total);
-    if (p < n) S[p] = add2(ex, carry);
+    const int2 ex = add2(block_excl_scan(f, &total), carry);
+    if (f.x && ex.x < cap) pairA[ex.x] = (int)p;
+    if (f.y) {
+      const int first = L.start[s];
+      const int last = first + L.count[s] - 1;
+      const int base = blockPrefix[first / perBlock].y + segFirst[s].y;
+      const int end = blockPrefix[last / perBlock].y + segLast[s].y;  // base + m
+      const int slot = base + end - 1 - ex.y;
+      if (slot >= 0 && slot < cap) pairB[slot] = (int)p;
+    }
     carry = add2(carry, total);
   }
 }
 
-template <typename T>
-__global__ void k_pairs(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                        int pass, const int2* __restrict__ S, int* pairA, int* pairB, const LevelState* st) {
-  if (st->nseg == 0) return;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-    int s;
-    const int2 f = misplaced(val, segOf, n, L, pass, p, &s);
-    if (f.x) pairA[S[p].x] = p;
-    if (f.y) {
-      const int st = L.start[s];
-      const int base = S[st].y;
-      const int m = S[st + L.count[s]].y - base;
-      const int j = S[p].y - base;
-      const int slot = base + m - 1 - j;
-      if (slot >= 0 && slot < n) pairB[slot] = p;
-    }
-  }
-}
-
+// A pair outside [0, n) (a slot the pairing missed) is skipped and flagged
+// in *err, which the build status reports.
 template <typename T, int D>
 __global__ void k_swap(Rec<T, D>* recs, T* val, const int* __restrict__ pairA, const int* __restrict__ pairB,
-                       const int2* __restrict__ total, int cap) {
+                       const int2* __restrict__ total, int cap, int n, int* err) {
   const int m = min(cap, min(total->x, total->y));
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
     const int a = pairA[t], b = pairB[t];
+    if ((unsigned)a >= (unsigned)n || (unsigned)b >= (unsigned)n) {
+      atomicOr(err, 1);
+      continue;
+    }
     const Rec<T, D> ra = recs[a];
     recs[a] = recs[b];
     recs[b] = ra;
@@ -1186,8 +1204,10 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
 
   // working arrays
   int* segOf;
-  int2* S;
+  int2* passTotal;
   int2* blockSums;
+  int2* segFirst;
+  int2* segLast;
   int* pairA;
   int* pairB;
   int* counters;
@@ -1204,8 +1224,10 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   T* val;
   NABO_CUDA_TRY(sc.get(&segOf, n));
   NABO_CUDA_TRY(sc.get(&val, n));
-  NABO_CUDA_TRY(sc.get(&S, n + 1));
+  NABO_CUDA_TRY(sc.get(&passTotal, 1));
   NABO_CUDA_TRY(sc.get(&blockSums, nb));
+  NABO_CUDA_TRY(sc.get(&segFirst, segCap));
+  NABO_CUDA_TRY(sc.get(&segLast, segCap));
   NABO_CUDA_TRY(sc.get(&pairA, pairCap));
   NABO_CUDA_TRY(sc.get(&pairB, pairCap));
   NABO_CUDA_TRY(sc.get(&counters, 4));
@@ -1263,11 +1285,12 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
     k_cut<T><<<sg, 128, 0, stream>>>(cur, st);
     k_count<T><<<grid, kBlock, 0, stream>>>(val, segOf, N, cur, st);
     for (int pass = 1; pass <= 2; ++pass) {
-      k_flag_sums<T><<<scanBlocks, kBlock, 0, stream>>>(val, segOf, N, cur, pass, tiles, blockSums, st);
-      k_scan_block_sums<<<1, kBlock, 0, stream>>>(blockSums, scanBlocks, S + n, st);
-      k_flag_ranks<T><<<scanBlocks, kBlock, 0, stream>>>(val, segOf, N, cur, pass, tiles, blockSums, S, st);
-      k_pairs<T><<<grid, kBlock, 0, stream>>>(val, segOf, N, cur, pass, S, pairA, pairB, st);
-      k_swap<T, D><<<grid, kBlock, 0, stream>>>(recs, val, pairA, pairB, S + n, (int)pairCap);
+      k_flag_sums<T><<<scanBlocks, kBlock, 0, stream>>>(val, segOf, N, cur, pass, tiles, blockSums, segFirst,
+                                                        segLast, st);
+      k_scan_block_sums<<<1, kBlock, 0, stream>>>(blockSums, scanBlocks, passTotal, st);
+      k_flag_pairs<T><<<scanBlocks, kBlock, 0, stream>>>(val, segOf, N, cur, pass, tiles, blockSums, segFirst,
+                                                         segLast, pairA, pairB, (int)pairCap, st);
+      k_swap<T, D><<<grid, kBlock, 0, stream>>>(recs, val, pairA, pairB, passTotal, (int)pairCap, N, counters + 3);
     }
     k_finalize<T><<<sg, 128, 0, stream>>>(cur, nxt, st, top, small, counters, dim, (int)segCap, (int)smallCap,
                                           (int)topCap);
@@ -1352,6 +1375,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   NABO_CUDA_TRY(cudaMemcpyAsync(hbox, rootBox, sizeof(hbox), cudaMemcpyDeviceToHost, stream));
   NABO_CUDA_TRY(cudaStreamSynchronize(stream));
   const int64_t total = hno[1];
+  if (hs[1]) return set_error(kErrInternal, "kd-tree build: internal check failed (capacity or pairing)");
   if (total <= 0 || total > nodeCap) return set_error(kErrInternal, "kd-tree build: inconsistent node count");
   if (total - 1 > (int64_t)kMaxNodeIndex)
     return set_error(kErrUnsupported, "kd-tree build: the tree has more nodes than the device layout indexes");
