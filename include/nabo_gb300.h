@@ -83,11 +83,11 @@ typedef struct nabo_cuda_params {
                               (0 = 128); chosen by the autotuner */
   int32_t pipelineChunks;  /* host-buffer searches of 2^18 queries or more
                               with page-locked result buffers: searched in
-                              this many chunks whose downloads overlap the
-                              next chunk's search (0 = default, 1 = one
-                              search then one download; at most 64); for a
-                              batch, the cloud groups of
-                              nabo_cuda_batch_run_host */
+                              this many chunks of shrinking size whose
+                              downloads overlap the next chunk's search
+                              (0 = default, 1 = one search then one
+                              download; at most 64); for a batch, the cloud
+                              groups of nabo_cuda_batch_run_host */
   int32_t reserved[2];
 } nabo_cuda_params;
 

@@ -88,7 +88,7 @@ int cuda_error(cudaError_t e, const char* what) {
 using namespace nabo_gb300;
 
 namespace nabo_gb300 {
-constexpr int kPipelineMaxChunks = 64;  // nabo_cuda_params::pipelineChunks
+constexpr int kPipelineMaxChunks = kMaxQueryChunks;  // nabo_cuda_params::pipelineChunks
 
 // Two compute streams, a copy stream and the events that order them.
 struct PipeRes {
@@ -286,9 +286,9 @@ int knn_given_order_any(const nabo_cuda_search* h, const KnnArgs& a, const int32
   NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_kdtree_given_order<T, D>(h->c, a, order, st)));
 }
 
-int chunk_order_any(const nabo_cuda_search* h, const void* query, int64_t nq, int64_t qStride, int64_t chunk,
-                    int32_t* order, cudaStream_t st) {
-  NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_chunk_order<T, D>(h->c, query, nq, qStride, chunk, order, st)));
+int chunk_order_any(const nabo_cuda_search* h, const void* query, int64_t nq, int64_t qStride,
+                    const QueryChunks& chunks, int32_t* order, cudaStream_t st) {
+  NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_chunk_order<T, D>(h->c, query, nq, qStride, chunks, order, st)));
 }
 
 void free_events(nabo_cuda_search* s) {
@@ -634,9 +634,10 @@ bool is_pinned(const void* p) {
 
 // Large host-buffer searches whose result buffers are pinned: the queries
 // are uploaded and ordered once, then searched in pipelineChunks
-// consecutive chunks, one launch each on alternating streams, and a copy
-// stream downloads each chunk's result rows as soon as its search is done,
-// while the next chunk searches. With query ordering the order is
+// consecutive chunks of shrinking size (the last chunk's download is the
+// part that no search hides), one launch each on alternating streams, and a
+// copy stream downloads each chunk's result rows as soon as its search is
+// done, while the next chunk searches. With query ordering the order is
 // chunk-major (each chunk's queries along the Morton curve), so a chunk's
 // launch covers a contiguous part of one order. Results are those of one
 // call: each query's result goes to its own column and the touched counter
@@ -644,7 +645,7 @@ bool is_pinned(const void* p) {
 // buffer is not pinned, or the cloud has more than 3 dimensions with
 // query ordering on.
 constexpr int64_t kPipelineMin = int64_t(1) << 18;
-constexpr int kPipelineChunks = 4;  // default
+constexpr int kPipelineChunks = 5;  // default
 
 int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride, int k,
                   double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii, int32_t* indices,
@@ -658,7 +659,7 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
   const size_t es = s->c.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
   const size_t qBytes = (size_t)((nq - 1) * qStride + qRows) * es;
   const size_t outN = (size_t)nq * (size_t)k;
-  const int64_t chunk = (nq + nChunks - 1) / nChunks;
+  const QueryChunks chunks = shrinking_chunks(nq, nChunks);
   cudaStream_t main = cudaStreamPerThread;
   // the object's streams and events, or this call's own while another call holds them
   PipeRes own;
@@ -685,12 +686,12 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
   if (e == cudaSuccess && maxRadii) e = cudaMemcpyAsync(dr, maxRadii, (size_t)nq * es, cudaMemcpyHostToDevice, main);
   if (e == cudaSuccess) e = cudaMemsetAsync(dt, 0, sizeof(unsigned long long), main);
   if (e != cudaSuccess) rc = cuda_error(e, "knn pipeline setup");
-  if (rc == kOk && ordered) rc = chunk_order_any(s, dq, nq, qStride, chunk, order, main);
+  if (rc == kOk && ordered) rc = chunk_order_any(s, dq, nq, qStride, chunks, order, main);
   if (rc == kOk && cudaEventRecord(ready, main) != cudaSuccess) rc = cuda_error(cudaGetLastError(), "knn pipeline");
-  for (int c = 0; c < nChunks && rc == kOk; ++c) {
-    const int64_t c0 = std::min<int64_t>(nq, chunk * c), c1 = std::min<int64_t>(nq, chunk * (c + 1));
+  for (int c = 0; c < chunks.n && rc == kOk; ++c) {
+    const int64_t c0 = c ? chunks.end[c - 1] : 0, c1 = chunks.end[c];
     const int64_t m = c1 - c0;
-    if (m <= 0) break;
+    if (m <= 0) continue;
     cudaStream_t cs = comp[c & 1];
     e = cudaStreamWaitEvent(cs, ready, 0);
     if (e != cudaSuccess) {

@@ -39,6 +39,17 @@ int cuda_error(cudaError_t e, const char* what);
 // users of cudaMallocAsync are unaffected.
 cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream);
 cudaError_t scratch_free(void* p, cudaStream_t stream);
+// Consecutive query chunks of a pipelined search: chunk c is the queries
+// [c ? end[c-1] : 0, end[c]).
+constexpr int kMaxQueryChunks = 64;
+struct QueryChunks {
+  int n = 0;
+  int64_t end[kMaxQueryChunks] = {};
+};
+// n chunks of shrinking size (weights n, n-1, ..., 1), so that the last
+// chunk's results, downloaded after every search has finished, are few.
+QueryChunks shrinking_chunks(int64_t nq, int n);
+
 // While set (calling thread only), scratch_alloc uses cudaMallocAsync so the
 // allocations can be captured into a CUDA graph.
 void set_capture_allocations(bool on);
@@ -186,7 +197,7 @@ int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream);
 template <typename T, int D>
 int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream);
 template <typename T, int D>
-int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int64_t chunk,
+int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, const QueryChunks& chunks,
                     int32_t* order, cudaStream_t stream);
 template <typename T, int D>
 int knn_leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int32_t* order,
@@ -227,13 +238,13 @@ const void* radius_model_owner(const RadiusModel& m);
 int radius_model_k(const RadiusModel& m);
 
 // Query ordering: writes a permutation of [0, nq) grouping nearby queries
-// (a stable sort by Morton code). With chunk > 0 the permutation is
-// chunk-major: the queries [c*chunk, (c+1)*chunk) come before those of
-// chunk c+1, in Morton order among themselves (the chunk number takes the
-// top bits of a 32-bit key, so more chunks leave a coarser curve).
+// (a stable sort by Morton code). With chunks (n > 1) the permutation is
+// chunk-major: chunk c's queries come before those of chunk c+1, in Morton
+// order among themselves (the chunk number takes the top bits of a 32-bit
+// key, so more chunks leave a coarser curve).
 template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
-                  int32_t* dOrder, cudaStream_t stream, int64_t chunk = 0);
+                  int32_t* dOrder, cudaStream_t stream, const QueryChunks* chunks = nullptr);
 
 // Counting-sort placement: dHist holds per-cell counts (turned into offsets
 // in place), dCell/dRank each query's cell and rank inside it.

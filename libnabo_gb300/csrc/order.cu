@@ -93,7 +93,10 @@ struct CellParams {
   int dims;
   int bits;
   int shift;
-  int64_t chunk;  // > 0: element i's key carries i / chunk above its dims*bits Morton bits
+  // nChunks > 1: element i's key carries its chunk number (the count of
+  // chunkEnd entries <= i) above its dims*bits Morton bits
+  int nChunks;
+  int64_t chunkEnd[kMaxQueryChunks];
 };
 
 __device__ __forceinline__ uint32_t spread3_10(uint32_t x) {
@@ -236,7 +239,11 @@ __global__ void k_morton_tiles(const T* __restrict__ q, int64_t n, int64_t qStri
 #pragma unroll
     for (int u = 0; u < kPre; ++u) {
       const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
-      if (p.chunk > 0) kk[u] |= (uint32_t)(i / p.chunk) << (p.bits * p.dims);
+      if (p.nChunks > 1) {
+        uint32_t cid = 0;
+        for (int c = 0; c + 1 < p.nChunks; ++c) cid += i >= p.chunkEnd[c] ? 1u : 0u;
+        kk[u] |= cid << (p.bits * p.dims);
+      }
       if (i < n) key[i] = kk[u];
       count_digit(h, i < n, kk[u] & (kRadix - 1));
     }
@@ -456,17 +463,18 @@ int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaSt
 
 template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
-                  int32_t* dOrder, cudaStream_t stream, int64_t chunk) {
+                  int32_t* dOrder, cudaStream_t stream, const QueryChunks* chunks) {
   if (nq <= 0) return kOk;
   if (nq > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
   CellParams p;
   p.dims = std::min(dim, kMortonDims);
   p.bits = 30 / p.dims;
   p.shift = 0;
-  p.chunk = chunk > 0 && chunk < nq ? chunk : 0;
+  p.nChunks = chunks && chunks->n > 1 ? std::min(chunks->n, kMaxQueryChunks) : 0;
+  for (int c = 0; c < kMaxQueryChunks; ++c) p.chunkEnd[c] = c < p.nChunks ? chunks->end[c] : nq;
   int chunkBits = 0;
-  if (p.chunk > 0) {
-    while ((int64_t(1) << chunkBits) < ceil_div(nq, p.chunk)) ++chunkBits;
+  if (p.nChunks > 1) {
+    while ((1 << chunkBits) < p.nChunks) ++chunkBits;
     // the chunk number above the Morton code, within 32 bits
     p.bits = std::min(p.bits, (32 - chunkBits) / p.dims);
   }
@@ -496,9 +504,21 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
   return rc;
 }
 
+QueryChunks shrinking_chunks(int64_t nq, int n) {
+  QueryChunks q;
+  q.n = std::max(1, std::min(n, kMaxQueryChunks));
+  const int64_t total = (int64_t)q.n * (q.n + 1) / 2;
+  int64_t w = 0;
+  for (int c = 0; c < q.n; ++c) {
+    w += q.n - c;
+    q.end[c] = c + 1 == q.n ? nq : (int64_t)((double)nq * (double)w / (double)total);
+  }
+  return q;
+}
+
 template int order_queries<float>(const float*, int64_t, int64_t, int, const double*, const double*, int32_t*,
-                                  cudaStream_t, int64_t);
+                                  cudaStream_t, const QueryChunks*);
 template int order_queries<double>(const double*, int64_t, int64_t, int, const double*, const double*, int32_t*,
-                                   cudaStream_t, int64_t);
+                                   cudaStream_t, const QueryChunks*);
 
 }  // namespace nabo_gb300

@@ -292,14 +292,14 @@ int knn_leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t 
   return rc;
 }
 
-// Chunk-major Morton order (queries [c*chunk, (c+1)*chunk) first by chunk,
-// then along the curve) for a search split into consecutive query chunks,
-// one launch each; clouds of up to 3 dimensions.
+// Chunk-major Morton order (first by chunk, then along the curve) for a
+// search split into consecutive query chunks, one launch each; clouds of up
+// to 3 dimensions.
 template <typename T, int D>
-int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int64_t chunk,
+int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, const QueryChunks& chunks,
                     int32_t* order, cudaStream_t stream) {
   if (c.dim > 3) return set_error(kErrUnsupported, "chunked query order: more than 3 dimensions");
-  return order_queries<T>(static_cast<const T*>(query), nq, qStride, c.dim, c.lo, c.hi, order, stream, chunk);
+  return order_queries<T>(static_cast<const T*>(query), nq, qStride, c.dim, c.lo, c.hi, order, stream, &chunks);
 }
 
 // Batched search over a forest: leaf order of all queries (each in its
@@ -381,6 +381,7 @@ int knn_batch(const BatchArgs& b, cudaStream_t stream) {
   template int knn_kdtree<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
   template int knn_bruteforce<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
   template int knn_kdtree_given_order<T, D>(const DeviceCloud&, const KnnArgs&, const int32_t*, cudaStream_t); \
-  template int knn_chunk_order<T, D>(const DeviceCloud&, const void*, int64_t, int64_t, int64_t, int32_t*, cudaStream_t);
+  template int knn_chunk_order<T, D>(const DeviceCloud&, const void*, int64_t, int64_t, const QueryChunks&, int32_t*, \
+                                     cudaStream_t);
 
 }  // namespace nabo_gb300
