@@ -312,10 +312,13 @@ __global__ void k_prepare(SegLevel<T> L, const LevelState* st, int dim) {
 
 // Also keeps each position's coordinate along its segment's cut dimension in
 // `val` for the rest of the level (4 or 8 bytes instead of a whole record;
-// the swaps move it with the records).
+// the swaps move it with the records). With `remap` (every level but the
+// first) it first moves each position to the segment it fell into at the
+// previous level `prev`: its left or right child segment, -1 once that is a
+// small segment.
 template <typename T, int D>
-__global__ void k_minmax(const Rec<T, D>* __restrict__ recs, const int* __restrict__ segOf, int n, SegLevel<T> L,
-                         const LevelState* st, T* __restrict__ val) {
+__global__ void k_minmax(const Rec<T, D>* __restrict__ recs, int* __restrict__ segOf, int n, SegLevel<T> L,
+                         SegLevel<T> prev, int remap, const LevelState* st, T* __restrict__ val) {
   using Key = typename KeyOf<T>::type;
   if (st->nseg == 0) return;
   for (int64_t tile = blockIdx.x; tile * kBlock < n; tile += gridDim.x) {
@@ -324,6 +327,10 @@ __global__ void k_minmax(const Rec<T, D>* __restrict__ recs, const int* __restri
     Key kmin = 0, kmax = 0;
     if (p < n) {
       s = segOf[p];
+      if (remap && s >= 0) {
+        s = (int)p - prev.start[s] < prev.leftCount[s] ? prev.newLeft[s] : prev.newRight[s];
+        segOf[p] = s;
+      }
       if (s >= 0) {
         const T v = recs[p].p.c[L.cutDim[s]];
         val[p] = v;
@@ -614,17 +621,6 @@ __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, const LevelState* st
       top.right[node] = ref;
       L.newRight[s] = newSeg;
     }
-  }
-}
-
-template <typename T>
-__global__ void k_update_segof(int* segOf, int n, SegLevel<T> L, const LevelState* st) {
-  if (st->nseg == 0) return;
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-    const int s = segOf[p];
-    if (s < 0) continue;
-    const int loc = p - L.start[s];
-    segOf[p] = loc < L.leftCount[s] ? L.newLeft[s] : L.newRight[s];
   }
 }
 
@@ -1281,7 +1277,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
       if (level >= lvCap) return set_error(kErrUnsupported, "kd-tree build: too many levels");
     }
     k_prepare<T><<<sg, 128, 0, stream>>>(cur, st, dim);
-    k_minmax<T, D><<<grid, kBlock, 0, stream>>>(recs, segOf, N, cur, st, val);
+    k_minmax<T, D><<<grid, kBlock, 0, stream>>>(recs, segOf, N, cur, nxt, level > 0 ? 1 : 0, st, val);
     k_cut<T><<<sg, 128, 0, stream>>>(cur, st);
     k_count<T><<<grid, kBlock, 0, stream>>>(val, segOf, N, cur, st);
     for (int pass = 1; pass <= 2; ++pass) {
@@ -1294,7 +1290,6 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
     }
     k_finalize<T><<<sg, 128, 0, stream>>>(cur, nxt, st, top, small, counters, dim, (int)segCap, (int)smallCap,
                                           (int)topCap);
-    k_update_segof<T><<<grid, kBlock, 0, stream>>>(segOf, N, cur, st);
     k_advance<<<1, 1, 0, stream>>>(st, counters, lv, lv + lvCap, lvCap);
     NABO_CUDA_TRY(cudaGetLastError());
     std::swap(cur, nxt);
