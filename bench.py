@@ -166,7 +166,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(cloud, q, k, cfg, reps=3):
+def cpu_baseline(cloud, q, k, cfg, reps=5):
     """The reference's OpenMP KDTREE_LINEAR_HEAP search (oracle restatement)
     on all host threads: build time and best-of-`reps` query throughput."""
     from oracle import oracle as O
