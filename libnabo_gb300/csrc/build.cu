@@ -123,17 +123,6 @@ struct Box {
 // ---------------------------------------------------------------------------
 // Phase 1: packing and bounds.
 
-// The kernels of the level loop are launched with programmatic stream
-// serialization (launch_level): a kernel may be scheduled while the one
-// before it drains, and waits here for that kernel's completion and memory
-// before touching anything; it then lets the next kernel be scheduled.
-// A dependent grid starts only once every block of this grid has passed
-// this point, so its waiting blocks never hold room this grid still needs.
-__device__ __forceinline__ void level_step_begin() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 template <typename T, int D>
 __global__ void k_pack(const T* __restrict__ cloud, int64_t n, int64_t stride, int dim, Rec<T, D>* __restrict__ recs) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -312,7 +301,7 @@ __device__ __forceinline__ int arg_max_extent(const T* lo, const T* hi, int dim)
 
 template <typename T>
 __global__ void k_prepare(SegLevel<T> L, const LevelState* st, int dim) {
-  level_step_begin();
+  pdl_begin();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= st->nseg) return;
   L.cutDim[s] = arg_max_extent(L.boxLo + (int64_t)s * kMaxDim, L.boxHi + (int64_t)s * kMaxDim, dim);
@@ -331,7 +320,7 @@ __global__ void k_prepare(SegLevel<T> L, const LevelState* st, int dim) {
 template <typename T, int D>
 __global__ void k_minmax(const Rec<T, D>* __restrict__ recs, int* __restrict__ segOf, int n, SegLevel<T> L,
                          SegLevel<T> prev, int remap, const LevelState* st, T* __restrict__ val) {
-  level_step_begin();
+  pdl_begin();
   using Key = typename KeyOf<T>::type;
   if (st->nseg == 0) return;
   for (int64_t tile = blockIdx.x; tile * kBlock < n; tile += gridDim.x) {
@@ -362,7 +351,7 @@ __global__ void k_minmax(const Rec<T, D>* __restrict__ recs, int* __restrict__ s
 
 template <typename T>
 __global__ void k_cut(SegLevel<T> L, const LevelState* st) {
-  level_step_begin();
+  pdl_begin();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= st->nseg) return;
   const int cd = L.cutDim[s];
@@ -390,7 +379,7 @@ __global__ void k_cut(SegLevel<T> L, const LevelState* st) {
 template <typename T>
 __global__ void k_count(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
                         const LevelState* st) {
-  level_step_begin();
+  pdl_begin();
   if (st->nseg == 0) return;
   for (int64_t tile = blockIdx.x; tile * kBlock < n; tile += gridDim.x) {
     const int64_t p = tile * kBlock + threadIdx.x;
@@ -455,7 +444,7 @@ template <typename T>
 __global__ void k_flag_sums(const T* __restrict__ val, const int* __restrict__ segOf, int n, SegLevel<T> L,
                             int pass, int tiles, int2* blockSums, int2* segFirst, int2* segLast,
                             const LevelState* st) {
-  level_step_begin();
+  pdl_begin();
   if (st->nseg == 0) return;
   int2 carry = make_int2(0, 0);
   for (int t = 0; t < tiles; ++t) {
@@ -479,7 +468,7 @@ __global__ void k_flag_sums(const T* __restrict__ val, const int* __restrict__ s
 // scan joins the runs (a loop of block-wide scans over the sums would
 // serialise on its barriers: 0.2 ms per call at 22 M points).
 __global__ void k_scan_block_sums(int2* sums, int nb, int2* total, const LevelState* st) {
-  level_step_begin();
+  pdl_begin();
   if (st->nseg == 0) {
     if (threadIdx.x == 0) *total = make_int2(0, 0);
     return;
@@ -510,7 +499,7 @@ __global__ void k_flag_pairs(const T* __restrict__ val, const int* __restrict__ 
                              int pass, int tiles, const int2* __restrict__ blockPrefix,
                              const int2* __restrict__ segFirst, const int2* __restrict__ segLast, int* pairA,
                              int* pairB, int cap, const LevelState* st) {
-  level_step_begin();
+  pdl_begin();
   if (st->nseg == 0) return;
   const int perBlock = tiles * kBlock;
   int2 carry = blockPrefix[blockIdx.x];
@@ -538,7 +527,7 @@ __global__ void k_flag_pairs(const T* __restrict__ val, const int* __restrict__ 
 template <typename T, int D>
 __global__ void k_swap(Rec<T, D>* recs, T* val, const int* __restrict__ pairA, const int* __restrict__ pairB,
                        const int2* __restrict__ total, int cap, int n, int* err) {
-  level_step_begin();
+  pdl_begin();
   const int m = min(cap, min(total->x, total->y));
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < m; t += gridDim.x * blockDim.x) {
     const int a = pairA[t], b = pairB[t];
@@ -559,7 +548,7 @@ __global__ void k_swap(Rec<T, D>* recs, T* val, const int* __restrict__ pairA, c
 template <typename T>
 __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, const LevelState* st, TopNodes<T> top,
                            SmallSegs<T> small, int* counters, int dim, int segCap, int smallCap, int topCap) {
-  level_step_begin();
+  pdl_begin();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   const int nseg = st->nseg;
   if (s >= nseg) return;
@@ -647,7 +636,7 @@ __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, const LevelState* st
 // Closes a level: records its top-node range and makes the segments the
 // level produced the current ones.
 __global__ void k_advance(LevelState* st, int* counters, int* lvStart, int* lvCount, int maxLevels) {
-  level_step_begin();
+  pdl_begin();
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (st->nseg > 0) {
     if (st->level < maxLevels) {
@@ -1185,23 +1174,6 @@ int pack_cloud(const T* dCloud, int64_t n, int64_t stride, int dim, cudaStream_t
   return kOk;
 }
 
-// A level-loop launch (see level_step_begin).
-template <typename... KArgs, typename... Args>
-cudaError_t launch_level(void (*kernel)(KArgs...), int grid, int block, size_t smem, cudaStream_t stream,
-                         Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3((unsigned)grid);
-  cfg.blockDim = dim3((unsigned)block);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-
 // Builds the trees of `nClouds` clouds stored back to back (cloud c =
 // points [off[c], off[c+1]) of dCloud) into one record array and one node
 // array: cloud c's tree is the pre-order range [nodeOffset[c],
@@ -1315,22 +1287,22 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
       if (level >= lvCap) return set_error(kErrUnsupported, "kd-tree build: too many levels");
     }
     const int remap = level > 0 ? 1 : 0;
-    NABO_CUDA_TRY(launch_level(k_prepare<T>, sg, 128, 0, stream, cur, st, dim));
-    NABO_CUDA_TRY(launch_level(k_minmax<T, D>, grid, kBlock, 0, stream, recs, segOf, N, cur, nxt, remap, st, val));
-    NABO_CUDA_TRY(launch_level(k_cut<T>, sg, 128, 0, stream, cur, st));
-    NABO_CUDA_TRY(launch_level(k_count<T>, grid, kBlock, 0, stream, val, segOf, N, cur, st));
+    NABO_CUDA_TRY(launch_pdl(k_prepare<T>, sg, 128, 0, stream, cur, st, dim));
+    NABO_CUDA_TRY(launch_pdl(k_minmax<T, D>, grid, kBlock, 0, stream, recs, segOf, N, cur, nxt, remap, st, val));
+    NABO_CUDA_TRY(launch_pdl(k_cut<T>, sg, 128, 0, stream, cur, st));
+    NABO_CUDA_TRY(launch_pdl(k_count<T>, grid, kBlock, 0, stream, val, segOf, N, cur, st));
     for (int pass = 1; pass <= 2; ++pass) {
-      NABO_CUDA_TRY(launch_level(k_flag_sums<T>, scanBlocks, kBlock, 0, stream, val, segOf, N, cur, pass, tiles,
+      NABO_CUDA_TRY(launch_pdl(k_flag_sums<T>, scanBlocks, kBlock, 0, stream, val, segOf, N, cur, pass, tiles,
                                  blockSums, segFirst, segLast, st));
-      NABO_CUDA_TRY(launch_level(k_scan_block_sums, 1, kBlock, 0, stream, blockSums, scanBlocks, passTotal, st));
-      NABO_CUDA_TRY(launch_level(k_flag_pairs<T>, scanBlocks, kBlock, 0, stream, val, segOf, N, cur, pass, tiles,
+      NABO_CUDA_TRY(launch_pdl(k_scan_block_sums, 1, kBlock, 0, stream, blockSums, scanBlocks, passTotal, st));
+      NABO_CUDA_TRY(launch_pdl(k_flag_pairs<T>, scanBlocks, kBlock, 0, stream, val, segOf, N, cur, pass, tiles,
                                  blockSums, segFirst, segLast, pairA, pairB, (int)pairCap, st));
-      NABO_CUDA_TRY(launch_level(k_swap<T, D>, grid, kBlock, 0, stream, recs, val, pairA, pairB, passTotal,
+      NABO_CUDA_TRY(launch_pdl(k_swap<T, D>, grid, kBlock, 0, stream, recs, val, pairA, pairB, passTotal,
                                  (int)pairCap, N, counters + 3));
     }
-    NABO_CUDA_TRY(launch_level(k_finalize<T>, sg, 128, 0, stream, cur, nxt, st, top, small, counters, dim,
+    NABO_CUDA_TRY(launch_pdl(k_finalize<T>, sg, 128, 0, stream, cur, nxt, st, top, small, counters, dim,
                                (int)segCap, (int)smallCap, (int)topCap));
-    NABO_CUDA_TRY(launch_level(k_advance, 1, 1, 0, stream, st, counters, lv, lv + lvCap, lvCap));
+    NABO_CUDA_TRY(launch_pdl(k_advance, 1, 1, 0, stream, st, counters, lv, lv + lvCap, lvCap));
     std::swap(cur, nxt);
   }
 

@@ -22,6 +22,17 @@
 
 namespace nabo_gb300 {
 
+// Kernels launched by launch_pdl (programmatic dependent launch) start with
+// this: wait for the previous kernel in the stream to complete and its
+// memory to be visible (griddepcontrol.wait) before touching anything, then
+// let the next kernel be scheduled. A dependent grid starts only once every
+// block of this grid has passed this point, so its waiting blocks never hold
+// room this grid still needs. Launched the ordinary way, both are no-ops.
+__device__ __forceinline__ void pdl_begin() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 constexpr int kMaxDim = 16;
 constexpr uint32_t kLeafDim = 31u;
 constexpr int kMetaShift = 5;

@@ -50,6 +50,24 @@ struct QueryChunks {
 // chunk's results, downloaded after every search has finished, are few.
 QueryChunks shrinking_chunks(int64_t nq, int n);
 
+// Launches a kernel that begins with pdl_begin() with programmatic stream
+// serialization, so that it is scheduled while the kernel before it drains.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
 // While set (calling thread only), scratch_alloc uses cudaMallocAsync so the
 // allocations can be captured into a CUDA graph.
 void set_capture_allocations(bool on);
