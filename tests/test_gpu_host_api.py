@@ -159,3 +159,35 @@ def test_single_point_calls():
         oi, od, ot = orc.knn(q.reshape(1, 3), 5, 0.0, 0, 0.1, mode=O.MODE_CANONICAL)
         H.assert_identical(gi, gd, oi, od, f"single point {i}")
         assert s.touched == ot
+
+
+@pytest.mark.parametrize("radii", [False, True], ids=["plain", "radii"])
+def test_repeated_pinned_calls_replay_a_graph(radii):
+    """A large call repeated with the same page-locked buffers and arguments
+    is captured into a CUDA graph on its first repeat and replayed after;
+    every call reads the buffers' current contents (new queries and radii
+    written in place) and returns the oracle's results and touched count."""
+    from libnabo_gb300 import _native
+    nb = _nb()
+    rng = np.random.default_rng(13)
+    cloud = rng.random((150_000, 3)).astype(np.float32)
+    nq, k = 300_000, 8
+    s = nb.NearestNeighbourSearch(cloud, creationOptionFlags=nb.TOUCH_STATISTICS)
+    orc = O.OracleTree(cloud, creation_flags=H.TOUCH_STATISTICS)
+    hq = _host((nq, 3), np.float32, True)
+    hr = _host((nq,), np.float32, True) if radii else None
+    idx = _host((nq, k), np.int32, True)
+    d2 = _host((nq, k), np.float32, True)
+    for it in range(4):
+        hq[:] = rng.random((nq, 3)).astype(np.float32)
+        if radii:
+            hr[:] = rng.uniform(0.003, 0.03, nq).astype(np.float32)
+        touched = ctypes.c_uint64(0)
+        rc = _native.lib.nabo_cuda_knn(s._h, hq.ctypes.data_as(ctypes.c_void_p), 3, nq, 3, k, 0.0, 0,
+                                         float("inf"), None if hr is None else hr.ctypes.data_as(ctypes.c_void_p),
+                                         idx.ctypes.data_as(ctypes.c_void_p), d2.ctypes.data_as(ctypes.c_void_p),
+                                         ctypes.byref(touched))
+        assert rc == 0, _native.lib.nabo_cuda_last_error().decode()
+        oi, od, ot = orc.knn(hq, k, max_radii=hr, mode=O.MODE_CANONICAL)
+        H.assert_identical(idx, d2, oi, od, f"call {it}")
+        assert int(touched.value) == ot, it
