@@ -144,6 +144,7 @@ struct PipeRes {
   PipeKey graphKey = {};
   PipeKey lastKey = {};
   bool hasLast = false;
+  bool noGraph = false;  // a capture failed once: direct calls only
   bool made = false;
 };
 
@@ -870,9 +871,10 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
   // current contents.
   const PipeKey key = make_pipe_key(query, maxRadii, indices, dists2, nq, qStride, epsilon, maxRadius, qRows, k,
                                     optionFlags, nChunks);
-  const bool graphable = pr == &s->pipe && is_pinned(query) && (!maxRadii || is_pinned(maxRadii));
+  const bool graphable =
+      pr == &s->pipe && !pr->noGraph && is_pinned(query) && (!maxRadii || is_pinned(maxRadii));
   const bool replay = graphable && pr->exec && same_key(pr->graphKey, key);
-  const bool capture = graphable && !replay && pr->hasLast && same_key(pr->lastKey, key);
+  bool capture = graphable && !replay && pr->hasLast && same_key(pr->lastKey, key);
   if (graphable) {
     pr->lastKey = key;
     pr->hasLast = true;
@@ -900,7 +902,16 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
       if (graph) cudaGraphDestroy(graph);
     }
     set_capture_allocations(false);
-    if (rc == kOk) pr->graphKey = key;
+    if (rc == kOk) {
+      pr->graphKey = key;
+    } else {  // not capturable here: direct calls from now on (a real error recurs there)
+      cudaGetLastError();
+      if (pr->exec) cudaGraphExecDestroy(pr->exec);
+      pr->exec = nullptr;
+      pr->noGraph = true;
+      capture = false;
+      rc = kOk;
+    }
   }
   if (rc == kOk && (replay || capture)) {
     cudaError_t e = cudaGraphLaunch(pr->exec, pr->main);
