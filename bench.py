@@ -620,17 +620,22 @@ def run_batched(args):
 C4_METRIC = "batched 8-D kNN queries/s (128 clouds, half f32 / half f64, k=32)"
 
 
-def c4_workload(n_clouds: int = 128):
+def c4_workload(n_clouds: int = 128, train_per_cloud: int = 3125):
+    """The 8-D batches: clouds, the timed queries (100,000 per cloud) and,
+    for the learned form, training queries drawn separately from the same
+    mixture (3,125 per cloud: 200,000 per scalar type)."""
     from libnabo_gb300 import synthetic as S
     seed = S.SEED_BASE + 400
     sizes = S.log_uniform_sizes(128, 50000, 2000000, seed)[:n_clouds]
-    out = {np.float32: ([], []), np.float64: ([], [])}
+    out = {np.float32: ([], [], []), np.float64: ([], [], [])}
     for i, n in enumerate(sizes):
         dt = np.float32 if i % 2 == 0 else np.float64
         cloud, centres, sig = S.clusters(int(n), 8, seed + 10 + i, dtype=dt)
         qs, _, _ = S.clusters(100000, 8, seed + 10000 + i, dtype=dt, centres=centres, sigmas=sig)
+        tr, _, _ = S.clusters(train_per_cloud, 8, seed + 20000 + i, dtype=dt, centres=centres, sigmas=sig)
         out[dt][0].append(cloud)
         out[dt][1].append(qs)
+        out[dt][2].append(tr)
     return out
 
 
@@ -645,7 +650,7 @@ def run_c4(args):
     k = 32
     batches = []
     t_gen = time.perf_counter()
-    for dt, (clouds, queries) in data.items():
+    for dt, (clouds, queries, train_queries) in data.items():
         if not clouds:
             continue
         pc = np.array([c.shape[0] for c in clouds], np.int64)
@@ -655,7 +660,7 @@ def run_c4(args):
         tc = torch.from_numpy(np.concatenate(clouds)).to(dev)
         tq = torch.from_numpy(np.concatenate(queries)).to(dev)
         batches.append(dict(dt=dt, b=b, tc=tc, tq=tq, out=b._outputs(dev), clouds=clouds, queries=queries,
-                            points=int(pc.sum()), nq=int(qc.sum())))
+                            train_queries=train_queries, points=int(pc.sum()), nq=int(qc.sum())))
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -709,6 +714,62 @@ def run_c4(args):
         ms = a0.elapsed_time(a1)
         per_type[np.dtype(x["dt"]).name] = {"ms": ms, "queries_per_s": x["nq"] / (ms / 1e3)}
     forms["eps0.0"]["per_type"] = per_type
+    # learned-radius form: one network per (dimension, scalar type), trained
+    # on queries disjoint from the timed ones (fresh draws from each cloud's
+    # mixture) with exact distances from the plain batched search
+    learned = None
+    if not args.no_learned:
+        learned = {}
+        t_train = time.perf_counter()
+        for x in batches:
+            b = x["b"]
+            trq = x["train_queries"]
+            b.set_queries([q.shape[0] for q in trq], np.full(len(x["clouds"]), k, np.int32))
+            tt = torch.from_numpy(np.concatenate(trq)).to(dev)
+            _, td2 = b.knn(tt)
+            x["model"] = b.train_radius_model(tt, td2)
+            b.set_queries([q.shape[0] for q in x["queries"]], np.full(len(x["clouds"]), k, np.int32))
+            x["train_n"] = int(tt.shape[0])
+            del tt, td2
+        torch.cuda.synchronize()
+        train_s = time.perf_counter() - t_train
+        fbs = [torch.zeros(1, dtype=torch.int32, device=dev) for _ in batches]
+
+        def lstep(eps, outs):
+            for j, x in enumerate(batches):
+                fbs[j].zero_()
+                x["b"].knn_learned(x["model"], x["tq"], epsilon=eps, out=outs[j], fallbacks=fbs[j])
+
+        for eps in (0.0, 0.5):
+            outs = [x["b"]._outputs(dev) for x in batches]
+            for _ in range(args.warmup):
+                lstep(eps, outs)
+            torch.cuda.synchronize()
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            for a0, a1 in ev:
+                a0.record()
+                lstep(eps, outs)
+                a1.record()
+            torch.cuda.synchronize()
+            ms = sum(a0.elapsed_time(a1) for a0, a1 in ev) / args.steps
+            entry = {"ms_per_step": ms, "queries_per_s": nq_total / (ms / 1e3),
+                     "fallbacks": int(sum(int(f.item()) for f in fbs)),
+                     "fallback_rate": sum(int(f.item()) for f in fbs) / nq_total}
+            if eps == 0.0:
+                entry["identical_to_plain"] = bool(all(
+                    torch.equal(outs[j][0], exact_out[j][0]) and torch.equal(outs[j][1], exact_out[j][1])
+                    for j in range(len(batches))))
+            else:
+                entry["within_bound_of_exact"] = bool(all(
+                    bool((outs[j][1] <= (1.5 ** 2) * exact_out[j][1] * (1 + 1e-6)).all())
+                    for j in range(len(batches))))
+            learned[f"eps{eps}"] = entry
+        learned["models"] = {np.dtype(x["dt"]).name: dict(x["model"].meta, train_queries=x["train_n"])
+                             for x in batches}
+        learned["train_s"] = train_s
+        learned["train_queries_from"] = "fresh draws from each cloud's mixture, disjoint from the timed queries"
+    forms["learned"] = learned
     # CPU baseline: the oracle (reference algorithm, all host threads) on the
     # two smallest clouds of each type, 5,000 queries each
     base = None
@@ -826,8 +887,34 @@ def run_bf(args):
         "cpu_baseline": {"value": sample / cpu_s, "unit": "queries/s", "cores": O.num_threads(), "kind": "port",
                          "sample": f"{sample} queries against all {n} points (oracle brute force)"},
         "clocks": clk.summary(), "gpu_launches": args.steps,
-        "fp64_fma_peak_tflops": nb.measure_fma_peak(np.float64) / 1e12,
     }
+    # the same search in double: bound by the FP64 pipe (1/64 of the FP32
+    # rate on this GPU), so fewer queries
+    nq64 = 20_000
+    cloud64, q64 = cloud.astype(np.float64), q[:nq64].astype(np.float64)
+    s64 = nb.NearestNeighbourSearch(cloud64, nb.SearchType.BRUTE_FORCE_CUDA)
+    tq64 = torch.from_numpy(q64).to(dev)
+    idx64 = torch.empty((nq64, k), dtype=torch.int32, device=dev)
+    d264 = torch.empty((nq64, k), dtype=torch.float64, device=dev)
+    s64.profile(True)
+    for _ in range(args.warmup):
+        s64.knn_device(tq64, k, out=(idx64, d264))
+    torch.cuda.synchronize()
+    kms64 = []
+    for _ in range(args.steps):
+        s64.knn_device(tq64, k, out=(idx64, d264))
+        kms64.append(s64.last_kernel_ms())
+    torch.cuda.synchronize()
+    kernel64 = statistics.mean(kms64)
+    peak64 = nb.measure_fma_peak(np.float64)
+    flops64 = float(nq64) * n * 3 * d
+    oi64, od64, _ = O.bf_knn(cloud64, q64[:500], k, mode=O.MODE_CANONICAL)
+    res["f64"] = {"queries": nq64, "points": n, "k": k, "kernel_ms": kernel64, "value": nq64 / (kernel64 / 1e3),
+                  "unit": "queries/s", "achieved_tflops": flops64 / (kernel64 * 1e-3) / 1e12,
+                  "peak_tflops": peak64 / 1e12, "frac": flops64 / (kernel64 * 1e-3) / peak64,
+                  "peak_source": "FP64 FMA chains measured in this run",
+                  "identical_vs_oracle": bool(np.array_equal(idx64[:500].cpu().numpy(), oi64)
+                                              and np.array_equal(d264[:500].cpu().numpy(), od64))}
     print(json.dumps(res))
 
 

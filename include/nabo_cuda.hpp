@@ -94,7 +94,7 @@ class NearestNeighbourSearch {
   using IndexMatrix = IndexMatrixType;
   using Vector = VectorType;
   using IndexVector = IndexVectorType;
-  using Index = long;
+  using Index = int;  // the reference's typedef int Index (nabo/nabo.h:267)
 
   // Values of the reference's enums (nabo/nabo.h:290-312), extended by the
   // two CUDA search types after BRUTE_FORCE_CL.
@@ -180,9 +180,8 @@ class NearestNeighbourSearch {
     nabo_cuda_params params;
     nabo_cuda_params_init(&params);
     params.bucketSize = p.bucketSize;
-    const int dimArg = d > (Index)INT32_MAX ? INT32_MAX : (int)d;
     detail::check(nabo_cuda_create(detail::dtype<T>(), c.data(), (int)c.rows(), (int64_t)c.cols(),
-                                   (int64_t)c.rows(), dimArg, (int)type, flags, &params, &h_));
+                                   (int64_t)c.rows(), (int)d, (int)type, flags, &params, &h_));
     minBound.resize((size_t)dim);
     maxBound.resize((size_t)dim);
     detail::check(nabo_cuda_get_bounds(h_, minBound.data(), maxBound.data()));

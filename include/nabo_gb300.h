@@ -122,12 +122,21 @@ int nabo_cuda_destroy(nabo_cuda_search* s);
  * radii overload (nabo/nabo.h:351) when maxRadii != NULL (nq values).
  * query: qRows x nq column-major, column stride qStride (>= qRows).
  * indices: k*nq int32; dists2: k*nq of the object's scalar type.
- * touched (may be NULL): receives the reference's TOUCH_STATISTICS count
- * (points examined in visited leaves; nq*n for brute force) when the
- * object was created with NABO_TOUCH_STATISTICS, else 0.
+ * touched (may be NULL): receives the TOUCH_STATISTICS count (points
+ * examined in visited leaves; nq*n for brute force) when the object was
+ * created with NABO_TOUCH_STATISTICS, else 0. Neighbours at equal distance
+ * are ranked by index (the lower index first, whatever the visit order), so
+ * a far subtree is visited when its box distance is <= the current k-th
+ * distance, where the reference requires < (nabo/kdtree_cpu.cpp:416-417):
+ * the count equals the reference's except when a box distance exactly
+ * equals the k-th distance at that moment (it then counts that subtree's
+ * points too; about 20 of 104 M points on a 1.15 M-point lidar scan).
  * Results are always sorted ascending (SORT_RESULTS is accepted).
- * k up to 32 runs one query per thread, k from 33 to 1024 one query per
- * warp (same results); larger k returns NABO_CUDA_ERR_UNSUPPORTED. */
+ * k up to 32 runs one query per thread, k from 33 to 1024 a group of lanes
+ * per query (same results); larger k returns NABO_CUDA_ERR_UNSUPPORTED.
+ * kd-trees of any height are searched: those taller than 256 levels (the
+ * split rule gives such trees on geometrically spaced coordinates) with
+ * their traversal stacks in global memory, taken from the scratch pool. */
 int nabo_cuda_knn(const nabo_cuda_search* s, const void* query, int qRows, int64_t nq, int64_t qStride, int k,
                   double epsilon, unsigned optionFlags, double maxRadius, const void* maxRadii, int32_t* indices,
                   void* dists2, uint64_t* touched);
@@ -279,6 +288,48 @@ int nabo_cuda_batch_build_device(nabo_cuda_batch* b, const void* clouds, void* s
  * into DEVICE arrays of sum(k_c * nq_c) entries. Stream-ordered. */
 int nabo_cuda_batch_knn_device(nabo_cuda_batch* b, const void* queries, double epsilon, unsigned optionFlags,
                                double maxRadius, int32_t* indices, void* dists2, void* stream);
+/* The same search with a radius per query (DEVICE, nq values of the
+ * batch's scalar type, in query order): the reference's per-query radius
+ * overload (nabo/nabo.h:351, nabo/kdtree_cpu.cpp:306-336) for every cloud.
+ * A query whose radius is below maxRadius and that finds fewer than its
+ * cloud's k neighbours inside it is searched again with maxRadius alone
+ * (the learned-radius form's exact fallback); `fallbacks` (DEVICE int32,
+ * may be NULL) receives how many were. With radii >= maxRadius it is the
+ * plain per-query radius search. Stream-ordered. */
+int nabo_cuda_batch_knn_radii_device(nabo_cuda_batch* b, const void* queries, const void* maxRadii, double epsilon,
+                                     unsigned optionFlags, double maxRadius, int32_t* indices, void* dists2,
+                                     int32_t* fallbacks, void* stream);
+/* Batched learned radius: one model per (dimension, scalar type) serves
+ * every cloud of batches of that kind. Its 8 inputs are taken from each
+ * query's own cloud and tree -- the query descends its tree to its home
+ * leaf (the search's first descent); the logs of the nearest, root-mean-
+ * square and farthest distances to that leaf's points and of their count,
+ * the log of the cloud's size and of its k, the leaf's depth and the mean
+ * log extent of its cell -- so the network sees local density rather than
+ * coordinates. Train with training queries laid out by the batch's current
+ * query plan (nabo_cuda_batch_set_queries) and their exact results (dists2
+ * of nabo_cuda_batch_knn_device); DEVICE buffers. Training as
+ * nabo_cuda_radius_model_train (targets log d_k, safety, calibrated
+ * margin). */
+int nabo_cuda_batch_radius_model_train(nabo_cuda_batch* b, const void* queries, const void* dists2,
+                                       const nabo_cuda_train_params* params, nabo_cuda_radius_model** out);
+/* Learned batched search: the model's radius per query (capped at
+ * maxRadius), then nabo_cuda_batch_knn_radii_device, so results equal the
+ * plain batched search's; `fallbacks` (DEVICE int32, may be NULL) receives
+ * the number of queries searched again. The model must be a batched model
+ * of the batch's dimension and scalar type. Stream-ordered. */
+int nabo_cuda_batch_knn_learned_device(nabo_cuda_batch* b, const nabo_cuda_radius_model* m, const void* queries,
+                                       double epsilon, unsigned optionFlags, double maxRadius, int32_t* indices,
+                                       void* dists2, int32_t* fallbacks, void* stream);
+/* A batched model's radii (DEVICE, nq values of the batch's scalar type,
+ * capped at maxRadius) and, if `raw` (DEVICE float) is given, standardised
+ * outputs, for the queries of the current plan; and its network inputs
+ * (DEVICE float, nq x 16), for checks. Stream-ordered. */
+int nabo_cuda_batch_radius_model_predict_device(nabo_cuda_batch* b, const nabo_cuda_radius_model* m,
+                                                const void* queries, double maxRadius, void* radii, float* raw,
+                                                void* stream);
+int nabo_cuda_batch_radius_model_features_device(nabo_cuda_batch* b, const nabo_cuda_radius_model* m,
+                                                 const void* queries, float* features, void* stream);
 /* Build + search as one CUDA graph: captured on the first call for these
  * buffers and arguments, replayed by later calls with the same ones (new
  * coordinates written into the same buffers). */
@@ -298,8 +349,11 @@ int nabo_cuda_batch_run_host(nabo_cuda_batch* b, const void* clouds, const void*
                              unsigned optionFlags, double maxRadius, int32_t* indices, void* dists2);
 /* Synchronises the device, then info[0] = status bits (1 non-finite input,
  * 2 capacity or level limit exceeded, 4 a tree taller than the search
- * stack), [1] total nodes, [2] tallest tree, [3] top levels run,
- * [4] result entries, [5] queries, [6] points, [7] clouds. */
+ * kernels' 256-level stacks -- not an error: its queries are searched again
+ * with stacks in global memory, inside the same launch sequence -- and 8
+ * one such stack did not fit the batch's stack memory, so those queries'
+ * results are not written), [1] total nodes, [2] tallest tree, [3] top
+ * levels run, [4] result entries, [5] queries, [6] points, [7] clouds. */
 int nabo_cuda_batch_status(nabo_cuda_batch* b, int64_t info[8]);
 /* One cloud's tree (indices local to the cloud), as nabo_cuda_export_tree;
  * with cutDim NULL only *nodeCount is set. */

@@ -483,6 +483,52 @@ class RadiusModel:
         return idx, d2
 
 
+class BatchRadiusModel:
+    """A learned-radius model for batched searches (one per dimension and
+    scalar type), made by :meth:`BatchSearch.train_radius_model`."""
+
+    def __init__(self, handle):
+        self._m = handle
+
+    def close(self) -> None:
+        m = getattr(self, "_m", None)
+        if m is not None and m.value:
+            _lib.nabo_cuda_radius_model_destroy(m)
+            self._m = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def meta(self) -> dict:
+        meta = (ctypes.c_float * 16)()
+        _check(_lib.nabo_cuda_radius_model_get(self._m, None, meta))
+        return dict(mu=meta[0], sigma=meta[1], safety=meta[2], k=int(meta[3]), train_loss=meta[4],
+                    train_samples=int(meta[5]), inputs=int(meta[6]), margin=meta[7])
+
+    def gradients(self, features, targets):
+        """(grad, summed squared error) of the MSE over given inputs and targets."""
+        import torch
+        X = _torch_device_array(features, torch.float32)
+        Y = _torch_device_array(targets, torch.float32)
+        grad = np.zeros(RADIUS_MODEL_PARAMS, np.float32)
+        loss = ctypes.c_float(0.0)
+        torch.cuda.synchronize()
+        _check(_lib.nabo_cuda_radius_model_gradients(self._m, ctypes.c_void_p(X.data_ptr()),
+                                                     ctypes.c_void_p(Y.data_ptr()), X.shape[0], _ptr(grad),
+                                                     ctypes.byref(loss)))
+        return grad, float(loss.value)
+
+    def get_params(self):
+        params = np.zeros(RADIUS_MODEL_PARAMS, np.float32)
+        meta = np.zeros(16, np.float32)
+        _check(_lib.nabo_cuda_radius_model_get(self._m, _ptr(params), _ptr(meta)))
+        return params, meta
+
+
 class BatchSearch:
     """Many clouds of uneven sizes built and searched together.
 
@@ -553,6 +599,80 @@ class BatchSearch:
                                                ctypes.c_void_p(d2.data_ptr()), ctypes.c_void_p(st)))
         return idx, d2
 
+    def knn_radii(self, queries, radii, epsilon: float = 0.0, optionFlags: int = 0, maxRadius: float = np.inf,
+                  out=None, fallbacks=None, stream=None):
+        """Search with a radius per query (CUDA tensor, one per query row);
+        a query whose radius is below ``maxRadius`` and that finds fewer than
+        its cloud's k neighbours is searched again with ``maxRadius`` alone,
+        counted in ``fallbacks`` (an int32 CUDA tensor of one element, added
+        to) when given."""
+        import torch
+        idx, d2 = out if out is not None else self._outputs(queries.device)
+        st = stream if stream is not None else torch.cuda.current_stream(queries.device).cuda_stream
+        fb = ctypes.c_void_p(fallbacks.data_ptr()) if fallbacks is not None else None
+        _check(_lib.nabo_cuda_batch_knn_radii_device(self._b, ctypes.c_void_p(queries.data_ptr()),
+                                                     ctypes.c_void_p(radii.data_ptr()), float(epsilon),
+                                                     int(optionFlags), float(maxRadius),
+                                                     ctypes.c_void_p(idx.data_ptr()), ctypes.c_void_p(d2.data_ptr()),
+                                                     fb, ctypes.c_void_p(st)))
+        return idx, d2
+
+    def train_radius_model(self, queries, dists2, epochs: int = 30, batch: int = 4096, lr: float = 3e-3,
+                           safety: float = 1.2, seed: int = 1234, targetMissRate: float = 0.01):
+        """A learned-radius model for batches of this dimension and scalar
+        type, from training queries laid out by the current query plan
+        (CUDA tensor) and their exact squared distances (the ``dists2`` of
+        ``knn`` on them). Returns a :class:`BatchRadiusModel`."""
+        import torch
+        p = nabo_cuda_train_params()
+        _lib.nabo_cuda_train_params_init(ctypes.byref(p))
+        p.epochs, p.batch, p.lr, p.safety, p.seed = int(epochs), int(batch), float(lr), float(safety), int(seed)
+        p.targetMissRate = float(targetMissRate)
+        m = ctypes.c_void_p()
+        torch.cuda.synchronize()
+        _check(_lib.nabo_cuda_batch_radius_model_train(self._b, ctypes.c_void_p(queries.data_ptr()),
+                                                       ctypes.c_void_p(dists2.data_ptr()), ctypes.byref(p),
+                                                       ctypes.byref(m)))
+        return BatchRadiusModel(m)
+
+    def predict_radii(self, model, queries, maxRadius: float = np.inf, raw: bool = False):
+        """A batched model's radius per query (CUDA tensor); with raw=True also
+        its standardised outputs."""
+        import torch
+        radii = torch.empty(queries.shape[0], dtype=queries.dtype, device=queries.device)
+        out = torch.empty(queries.shape[0], dtype=torch.float32, device=queries.device) if raw else None
+        st = torch.cuda.current_stream(queries.device).cuda_stream
+        _check(_lib.nabo_cuda_batch_radius_model_predict_device(
+            self._b, model._m, ctypes.c_void_p(queries.data_ptr()), float(maxRadius),
+            ctypes.c_void_p(radii.data_ptr()), None if out is None else ctypes.c_void_p(out.data_ptr()),
+            ctypes.c_void_p(st)))
+        return (radii, out) if raw else radii
+
+    def radius_features(self, model, queries):
+        """A batched model's network inputs (nq, 16) float32 CUDA tensor."""
+        import torch
+        X = torch.empty((queries.shape[0], RADIUS_MODEL_INPUTS), dtype=torch.float32, device=queries.device)
+        st = torch.cuda.current_stream(queries.device).cuda_stream
+        _check(_lib.nabo_cuda_batch_radius_model_features_device(self._b, model._m,
+                                                                 ctypes.c_void_p(queries.data_ptr()),
+                                                                 ctypes.c_void_p(X.data_ptr()), ctypes.c_void_p(st)))
+        return X
+
+    def knn_learned(self, model, queries, epsilon: float = 0.0, optionFlags: int = 0, maxRadius: float = np.inf,
+                    out=None, fallbacks=None, stream=None):
+        """Search with the model's radius per query; results equal ``knn``'s.
+        ``fallbacks`` (int32 CUDA tensor of one element) receives how many
+        queries were searched again."""
+        import torch
+        idx, d2 = out if out is not None else self._outputs(queries.device)
+        st = stream if stream is not None else torch.cuda.current_stream(queries.device).cuda_stream
+        fb = ctypes.c_void_p(fallbacks.data_ptr()) if fallbacks is not None else None
+        _check(_lib.nabo_cuda_batch_knn_learned_device(self._b, model._m, ctypes.c_void_p(queries.data_ptr()),
+                                                       float(epsilon), int(optionFlags), float(maxRadius),
+                                                       ctypes.c_void_p(idx.data_ptr()),
+                                                       ctypes.c_void_p(d2.data_ptr()), fb, ctypes.c_void_p(st)))
+        return idx, d2
+
     def run(self, clouds, queries, epsilon: float = 0.0, optionFlags: int = 0, maxRadius: float = np.inf,
             out=None, stream=None):
         """Build + search as one CUDA graph launch (captured on first use)."""
@@ -593,7 +713,9 @@ class BatchSearch:
     def status(self) -> dict:
         info = (ctypes.c_int64 * 8)()
         _check(_lib.nabo_cuda_batch_status(self._b, info))
-        return dict(ok=info[0] == 0, flags=int(info[0]), nodes=int(info[1]), height=int(info[2]),
+        # bit 4 (a tree taller than the search kernels' stacks, searched with
+        # stacks in global memory) is informational
+        return dict(ok=(info[0] & ~4) == 0, flags=int(info[0]), nodes=int(info[1]), height=int(info[2]),
                     levels=int(info[3]), results=int(info[4]), queries=int(info[5]), points=int(info[6]),
                     clouds=int(info[7]))
 

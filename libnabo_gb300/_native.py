@@ -38,6 +38,11 @@ SIGNATURES = {
     "nabo_cuda_radius_model_set": (_I, [_P, _P, _P]),
     "nabo_cuda_batch_create": (_I, [_I, _I, _I, _P, _P, _I, _P]),
     "nabo_cuda_batch_destroy": (_I, [_P]),
+    "nabo_cuda_batch_knn_radii_device": (_I, [_P, _P, _P, _D, _U, _D, _P, _P, _P, _P]),
+    "nabo_cuda_batch_radius_model_train": (_I, [_P, _P, _P, _P, _P]),
+    "nabo_cuda_batch_knn_learned_device": (_I, [_P, _P, _P, _D, _U, _D, _P, _P, _P, _P]),
+    "nabo_cuda_batch_radius_model_predict_device": (_I, [_P, _P, _P, _D, _P, _P, _P]),
+    "nabo_cuda_batch_radius_model_features_device": (_I, [_P, _P, _P, _P, _P]),
     "nabo_cuda_batch_set_queries": (_I, [_P, _P, _P]),
     "nabo_cuda_batch_build_device": (_I, [_P, _P, _P]),
     "nabo_cuda_batch_knn_device": (_I, [_P, _P, _D, _U, _D, _P, _P, _P]),

@@ -51,6 +51,13 @@ struct nabo_cuda_batch {
   uint32_t* hist = nullptr;
   uint32_t* cell = nullptr;
   uint32_t* rank = nullptr;
+  // trees taller than the search kernels' stacks: the queries handed to the
+  // deep search, their count, and its stacks
+  int64_t nMax = 0;  // points of the largest cloud
+  int32_t* ovfList = nullptr;
+  int32_t* ovfCount = nullptr;
+  void* slab = nullptr;
+  int64_t slabBytes = 0;
   // captured graph and the arguments it was captured with
   cudaGraphExec_t exec = nullptr;
   const void* gClouds = nullptr;
@@ -109,8 +116,12 @@ void drop_graph(nabo_cuda_batch* b) {
 
 void free_query_plan(nabo_cuda_batch* b) {
   for (void* p : {(void*)b->dQOff, (void*)b->dOutOff, (void*)b->dK, (void*)b->order, (void*)b->hist,
-                  (void*)b->cell, (void*)b->rank, b->devQueries, (void*)b->devIdx, b->devD2})
+                  (void*)b->cell, (void*)b->rank, b->devQueries, (void*)b->devIdx, b->devD2, (void*)b->ovfList,
+                  (void*)b->ovfCount, b->slab})
     if (p) cudaFree(p);
+  b->ovfList = b->ovfCount = nullptr;
+  b->slab = nullptr;
+  b->slabBytes = 0;
   b->dQOff = b->dOutOff = nullptr;
   b->dK = b->order = nullptr;
   b->hist = b->cell = b->rank = nullptr;
@@ -155,6 +166,9 @@ int build(nabo_cuda_batch* b, const void* clouds, cudaStream_t st) {
   f.rootLo = b->rootBox;
   f.rootHi = static_cast<unsigned char*>(b->rootBox) + (size_t)b->nClouds * kMaxDim * es;
   f.status = b->status;
+  // status[4]: the deep search's failure flag, cleared with each build
+  const cudaError_t e = cudaMemsetAsync(b->status + 4, 0, sizeof(int), st);
+  if (e != cudaSuccess) return cuda_error(e, "batch status");
 #define NABO_B_CASE(TT, DD)                                                                                \
   if (b->dpad == DD) {                                                                                     \
     const int rc = build_forest<TT, DD>(static_cast<const TT*>(clouds), b->nTotal, b->dim, b->dim,        \
@@ -200,16 +214,37 @@ BatchArgs batch_args(const nabo_cuda_batch* b, const void* query, double eps, un
   a.blockSize = b->blockSize;
   a.recs32 = b->recs32;
   a.coordMax = b->coordMax;
+  a.ovfList = b->ovfList;
+  a.ovfCount = b->ovfCount;
+  a.slab = b->slab;
+  a.slabBytes = b->slabBytes;
+  a.heightDev = b->status + 2;
+  a.deepFail = b->status + 4;
+  a.maxRadii = nullptr;
+  a.fallbacks = nullptr;
   return a;
 }
 
 int search(nabo_cuda_batch* b, const void* query, double eps, unsigned flags, double maxRadius, int32_t* indices,
-           void* dists2, cudaStream_t st) {
-  const BatchArgs a = batch_args(b, query, eps, flags, maxRadius, indices, dists2);
+           void* dists2, cudaStream_t st, const void* radii = nullptr, int32_t* fallbacks = nullptr) {
+  BatchArgs a = batch_args(b, query, eps, flags, maxRadius, indices, dists2);
+  a.maxRadii = radii;
+  a.fallbacks = fallbacks;
   return dispatch(b, [&](auto t, auto d) { return knn_batch<decltype(t), decltype(d)::value>(a, st); });
 }
 
 size_t elem_bytes(const nabo_cuda_batch* b) { return b->dtype == NABO_CUDA_FLOAT32 ? 4 : 8; }
+
+// Bytes one tree level takes in a deep search's stack: the one-thread
+// search's entry (rd, the offsets and the node in 16-byte chunks) or the
+// group search's (the same without padding), whichever is larger.
+int64_t stack_level_bytes(const nabo_cuda_batch* b) {
+  const int64_t tw = (int64_t)elem_bytes(b) / 4;
+  const int64_t words = tw * (b->dpad + 1) + 1;
+  const int64_t one = (words + 3) / 4 * 16;
+  const int64_t group = (b->dpad + 1) * (int64_t)elem_bytes(b) + 4;
+  return std::max(one, group);
+}
 
 // Device copies of a host run's inputs and results, streams; made on first use.
 int host_buffers(nabo_cuda_batch* b) {
@@ -329,6 +364,30 @@ int capture_host(nabo_cuda_batch* b, const void* clouds, const void* queries, do
 
 }  // namespace
 
+namespace nabo_gb300 {
+int batch_view(const nabo_cuda_batch* b, BatchView* v) {
+  if (!b) return set_error(kErrArgument, "NULL batch");
+  if (!b->dQOff) return set_error(kErrArgument, "call nabo_cuda_batch_set_queries first");
+  v->dtype = b->dtype;
+  v->dim = b->dim;
+  v->dpad = b->dpad;
+  v->nClouds = b->nClouds;
+  v->kMax = b->kMax;
+  v->device = b->device;
+  v->nq = b->nq;
+  v->nodes = b->nodes;
+  v->recs = b->recs;
+  v->pointOff = b->dOff;
+  v->nodeOffset = b->nodeOffset;
+  v->rootLo = b->rootBox;
+  v->rootHi = static_cast<const unsigned char*>(b->rootBox) + (size_t)b->nClouds * kMaxDim * elem_bytes(b);
+  v->qOffset = b->dQOff;
+  v->outOffset = b->dOutOff;
+  v->kOf = b->dK;
+  return kOk;
+}
+}  // namespace nabo_gb300
+
 extern "C" {
 
 int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* pointCounts,
@@ -376,20 +435,23 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
   const size_t recBytes = ((size_t)dpad * es + 4 + 15) / 16 * 16;
   const size_t nodeBytes = dtype == NABO_CUDA_FLOAT32 ? 8 : 16;
   std::vector<int64_t> off((size_t)nClouds + 1, 0);
-  for (int c = 0; c < nClouds; ++c) off[(size_t)c + 1] = off[(size_t)c] + pointCounts[c];
+  for (int c = 0; c < nClouds; ++c) {
+    off[(size_t)c + 1] = off[(size_t)c] + pointCounts[c];
+    b->nMax = std::max<int64_t>(b->nMax, pointCounts[c]);
+  }
   cudaError_t e = cudaMalloc((void**)&b->dOff, off.size() * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->recs, (size_t)total * recBytes);
   if (e == cudaSuccess) e = cudaMalloc(&b->nodes, (size_t)2 * total * nodeBytes);
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->nodeOffset, off.size() * sizeof(int64_t));
   if (e == cudaSuccess) e = cudaMalloc(&b->rootBox, (size_t)2 * nClouds * kMaxDim * es);
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->status, 4 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->status, 8 * sizeof(int));
   if (e == cudaSuccess && dtype == NABO_CUDA_FLOAT64) {
     const size_t rec32 = ((size_t)dpad * 4 + 4 + 15) / 16 * 16;  // sizeof(Rec<float, dpad>)
     e = cudaMalloc(&b->recs32, (size_t)total * rec32);
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->coordMax, sizeof(float));
   }
   if (e == cudaSuccess) e = cudaMemcpy(b->dOff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
-  if (e == cudaSuccess) e = cudaMemset(b->status, 0, 4 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(b->status, 0, 8 * sizeof(int));
   if (e != cudaSuccess) {
     nabo_cuda_batch_destroy(b);
     return cuda_error(e, "batch allocation");
@@ -453,6 +515,17 @@ int nabo_cuda_batch_set_queries(nabo_cuda_batch* b, const int64_t* queryCounts, 
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->cell, (size_t)std::max<int64_t>(nq, 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->rank, (size_t)std::max<int64_t>(nq, 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->hist, (size_t)2 * b->nTotal * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->ovfList, (size_t)std::max<int64_t>(nq, 1) * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&b->ovfCount, sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMemset(b->ovfCount, 0, sizeof(int32_t));
+  if (e == cudaSuccess) {
+    // the deep search's stacks: room for one stack as tall as the largest
+    // cloud (a tree's height is below its point count), 16 MiB at least so
+    // that several queries search at once, 256 MiB at most
+    b->slabBytes = std::min<int64_t>(int64_t(256) << 20, std::max<int64_t>(int64_t(16) << 20,
+                                                                           (b->nMax + 2) * stack_level_bytes(b)));
+    e = cudaMalloc(&b->slab, (size_t)b->slabBytes);
+  }
   if (e == cudaSuccess) e = cudaMemcpy(b->dQOff, qoff.data(), qoff.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(b->dOutOff, ooff.data(), ooff.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(b->dK, ks.data(), ks.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
@@ -482,6 +555,22 @@ int nabo_cuda_batch_knn_device(nabo_cuda_batch* b, const void* queries, double e
   if (!queries || !indices || !dists2) return set_error(kErrArgument, "NULL query or result buffer");
   Guard g(b->device);
   return search(b, queries, epsilon, optionFlags, maxRadius, indices, dists2, static_cast<cudaStream_t>(stream));
+}
+
+
+int nabo_cuda_batch_knn_radii_device(nabo_cuda_batch* b, const void* queries, const void* maxRadii, double epsilon,
+                                     unsigned optionFlags, double maxRadius, int32_t* indices, void* dists2,
+                                     int32_t* fallbacks, void* stream) {
+  if (!b) return set_error(kErrArgument, "NULL batch");
+  if (!b->dQOff) return set_error(kErrArgument, "call nabo_cuda_batch_set_queries first");
+  if (optionFlags & NABO_ALLOW_SELF_MATCH)
+    return set_error(kErrUnsupported, "batched searches forbid self matches (the plan checks k <= points - 1)");
+  if (optionFlags > 3) return set_error(kErrArgument, "OR-ed value of option flags is larger than maximal valid value (3)");
+  if (b->nq == 0) return kOk;
+  if (!queries || !maxRadii || !indices || !dists2) return set_error(kErrArgument, "NULL query, radii or result buffer");
+  Guard g(b->device);
+  return search(b, queries, epsilon, optionFlags, maxRadius, indices, dists2, static_cast<cudaStream_t>(stream),
+                maxRadii, fallbacks);
 }
 
 int nabo_cuda_batch_run(nabo_cuda_batch* b, const void* clouds, const void* queries, double epsilon,
@@ -589,15 +678,16 @@ int nabo_cuda_batch_run_host(nabo_cuda_batch* b, const void* clouds, const void*
 int nabo_cuda_batch_status(nabo_cuda_batch* b, int64_t info[8]) {
   if (!b || !info) return set_error(kErrArgument, "NULL argument");
   Guard g(b->device);
-  int hs[4];
+  int hs[8];
   int64_t total = 0;
   cudaError_t e = cudaDeviceSynchronize();
   if (e == cudaSuccess) e = cudaMemcpy(hs, b->status, sizeof(hs), cudaMemcpyDeviceToHost);
   if (e == cudaSuccess)
     e = cudaMemcpy(&total, b->nodeOffset + b->nClouds, sizeof(int64_t), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_error(e, "batch status");
-  // a tree taller than the search's stack (256) is reported as an overflow
-  info[0] = (hs[0] ? 1 : 0) | (hs[1] ? 2 : 0) | (hs[2] > 256 ? 4 : 0);
+  // a tree taller than the search kernels' stacks (256) is searched with
+  // stacks in global memory (bit 4); bit 8: one such stack did not fit
+  info[0] = (hs[0] ? 1 : 0) | (hs[1] ? 2 : 0) | (hs[2] > 256 ? 4 : 0) | (hs[4] ? 8 : 0);
   info[1] = total;
   info[2] = hs[2];
   info[3] = hs[3];

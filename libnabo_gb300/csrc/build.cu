@@ -1226,7 +1226,10 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   const int64_t segCap = n / (kSmallMax + 1) + 2;
   const int64_t topCap = n + 1;
   const int64_t smallCap = n + nClouds + 1;
-  const int lvCap = hostDriven ? 4096 : std::max(maxLevels, 1);
+  // levels recorded for the numbering; a host-driven build grows the record
+  // when a tree needs more (the split rule gives trees as tall as the cloud
+  // is large on geometrically spaced coordinates)
+  int lvCap = hostDriven ? 4096 : std::max(maxLevels, 1);
   T* val;
   NABO_CUDA_TRY(sc.get(&segOf, n));
   NABO_CUDA_TRY(sc.get(&val, n));
@@ -1284,7 +1287,17 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
       NABO_CUDA_TRY(cudaMemcpyAsync(&nseg, &st->nseg, sizeof(int), cudaMemcpyDeviceToHost, stream));
       NABO_CUDA_TRY(cudaStreamSynchronize(stream));
       if (nseg == 0) break;
-      if (level >= lvCap) return set_error(kErrUnsupported, "kd-tree build: too many levels");
+      if (level >= lvCap) {
+        if (level >= N) return set_error(kErrInternal, "kd-tree build: more levels than points");
+        const int grown = (int)std::min<int64_t>(2 * (int64_t)lvCap, (int64_t)N + 1);
+        int* lv2 = nullptr;
+        NABO_CUDA_TRY(sc.get(&lv2, 2 * (int64_t)grown));
+        NABO_CUDA_TRY(cudaMemcpyAsync(lv2, lv, (size_t)lvCap * sizeof(int), cudaMemcpyDeviceToDevice, stream));
+        NABO_CUDA_TRY(cudaMemcpyAsync(lv2 + grown, lv + lvCap, (size_t)lvCap * sizeof(int),
+                                      cudaMemcpyDeviceToDevice, stream));
+        lv = lv2;
+        lvCap = grown;
+      }
     }
     const int remap = level > 0 ? 1 : 0;
     NABO_CUDA_TRY(launch_pdl(k_prepare<T>, sg, 128, 0, stream, cur, st, dim));

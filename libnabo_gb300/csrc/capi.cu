@@ -21,6 +21,7 @@ namespace nabo_gb300 {
 
 namespace {
 thread_local std::string g_lastError;
+thread_local cudaError_t g_lastCudaError = cudaSuccess;  // the code behind the last kErrCuda
 }
 
 int set_error(int code, const std::string& msg) {
@@ -79,6 +80,7 @@ cudaError_t scratch_alloc(void** p, size_t bytes, cudaStream_t stream) {
 cudaError_t scratch_free(void* p, cudaStream_t stream) { return cudaFreeAsync(p, stream); }
 
 int cuda_error(cudaError_t e, const char* what) {
+  g_lastCudaError = e;
   g_lastError = std::string("CUDA error in ") + what + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
   return kErrCuda;
 }
@@ -549,6 +551,7 @@ HandleView handle_view(const nabo_cuda_search* s) {
   v.creationFlags = s->creationFlags;
   v.device = s->device;
   v.traversal = s->traversal;
+  v.sortQueries = s->queryOrdering != 0;
   v.evStart = s->evStart;
   v.evStop = s->evStop;
   return v;
@@ -736,6 +739,23 @@ int knn_staged(const nabo_cuda_search* s, const void* query, int qRows, int64_t 
   return kOk;
 }
 
+// Errors by which the runtime refuses a stream capture or a graph as such
+// (as opposed to a capture that some concurrent work invalidated).
+bool capture_refused(cudaError_t e) {
+  switch (e) {
+    case cudaErrorStreamCaptureUnsupported:
+    case cudaErrorStreamCaptureUnmatched:
+    case cudaErrorStreamCaptureUnjoined:
+    case cudaErrorStreamCaptureIsolation:
+    case cudaErrorStreamCaptureImplicit:
+    case cudaErrorStreamCaptureWrongThread:
+    case cudaErrorNotSupported:
+      return true;
+    default:
+      return false;
+  }
+}
+
 bool is_pinned(const void* p) {
   cudaPointerAttributes attr;
   if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
@@ -883,6 +903,7 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
     if (pr->exec) cudaGraphExecDestroy(pr->exec);
     pr->exec = nullptr;
     set_capture_allocations(true);
+    g_lastCudaError = cudaSuccess;
     cudaError_t e = cudaStreamBeginCapture(pr->main, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) {
       rc = cuda_error(e, "cudaStreamBeginCapture");
@@ -904,13 +925,20 @@ int knn_pipelined(const nabo_cuda_search* s, const void* query, int qRows, int64
     set_capture_allocations(false);
     if (rc == kOk) {
       pr->graphKey = key;
-    } else {  // not capturable here: direct calls from now on (a real error recurs there)
+    } else {
+      // This call runs directly instead (a real error recurs there). A
+      // capture the runtime refuses (capture or graph not supported here)
+      // turns graphs off for this object; any other failure, for example
+      // another thread's legacy-stream work invalidating the capture, only
+      // drops this graph, and a later repeat captures again.
       cudaGetLastError();
       if (pr->exec) cudaGraphExecDestroy(pr->exec);
       pr->exec = nullptr;
-      pr->noGraph = true;
+      pr->hasLast = false;
+      if (capture_refused(g_lastCudaError)) pr->noGraph = true;
       capture = false;
       rc = kOk;
+      g_lastError.clear();
     }
   }
   if (rc == kOk && (replay || capture)) {

@@ -10,6 +10,7 @@
 #include "nabo_gb300.h"
 
 struct nabo_cuda_search;
+struct nabo_cuda_batch;
 
 namespace nabo_gb300 {
 
@@ -147,6 +148,23 @@ struct BatchArgs {
   int blockSize;                // threads per block of the search kernel
   const void* recs32;           // f64: float copies of recs, or null
   const float* coordMax;        // f64: device float, largest coordinate magnitude
+  // Trees taller than the search kernels' stacks (256 levels): the queries
+  // listed in ovfList (nq entries; *ovfCount, zero between searches) are
+  // searched again with stacks in `slab`, sized by *heightDev (the tallest
+  // tree); *deepFail is set to -1 if one stack does not fit the slab.
+  int32_t* ovfList;
+  int32_t* ovfCount;
+  void* slab;
+  int64_t slabBytes;
+  const int* heightDev;
+  int32_t* deepFail;
+  // Optional per-query radii (device, nq values in query order, the batch's
+  // scalar type), the reference's maxRadii overload (nabo/nabo.h:351) for
+  // every cloud; a query whose radius is below maxRadius and that finds
+  // fewer than its cloud's k neighbours inside it searches again with
+  // maxRadius, counted in *fallbacks (may be null).
+  const void* maxRadii;
+  int32_t* fallbacks;
 };
 template <typename T, int D>
 int knn_batch(const BatchArgs& b, cudaStream_t stream);
@@ -195,6 +213,11 @@ struct KnnArgs {
   int32_t* fallbacks = nullptr;
   cudaEvent_t evStart = nullptr; // optional: recorded right before / after the search kernel
   cudaEvent_t evStop = nullptr;
+  // Optional device memory for the traversal stacks of a kd-tree taller than
+  // the compiled stacks (256 levels); without it such a search takes them
+  // from the scratch pool.
+  void* stackSlab = nullptr;
+  size_t stackSlabBytes = 0;
 };
 
 // Whether a search runs its queries in a sorted order. The sort costs about
@@ -229,12 +252,29 @@ struct HandleView {
   unsigned creationFlags;
   int device;
   int traversal;
+  bool sortQueries;     // the object's queryOrdering parameter
   cudaEvent_t evStart;  // profiling events (null when profiling is off)
   cudaEvent_t evStop;
 };
 HandleView handle_view(const struct ::nabo_cuda_search* s);
 int handle_check_knn(const struct ::nabo_cuda_search* s, int qRows, int64_t nq, int64_t qStride, int k,
                      unsigned optionFlags, const void* maxRadii);
+
+// Read access to a batch for the learned batched form (learned.cu).
+struct BatchView {
+  int dtype, dim, dpad, nClouds, kMax, device;
+  int64_t nq;
+  const void* nodes;
+  const void* recs;
+  const int64_t* pointOff;   // device, nClouds+1: the clouds' point offsets
+  const int64_t* nodeOffset; // device, nClouds+1
+  const void* rootLo;        // device, nClouds x kMaxDim (scalar type)
+  const void* rootHi;
+  const int64_t* qOffset;    // device, nClouds+1 (current query plan)
+  const int64_t* outOffset;  // device, nClouds+1
+  const int32_t* kOf;        // device, nClouds
+};
+int batch_view(const struct ::nabo_cuda_batch* b, BatchView* out);
 
 // Learned search radius (learned.cu).
 struct RadiusModel;

@@ -430,27 +430,123 @@ struct RadiusOut {
 
 constexpr int kInferWarps = 8;
 
+// The network's weights in shared memory.
+struct InferSmem {
+  __nv_bfloat16 W1[kH * kF];
+  __nv_bfloat16 W2[kH * kH];
+  float b1[kH], b2[kH], w3[kH];
+  float b3;
+  __nv_bfloat16 X[kInferWarps][16 * kF];
+};
+
+__device__ __forceinline__ void stage_weights(InferSmem& sm, const __nv_bfloat16* __restrict__ Wb) {
+  const int tid = threadIdx.x;
+  for (int i = tid; i < kH * kF; i += blockDim.x) sm.W1[i] = Wb[kOffW1 + i];
+  for (int i = tid; i < kH * kH; i += blockDim.x) sm.W2[i] = Wb[kOffW2 + i];
+  for (int i = tid; i < kH; i += blockDim.x) {
+    sm.b1[i] = __bfloat162float(Wb[kOffB1 + i]);
+    sm.b2[i] = __bfloat162float(Wb[kOffB2 + i]);
+    sm.w3[i] = __bfloat162float(Wb[kOffW3 + i]);
+  }
+  if (tid == 0) sm.b3 = __bfloat162float(Wb[kOffB3]);
+}
+
+// The network on the warp's 16 feature rows (sm.X[warp], queries q0 ..
+// q0 + 15) on the tensor cores; writes each query's radius (capped at
+// ro.maxRadius) and, if rawOut, its standardised output.
+template <typename T>
+__device__ __forceinline__ void mlp_tile(const InferSmem& sm, int warp, int lane, int64_t q0, int64_t nq,
+                                         const RadiusOut& ro, T* radii, float* rawOut) {
+  const int g = lane >> 2, tig = lane & 3;
+  const uint32_t* X32 = reinterpret_cast<const uint32_t*>(sm.X[warp]);  // row = 8 words
+  uint32_t a[4];
+  a[0] = X32[g * 8 + tig];
+  a[1] = X32[(g + 8) * 8 + tig];
+  a[2] = X32[g * 8 + 4 + tig];
+  a[3] = X32[(g + 8) * 8 + 4 + tig];
+  // layer 1: 8 n-tiles of 8 hidden units
+  const uint32_t* W1w = reinterpret_cast<const uint32_t*>(sm.W1);  // row j = 8 words
+  float z1[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    z1[j][0] = z1[j][1] = z1[j][2] = z1[j][3] = 0.0f;
+    const int n = 8 * j + g;
+    mma16816(z1[j], a, W1w[n * 8 + tig], W1w[n * 8 + 4 + tig]);
+  }
+  // SiLU, BF16, repacked as the A operand of layer 2 (4 k-steps); fragment
+  // order for m16n8k16 A: {row g k0-7, row g+8 k0-7, row g k8-15, row g+8
+  // k8-15}
+  uint32_t A2[4][4];
+#pragma unroll
+  for (int s = 0; s < 4; ++s) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int j = 2 * s + h;
+      const int c = 8 * j + 2 * tig;
+      float v[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float z = z1[j][e] + sm.b1[c + (e & 1)];
+        v[e] = silu_fast(z);
+      }
+      A2[s][2 * h + 0] = pack2(v[0], v[1]);
+      A2[s][2 * h + 1] = pack2(v[2], v[3]);
+    }
+  }
+  // layer 2
+  const uint32_t* W2w = reinterpret_cast<const uint32_t*>(sm.W2);  // row j = 32 words
+  float z2[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    z2[j][0] = z2[j][1] = z2[j][2] = z2[j][3] = 0.0f;
+    const int n = 8 * j + g;
+#pragma unroll
+    for (int s = 0; s < 4; ++s) mma16816(z2[j], A2[s], W2w[n * 32 + 8 * s + tig], W2w[n * 32 + 8 * s + 4 + tig]);
+  }
+  // output layer: rows g and g+8
+  float y0 = 0.0f, y1 = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const int c = 8 * j + 2 * tig;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const float z = z2[j][e] + sm.b2[c + (e & 1)];
+      const float act = silu_fast(z) * sm.w3[c + (e & 1)];
+      if (e < 2)
+        y0 += act;
+      else
+        y1 += act;
+    }
+  }
+  y0 += __shfl_xor_sync(0xffffffffu, y0, 1);
+  y0 += __shfl_xor_sync(0xffffffffu, y0, 2);
+  y1 += __shfl_xor_sync(0xffffffffu, y1, 1);
+  y1 += __shfl_xor_sync(0xffffffffu, y1, 2);
+  if (tig == 0) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int64_t qi = q0 + g + 8 * h;
+      if (qi < nq) {
+        const float yn = (h == 0 ? y0 : y1) + sm.b3;
+        if (rawOut) rawOut[qi] = yn;
+        // single precision: the radius only steers the search, the
+        // results are exact whatever it is
+        const float r = ro.safety * expf(ro.mu + ro.sigma * (yn + ro.margin));
+        radii[qi] = (double)r < ro.maxRadius ? (T)r : (T)ro.maxRadius;
+      }
+    }
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __restrict__ query, int64_t nq,
                                                                  int64_t qStride, FeatureSpace fs,
                                                                  const __nv_bfloat16* __restrict__ Wb, RadiusOut ro,
                                                                  T* radii, float* rawOut) {
-  __shared__ __align__(16) __nv_bfloat16 sW1[kH * kF];
-  __shared__ __align__(16) __nv_bfloat16 sW2[kH * kH];
-  __shared__ float sb1[kH], sb2[kH], sw3[kH];
-  __shared__ __align__(16) __nv_bfloat16 sX[kInferWarps][16 * kF];
-  const int tid = threadIdx.x;
-  for (int i = tid; i < kH * kF; i += blockDim.x) sW1[i] = Wb[kOffW1 + i];
-  for (int i = tid; i < kH * kH; i += blockDim.x) sW2[i] = Wb[kOffW2 + i];
-  for (int i = tid; i < kH; i += blockDim.x) {
-    sb1[i] = __bfloat162float(Wb[kOffB1 + i]);
-    sb2[i] = __bfloat162float(Wb[kOffB2 + i]);
-    sw3[i] = __bfloat162float(Wb[kOffW3 + i]);
-  }
-  const float b3 = __bfloat162float(Wb[kOffB3]);
+  __shared__ __align__(16) InferSmem sm;
+  stage_weights(sm, Wb);
   __syncthreads();
-  const int warp = tid >> 5, lane = tid & 31;
-  const int g = lane >> 2, tig = lane & 3;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t tiles = (nq + 15) / 16;
   for (int64_t tile = (int64_t)blockIdx.x * kInferWarps + warp; tile < tiles; tile += (int64_t)gridDim.x * kInferWarps) {
     const int64_t q0 = tile * 16;
@@ -461,7 +557,7 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __rest
       const int row = lane & 15;
       const bool second = lane >= 16;
       const int64_t qi = q0 + row;
-      __nv_bfloat16* xr = sX[warp] + row * kF;
+      __nv_bfloat16* xr = sm.X[warp] + row * kF;
       if (qi < nq) {
         const T* qp = query + qi * qStride;
         if (fs.useGrid) {
@@ -490,91 +586,160 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius(const T* __rest
       }
     }
     __syncwarp();
-    const uint32_t* X32 = reinterpret_cast<const uint32_t*>(sX[warp]);  // row = 8 words
-    uint32_t a[4];
-    a[0] = X32[g * 8 + tig];
-    a[1] = X32[(g + 8) * 8 + tig];
-    a[2] = X32[g * 8 + 4 + tig];
-    a[3] = X32[(g + 8) * 8 + 4 + tig];
-    // layer 1: 8 n-tiles of 8 hidden units
-    const uint32_t* W1w = reinterpret_cast<const uint32_t*>(sW1);  // row j = 8 words
-    float z1[8][4];
+    mlp_tile<T>(sm, warp, lane, q0, nq, ro, radii, rawOut);
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// batched models: one network per (dimension, scalar type) for the clouds of
+// batches, its 8 inputs taken from each query's own cloud and tree, so that
+// one network serves clouds of every size and density
+
+constexpr int kBatchInputs = 8;
+
+template <typename T>
+struct BatchFeat {
+  const Node<T>* nodes;
+  const void* recs;  // Rec<T, D>
+  const int64_t* pointOff;
+  const int64_t* nodeOffset;
+  const T* rootLo;
+  const T* rootHi;
+  const int64_t* qOffset;
+  const int32_t* kOf;
+  int nClouds;
+  int dim;
+};
+
+// Raw inputs of query qi: the query descends its cloud's tree to its home
+// leaf (the near side at every node, as the search's first descent does);
+// from that leaf's points the logs of the nearest, root-mean-square and
+// farthest distances and of the point count; the log of the cloud's size
+// and of its k; the leaf's depth; the mean log extent of the leaf's cell
+// (the cloud's root box narrowed by the cuts on the way).
+template <typename T, int D>
+__device__ void batch_raw_features(const T* __restrict__ q, int64_t qi, const BatchFeat<T>& bf,
+                                   float (&f)[kBatchInputs]) {
+  const int c = cloud_of(bf.qOffset, bf.nClouds, qi);
+  T qv[D];
+  float lo[D], hi[D];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      z1[j][0] = z1[j][1] = z1[j][2] = z1[j][3] = 0.0f;
-      const int n = 8 * j + g;
-      mma16816(z1[j], a, W1w[n * 8 + tig], W1w[n * 8 + 4 + tig]);
+  for (int d = 0; d < D; ++d) {
+    qv[d] = d < bf.dim ? q[d] : T(0);
+    lo[d] = d < bf.dim ? (float)bf.rootLo[(int64_t)c * kMaxDim + d] : 0.0f;
+    hi[d] = d < bf.dim ? (float)bf.rootHi[(int64_t)c * kMaxDim + d] : 0.0f;
+  }
+  uint32_t node = (uint32_t)bf.nodeOffset[c];
+  int depth = 0;
+  Node<T> nd = load_node(bf.nodes, node);
+  while (!node_is_leaf(nd.meta)) {
+    const int cd = (int)node_dim(nd.meta);
+    T qc = qv[0];
+#pragma unroll
+    for (int d = 1; d < D; ++d)
+      if (cd == d) qc = qv[d];
+    const bool right = qc - nd.cut > T(0);
+    const float cut = (float)nd.cut;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      if (cd == d && right) lo[d] = cut;
+      if (cd == d && !right) hi[d] = cut;
     }
-    // SiLU, BF16, repacked as the A operand of layer 2 (4 k-steps)
-    uint32_t a1[4][4];
+    node = right ? node_payload(nd.meta) : node + 1;
+    ++depth;
+    nd = load_node(bf.nodes, node);
+  }
+  const uint32_t cnt = node_payload(nd.meta), start = node_start(nd);
+  const Rec<T, D>* recs = static_cast<const Rec<T, D>*>(bf.recs);
+  float mn = 3.0e38f, mx = 0.0f, sum = 0.0f;
+  for (uint32_t j = 0; j < cnt; ++j) {
+    Rec<T, D> r;
+    load_rec(recs, (int64_t)start + j, r);
+    float d2 = 0.0f;
 #pragma unroll
-    for (int s = 0; s < 4; ++s) {
+    for (int d = 0; d < D; ++d) {
+      const float v = (float)(qv[d] - r.p.c[d]);
+      d2 += v * v;
+    }
+    mn = fminf(mn, d2);
+    mx = fmaxf(mx, d2);
+    sum += d2;
+  }
+  const float tiny = 1e-30f;
+  const float n = (float)(cnt > 0 ? cnt : 1u);
+  f[0] = 0.5f * logf(fmaxf(mn, tiny));
+  f[1] = 0.5f * logf(fmaxf(sum / n, tiny));
+  f[2] = 0.5f * logf(fmaxf(mx, tiny));
+  f[3] = logf(n);
+  f[4] = logf((float)(bf.pointOff[c + 1] - bf.pointOff[c]));
+  f[5] = logf((float)bf.kOf[c]);
+  f[6] = (float)depth;
+  float le = 0.0f;
+  for (int d = 0; d < bf.dim && d < D; ++d) le += logf(fmaxf(hi[d] - lo[d], tiny));
+  f[7] = le / (float)(bf.dim > 0 ? bf.dim : 1);
+}
+
+// The network's inputs: raw inputs centred and scaled by the training set's
+// statistics (fs.center, fs.invHalf), clamped to [-4, 4]; padding 0.
+__device__ __forceinline__ float batch_input(const float (&f)[kBatchInputs], const FeatureSpace& fs, int j) {
+  return j < kBatchInputs ? fminf(fmaxf((f[j] - fs.center[j]) * fs.invHalf[j], -4.f), 4.f) : 0.0f;
+}
+
+// Raw inputs (normalise = 0) or network inputs (1) of nq queries into X
+// (nq x kF floats).
+template <typename T, int D>
+__global__ void k_batch_features(const T* __restrict__ query, int64_t nq, BatchFeat<T> bf, FeatureSpace fs,
+                                 int normalise, float* X) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  float f[kBatchInputs];
+  batch_raw_features<T, D>(query + i * bf.dim, i, bf, f);
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int j = 2 * s + h;
-        const int c = 8 * j + 2 * tig;
-        float v[4];
+  for (int j = 0; j < kF; ++j) X[i * kF + j] = normalise ? batch_input(f, fs, j) : (j < kBatchInputs ? f[j] : 0.0f);
+}
+
+// Targets of batched training queries: log of the k-th distance of each
+// query's own cloud's k (NaN when it has fewer neighbours).
+template <typename T>
+__global__ void k_batch_targets(const T* __restrict__ d2, int64_t nq, const int64_t* __restrict__ qOffset,
+                                const int64_t* __restrict__ outOffset, const int32_t* __restrict__ kOf, int nClouds,
+                                double minD2, float* y) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  const int c = cloud_of(qOffset, nClouds, i);
+  const int k = kOf[c];
+  const T v = d2[outOffset[c] + (i - qOffset[c]) * k + (k - 1)];
+  y[i] = isinf((double)v) ? __int_as_float(0x7fc00000) : (float)(0.5 * log(fmax((double)v, minD2)));
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(kInferWarps * 32) k_mlp_radius_batch(const T* __restrict__ query, int64_t nq,
+                                                                       BatchFeat<T> bf, FeatureSpace fs,
+                                                                       const __nv_bfloat16* __restrict__ Wb,
+                                                                       RadiusOut ro, T* radii, float* rawOut) {
+  __shared__ __align__(16) InferSmem sm;
+  stage_weights(sm, Wb);
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tiles = (nq + 15) / 16;
+  for (int64_t tile = (int64_t)blockIdx.x * kInferWarps + warp; tile < tiles; tile += (int64_t)gridDim.x * kInferWarps) {
+    const int64_t q0 = tile * 16;
+    if (lane < 16) {
+      const int64_t qi = q0 + lane;
+      __nv_bfloat16* xr = sm.X[warp] + lane * kF;
+      float f[kBatchInputs];
+      if (qi < nq) {
+        batch_raw_features<T, D>(query + qi * bf.dim, qi, bf, f);
+      } else {
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float z = z1[j][e] + sb1[c + (e & 1)];
-          v[e] = silu_fast(z);
-        }
-        a1[s][2 * h + 0] = pack2(v[0], v[1]);
-        a1[s][2 * h + 1] = pack2(v[2], v[3]);
+        for (int j = 0; j < kBatchInputs; ++j) f[j] = fs.center[j];
       }
+#pragma unroll
+      for (int j = 0; j < kF; ++j) xr[j] = __float2bfloat16_rn(batch_input(f, fs, j));
     }
-    // fragment order for m16n8k16 A: {row g k0-7, row g+8 k0-7, row g k8-15, row g+8 k8-15}
-    uint32_t A2[4][4];
-#pragma unroll
-    for (int s = 0; s < 4; ++s) {
-      A2[s][0] = a1[s][0];
-      A2[s][1] = a1[s][1];
-      A2[s][2] = a1[s][2];
-      A2[s][3] = a1[s][3];
-    }
-    // layer 2
-    const uint32_t* W2w = reinterpret_cast<const uint32_t*>(sW2);  // row j = 32 words
-    float z2[8][4];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      z2[j][0] = z2[j][1] = z2[j][2] = z2[j][3] = 0.0f;
-      const int n = 8 * j + g;
-#pragma unroll
-      for (int s = 0; s < 4; ++s) mma16816(z2[j], A2[s], W2w[n * 32 + 8 * s + tig], W2w[n * 32 + 8 * s + 4 + tig]);
-    }
-    // output layer: rows g and g+8
-    float y0 = 0.0f, y1 = 0.0f;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const int c = 8 * j + 2 * tig;
-#pragma unroll
-      for (int e = 0; e < 4; ++e) {
-        const float z = z2[j][e] + sb2[c + (e & 1)];
-        const float act = silu_fast(z) * sw3[c + (e & 1)];
-        if (e < 2)
-          y0 += act;
-        else
-          y1 += act;
-      }
-    }
-    y0 += __shfl_xor_sync(0xffffffffu, y0, 1);
-    y0 += __shfl_xor_sync(0xffffffffu, y0, 2);
-    y1 += __shfl_xor_sync(0xffffffffu, y1, 1);
-    y1 += __shfl_xor_sync(0xffffffffu, y1, 2);
-    if (tig == 0) {
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int64_t qi = q0 + g + 8 * h;
-        if (qi < nq) {
-          const float yn = (h == 0 ? y0 : y1) + b3;
-          if (rawOut) rawOut[qi] = yn;
-          // single precision: the radius only steers the search, the
-          // results are exact whatever it is
-          const float r = ro.safety * expf(ro.mu + ro.sigma * (yn + ro.margin));
-          radii[qi] = (double)r < ro.maxRadius ? (T)r : (T)ro.maxRadius;
-        }
-      }
-    }
+    __syncwarp();
+    mlp_tile<T>(sm, warp, lane, q0, nq, ro, radii, rawOut);
     __syncwarp();
   }
 }
@@ -602,6 +767,7 @@ struct RadiusModel {
   float mu = 0.0f, sigma = 1.0f, safety = 1.2f;
   float trainLoss = 0.0f;
   int64_t trainSamples = 0;
+  int kind = 0;  // 0: one cloud's model; 1: a batched model (inputs from the query's own cloud and tree)
 };
 
 namespace {
@@ -792,6 +958,98 @@ int search_given(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, c
 
 }  // namespace
 
+// Fits the parameters to standardised targets Y over the samples `valid`
+// (features X): minibatches of tp.batch, Adam with a cosine learning-rate
+// decay over tp.epochs; `order` (as many ints as samples) and `loss` (one
+// float) are scratch. Leaves the last epoch's mean loss in m->trainLoss.
+int fit_params(RadiusModel* m, const float* X, const float* Y, const std::vector<int32_t>& valid,
+               const nabo_cuda_train_params& tp, int32_t* order, float* loss, cudaStream_t st) {
+  const std::vector<float> p0 = init_params(tp.seed, m->fs.nIn);
+  cudaError_t e = cudaMemcpyAsync(m->params, p0.data(), kParams * sizeof(float), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->adamM, 0, kParams * sizeof(float), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->adamV, 0, kParams * sizeof(float), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(m->grad, 0, kParams * sizeof(float), st);
+  if (e != cudaSuccess) return cuda_error(e, "model init");
+  k_to_bf16<<<ceil_div(kParams, 256), 256, 0, st>>>(m->params, m->pb, kParams);
+  int rc = kOk;
+  std::mt19937_64 rng(tp.seed ^ 0x9e3779b97f4a7c15ull);
+  const int nValid = (int)valid.size();
+  const int batch = std::max(32, std::min(tp.batch, nValid));
+  const int stepsPerEpoch = std::max(1, nValid / batch);
+  const int epochs = std::max(1, tp.epochs);
+  const int total = epochs * stepsPerEpoch;
+  std::vector<int32_t> perm(valid);
+  int step = 0;
+  float lastLoss = 0.0f;
+  for (int ep = 0; ep < epochs && rc == kOk; ++ep) {
+    std::shuffle(perm.begin(), perm.end(), rng);
+    e = cudaMemcpyAsync(order, perm.data(), perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_error(e, "batch upload");
+    const bool lastEpoch = ep + 1 == epochs;
+    if (lastEpoch) cudaMemsetAsync(loss, 0, sizeof(float), st);
+    for (int b = 0; b < stepsPerEpoch && rc == kOk; ++b, ++step) {
+      rc = grad_step(*m, X, Y, order + (size_t)b * batch, batch, lastEpoch ? loss : nullptr, st);
+      const double lr = tp.lr * 0.5 * (1.0 + std::cos(3.14159265358979323846 * step / total));
+      const float b1 = 0.9f, b2 = 0.999f;
+      const float c1 = (float)(1.0 / (1.0 - std::pow(b1, step + 1)));
+      const float c2 = (float)(1.0 / (1.0 - std::pow(b2, step + 1)));
+      k_adam<<<ceil_div(kParams, 256), 256, 0, st>>>(m->params, m->adamM, m->adamV, m->grad, m->pb, kParams,
+                                                     (float)lr, b1, b2, c1, c2, 1e-8f);
+    }
+    if (lastEpoch && rc == kOk) {
+      e = cudaMemcpyAsync(&lastLoss, loss, sizeof(float), cudaMemcpyDeviceToHost, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+      if (e != cudaSuccess) rc = cuda_error(e, "training");
+    }
+  }
+  m->trainLoss = lastLoss / (float)((size_t)stepsPerEpoch * batch);
+  m->trainSamples = nValid;
+  return rc;
+}
+
+// The margin: the residual quantile such that about tp.targetMissRate of the
+// training samples would fall outside their radius. hy holds the
+// standardised targets, raw (device, n) the network's outputs on them.
+int calibrate_margin(RadiusModel* m, const std::vector<float>& hy, const std::vector<int32_t>& valid, const float* raw,
+                     int64_t n, const nabo_cuda_train_params& tp, cudaStream_t st) {
+  std::vector<float> hraw((size_t)n);
+  cudaError_t e = cudaMemcpyAsync(hraw.data(), raw, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_error(e, "calibration");
+  std::vector<float> res;
+  res.reserve(valid.size());
+  for (int32_t i : valid) res.push_back(hy[(size_t)i] - hraw[(size_t)i]);
+  const size_t qi = std::min(res.size() - 1, (size_t)std::ceil((1.0 - tp.targetMissRate) * (double)res.size()));
+  std::nth_element(res.begin(), res.begin() + qi, res.end());
+  const double need = (double)res[qi] - std::log((double)m->safety) / (double)m->sigma;
+  m->margin = (float)std::max(0.0, need);
+  return kOk;
+}
+
+// Standardises the targets in hy (NaN: no k-th neighbour, left out): sets
+// m->mu and m->sigma, returns the valid samples and the median d_k.
+int standardise_targets(RadiusModel* m, std::vector<float>& hy, std::vector<int32_t>* valid, double* medianDk) {
+  double sum = 0.0, sq = 0.0;
+  std::vector<float> logs;
+  for (size_t i = 0; i < hy.size(); ++i) {
+    if (std::isnan(hy[i])) continue;
+    valid->push_back((int32_t)i);
+    logs.push_back(hy[i]);
+    sum += hy[i];
+    sq += (double)hy[i] * hy[i];
+  }
+  if (valid->size() < 16) return set_error(kErrArgument, "too few training queries have k neighbours within maxRadius");
+  std::nth_element(logs.begin(), logs.begin() + logs.size() / 2, logs.end());
+  *medianDk = std::exp((double)logs[logs.size() / 2]);
+  const double mean = sum / valid->size();
+  const double var = std::max(sq / valid->size() - mean * mean, 1e-12);
+  m->mu = (float)mean;
+  m->sigma = (float)std::sqrt(var);
+  for (float& y : hy)
+    if (!std::isnan(y)) y = (float)((y - mean) / m->sigma);
+  return kOk;
+}
+
 // Trains a radius model for k-NN searches of `s` on `nTrain` training
 // queries (device memory).
 int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nTrain, int64_t qStride, int k,
@@ -864,29 +1122,10 @@ int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nT
   // standardise the targets; keep samples with a k-th neighbour
   std::vector<int32_t> valid;
   double medianDk = 0.0;
+  if (rc == kOk) rc = standardise_targets(m, hy, &valid, &medianDk);
   if (rc == kOk) {
-    double sum = 0.0, sq = 0.0;
-    std::vector<float> logs;
-    for (int64_t i = 0; i < nTrain; ++i) {
-      if (std::isnan(hy[(size_t)i])) continue;
-      valid.push_back((int32_t)i);
-      logs.push_back(hy[(size_t)i]);
-      sum += hy[(size_t)i];
-      sq += (double)hy[(size_t)i] * hy[(size_t)i];
-    }
-    if (valid.size() < 16) rc = set_error(kErrArgument, "too few training queries have k neighbours within maxRadius");
-    if (rc == kOk) {
-      std::nth_element(logs.begin(), logs.begin() + logs.size() / 2, logs.end());
-      medianDk = std::exp((double)logs[logs.size() / 2]);
-      const double mean = sum / valid.size();
-      const double var = std::max(sq / valid.size() - mean * mean, 1e-12);
-      m->mu = (float)mean;
-      m->sigma = (float)std::sqrt(var);
-      for (int64_t i = 0; i < nTrain; ++i)
-        if (!std::isnan(hy[(size_t)i])) hy[(size_t)i] = (float)((hy[(size_t)i] - mean) / m->sigma);
-      e = cudaMemcpyAsync(Y, hy.data(), (size_t)nTrain * sizeof(float), cudaMemcpyHostToDevice, st);
-      if (e != cudaSuccess) rc = cuda_error(e, "training targets upload");
-    }
+    e = cudaMemcpyAsync(Y, hy.data(), (size_t)nTrain * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "training targets upload");
   }
   // voxel tables (finest voxel = half the median k-th distance), features
   if (rc == kOk) {
@@ -894,73 +1133,13 @@ int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nT
     rc = c.dtype == NABO_CUDA_FLOAT32 ? dispatch_grid<float>(c, m, h0, st) : dispatch_grid<double>(c, m, h0, st);
   }
   if (rc == kOk) rc = launch_features(*m, dTrain, nTrain, qStride, X, st);
-  if (rc == kOk) {
-    const std::vector<float> p0 = init_params(tp.seed, m->fs.nIn);
-    e = cudaMemcpyAsync(m->params, p0.data(), kParams * sizeof(float), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(m->adamM, 0, kParams * sizeof(float), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(m->adamV, 0, kParams * sizeof(float), st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(m->grad, 0, kParams * sizeof(float), st);
-    if (e != cudaSuccess) rc = cuda_error(e, "model init");
-    k_to_bf16<<<ceil_div(kParams, 256), 256, 0, st>>>(m->params, m->pb, kParams);
-  }
   // Adam with a cosine learning-rate decay
-  if (rc == kOk) {
-    std::mt19937_64 rng(tp.seed ^ 0x9e3779b97f4a7c15ull);
-    const int nValid = (int)valid.size();
-    const int batch = std::max(32, std::min(tp.batch, nValid));
-    const int stepsPerEpoch = std::max(1, nValid / batch);
-    const int total = std::max(1, tp.epochs) * stepsPerEpoch;
-    std::vector<int32_t> perm(valid);
-    int step = 0;
-    float lastLoss = 0.0f;
-    for (int ep = 0; ep < std::max(1, tp.epochs) && rc == kOk; ++ep) {
-      std::shuffle(perm.begin(), perm.end(), rng);
-      e = cudaMemcpyAsync(order, perm.data(), perm.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
-      if (e != cudaSuccess) {
-        rc = cuda_error(e, "batch upload");
-        break;
-      }
-      const bool lastEpoch = ep + 1 == std::max(1, tp.epochs);
-      if (lastEpoch) cudaMemsetAsync(loss, 0, sizeof(float), st);
-      for (int b = 0; b < stepsPerEpoch && rc == kOk; ++b, ++step) {
-        rc = grad_step(*m, X, Y, order + (size_t)b * batch, batch, lastEpoch ? loss : nullptr, st);
-        const double lr = tp.lr * 0.5 * (1.0 + std::cos(3.14159265358979323846 * step / total));
-        const float b1 = 0.9f, b2 = 0.999f;
-        const float c1 = (float)(1.0 / (1.0 - std::pow(b1, step + 1)));
-        const float c2 = (float)(1.0 / (1.0 - std::pow(b2, step + 1)));
-        k_adam<<<ceil_div(kParams, 256), 256, 0, st>>>(m->params, m->adamM, m->adamV, m->grad, m->pb, kParams,
-                                                       (float)lr, b1, b2, c1, c2, 1e-8f);
-      }
-      if (lastEpoch && rc == kOk) {
-        e = cudaMemcpyAsync(&lastLoss, loss, sizeof(float), cudaMemcpyDeviceToHost, st);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-        if (e != cudaSuccess) rc = cuda_error(e, "training");
-      }
-    }
-    m->trainLoss = lastLoss / (float)((size_t)stepsPerEpoch * batch);
-    m->trainSamples = nValid;
-  }
+  if (rc == kOk) rc = fit_params(m, X, Y, valid, tp, order, loss, st);
   // margin: residual quantile so that ~targetMissRate of the training
   // queries would fall outside their radius
   m->margin = 0.0f;
-  if (rc == kOk && tp.targetMissRate > 0.0f) {
-    rc = launch_radius(*m, dTrain, nTrain, qStride, 1e300, radii, raw, st);
-    std::vector<float> hraw((size_t)nTrain);
-    if (rc == kOk) {
-      e = cudaMemcpyAsync(hraw.data(), raw, (size_t)nTrain * sizeof(float), cudaMemcpyDeviceToHost, st);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-      if (e != cudaSuccess) rc = cuda_error(e, "calibration");
-    }
-    if (rc == kOk) {
-      std::vector<float> res;
-      res.reserve(valid.size());
-      for (int32_t i : valid) res.push_back(hy[(size_t)i] - hraw[(size_t)i]);
-      const size_t qi = std::min(res.size() - 1, (size_t)std::ceil((1.0 - tp.targetMissRate) * (double)res.size()));
-      std::nth_element(res.begin(), res.begin() + qi, res.end());
-      const double need = (double)res[qi] - std::log((double)m->safety) / (double)m->sigma;
-      m->margin = (float)std::max(0.0, need);
-    }
-  }
+  if (rc == kOk && tp.targetMissRate > 0.0f) rc = launch_radius(*m, dTrain, nTrain, qStride, 1e300, radii, raw, st);
+  if (rc == kOk && tp.targetMissRate > 0.0f) rc = calibrate_margin(m, hy, valid, raw, nTrain, tp, st);
   if (idx) scratch_free(idx, st);
   if (d2) scratch_free(d2, st);
   if (X) scratch_free(X, st);
@@ -969,6 +1148,176 @@ int radius_model_train(const nabo_cuda_search* s, const void* dTrain, int64_t nT
   if (order) scratch_free(order, st);
   if (raw) scratch_free(raw, st);
   if (radii) scratch_free(radii, st);
+  if (rc != kOk) return fail(rc);
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return fail(cuda_error(e, "training"));
+  *out = m;
+  return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// batched models
+
+template <typename T>
+BatchFeat<T> batch_feat(const BatchView& v) {
+  BatchFeat<T> bf;
+  bf.nodes = static_cast<const Node<T>*>(v.nodes);
+  bf.recs = v.recs;
+  bf.pointOff = v.pointOff;
+  bf.nodeOffset = v.nodeOffset;
+  bf.rootLo = static_cast<const T*>(v.rootLo);
+  bf.rootHi = static_cast<const T*>(v.rootHi);
+  bf.qOffset = v.qOffset;
+  bf.kOf = v.kOf;
+  bf.nClouds = v.nClouds;
+  bf.dim = v.dim;
+  return bf;
+}
+
+// f(T(), integral_constant<int, D>()) for the batch's scalar type and
+// compiled record dimension.
+template <typename F>
+int batch_dispatch(const BatchView& v, F&& f) {
+  using std::integral_constant;
+  if (v.dtype == NABO_CUDA_FLOAT32) {
+    switch (v.dpad) {
+      case 2: return f(float(), integral_constant<int, 2>());
+      case 3: return f(float(), integral_constant<int, 3>());
+      case 4: return f(float(), integral_constant<int, 4>());
+      case 8: return f(float(), integral_constant<int, 8>());
+      case 16: return f(float(), integral_constant<int, 16>());
+    }
+  } else {
+    switch (v.dpad) {
+      case 2: return f(double(), integral_constant<int, 2>());
+      case 3: return f(double(), integral_constant<int, 3>());
+      case 4: return f(double(), integral_constant<int, 4>());
+      case 8: return f(double(), integral_constant<int, 8>());
+      case 16: return f(double(), integral_constant<int, 16>());
+    }
+  }
+  return set_error(kErrInternal, "bad dispatch");
+}
+
+int launch_radius_batch(const RadiusModel& m, const BatchView& v, const void* query, double maxRadius, void* radii,
+                        float* raw, cudaStream_t st) {
+  if (v.nq == 0) return kOk;
+  RadiusOut ro;
+  ro.mu = m.mu;
+  ro.sigma = m.sigma;
+  ro.safety = m.safety;
+  ro.margin = m.margin;
+  ro.maxRadius = maxRadius;
+  const int64_t tiles = (v.nq + 15) / 16;
+  const int grid = (int)std::min<int64_t>(ceil_div(tiles, kInferWarps), 152 * 16);
+  const int rc = batch_dispatch(v, [&](auto t, auto d) {
+    using T = decltype(t);
+    k_mlp_radius_batch<T, decltype(d)::value><<<grid, kInferWarps * 32, 0, st>>>(
+        static_cast<const T*>(query), v.nq, batch_feat<T>(v), m.fs, m.pb, ro, static_cast<T*>(radii), raw);
+    return kOk;
+  });
+  if (rc != kOk) return rc;
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_error(e, "batched learned radius kernel");
+  return kOk;
+}
+
+// Trains a batched model from the queries of the batch's current plan and
+// their exact results (dists2 of a plain batched search of them).
+int batch_radius_model_train(const BatchView& v, const void* query, const void* d2, const nabo_cuda_train_params& tp,
+                             RadiusModel** out, cudaStream_t st) {
+  RadiusModel* m = new RadiusModel();
+  m->dtype = v.dtype;
+  m->dim = v.dim;
+  m->dpad = v.dpad;
+  m->k = v.kMax;
+  m->kind = 1;
+  m->safety = tp.safety;
+  const int64_t n = v.nq;
+  const size_t es = v.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  int rc = kOk;
+  auto fail = [&](int code) {
+    cudaStreamSynchronize(st);
+    free_model(m);
+    delete m;
+    return code;
+  };
+  cudaError_t e = cudaMalloc((void**)&m->params, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->adamM, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->adamV, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->grad, kParams * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&m->pb, kParams * sizeof(__nv_bfloat16));
+  if (e != cudaSuccess) return fail(cuda_error(e, "model allocation"));
+  float *X = nullptr, *Y = nullptr, *loss = nullptr, *raw = nullptr;
+  int32_t* order = nullptr;
+  void* radii = nullptr;
+  e = scratch_alloc((void**)&X, (size_t)n * kF * sizeof(float), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&Y, (size_t)n * sizeof(float), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&loss, sizeof(float), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&order, (size_t)n * sizeof(int32_t), st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&raw, (size_t)n * sizeof(float), st);
+  if (e == cudaSuccess) e = scratch_alloc(&radii, (size_t)n * es, st);
+  if (e != cudaSuccess) rc = cuda_error(e, "training buffers");
+  // targets (log d_k of each query's own k) and raw inputs
+  if (rc == kOk) {
+    rc = batch_dispatch(v, [&](auto t, auto d) {
+      using T = decltype(t);
+      k_batch_targets<T><<<ceil_div(n, 256), 256, 0, st>>>(static_cast<const T*>(d2), n, v.qOffset, v.outOffset,
+                                                           v.kOf, v.nClouds, 1e-30, Y);
+      k_batch_features<T, decltype(d)::value><<<ceil_div(n, 128), 128, 0, st>>>(
+          static_cast<const T*>(query), n, batch_feat<T>(v), m->fs, 0, X);
+      return kOk;
+    });
+  }
+  std::vector<float> hy((size_t)n), hx;
+  if (rc == kOk) {
+    hx.resize((size_t)n * kF);
+    e = cudaMemcpyAsync(hy.data(), Y, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hx.data(), X, hx.size() * sizeof(float), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = cuda_error(e, "training data");
+  }
+  std::vector<int32_t> valid;
+  double medianDk = 0.0;
+  if (rc == kOk) rc = standardise_targets(m, hy, &valid, &medianDk);
+  // input normalisation from the training samples: centre = mean, scale so
+  // that two standard deviations map to 1
+  if (rc == kOk) {
+    FeatureSpace& fs = m->fs;
+    fs.dim = v.dim;
+    fs.nIn = kBatchInputs;
+    fs.useGrid = 0;
+    for (int j = 0; j < kMaxDim; ++j) {
+      fs.center[j] = 0.0f;
+      fs.invHalf[j] = 0.0f;
+    }
+    for (int j = 0; j < kBatchInputs; ++j) {
+      double sum = 0.0, sq = 0.0;
+      for (int32_t i : valid) {
+        const double x = hx[(size_t)i * kF + j];
+        sum += x;
+        sq += x * x;
+      }
+      const double mean = sum / valid.size();
+      const double sd = std::sqrt(std::max(sq / valid.size() - mean * mean, 0.0));
+      fs.center[j] = (float)mean;
+      fs.invHalf[j] = sd > 1e-12 ? (float)(0.5 / sd) : 0.0f;
+    }
+    for (int64_t i = 0; i < n; ++i)
+      for (int j = 0; j < kF; ++j) {
+        float& x = hx[(size_t)i * kF + j];
+        x = j < kBatchInputs ? std::min(4.0f, std::max(-4.0f, (x - fs.center[j]) * fs.invHalf[j])) : 0.0f;
+      }
+    e = cudaMemcpyAsync(X, hx.data(), hx.size() * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(Y, hy.data(), (size_t)n * sizeof(float), cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "training data upload");
+  }
+  if (rc == kOk) rc = fit_params(m, X, Y, valid, tp, order, loss, st);
+  m->margin = 0.0f;
+  if (rc == kOk && tp.targetMissRate > 0.0f) rc = launch_radius_batch(*m, v, query, 1e300, radii, raw, st);
+  if (rc == kOk && tp.targetMissRate > 0.0f) rc = calibrate_margin(m, hy, valid, raw, n, tp, st);
+  for (void* p : {(void*)X, (void*)Y, (void*)loss, (void*)raw, (void*)order, radii})
+    if (p) scratch_free(p, st);
   if (rc != kOk) return fail(rc);
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return fail(cuda_error(e, "training"));
@@ -1133,6 +1482,31 @@ struct DevGuard {
 };
 }  // namespace
 
+extern "C" void nabo_cuda_train_params_init(nabo_cuda_train_params* p);
+
+namespace {
+const char* const kBatchModelOnly =
+    "a batched radius model serves nabo_cuda_batch_knn_learned_device only (its inputs come from a batch's trees)";
+
+// The caller's training parameters (defaults for NULL), checked.
+int read_train_params(const nabo_cuda_train_params* params, nabo_cuda_train_params* tp) {
+  nabo_cuda_train_params_init(tp);
+  if (params) {
+    tp->epochs = params->epochs;
+    tp->batch = params->batch;
+    tp->lr = params->lr;
+    tp->safety = params->safety;
+    tp->targetMissRate = params->targetMissRate;
+    tp->seed = params->seed;
+  }
+  if (tp->epochs < 1 || tp->batch < 32 || !(tp->lr > 0.0f) || !(tp->safety >= 1.0f) ||
+      !(tp->targetMissRate >= 0.0f && tp->targetMissRate < 1.0f))
+    return set_error(kErrArgument,
+                     "training parameters: epochs >= 1, batch >= 32, lr > 0, safety >= 1, 0 <= targetMissRate < 1");
+  return kOk;
+}
+}  // namespace
+
 extern "C" {
 
 void nabo_cuda_train_params_init(nabo_cuda_train_params* p) {
@@ -1160,19 +1534,8 @@ int nabo_cuda_radius_model_train(const nabo_cuda_search* s, const void* trainQue
   if (n < 16 || !trainQueries) return set_error(kErrArgument, "at least 16 training queries are needed");
   if (n > (int64_t)1 << 30) return set_error(kErrUnsupported, "too many training queries");
   nabo_cuda_train_params tp;
-  nabo_cuda_train_params_init(&tp);
-  if (params) {
-    tp.epochs = params->epochs;
-    tp.batch = params->batch;
-    tp.lr = params->lr;
-    tp.safety = params->safety;
-    tp.targetMissRate = params->targetMissRate;
-    tp.seed = params->seed;
-  }
-  if (tp.epochs < 1 || tp.batch < 32 || !(tp.lr > 0.0f) || !(tp.safety >= 1.0f) ||
-      !(tp.targetMissRate >= 0.0f && tp.targetMissRate < 1.0f))
-    return set_error(kErrArgument,
-                     "training parameters: epochs >= 1, batch >= 32, lr > 0, safety >= 1, 0 <= targetMissRate < 1");
+  rc = read_train_params(params, &tp);
+  if (rc != kOk) return rc;
   DevGuard g(h.device);
   RadiusModel* m = nullptr;
   rc = radius_model_train(s, trainQueries, n, qStride, k, optionFlags, maxRadius, tp, &m, cudaStreamPerThread);
@@ -1192,6 +1555,7 @@ int nabo_cuda_radius_model_destroy(nabo_cuda_radius_model* m) {
 int nabo_cuda_radius_model_predict_device(const nabo_cuda_radius_model* m, const void* query, int qRows, int64_t nq,
                                           int64_t qStride, double maxRadius, void* radii, float* raw, void* stream) {
   if (!m) return set_error(kErrArgument, "radius model is NULL");
+  if (m->m->kind != 0) return set_error(kErrArgument, kBatchModelOnly);
   if (nq < 0 || qStride < qRows || qRows < m->m->dim) return set_error(kErrArgument, "bad query shape");
   if (nq == 0) return kOk;
   if (!query || !radii) return set_error(kErrArgument, "NULL query or radii buffer");
@@ -1284,6 +1648,7 @@ int nabo_cuda_knn_learned(const nabo_cuda_search* s, const nabo_cuda_radius_mode
 int nabo_cuda_radius_model_features_device(const nabo_cuda_radius_model* m, const void* query, int qRows, int64_t nq,
                                            int64_t qStride, float* features, void* stream) {
   if (!m) return set_error(kErrArgument, "radius model is NULL");
+  if (m->m->kind != 0) return set_error(kErrArgument, kBatchModelOnly);
   if (nq < 0 || qStride < qRows || qRows < m->m->dim) return set_error(kErrArgument, "bad query shape");
   if (nq == 0) return kOk;
   DevGuard g(m->device);
@@ -1306,8 +1671,103 @@ int nabo_cuda_radius_model_get(const nabo_cuda_radius_model* m, float* params, f
 
 int nabo_cuda_radius_model_set(nabo_cuda_radius_model* m, const float* params, const float* meta) {
   if (!m) return set_error(kErrArgument, "radius model is NULL");
+  if (m->m->kind != 0) return set_error(kErrArgument, "a batched radius model keeps its trained input scaling; it is not set");
   DevGuard g(m->device);
   return radius_model_set(*m->m, params, meta);
+}
+
+int nabo_cuda_batch_radius_model_train(nabo_cuda_batch* b, const void* queries, const void* dists2,
+                                       const nabo_cuda_train_params* params, nabo_cuda_radius_model** out) {
+  if (!b || !out) return set_error(kErrArgument, "NULL batch or output pointer");
+  *out = nullptr;
+  BatchView v;
+  int rc = batch_view(b, &v);
+  if (rc != kOk) return rc;
+  if (v.nq < 16 || !queries || !dists2) return set_error(kErrArgument, "at least 16 training queries are needed");
+  if (v.nq > (int64_t)1 << 30) return set_error(kErrUnsupported, "too many training queries");
+  nabo_cuda_train_params tp;
+  rc = read_train_params(params, &tp);
+  if (rc != kOk) return rc;
+  DevGuard g(v.device);
+  RadiusModel* m = nullptr;
+  rc = batch_radius_model_train(v, queries, dists2, tp, &m, cudaStreamPerThread);
+  if (rc != kOk) return rc;
+  *out = new nabo_cuda_radius_model{m, v.device};
+  return kOk;
+}
+
+int nabo_cuda_batch_knn_learned_device(nabo_cuda_batch* b, const nabo_cuda_radius_model* m, const void* queries,
+                                       double epsilon, unsigned optionFlags, double maxRadius, int32_t* indices,
+                                       void* dists2, int32_t* fallbacks, void* stream) {
+  if (!b || !m) return set_error(kErrArgument, "NULL batch or radius model");
+  BatchView v;
+  int rc = batch_view(b, &v);
+  if (rc != kOk) return rc;
+  const RadiusModel& rm = *m->m;
+  if (rm.kind != 1 || rm.dtype != v.dtype || rm.dim != v.dim)
+    return set_error(kErrArgument, "the radius model was not trained for batches of this dimension and scalar type");
+  if (v.nq == 0) return kOk;
+  if (!queries || !indices || !dists2) return set_error(kErrArgument, "NULL query or result buffer");
+  DevGuard g(v.device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t es = v.dtype == NABO_CUDA_FLOAT32 ? 4 : 8;
+  void* radii = nullptr;
+  int32_t* count = nullptr;
+  cudaError_t e = scratch_alloc(&radii, (size_t)v.nq * es, st);
+  if (e == cudaSuccess) e = scratch_alloc((void**)&count, sizeof(int32_t), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(count, 0, sizeof(int32_t), st);
+  rc = e == cudaSuccess ? kOk : cuda_error(e, "learned batch buffers");
+  if (rc == kOk) rc = launch_radius_batch(rm, v, queries, maxRadius, radii, nullptr, st);
+  if (rc == kOk)
+    rc = nabo_cuda_batch_knn_radii_device(b, queries, radii, epsilon, optionFlags, maxRadius, indices, dists2, count,
+                                          stream);
+  if (rc == kOk && fallbacks) {
+    e = cudaMemcpyAsync(fallbacks, count, sizeof(int32_t), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) rc = cuda_error(e, "fallback count");
+  }
+  if (radii) scratch_free(radii, st);
+  if (count) scratch_free(count, st);
+  return rc;
+}
+
+int nabo_cuda_batch_radius_model_predict_device(nabo_cuda_batch* b, const nabo_cuda_radius_model* m,
+                                                const void* queries, double maxRadius, void* radii, float* raw,
+                                                void* stream) {
+  if (!b || !m) return set_error(kErrArgument, "NULL batch or radius model");
+  BatchView v;
+  int rc = batch_view(b, &v);
+  if (rc != kOk) return rc;
+  const RadiusModel& rm = *m->m;
+  if (rm.kind != 1 || rm.dtype != v.dtype || rm.dim != v.dim)
+    return set_error(kErrArgument, "the radius model was not trained for batches of this dimension and scalar type");
+  if (v.nq == 0) return kOk;
+  if (!queries || !radii) return set_error(kErrArgument, "NULL query or radii buffer");
+  DevGuard g(v.device);
+  return launch_radius_batch(rm, v, queries, maxRadius, radii, raw, static_cast<cudaStream_t>(stream));
+}
+
+int nabo_cuda_batch_radius_model_features_device(nabo_cuda_batch* b, const nabo_cuda_radius_model* m,
+                                                 const void* queries, float* features, void* stream) {
+  if (!b || !m) return set_error(kErrArgument, "NULL batch or radius model");
+  BatchView v;
+  int rc = batch_view(b, &v);
+  if (rc != kOk) return rc;
+  const RadiusModel& rm = *m->m;
+  if (rm.kind != 1 || rm.dtype != v.dtype || rm.dim != v.dim)
+    return set_error(kErrArgument, "the radius model was not trained for batches of this dimension and scalar type");
+  if (v.nq == 0) return kOk;
+  if (!queries || !features) return set_error(kErrArgument, "NULL query or feature buffer");
+  DevGuard g(v.device);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rc = batch_dispatch(v, [&](auto t, auto d) {
+    using T = decltype(t);
+    k_batch_features<T, decltype(d)::value><<<ceil_div(v.nq, 128), 128, 0, st>>>(
+        static_cast<const T*>(queries), v.nq, batch_feat<T>(v), rm.fs, 1, features);
+    return kOk;
+  });
+  if (rc != kOk) return rc;
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? kOk : cuda_error(e, "batched features kernel");
 }
 
 }  // extern "C"

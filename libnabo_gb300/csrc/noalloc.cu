@@ -11,9 +11,12 @@
 // query's cell and its rank inside the cell, plus a kBins-entry cell
 // histogram. Queries are grouped by a Morton (Z-order) cell of the cloud's
 // bounding box, counted, scanned and placed, then the kd-tree search kernel
-// runs with that order. Every call on a device reuses the array: the
-// histogram is cleared at the start of each call, and calls that overlap on
-// the GPU race.
+// runs with that order. Queries are ordered under the same rule as the
+// regular search (the object's queryOrdering parameter, and enough work for
+// the order to pay). A kd-tree taller than the search kernels' stacks (256
+// levels) is searched unordered with its traversal stacks in the array
+// instead. Every call on a device reuses the array: the histogram is
+// cleared at the start of each call, and calls that overlap on the GPU race.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -41,16 +44,27 @@ constexpr int kMaxDevices = 64;
 std::mutex g_addrMutex;
 unsigned char* g_addr[kMaxDevices] = {};
 
-// Device address of the scratch on the current device, looked up once per
-// device (the first call must therefore come before any stream capture).
-int scratch_address(int device, unsigned char** out) {
+// Device address of the scratch on the current device. It is looked up on
+// every call made outside a stream capture, so that it follows the module
+// if the device's context is torn down and made again (cudaDeviceReset);
+// a call made while `stream` is capturing uses the address of the last call
+// outside capture, because the lookup may load the module. So the first
+// call on a device comes before any capture, and after a cudaDeviceReset
+// one call outside capture comes before capturing again.
+int scratch_address(int device, cudaStream_t stream, unsigned char** out) {
   if (device < 0 || device >= kMaxDevices) return set_error(kErrUnsupported, "device ordinal out of range");
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(stream, &cs);
+  if (e != cudaSuccess) return cuda_error(e, "cudaStreamIsCapturing");
   std::lock_guard<std::mutex> lock(g_addrMutex);
-  if (!g_addr[device]) {
+  if (cs == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
+    e = cudaGetSymbolAddress(&p, g_noallocScratch);
     if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(no-alloc scratch)");
     g_addr[device] = static_cast<unsigned char*>(p);
+  } else if (!g_addr[device]) {
+    return set_error(kErrArgument, "nabo_cuda_knn_device_noalloc: the first call on a device must come before "
+                                   "any stream capture");
   }
   *out = g_addr[device];
   return kOk;
@@ -71,6 +85,10 @@ Layout layout(unsigned char* base) {
   l.hist = reinterpret_cast<uint32_t*>(base + (size_t)kMaxQueries * 12);
   return l;
 }
+
+// Levels the search kernels' own stacks hold (taller trees search with
+// their stacks in the array).
+constexpr int kSearchStackLevels = 256;
 
 constexpr int kCellDims = 10;
 struct CellGrid {
@@ -187,6 +205,7 @@ int search_noalloc(const DeviceCloud& c, const KnnArgs& a, const Layout* l, cuda
     if (rc != kOk) return rc;
     order = l->order;
   }
+  // a.stackSlab (set for tall trees) keeps this from allocating stacks
   return knn_kdtree_given_order<T, D>(c, a, order, st);
 }
 
@@ -245,15 +264,23 @@ extern "C" int nabo_cuda_knn_device_noalloc(const nabo_cuda_search* s, const voi
   a.indices = indices;
   a.dists2 = dists2;
   a.traversal = h.traversal;
+  a.evStart = h.evStart;
+  a.evStop = h.evStop;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (h.searchType == NABO_SEARCH_KDTREE_CUDA) {
     a.touchStats = (h.creationFlags & NABO_TOUCH_STATISTICS) != 0;
     a.touched = reinterpret_cast<unsigned long long*>(touched);
     unsigned char* base = nullptr;
-    rc = scratch_address(h.device, &base);
+    rc = scratch_address(h.device, st, &base);
     if (rc == kOk) {
       const Layout l = layout(base);
-      rc = dispatch(*h.cloud, a, nq >= 4096 ? &l : nullptr, st);
+      const bool tall = h.cloud->height > kSearchStackLevels;
+      if (tall) {  // the whole array holds the traversal stacks; no ordering
+        a.stackSlab = base;
+        a.stackSlabBytes = kScratchBytes;
+      }
+      const bool ordered = !tall && h.sortQueries && worth_sorting(nq, k, h.cloud->dim);
+      rc = dispatch(*h.cloud, a, ordered ? &l : nullptr, st);
     }
   } else {
     rc = set_error(kErrArgument, "nabo_cuda_knn_device_noalloc serves kd-tree objects; "

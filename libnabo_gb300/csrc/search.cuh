@@ -236,6 +236,24 @@ struct KnnLaunch {
   const int32_t* bK;
   const int64_t* bOutOffset;
   int bClouds;
+  // Trees taller than the compiled stacks (the reference's recursion has no
+  // depth limit, nabo/kdtree_cpu.cpp:367-447):
+  //  - ovfList/ovfCount (the batch's local-stack kernels): a query whose
+  //    stack would overflow stops without writing anything and appends its
+  //    order position (+ ovfBase) to ovfList, for k_knn_kdtree_deep;
+  //  - slab/slabBytes: traversal stacks in global memory for the deep
+  //    kernels, `cap` entries per query (stackCap, or the tree height read
+  //    from *stackHeightDev plus one); list/listCount: the positions to
+  //    search (null: all nq).
+  int32_t* ovfList;
+  int32_t* ovfCount;
+  int64_t ovfBase;
+  void* slab;
+  int64_t slabBytes;
+  int stackCap;
+  const int* stackHeightDev;
+  const int32_t* list;
+  const int32_t* listCount;
 };
 
 // Leaf scan shared by the kernels: the bucket's records are read in chunks
@@ -402,7 +420,7 @@ __device__ __forceinline__ double get_t<double>(const uint32_t* w, int i) {
 }
 
 template <typename T, int D>
-__device__ __forceinline__ void stack_push(StackRec<T, D>* stk, int sp, T rd, const T (&off)[D], int cd, T newOff,
+__device__ __forceinline__ void stack_push(StackRec<T, D>& e, T rd, const T (&off)[D], int cd, T newOff,
                                            uint32_t node) {
   using R = StackRec<T, D>;
   uint32_t w[R::kChunks * 4];
@@ -415,30 +433,30 @@ __device__ __forceinline__ void stack_push(StackRec<T, D>* stk, int sp, T rd, co
 #pragma unroll
   for (int c = 0; c < R::kChunks; ++c) {
     if (c == R::kChunks - 1 && R::kWords % 4 == 1)
-      stk[sp].v[c].x = w[4 * c];
+      e.v[c].x = w[4 * c];
     else
-      stk[sp].v[c] = make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
+      e.v[c] = make_uint4(w[4 * c], w[4 * c + 1], w[4 * c + 2], w[4 * c + 3]);
   }
 }
 
 template <typename T, int D>
-__device__ __forceinline__ T stack_rd(const StackRec<T, D>* stk, int sp) {
-  const uint4 c0 = stk[sp].v[0];
+__device__ __forceinline__ T stack_rd(const StackRec<T, D>& e) {
+  const uint4 c0 = e.v[0];
   const uint32_t w[4] = {c0.x, c0.y, c0.z, c0.w};
   return get_t<T>(w, 0);
 }
 
 template <typename T, int D>
-__device__ __forceinline__ uint32_t stack_take(const StackRec<T, D>* stk, int sp, T (&off)[D]) {
+__device__ __forceinline__ uint32_t stack_take(const StackRec<T, D>& e, T (&off)[D]) {
   using R = StackRec<T, D>;
   uint32_t w[R::kChunks * 4];
 #pragma unroll
   for (int c = 0; c < R::kChunks; ++c) {
     if (c == R::kChunks - 1 && R::kWords % 4 == 1) {
-      w[4 * c] = stk[sp].v[c].x;
+      w[4 * c] = e.v[c].x;
       w[4 * c + 1] = w[4 * c + 2] = w[4 * c + 3] = 0u;
     } else {
-      const uint4 v = stk[sp].v[c];
+      const uint4 v = e.v[c];
       w[4 * c] = v.x;
       w[4 * c + 1] = v.y;
       w[4 * c + 2] = v.z;
@@ -450,14 +468,34 @@ __device__ __forceinline__ uint32_t stack_take(const StackRec<T, D>* stk, int sp
   return w[R::kNode];
 }
 
-// Reference-order traversal, structured descend / leaf / pop so the lanes
-// of a warp run each phase together: all lanes descend until every lane
-// stands on a leaf, then all scan their leaves, then all pop.
+// Where a query's traversal stack lives: a local array of N entries (the
+// compiled kernels), or entries of a global-memory slab shared by the threads
+// of a deep launch, thread g's entry sp at slab[sp * stride + g] so that the
+// pushes of a warp at one depth are coalesced.
+template <typename T, int D, int N>
+struct LocalStack {
+  StackRec<T, D> s[N];
+  __device__ __forceinline__ StackRec<T, D>& operator[](int sp) { return s[sp]; }
+};
+template <typename T, int D>
+struct SlabStack {
+  StackRec<T, D>* base;
+  int64_t stride;
+  __device__ __forceinline__ StackRec<T, D>& operator[](int sp) { return base[(int64_t)sp * stride]; }
+};
+
+// One query (order position t) in the reference's visit order, structured
+// descend / leaf / pop so the lanes of a warp run each phase together: all
+// lanes descend until every lane stands on a leaf, then all scan their
+// leaves, then all pop. `cap` entries of `stk` are available; the caller
+// guarantees cap > tree height, except with OVF, where a push beyond cap
+// abandons the query (nothing written, false returned) so that a deep
+// launch can search it again. Adds the points examined to `touchedOut`.
 // EXACT (epsilon 0, so maxError2 = 1 and rd * maxError2 = rd exactly): the
 // push test rd <= maxRadius2 && rd <= head is one compare against
 // min(maxRadius2, head), refreshed after each leaf; decisions are the same.
-template <typename T, int D, int K, int STACK, bool EXACT>
-__device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
+template <typename T, int D, int K, bool EXACT, bool OVF, typename S>
+__device__ __forceinline__ bool knn_query(const KnnLaunch& a, int64_t t, S& stk, int cap, uint32_t& touchedOut) {
   // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396): without
   // ALLOW_SELF_MATCH a point at distance <= epsilon is skipped; one compare
   // against -1 (everything passes) or epsilon
@@ -465,92 +503,102 @@ __device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
   const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
   const T* __restrict__ query = static_cast<const T*>(a.query);
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   uint32_t touched = 0;  // a query touches at most the cloud's n < 2^31 points
-  if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
-    const int64_t qi = a.order ? (int64_t)a.order[t] : t;
-    int k = a.k;
-    uint32_t root = 0;
-    int64_t outBase = qi * (int64_t)a.k;
-    if (a.bQueryOffset) {
-      const int c = cloud_of(a.bQueryOffset, a.bClouds, qi);
-      k = a.bK[c];
-      root = (uint32_t)a.bNodeOffset[c];
-      outBase = a.bOutOffset[c] + (qi - a.bQueryOffset[c]) * (int64_t)k;
-    }
-    T q[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) q[d] = d < a.dim ? query[qi * a.qStride + d] : T(0);
-    T maxRadius2 = (T)a.maxRadius2;
-    // a bounded search (per-query radius) that misses may run once more
-    // without its bound (the learned-radius form's fallback)
-    bool mayFall = false;
-    if (a.maxRadii) {
-      const T r = static_cast<const T*>(a.maxRadii)[qi];
-      maxRadius2 = Ar<T>::mul(r, r);
-      mayFall = a.fallbackRadius >= 0.0 && (double)r < a.fallbackRadius;
-    }
-    const T maxError2 = (T)a.maxError2;
-    TopK<T, K> heap;
-    heap.init(k);
-    LeafFilter<T, D> flt;
-    flt.init(a.recs32, a.coordMax, q);
-    T off[D];
-    StackRec<T, D> stk[STACK];
-    for (;;) {  // the search, and at most once more without the bound
-#pragma unroll
-      for (int d = 0; d < D; ++d) off[d] = T(0);
-      int sp = 0;
-      uint32_t node = root;
-      T rd = T(0);
-      for (;;) {
-        // descend to a leaf, pushing far children
-        // min(maxRadius2, head), where a NaN radius (which passes nothing) wins
-        const T bound = EXACT ? (heap.head() < maxRadius2 ? heap.head() : maxRadius2) : T(0);
-        Node<T> nd = load_node(nodes, node);
-        while (!node_is_leaf(nd.meta)) {
-          const int cd = (int)node_dim(nd.meta);
-          const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
-          const T oldOff = pick(off, cd);
-          const T rdFar = Ar<T>::add(rd, Ar<T>::add(-Ar<T>::mul(oldOff, oldOff), Ar<T>::mul(newOff, newOff)));
-          const uint32_t right = node_payload(nd.meta);
-          const uint32_t nearN = newOff > T(0) ? right : node + 1;
-          const uint32_t farN = newOff > T(0) ? node + 1 : right;
-          // sp <= tree height <= STACK (checked on the host); the test only
-          // makes the bound explicit
-          const bool far = EXACT ? rdFar <= bound
-                                 : (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head());
-          if (far && sp < STACK) stack_push(stk, sp++, rdFar, off, cd, newOff, farN);
-          node = nearN;
-          nd = load_node(nodes, node);
-        }
-        // leaf
-        const uint32_t cnt = node_payload(nd.meta);
-        scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap, flt);
-        touched += cnt;
-        // pop the next far child that can still hold a better neighbour
-        bool more = false;
-        while (sp > 0) {
-          --sp;
-          const T e = stack_rd(stk, sp);
-          if ((EXACT ? e : Ar<T>::mul(e, maxError2)) <= heap.head()) {
-            rd = e;
-            node = stack_take(stk, sp, off);
-            more = true;
-            break;
-          }
-        }
-        if (!more) break;
-      }
-      if (!mayFall || heap.count(k) == k) break;
-      mayFall = false;
-      maxRadius2 = (T)a.maxRadius2;
-      heap.init(k);
-      if (a.fallbacks) atomicAdd(a.fallbacks, 1);
-    }
-    const int f = heap.store(k, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
-    if (a.found) a.found[qi] = f;
+  const int64_t qi = a.order ? (int64_t)a.order[t] : t;
+  int k = a.k;
+  uint32_t root = 0;
+  int64_t outBase = qi * (int64_t)a.k;
+  if (a.bQueryOffset) {
+    const int c = cloud_of(a.bQueryOffset, a.bClouds, qi);
+    k = a.bK[c];
+    root = (uint32_t)a.bNodeOffset[c];
+    outBase = a.bOutOffset[c] + (qi - a.bQueryOffset[c]) * (int64_t)k;
   }
+  T q[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) q[d] = d < a.dim ? query[qi * a.qStride + d] : T(0);
+  T maxRadius2 = (T)a.maxRadius2;
+  // a bounded search (per-query radius) that misses may run once more
+  // without its bound (the learned-radius form's fallback)
+  bool mayFall = false;
+  if (a.maxRadii) {
+    const T r = static_cast<const T*>(a.maxRadii)[qi];
+    maxRadius2 = Ar<T>::mul(r, r);
+    mayFall = a.fallbackRadius >= 0.0 && (double)r < a.fallbackRadius;
+  }
+  const T maxError2 = (T)a.maxError2;
+  TopK<T, K> heap;
+  heap.init(k);
+  LeafFilter<T, D> flt;
+  flt.init(a.recs32, a.coordMax, q);
+  T off[D];
+  for (;;) {  // the search, and at most once more without the bound
+#pragma unroll
+    for (int d = 0; d < D; ++d) off[d] = T(0);
+    int sp = 0;
+    uint32_t node = root;
+    T rd = T(0);
+    for (;;) {
+      // descend to a leaf, pushing far children
+      // min(maxRadius2, head), where a NaN radius (which passes nothing) wins
+      const T bound = EXACT ? (heap.head() < maxRadius2 ? heap.head() : maxRadius2) : T(0);
+      Node<T> nd = load_node(nodes, node);
+      while (!node_is_leaf(nd.meta)) {
+        const int cd = (int)node_dim(nd.meta);
+        const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
+        const T oldOff = pick(off, cd);
+        const T rdFar = Ar<T>::add(rd, Ar<T>::add(-Ar<T>::mul(oldOff, oldOff), Ar<T>::mul(newOff, newOff)));
+        const uint32_t right = node_payload(nd.meta);
+        const uint32_t nearN = newOff > T(0) ? right : node + 1;
+        const uint32_t farN = newOff > T(0) ? node + 1 : right;
+        const bool far = EXACT ? rdFar <= bound
+                               : (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head());
+        if constexpr (OVF) {
+          if (far) {
+            if (sp >= cap) return false;
+            stack_push(stk[sp++], rdFar, off, cd, newOff, farN);
+          }
+        } else {
+          // sp <= tree height < cap (checked by the caller); the test only
+          // makes the bound explicit
+          if (far && sp < cap) stack_push(stk[sp++], rdFar, off, cd, newOff, farN);
+        }
+        node = nearN;
+        nd = load_node(nodes, node);
+      }
+      // leaf
+      const uint32_t cnt = node_payload(nd.meta);
+      scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap, flt);
+      touched += cnt;
+      // pop the next far child that can still hold a better neighbour
+      bool more = false;
+      while (sp > 0) {
+        --sp;
+        const T e = stack_rd(stk[sp]);
+        if ((EXACT ? e : Ar<T>::mul(e, maxError2)) <= heap.head()) {
+          rd = e;
+          node = stack_take(stk[sp], off);
+          more = true;
+          break;
+        }
+      }
+      if (!more) break;
+    }
+    if (!mayFall || heap.count(k) == k) break;
+    mayFall = false;
+    maxRadius2 = (T)a.maxRadius2;
+    heap.init(k);
+    if (a.fallbacks) atomicAdd(a.fallbacks, 1);
+  }
+  const int f = heap.store(k, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
+  if (a.found) a.found[qi] = f;
+  touchedOut += touched;
+  return true;
+}
+
+// The warp's TOUCH_STATISTICS counts summed into a.touched (every lane of
+// the warp calls this).
+__device__ __forceinline__ void add_touched(const KnnLaunch& a, uint32_t touched) {
   if (a.stats) {
     unsigned long long sum = touched;
 #pragma unroll
@@ -559,34 +607,92 @@ __device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
   }
 }
 
-template <typename T, int D, int K, int STACK, bool EXACT>
+// One thread per query, stack of STACK entries in local memory. With OVF
+// (batches, whose tree heights are known only on the device) a query whose
+// tree is taller than STACK is handed to k_knn_kdtree_deep through
+// a.ovfList.
+template <typename T, int D, int K, int STACK, bool EXACT, bool OVF>
+__device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
+  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  uint32_t touched = 0;
+  if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
+    LocalStack<T, D, STACK> stk;
+    if (!knn_query<T, D, K, EXACT, OVF>(a, t, stk, STACK, touched)) {
+      if constexpr (OVF) a.ovfList[atomicAdd(a.ovfCount, 1)] = (int32_t)(t + a.ovfBase);
+    }
+  }
+  add_touched(a, touched);
+}
+
+template <typename T, int D, int K, int STACK, bool EXACT, bool OVF>
 __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
-  knn_kdtree_body<T, D, K, STACK, EXACT>(a);
+  knn_kdtree_body<T, D, K, STACK, EXACT, OVF>(a);
 }
 
 // Double searches with a long top-k hold ~100 registers of heap alone;
 // limited to 128 registers a thread, 4 blocks share an SM, and the FP64 pipe
 // gets the extra warps it needs to hide its latency (12 % faster on 8-D
 // clouds, k = 32).
-template <typename T, int D, int K, int STACK, bool EXACT>
+template <typename T, int D, int K, int STACK, bool EXACT, bool OVF>
 __global__ void __launch_bounds__(128, 4) k_knn_kdtree_lean(KnnLaunch a) {
-  knn_kdtree_body<T, D, K, STACK, EXACT>(a);
+  knn_kdtree_body<T, D, K, STACK, EXACT, OVF>(a);
 }
 
-template <typename T, int D, int K, int STACK, bool EXACT>
+// Trees of any height: the stacks in a.slab, cap = a.stackCap entries per
+// query (or the tree height read from *a.stackHeightDev, plus one, for
+// batches whose heights the host does not know). As many threads as the
+// slab holds stacks search (the others idle), each taking every active-th
+// item of a.list (or of 0..nq-1). A slab too small for one stack searches
+// nothing and sets *a.ovfCount to -1.
+template <typename T, int D, int K, bool EXACT>
+__global__ void __launch_bounds__(128) k_knn_kdtree_deep(KnnLaunch a) {
+  const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t threads = (int64_t)gridDim.x * blockDim.x;
+  const int cap = a.stackCap > 0 ? a.stackCap : (a.stackHeightDev ? *a.stackHeightDev + 1 : 0);
+  int64_t active = cap > 0 ? a.slabBytes / ((int64_t)sizeof(StackRec<T, D>) * cap) : 0;
+  if (active > threads) active = threads;
+  const int64_t count = a.list ? (int64_t)*a.listCount : a.nq;
+  if (active <= 0 && count > 0 && g == 0 && a.ovfCount) *a.ovfCount = -1;
+  uint32_t touched = 0;
+  if (g < active) {
+    SlabStack<T, D> stk{static_cast<StackRec<T, D>*>(a.slab) + g, active};
+    for (int64_t w = g; w < count; w += active) {
+      const int64_t t = a.list ? (int64_t)a.list[w] : w;
+      if (a.nqDevice && t >= (int64_t)*a.nqDevice) continue;
+      knn_query<T, D, K, EXACT, false>(a, t, stk, cap, touched);
+    }
+  }
+  add_touched(a, touched);
+}
+
+// Bytes of one query's stack in a deep launch's slab, for `cap` entries.
+template <typename T, int D>
+constexpr size_t deep_stack_bytes(int cap) {
+  return sizeof(StackRec<T, D>) * (size_t)cap;
+}
+
+template <typename T, int D, int K, int STACK, bool EXACT, bool OVF>
 void launch_kdtree_as(int grid, int block, cudaStream_t stream, const KnnLaunch& L) {
   if constexpr (sizeof(T) == 8 && K >= 16)
-    k_knn_kdtree_lean<T, D, K, STACK, EXACT><<<grid, block, 0, stream>>>(L);
+    k_knn_kdtree_lean<T, D, K, STACK, EXACT, OVF><<<grid, block, 0, stream>>>(L);
   else
-    k_knn_kdtree<T, D, K, STACK, EXACT><<<grid, block, 0, stream>>>(L);
+    k_knn_kdtree<T, D, K, STACK, EXACT, OVF><<<grid, block, 0, stream>>>(L);
 }
 
-template <typename T, int D, int K, int STACK>
+template <typename T, int D, int K, int STACK, bool OVF = false>
 void launch_kdtree(int grid, int block, cudaStream_t stream, const KnnLaunch& L) {
   if (L.maxError2 == 1.0)
-    launch_kdtree_as<T, D, K, STACK, true>(grid, block, stream, L);
+    launch_kdtree_as<T, D, K, STACK, true, OVF>(grid, block, stream, L);
   else
-    launch_kdtree_as<T, D, K, STACK, false>(grid, block, stream, L);
+    launch_kdtree_as<T, D, K, STACK, false, OVF>(grid, block, stream, L);
+}
+
+template <typename T, int D, int K>
+void launch_kdtree_deep(int grid, cudaStream_t stream, const KnnLaunch& L) {
+  if (L.maxError2 == 1.0)
+    k_knn_kdtree_deep<T, D, K, true><<<grid, 128, 0, stream>>>(L);
+  else
+    k_knn_kdtree_deep<T, D, K, false><<<grid, 128, 0, stream>>>(L);
 }
 
 // Warp-packet traversal for exact search (epsilon = 0).
@@ -697,33 +803,62 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
 }
 
 // Brute force (nabo/brute_force_cpu.cpp:63-103): every query against every
-// point, points staged through shared memory in tiles; each thread owns one
-// query and its top-k. Points are offered in index order.
-template <typename T, int D, int K>
-__global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a) {
-  // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396): without
-  // ALLOW_SELF_MATCH a point at distance <= epsilon is skipped; one compare
-  // against -1 (everything passes) or epsilon
+// point. The points are staged through shared memory in tiles of 24 KB; a
+// thread owns QT queries (blockDim.x apart) and their top-k, so each record
+// read from shared memory (a broadcast: every lane reads the same one) feeds
+// QT distances. The distance is the reference's separately rounded
+// sequential sum; a point is first compared with one float threshold,
+// min(head, maxRadius^2) (NaN radius: NaN, which passes nothing), and only
+// the rare points at or below it take the exact test -- the reference's
+// radius and self-match rules and the (dist2, index) order against the head
+// (nabo/kdtree_cpu.cpp:392-396 with the lower index kept on ties). The
+// result, the k smallest pairs, does not depend on the order points are
+// offered in.
+template <typename T>
+__device__ __forceinline__ T bf_threshold(T head, T maxRadius2) {
+  return head < maxRadius2 ? head : maxRadius2;
+}
+
+// With gridDim.y > 1 the points are split into chunks of `chunk` (a
+// multiple of the tile): block row y offers points [y*chunk, (y+1)*chunk) and
+// writes its k best to a.outIdx / a.outD2 + y*partStride, and
+// k_bf_merge combines the rows (for searches with too few queries to give
+// every SM several blocks).
+template <typename T, int D, int K, int QT>
+__global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a, int64_t chunk, int64_t partStride) {
   const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
   constexpr int kTile = (int)((24 * 1024) / sizeof(Rec<T, D>));
   __shared__ Rec<T, D> tile[kTile];
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
   const T* __restrict__ query = static_cast<const T*>(a.query);
-  const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  const bool active = t < a.nq;
-  const int64_t qi = active ? (a.order ? (int64_t)a.order[t] : t) : 0;
-  T q[D];
+  const int64_t base0 = (int64_t)blockIdx.x * blockDim.x * QT + threadIdx.x;
+  T q[QT][D];
+  T maxRadius2[QT];
+  T thr[QT];
+  int64_t qi[QT];
+  bool active[QT];
+  TopK<T, K> heap[QT];
 #pragma unroll
-  for (int d = 0; d < D; ++d) q[d] = (active && d < a.dim) ? query[qi * a.qStride + d] : T(0);
-  T maxRadius2 = (T)a.maxRadius2;
-  if (a.maxRadii && active) {
-    const T r = static_cast<const T*>(a.maxRadii)[qi];
-    maxRadius2 = Ar<T>::mul(r, r);
+  for (int u = 0; u < QT; ++u) {
+    const int64_t t = base0 + (int64_t)u * blockDim.x;
+    active[u] = t < a.nq;
+    qi[u] = active[u] ? (a.order ? (int64_t)a.order[t] : t) : 0;
+#pragma unroll
+    for (int d = 0; d < D; ++d) q[u][d] = (active[u] && d < a.dim) ? query[qi[u] * a.qStride + d] : T(0);
+    maxRadius2[u] = (T)a.maxRadius2;
+    if (a.maxRadii && active[u]) {
+      const T r = static_cast<const T*>(a.maxRadii)[qi[u]];
+      maxRadius2[u] = Ar<T>::mul(r, r);
+    }
+    // an idle slot wants nothing (a NaN threshold passes no point)
+    if (!active[u]) maxRadius2[u] = __builtin_nan("");
+    heap[u].init(a.k);
+    thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
   }
-  TopK<T, K> heap;
-  heap.init(a.k);
-  for (int64_t base = 0; base < a.n; base += kTile) {
-    const int m = (int)((a.n - base) < kTile ? (a.n - base) : kTile);
+  const int64_t first = (int64_t)blockIdx.y * chunk;
+  const int64_t last = first + chunk < a.n ? first + chunk : a.n;
+  for (int64_t base = first; base < last; base += kTile) {
+    const int m = (int)((last - base) < kTile ? (last - base) : kTile);
     __syncthreads();
     {
       const uint4* src = reinterpret_cast<const uint4*>(recs + base);
@@ -732,19 +867,58 @@ __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a) {
       for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = __ldg(src + w);
     }
     __syncthreads();
-    if (active) {
-      for (int j = 0; j < m; ++j) {
-        const Rec<T, D>& r = tile[j];
-        const T dist = dist2_seq(q, r);
-        if (dist <= maxRadius2 && heap.accepts(dist, r.p.idx) && dist > minDist)
-          heap.insert(dist, r.p.idx);
+#pragma unroll 4
+    for (int j = 0; j < m; ++j) {
+      const Rec<T, D> r = tile[j];
+#pragma unroll
+      for (int u = 0; u < QT; ++u) {
+        const T dist = dist2_seq(q[u], r);
+        if (dist <= thr[u]) {
+          if (dist <= maxRadius2[u] && heap[u].accepts(dist, r.p.idx) && dist > minDist) {
+            heap[u].insert(dist, r.p.idx);
+            thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
+          }
+        }
       }
     }
   }
-  if (active) {
-    const int f = heap.store(a.k, a.outIdx + qi * a.k, static_cast<T*>(a.outD2) + qi * a.k);
-    if (a.found) a.found[qi] = f;
+  const int64_t part = (int64_t)blockIdx.y * partStride;
+#pragma unroll
+  for (int u = 0; u < QT; ++u) {
+    if (active[u]) {
+      const int f = heap[u].store(a.k, a.outIdx + part + qi[u] * a.k, static_cast<T*>(a.outD2) + part + qi[u] * a.k);
+      if (a.found) a.found[qi[u]] = f;
+    }
   }
 }
+
+// The k best of `parts` partial results per query (each k entries, ascending,
+// unfound slots index -1), written as the search's result.
+template <typename T, int K>
+__global__ void k_bf_merge(const int32_t* __restrict__ pIdx, const T* __restrict__ pD2, int parts, int64_t partStride,
+                           int64_t nq, int k, int32_t* outIdx, T* outD2, int32_t* found) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nq) return;
+  TopK<T, K> heap;
+  heap.init(k);
+  for (int p = 0; p < parts; ++p) {
+    const int64_t o = p * partStride + i * k;
+    for (int j = 0; j < k; ++j) {
+      const int32_t idx = pIdx[o + j];
+      if (idx < 0) break;
+      const T d = pD2[o + j];
+      if (heap.accepts(d, idx)) heap.insert(d, idx);
+    }
+  }
+  const int f = heap.store(k, outIdx + i * k, outD2 + i * k);
+  if (found) found[i] = f;
+}
+
+// Queries per thread of the brute force: more share each shared-memory read,
+// fewer keep long top-k lists in registers.
+template <typename T, int K>
+struct BfQueries {
+  static constexpr int value = sizeof(T) == 8 ? 1 : (K <= 8 ? 4 : (K <= 16 ? 2 : 1));
+};
 
 }  // namespace nabo_gb300

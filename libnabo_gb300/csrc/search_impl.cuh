@@ -6,7 +6,9 @@
 #include "search.cuh"
 #include "search_wide.cuh"
 
+#include <algorithm>
 #include <cstring>
+#include <string>
 
 namespace nabo_gb300 {
 
@@ -54,31 +56,79 @@ inline int k_unsupported() {
   return set_error(kErrUnsupported, "k larger than 1024 is not supported by the CUDA search types");
 }
 
-template <typename T, int D, int M, int G>
+// Shared memory the wide kernel's stacks may take per block; trees too tall
+// for one warp's stacks there search with the stacks in global memory.
+constexpr size_t kWideSmemMax = 160 * 1024;
+// Internal: the search needs its stacks in global memory.
+constexpr int kNeedsSlab = -100;
+
+template <typename T, int D, int M, int G, bool OVF>
 int launch_wide_kdtree_as(const KnnLaunch& L, int height, cudaStream_t stream) {
   const int cap = height + 1;
   // the groups' stacks in shared memory: smaller blocks for tall trees of
   // long records
   int threads = kWideThreads;
-  while (threads > 32 && wide_stack_bytes<T, D>(threads / G, cap) > (size_t)160 * 1024) threads /= 2;
+  while (threads > 32 && wide_stack_bytes<T, D>(threads / G, cap) > kWideSmemMax) threads /= 2;
   const size_t smem = wide_stack_bytes<T, D>(threads / G, cap);
+  if (smem > kWideSmemMax) return kNeedsSlab;
   cudaError_t e = cudaSuccess;
   if (smem > 48 * 1024)
-    e = cudaFuncSetAttribute(k_knn_kdtree_wide<T, D, M, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaFuncSetAttribute(k_knn_kdtree_wide<T, D, M, G, OVF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "wide kd-tree search shared memory");
   const int grid = ceil_div(L.nq, threads / G);
-  k_knn_kdtree_wide<T, D, M, G><<<grid, threads, smem, stream>>>(L, cap);
+  k_knn_kdtree_wide<T, D, M, G, OVF><<<grid, threads, smem, stream>>>(L, cap);
   return kOk;
 }
 
 // Launches the group-per-query kd-tree search for L.k (or the batch's
-// largest k) above kMaxK; `height` bounds the traversal stack.
-template <typename T, int D>
+// largest k) above kMaxK; `height` bounds the traversal stack. Returns
+// kNeedsSlab when one warp's stacks do not fit in shared memory.
+template <typename T, int D, bool OVF = false>
 int launch_wide_kdtree(const KnnLaunch& L, int kMax, int height, cudaStream_t stream) {
   switch (wide_k(kMax)) {
 #define NABO_WIDE(KK) \
   case KK:            \
-    return launch_wide_kdtree_as<T, D, WideShape<KK>::M, WideShape<KK>::G>(L, height, stream);
+    return launch_wide_kdtree_as<T, D, WideShape<KK>::M, WideShape<KK>::G, OVF>(L, height, stream);
+    NABO_WIDE_LIST(NABO_WIDE)
+#undef NABO_WIDE
+  }
+  return k_unsupported();
+}
+
+// Bytes of global memory one query's stack takes in a deep search (trees
+// taller than the compiled stacks): `kMax` above kMaxK searches by groups.
+template <typename T, int D>
+int64_t deep_unit_bytes(int kMax, int height) {
+  const int cap = height + 1;
+  return kMax > kMaxK ? wide_group_slab_bytes<T, D>(cap) : (int64_t)deep_stack_bytes<T, D>(cap);
+}
+
+// Launches the deep search over L (L.slab, L.slabBytes, the cap or the
+// device height, and optionally L.list set by the caller) with room for
+// `units` concurrent queries.
+template <typename T, int D>
+int launch_deep(const KnnLaunch& L, int kMax, int64_t units, cudaStream_t stream) {
+  if (units < 1) units = 1;
+  if (kMax <= kMaxK) {
+    const int grid = ceil_div(units, 128);
+    switch (round_k(kMax)) {
+#define NABO_DEEP(KK)                                 \
+  case KK:                                            \
+    launch_kdtree_deep<T, D, KK>(grid, stream, L);    \
+    return kOk;
+      NABO_K_LIST(NABO_DEEP)
+#undef NABO_DEEP
+    }
+    return k_unsupported();
+  }
+  switch (wide_k(kMax)) {
+#define NABO_WIDE(KK)                                                                                     \
+  case KK: {                                                                                              \
+    constexpr int G = WideShape<KK>::G;                                                                   \
+    k_knn_kdtree_wide_deep<T, D, WideShape<KK>::M, G><<<ceil_div(units * G, 128), 128, 0, stream>>>(L);   \
+    return kOk;                                                                                           \
+  }
     NABO_WIDE_LIST(NABO_WIDE)
 #undef NABO_WIDE
   }
@@ -134,16 +184,103 @@ KnnLaunch make_launch(const DeviceCloud& c, const KnnArgs& a, const int32_t* ord
   L.bK = nullptr;
   L.bOutOffset = nullptr;
   L.bClouds = 0;
+  L.ovfList = nullptr;
+  L.ovfCount = nullptr;
+  L.ovfBase = 0;
+  L.slab = nullptr;
+  L.slabBytes = 0;
+  L.stackCap = 0;
+  L.stackHeightDev = nullptr;
+  L.list = nullptr;
+  L.listCount = nullptr;
   return L;
+}
+
+// The kd-tree search kernel(s) for one query order: one thread per query
+// for k <= kMaxK (stack in local memory, 64 or 256 entries by the tree's
+// height), a lane group per query above (stacks in shared memory), or, for
+// trees too tall for those stacks, the deep kernels with the stacks in
+// global memory: a.stackSlab when the caller gives one (a.stackSlabBytes),
+// else scratch from the pool (at most kDeepSlabMax bytes; fewer queries then
+// search at once).
+constexpr int64_t kDeepSlabMax = int64_t(256) << 20;
+
+template <typename T, int D>
+int launch_search(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream) {
+  const int K = round_k(a.k);
+  if (K < 0 && a.k > kMaxWideK) return k_unsupported();
+  KnnLaunch L = make_launch<T, D>(c, a, order);
+  const int grid = ceil_div(a.nq, 128);
+  const bool small = c.height <= kStackSmall;
+  // Default: the reference visit order (it is also the faster one on the
+  // measured workloads); the warp packet is opt-in for exact searches with
+  // k <= kMaxK.
+  const bool packet = a.traversal == 2 && K > 0;
+  if (packet && (a.eps != 0.0 || L.stats))
+    return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
+  if (packet && c.height > kStackLarge)
+    return set_error(kErrUnsupported, "the warp-packet traversal serves kd-trees of at most 256 levels");
+  if (a.evStart) cudaEventRecord(a.evStart, stream);
+  int rc = kOk;
+  bool deep = K > 0 && !packet && c.height > kStackLarge;
+  if (K < 0) {
+    rc = launch_wide_kdtree<T, D>(L, a.k, c.height, stream);
+    if (rc == kNeedsSlab) {
+      deep = true;
+      rc = kOk;
+    }
+  } else if (!deep) {
+#define NABO_LAUNCH(KK)                                                            \
+  case KK:                                                                         \
+    if (packet) {                                                                  \
+      if (small)                                                                   \
+        k_knn_kdtree_packet<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);   \
+      else                                                                         \
+        k_knn_kdtree_packet<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);   \
+    } else {                                                                       \
+      if (small)                                                                   \
+        launch_kdtree<T, D, KK, kStackSmall>(grid, 128, stream, L);                \
+      else                                                                         \
+        launch_kdtree<T, D, KK, kStackLarge>(grid, 128, stream, L);                \
+    }                                                                              \
+    break;
+    switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+#undef NABO_LAUNCH
+  }
+  void* owned = nullptr;
+  if (rc == kOk && deep) {
+    const int64_t unit = deep_unit_bytes<T, D>(a.k, c.height);
+    int64_t bytes = a.stackSlab ? (int64_t)a.stackSlabBytes : std::min<int64_t>(kDeepSlabMax, unit * a.nq);
+    if (bytes < unit) bytes = a.stackSlab ? 0 : unit;
+    if (bytes < unit) {
+      rc = set_error(kErrUnsupported, "kd-tree of height " + std::to_string(c.height) +
+                                          ": one query's traversal stack does not fit the given scratch");
+    } else {
+      L.slab = a.stackSlab;
+      if (!L.slab) {
+        const cudaError_t e = scratch_alloc(&owned, (size_t)bytes, stream);
+        if (e != cudaSuccess) rc = cuda_error(e, "deep search stacks");
+        L.slab = owned;
+      }
+      if (rc == kOk) {
+        L.slabBytes = bytes;
+        L.stackCap = c.height + 1;
+        rc = launch_deep<T, D>(L, a.k, std::min<int64_t>(a.nq, bytes / unit), stream);
+      }
+    }
+  }
+  if (a.evStop) cudaEventRecord(a.evStop, stream);
+  const cudaError_t e = cudaGetLastError();
+  if (owned) scratch_free(owned, stream);
+  if (rc != kOk) return rc;
+  if (e != cudaSuccess) return cuda_error(e, "kd-tree search launch");
+  return kOk;
 }
 
 template <typename T, int D>
 int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
   if (a.nq == 0) return kOk;
-  const int K = round_k(a.k);
-  if (K < 0 && a.k > kMaxWideK) return k_unsupported();
-  if (c.height > kStackLarge)
-    return set_error(kErrUnsupported, "kd-tree height exceeds the traversal stack of the CUDA search");
+  if (round_k(a.k) < 0 && a.k > kMaxWideK) return k_unsupported();
   int32_t* order = nullptr;
   if (a.sortQueries && worth_sorting(a.nq, a.k, c.dim)) {
     NABO_CUDA_TRY(scratch_alloc((void**)&order, (size_t)a.nq * sizeof(int32_t), stream));
@@ -153,47 +290,47 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
       return rc;
     }
   }
-  const KnnLaunch L = make_launch<T, D>(c, a, order);
-  const int grid = ceil_div(a.nq, 128);
-  const bool small = c.height <= kStackSmall;
-  // Default: the reference visit order (it is also the faster one on the
-  // measured workloads); the warp packet is opt-in for exact searches with
-  // k <= kMaxK.
-  const bool packet = a.traversal == 2 && K > 0;
-  if (packet && (a.eps != 0.0 || L.stats)) {
-    if (order) scratch_free(order, stream);
-    return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
-  }
-  if (a.evStart) cudaEventRecord(a.evStart, stream);
-  if (K < 0) {
-    const int rc = launch_wide_kdtree<T, D>(L, a.k, c.height, stream);
-    if (a.evStop) cudaEventRecord(a.evStop, stream);
-    const cudaError_t e = cudaGetLastError();
-    if (order) scratch_free(order, stream);
-    if (rc != kOk) return rc;
-    if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree_wide launch");
+  const int rc = launch_search<T, D>(c, a, order, stream);
+  if (order) scratch_free(order, stream);
+  return rc;
+}
+
+// Brute force for k <= kMaxK. A search with too few queries to give every
+// SM several blocks splits the points into row chunks (block rows), each
+// writing its k best per query to scratch, merged by k_bf_merge.
+template <typename T, int D, int K>
+int launch_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
+  constexpr int QT = BfQueries<T, K>::value;
+  constexpr int64_t kTile = (int64_t)((24 * 1024) / sizeof(Rec<T, D>));
+  const int qBlocks = ceil_div(L.nq, 128 * QT);
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t tiles = std::max<int64_t>(1, (L.n + kTile - 1) / kTile);
+  int64_t rows = std::min<int64_t>({(4 * (int64_t)sms + qBlocks - 1) / qBlocks, tiles / 4, 64});
+  if (rows <= 1) {
+    k_knn_bruteforce<T, D, K, QT><<<qBlocks, 128, 0, stream>>>(L, L.n, 0);
     return kOk;
   }
-#define NABO_LAUNCH(KK)                                                            \
-  case KK:                                                                         \
-    if (packet) {                                                                  \
-      if (small)                                                                   \
-        k_knn_kdtree_packet<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);   \
-      else                                                                         \
-        k_knn_kdtree_packet<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);   \
-    } else {                                                                       \
-      if (small)                                                                   \
-        launch_kdtree<T, D, KK, kStackSmall>(grid, 128, stream, L);          \
-      else                                                                         \
-        launch_kdtree<T, D, KK, kStackLarge>(grid, 128, stream, L);          \
-    }                                                                              \
-    break;
-  switch (K) { NABO_K_LIST(NABO_LAUNCH) }
-#undef NABO_LAUNCH
-  if (a.evStop) cudaEventRecord(a.evStop, stream);
-  const cudaError_t e = cudaGetLastError();
-  if (order) scratch_free(order, stream);
-  if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree launch");
+  const int64_t chunk = (tiles + rows - 1) / rows * kTile;
+  rows = (L.n + chunk - 1) / chunk;
+  const int64_t stride = L.nq * (int64_t)L.k;
+  int32_t* pIdx = nullptr;
+  T* pD2 = nullptr;
+  NABO_CUDA_TRY(scratch_alloc((void**)&pIdx, (size_t)(rows * stride) * sizeof(int32_t), stream));
+  cudaError_t e = scratch_alloc((void**)&pD2, (size_t)(rows * stride) * sizeof(T), stream);
+  if (e != cudaSuccess) {
+    scratch_free(pIdx, stream);
+    return cuda_error(e, "brute-force partial results");
+  }
+  KnnLaunch P = L;
+  P.outIdx = pIdx;
+  P.outD2 = pD2;
+  P.found = nullptr;
+  k_knn_bruteforce<T, D, K, QT><<<dim3(qBlocks, (unsigned)rows), 128, 0, stream>>>(P, chunk, stride);
+  k_bf_merge<T, K><<<ceil_div(L.nq, 128), 128, 0, stream>>>(pIdx, pD2, (int)rows, stride, L.nq, L.k, L.outIdx,
+                                                           static_cast<T*>(L.outD2), L.found);
+  scratch_free(pIdx, stream);
+  scratch_free(pD2, stream);
   return kOk;
 }
 
@@ -203,68 +340,30 @@ int knn_bruteforce(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) 
   const int K = round_k(a.k);
   if (K < 0 && a.k > kMaxWideK) return k_unsupported();
   const KnnLaunch L = make_launch<T, D>(c, a, nullptr);
-  const int grid = ceil_div(a.nq, 128);
   if (a.evStart) cudaEventRecord(a.evStart, stream);
-  if (K < 0) {
-    const int rc = launch_wide_bruteforce<T, D>(L, stream);
-    if (rc != kOk) return rc;
-  }
-#define NABO_LAUNCH(KK)                                              \
-  case KK:                                                           \
-    k_knn_bruteforce<T, D, KK><<<grid, 128, 0, stream>>>(L);         \
+  int rc = kOk;
+  if (K < 0) rc = launch_wide_bruteforce<T, D>(L, stream);
+#define NABO_LAUNCH(KK)                                 \
+  case KK:                                              \
+    rc = launch_bruteforce<T, D, KK>(L, stream);        \
     break;
   if (K > 0) switch (K) { NABO_K_LIST(NABO_LAUNCH) }
 #undef NABO_LAUNCH
   if (a.evStop) cudaEventRecord(a.evStop, stream);
+  if (rc != kOk) return rc;
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "k_knn_bruteforce launch");
   return kOk;
 }
 
 // kd-tree search with a query order computed by the caller (`order` may be
-// null); launches the search kernel only and allocates nothing.
+// null); launches the search kernel only. It allocates nothing, except the
+// traversal stacks of a tree taller than the compiled stacks when the
+// caller gives no a.stackSlab.
 template <typename T, int D>
 int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream) {
   if (a.nq == 0) return kOk;
-  const int K = round_k(a.k);
-  if (K < 0 && a.k > kMaxWideK) return k_unsupported();
-  if (c.height > kStackLarge)
-    return set_error(kErrUnsupported, "kd-tree height exceeds the traversal stack of the CUDA search");
-  const KnnLaunch L = make_launch<T, D>(c, a, order);
-  const int grid = ceil_div(a.nq, 128);
-  const bool small = c.height <= kStackSmall;
-  const bool packet = a.traversal == 2 && K > 0;
-  if (packet && (a.eps != 0.0 || L.stats))
-    return set_error(kErrArgument, "the warp-packet traversal serves exact searches without TOUCH_STATISTICS only");
-  if (a.evStart) cudaEventRecord(a.evStart, stream);
-  if (K < 0) {
-    const int rc = launch_wide_kdtree<T, D>(L, a.k, c.height, stream);
-    if (a.evStop) cudaEventRecord(a.evStop, stream);
-    if (rc != kOk) return rc;
-    const cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree_wide launch");
-    return kOk;
-  }
-#define NABO_LAUNCH(KK)                                                            \
-  case KK:                                                                         \
-    if (packet) {                                                                  \
-      if (small)                                                                   \
-        k_knn_kdtree_packet<T, D, KK, kStackSmall><<<grid, 128, 0, stream>>>(L);   \
-      else                                                                         \
-        k_knn_kdtree_packet<T, D, KK, kStackLarge><<<grid, 128, 0, stream>>>(L);   \
-    } else {                                                                       \
-      if (small)                                                                   \
-        launch_kdtree<T, D, KK, kStackSmall>(grid, 128, stream, L);          \
-      else                                                                         \
-        launch_kdtree<T, D, KK, kStackLarge>(grid, 128, stream, L);          \
-    }                                                                              \
-    break;
-  switch (K) { NABO_K_LIST(NABO_LAUNCH) }
-#undef NABO_LAUNCH
-  if (a.evStop) cudaEventRecord(a.evStop, stream);
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_error(e, "k_knn_kdtree launch");
-  return kOk;
+  return launch_search<T, D>(c, a, order, stream);
 }
 
 // The query order the kd-tree search uses (written to `order`, nq entries,
@@ -350,17 +449,47 @@ int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t st
   L.bClouds = b.nClouds;
   L.recs32 = b.recs32;
   L.coordMax = b.coordMax;
+  L.ovfList = b.ovfList;
+  L.ovfCount = b.ovfCount;
+  L.ovfBase = begin;
+  L.maxRadii = b.maxRadii;
+  L.fallbackRadius = b.maxRadii ? b.maxRadius : -1.0;
+  L.fallbacks = b.fallbacks;
   const int grid = ceil_div(L.nq, b.blockSize);
-  if (K < 0) {  // some cloud wants more than kMaxK: the whole batch runs one warp per query
-    rc = launch_wide_kdtree<T, D>(L, b.kMax, kStackLarge, stream);  // taller trees are flagged by the build
-    if (rc != kOk) return rc;
+  // The trees' heights are known only on the device: the kernels search
+  // with stacks of kStackLarge entries and list the queries of taller trees,
+  // which the deep kernel then searches with stacks in b.slab sized by the
+  // tallest tree (it returns at once when the list is empty).
+  if (K < 0) {  // some cloud wants more than kMaxK: the whole batch runs a lane group per query
+    rc = launch_wide_kdtree<T, D, true>(L, b.kMax, kStackLarge, stream);
+    if (rc != kOk) return rc == kNeedsSlab ? set_error(kErrInternal, "batched wide search stacks") : rc;
   }
 #define NABO_LAUNCH(KK)                                                                     \
   case KK:                                                                                  \
-    launch_kdtree<T, D, KK, kStackLarge>(grid, b.blockSize, stream, L);               \
+    launch_kdtree<T, D, KK, kStackLarge, true>(grid, b.blockSize, stream, L);               \
     break;
   if (K > 0) switch (K) { NABO_K_LIST(NABO_LAUNCH) }
 #undef NABO_LAUNCH
+  {
+    KnnLaunch R = L;
+    R.nq = b.nq;
+    R.order = b.order;
+    R.ovfList = nullptr;
+    R.ovfBase = 0;
+    R.ovfCount = b.deepFail;
+    R.list = b.ovfList;
+    R.listCount = b.ovfCount;
+    R.slab = b.slab;
+    R.slabBytes = b.slabBytes;
+    R.stackCap = 0;
+    R.stackHeightDev = b.heightDev;
+    // enough threads for every stack the slab holds once trees are taller
+    // than kStackLarge
+    const int64_t units = std::max<int64_t>(1, b.slabBytes / deep_unit_bytes<T, D>(b.kMax, kStackLarge + 1));
+    rc = launch_deep<T, D>(R, b.kMax, units, stream);
+    if (rc != kOk) return rc;
+    NABO_CUDA_TRY(cudaMemsetAsync(b.ovfCount, 0, sizeof(int32_t), stream));
+  }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "batched search launch");
   return kOk;

@@ -214,19 +214,133 @@ __device__ __forceinline__ void wide_offer(const Rec<T, D>* __restrict__ recs, i
   }
 }
 
-// Shared memory of one group's traversal stack: cap entries of rd, off[D]
-// (T each) and the node (uint32), laid out per block as all groups' T parts
-// followed by all groups' node parts.
+// Memory of one group's traversal stack: cap entries of rd, off[D] (T each)
+// and the node (uint32). In shared memory a block lays out all groups' T
+// parts followed by all groups' node parts; in a deep launch's global slab
+// each group has its own region of this size (rounded up to 16 bytes).
 template <typename T, int D>
 inline size_t wide_stack_bytes(int groups, int cap) {
   return (size_t)groups * (size_t)cap * ((D + 1) * sizeof(T) + sizeof(uint32_t));
 }
+template <typename T, int D>
+__host__ __device__ inline int64_t wide_group_slab_bytes(int cap) {
+  return ((int64_t)cap * (int64_t)((D + 1) * sizeof(T) + sizeof(uint32_t)) + 15) & ~int64_t(15);
+}
+
+// One query (order position t) searched by the G-lane group: the
+// reference's visit order with the stack at sRd / sOff / sNode (cap
+// entries), written by the group's first lane and read by all its lanes.
+// With OVF a push beyond cap abandons the query (nothing written, false
+// returned, the same in every lane of the group); without it the caller
+// guarantees cap > tree height.
+template <typename T, int D, int M, int G, bool OVF>
+__device__ __forceinline__ bool wide_query(const KnnLaunch& a, int64_t t, T* sRd, T* sOff, uint32_t* sNode, int cap,
+                                           int g, unsigned gm, uint32_t& touchedOut) {
+  // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396)
+  const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
+  const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
+  const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
+  const T* __restrict__ query = static_cast<const T*>(a.query);
+  uint32_t touched = 0;
+  const int64_t qi = a.order ? (int64_t)a.order[t] : t;
+  int k = a.k;
+  uint32_t root = 0;
+  int64_t outBase = qi * (int64_t)a.k;
+  if (a.bQueryOffset) {
+    const int c = cloud_of(a.bQueryOffset, a.bClouds, qi);
+    k = a.bK[c];
+    root = (uint32_t)a.bNodeOffset[c];
+    outBase = a.bOutOffset[c] + (qi - a.bQueryOffset[c]) * (int64_t)k;
+  }
+  T q[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) q[d] = d < a.dim ? query[qi * a.qStride + d] : T(0);
+  T maxRadius2 = (T)a.maxRadius2;
+  bool mayFall = false;
+  if (a.maxRadii) {
+    const T r = static_cast<const T*>(a.maxRadii)[qi];
+    maxRadius2 = Ar<T>::mul(r, r);
+    mayFall = a.fallbackRadius >= 0.0 && (double)r < a.fallbackRadius;
+  }
+  const T maxError2 = (T)a.maxError2;
+  GroupTopK<T, M, G> heap;
+  heap.init(k, g);
+  LeafFilter<T, D> flt;
+  flt.init(a.recs32, a.coordMax, q);
+  T off[D];
+  for (;;) {  // the search, and at most once more without the bound
+#pragma unroll
+    for (int d = 0; d < D; ++d) off[d] = T(0);
+    int sp = 0;
+    uint32_t node = root;
+    T rd = T(0);
+    for (;;) {
+      __syncwarp(gm);  // the last pop's reads come before the next pushes
+      Node<T> nd = load_node(nodes, node);
+      while (!node_is_leaf(nd.meta)) {
+        const int cd = (int)node_dim(nd.meta);
+        const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
+        const T oldOff = pick(off, cd);
+        const T rdFar = Ar<T>::add(rd, Ar<T>::add(-Ar<T>::mul(oldOff, oldOff), Ar<T>::mul(newOff, newOff)));
+        const uint32_t right = node_payload(nd.meta);
+        const uint32_t nearN = newOff > T(0) ? right : node + 1;
+        const uint32_t farN = newOff > T(0) ? node + 1 : right;
+        bool far = rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head();
+        if (far && sp >= cap) {
+          if constexpr (OVF) return false;
+          far = false;
+        }
+        if (far) {
+          if (g == 0) {
+            sRd[sp] = rdFar;
+#pragma unroll
+            for (int d = 0; d < D; ++d) sOff[(size_t)sp * D + d] = d == cd ? newOff : off[d];
+            sNode[sp] = farN;
+          }
+          ++sp;
+        }
+        node = nearN;
+        nd = load_node(nodes, node);
+      }
+      const uint32_t cnt = node_payload(nd.meta);
+      const uint32_t st = node_start(nd);
+      for (uint32_t base = 0; base < cnt; base += G)
+        wide_offer<T, D, M, G, false>(recs, (int64_t)st + base, (int)(cnt - base), q, maxRadius2, minDist, heap,
+                                      flt, g, gm);
+      touched += cnt;
+      __syncwarp(gm);  // the first lane's pushes are visible to the group
+      bool more = false;
+      while (sp > 0) {
+        --sp;
+        const T e = sRd[sp];
+        if (Ar<T>::mul(e, maxError2) <= heap.head()) {
+          rd = e;
+#pragma unroll
+          for (int d = 0; d < D; ++d) off[d] = sOff[(size_t)sp * D + d];
+          node = sNode[sp];
+          more = true;
+          break;
+        }
+      }
+      if (!more) break;
+    }
+    if (!mayFall || heap.count(k, g, gm) == k) break;
+    mayFall = false;
+    maxRadius2 = (T)a.maxRadius2;
+    heap.init(k, g);
+    if (a.fallbacks && g == 0) atomicAdd(a.fallbacks, 1);
+  }
+  const int f = heap.store(k, g, gm, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
+  if (a.found && g == 0) a.found[qi] = f;
+  touchedOut += touched;
+  return true;
+}
 
 // Reference-order kd-tree search, one G-lane group per query (blockDim.x / G
-// queries per block). The traversal stack sits in shared memory, written by
-// the group's first lane and read by all its lanes; `cap` >= the tree height
-// bounds it.
-template <typename T, int D, int M, int G>
+// queries per block), stacks in shared memory; `cap` > the tree height
+// bounds them (with OVF, batches: a taller tree hands the query to
+// k_knn_kdtree_wide_deep through a.ovfList).
+template <typename T, int D, int M, int G, bool OVF>
 __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
   extern __shared__ __align__(16) unsigned char wideSmem[];
   const int lane = threadIdx.x & 31;
@@ -238,99 +352,47 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
   T* const sOff = sRd + cap;
   uint32_t* const sNode = reinterpret_cast<uint32_t*>(reinterpret_cast<T*>(wideSmem) + (size_t)groups * cap * (D + 1)) +
                           (size_t)group * cap;
-  // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396)
-  const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
-  const Node<T>* __restrict__ nodes = static_cast<const Node<T>*>(a.nodes);
-  const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
-  const T* __restrict__ query = static_cast<const T*>(a.query);
   const int64_t t = (int64_t)blockIdx.x * groups + group;
   uint32_t touched = 0;
   if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
-    const int64_t qi = a.order ? (int64_t)a.order[t] : t;
-    int k = a.k;
-    uint32_t root = 0;
-    int64_t outBase = qi * (int64_t)a.k;
-    if (a.bQueryOffset) {
-      const int c = cloud_of(a.bQueryOffset, a.bClouds, qi);
-      k = a.bK[c];
-      root = (uint32_t)a.bNodeOffset[c];
-      outBase = a.bOutOffset[c] + (qi - a.bQueryOffset[c]) * (int64_t)k;
-    }
-    T q[D];
-#pragma unroll
-    for (int d = 0; d < D; ++d) q[d] = d < a.dim ? query[qi * a.qStride + d] : T(0);
-    T maxRadius2 = (T)a.maxRadius2;
-    bool mayFall = false;
-    if (a.maxRadii) {
-      const T r = static_cast<const T*>(a.maxRadii)[qi];
-      maxRadius2 = Ar<T>::mul(r, r);
-      mayFall = a.fallbackRadius >= 0.0 && (double)r < a.fallbackRadius;
-    }
-    const T maxError2 = (T)a.maxError2;
-    GroupTopK<T, M, G> heap;
-    heap.init(k, g);
-    LeafFilter<T, D> flt;
-    flt.init(a.recs32, a.coordMax, q);
-    T off[D];
-    for (;;) {  // the search, and at most once more without the bound
-#pragma unroll
-      for (int d = 0; d < D; ++d) off[d] = T(0);
-      int sp = 0;
-      uint32_t node = root;
-      T rd = T(0);
-      for (;;) {
-        __syncwarp(gm);  // the last pop's reads come before the next pushes
-        Node<T> nd = load_node(nodes, node);
-        while (!node_is_leaf(nd.meta)) {
-          const int cd = (int)node_dim(nd.meta);
-          const T newOff = Ar<T>::sub(pick(q, cd), nd.cut);
-          const T oldOff = pick(off, cd);
-          const T rdFar = Ar<T>::add(rd, Ar<T>::add(-Ar<T>::mul(oldOff, oldOff), Ar<T>::mul(newOff, newOff)));
-          const uint32_t right = node_payload(nd.meta);
-          const uint32_t nearN = newOff > T(0) ? right : node + 1;
-          const uint32_t farN = newOff > T(0) ? node + 1 : right;
-          if (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < cap) {
-            if (g == 0) {
-              sRd[sp] = rdFar;
-#pragma unroll
-              for (int d = 0; d < D; ++d) sOff[(size_t)sp * D + d] = d == cd ? newOff : off[d];
-              sNode[sp] = farN;
-            }
-            ++sp;
-          }
-          node = nearN;
-          nd = load_node(nodes, node);
-        }
-        const uint32_t cnt = node_payload(nd.meta);
-        const uint32_t st = node_start(nd);
-        for (uint32_t base = 0; base < cnt; base += G)
-          wide_offer<T, D, M, G, false>(recs, (int64_t)st + base, (int)(cnt - base), q, maxRadius2, minDist, heap,
-                                        flt, g, gm);
-        touched += cnt;
-        __syncwarp(gm);  // the first lane's pushes are visible to the group
-        bool more = false;
-        while (sp > 0) {
-          --sp;
-          const T e = sRd[sp];
-          if (Ar<T>::mul(e, maxError2) <= heap.head()) {
-            rd = e;
-#pragma unroll
-            for (int d = 0; d < D; ++d) off[d] = sOff[(size_t)sp * D + d];
-            node = sNode[sp];
-            more = true;
-            break;
-          }
-        }
-        if (!more) break;
+    if (!wide_query<T, D, M, G, OVF>(a, t, sRd, sOff, sNode, cap, g, gm, touched)) {
+      if constexpr (OVF) {
+        if (g == 0) a.ovfList[atomicAdd(a.ovfCount, 1)] = (int32_t)(t + a.ovfBase);
       }
-      if (!mayFall || heap.count(k, g, gm) == k) break;
-      mayFall = false;
-      maxRadius2 = (T)a.maxRadius2;
-      heap.init(k, g);
-      if (a.fallbacks && g == 0) atomicAdd(a.fallbacks, 1);
     }
-    const int f = heap.store(k, g, gm, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
-    if (a.found && g == 0) a.found[qi] = f;
+  }
+  if (a.stats && g == 0 && touched) atomicAdd(a.touched, (unsigned long long)touched);
+}
+
+// Trees of any height, k above 32: each group's stack in its own region of
+// the global slab a.slab (cap = a.stackCap, or the height read from
+// *a.stackHeightDev plus one); as many groups as the slab holds search, each
+// taking every active-th item of a.list (or of 0..nq-1). A slab too small
+// for one stack searches nothing and sets *a.ovfCount to -1.
+template <typename T, int D, int M, int G>
+__global__ void __launch_bounds__(128) k_knn_kdtree_wide_deep(KnnLaunch a) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane & (G - 1);
+  const unsigned gm = group_mask<G>(lane);
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int64_t groupsAll = ((int64_t)gridDim.x * blockDim.x) / G;
+  const int cap = a.stackCap > 0 ? a.stackCap : (a.stackHeightDev ? *a.stackHeightDev + 1 : 0);
+  const int64_t per = wide_group_slab_bytes<T, D>(cap);
+  int64_t active = cap > 0 ? a.slabBytes / per : 0;
+  if (active > groupsAll) active = groupsAll;
+  const int64_t count = a.list ? (int64_t)*a.listCount : a.nq;
+  if (active <= 0 && count > 0 && gid == 0 && g == 0 && a.ovfCount) *a.ovfCount = -1;
+  uint32_t touched = 0;
+  if (gid < active) {
+    unsigned char* region = static_cast<unsigned char*>(a.slab) + gid * per;
+    T* sRd = reinterpret_cast<T*>(region);
+    T* sOff = sRd + cap;
+    uint32_t* sNode = reinterpret_cast<uint32_t*>(sRd + (size_t)cap * (D + 1));
+    for (int64_t w = gid; w < count; w += active) {
+      const int64_t t = a.list ? (int64_t)a.list[w] : w;
+      if (a.nqDevice && t >= (int64_t)*a.nqDevice) continue;
+      wide_query<T, D, M, G, false>(a, t, sRd, sOff, sNode, cap, g, gm, touched);
+    }
   }
   if (a.stats && g == 0 && touched) atomicAdd(a.touched, (unsigned long long)touched);
 }

@@ -7,12 +7,18 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "nabo_cuda.hpp"
 
 template <typename S>
 using M = nabo_cuda::DenseMatrix<S>;
+
+// the reference's index type (nabo/nabo.h:267), so code that declares
+// NNS::Index or stores it in int containers compiles unchanged
+static_assert(std::is_same<nabo_cuda::NNSearchF::Index, int>::value, "Index must be int");
+static_assert(std::is_same<nabo_cuda::NNSearchD::Index, int>::value, "Index must be int");
 
 static int expect_error(const char* what, const std::string& needle, void (*fn)()) {
   try {
