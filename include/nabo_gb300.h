@@ -88,7 +88,17 @@ typedef struct nabo_cuda_params {
                               (0 = default, 1 = one search then one
                               download; at most 64); for a batch, the cloud
                               groups of nabo_cuda_batch_run_host */
-  int32_t reserved[2];
+  int32_t splitRule;       /* kd-tree split. 0 (default): the reference's
+                              sliding midpoint (nabo/kdtree_cpu.cpp:134-190),
+                              the reference's tree node for node; 1: the
+                              median of the cell's widest dimension -- a
+                              balanced tree with the same node layout (the
+                              balanced trees of nabo/kdtree_opencl.cpp:474-514
+                              with buckets), an autotuner candidate for
+                              callers that need neither the reference's tree
+                              nor its TOUCH_STATISTICS counts (refused with
+                              NABO_TOUCH_STATISTICS); exact results */
+  int32_t reserved[1];
 } nabo_cuda_params;
 
 typedef struct nabo_cuda_search nabo_cuda_search; /* opaque */

@@ -82,7 +82,8 @@ class nabo_cuda_params(ctypes.Structure):
         ("traversal", ctypes.c_int32),
         ("threadsPerBlock", ctypes.c_int32),
         ("pipelineChunks", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 2),
+        ("splitRule", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 1),
     ]
 
 

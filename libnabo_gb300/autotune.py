@@ -1,10 +1,12 @@
 """Autotuner for batched searches.
 
 Times the batched build + search (one CUDA-graph launch) on a sample of the
-batch for every candidate configuration -- kd-tree bucket size and threads
-per block of the search kernel -- and keeps the fastest. Results do not
-depend on the choice (every configuration returns the exact neighbours);
-only speed does. Choices are cached per workload shape (dimension, scalar
+batch for every candidate configuration -- kd-tree bucket size, split rule
+(the reference's sliding midpoint, or the median: a balanced tree with the
+same layout), and threads per block of the search kernel -- and keeps the
+fastest. Every configuration returns the exact neighbours; only speed
+differs. The median split builds another tree than the reference's, so
+callers that need the reference's own trees pass ``split_rules=(0,)``. Choices are cached per workload shape (dimension, scalar
 type, largest k, point-count scale), in memory and optionally in a JSON file.
 """
 from __future__ import annotations
@@ -16,7 +18,7 @@ import time
 
 import numpy as np
 
-CANDIDATES = {"bucketSize": (4, 6, 8, 12, 16), "threadsPerBlock": (64, 128)}
+CANDIDATES = {"bucketSize": (4, 6, 8, 12, 16), "threadsPerBlock": (64, 128), "splitRule": (0, 1)}
 _cache: dict = {}
 
 
@@ -25,11 +27,11 @@ def shape_key(point_counts, dim, dtype, k) -> str:
     return f"d{dim}-{np.dtype(dtype).name}-k{int(np.max(k))}-n2^{int(round(math.log2(max(mean, 1.0))))}"
 
 
-def _time_config(clouds, queries, pc, qc, ks, dim, dtype, bucket, tpb, repeats):
+def _time_config(clouds, queries, pc, qc, ks, dim, dtype, bucket, tpb, rule, repeats):
     import torch
 
     from . import BatchSearch
-    b = BatchSearch(pc, dim=dim, dtype=dtype, bucketSize=bucket, threadsPerBlock=tpb)
+    b = BatchSearch(pc, dim=dim, dtype=dtype, bucketSize=bucket, threadsPerBlock=tpb, splitRule=rule)
     b.set_queries(qc, ks)
     out = b._outputs(queries.device)
     b.run(clouds, queries, out=out)  # capture + first launch
@@ -50,12 +52,12 @@ def _time_config(clouds, queries, pc, qc, ks, dim, dtype, bucket, tpb, repeats):
     return best, st
 
 
-def _levels_of(cloud, queries, k, dim, dtype, bucket) -> int:
+def _levels_of(cloud, queries, k, dim, dtype, bucket, rule) -> int:
     """Top-phase levels the forest build needs for one cloud."""
     import torch
 
     from . import BatchSearch
-    b = BatchSearch([cloud.shape[0]], dim=dim, dtype=dtype, bucketSize=bucket, maxLevels=256)
+    b = BatchSearch([cloud.shape[0]], dim=dim, dtype=dtype, bucketSize=bucket, maxLevels=256, splitRule=rule)
     b.set_queries([0], [k])
     b.build(torch.from_numpy(np.ascontiguousarray(cloud, dtype=dtype)).cuda())
     torch.cuda.synchronize()
@@ -65,12 +67,13 @@ def _levels_of(cloud, queries, k, dim, dtype, bucket) -> int:
 
 
 def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int = 64, repeats: int = 3,
-         cache_path: str | None = None, seed: int = 0) -> dict:
-    """Best {bucketSize, threadsPerBlock} for a batch (lists of (n_c, dim) arrays)."""
+         cache_path: str | None = None, seed: int = 0, split_rules=CANDIDATES["splitRule"]) -> dict:
+    """Best {bucketSize, threadsPerBlock, splitRule} for a batch (lists of (n_c, dim) arrays)."""
     import torch
     ks = np.broadcast_to(np.asarray(k, dtype=np.int32), (len(cloud_list),))
     pcs = np.array([c.shape[0] for c in cloud_list], np.int64)
-    key = shape_key(pcs, dim, dtype, ks)
+    split_rules = tuple(int(r) for r in split_rules)
+    key = shape_key(pcs, dim, dtype, ks) + ("" if split_rules == (0, 1) else "-s" + "".join(map(str, split_rules)))
     if key in _cache:
         return dict(_cache[key], key=key, cached=True)
     if cache_path and os.path.exists(cache_path):
@@ -87,19 +90,21 @@ def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int 
     queries = torch.from_numpy(np.concatenate([query_list[i] for i in pick]).astype(dtype)).cuda()
     trials = []
     t0 = time.perf_counter()
-    for bucket in CANDIDATES["bucketSize"]:
-        for tpb in CANDIDATES["threadsPerBlock"]:
-            ms, st = _time_config(clouds, queries, pc, qc, ks[pick], dim, dtype, bucket, tpb, repeats)
-            trials.append({"bucketSize": bucket, "threadsPerBlock": tpb, "ms": ms, "levels": st["levels"]})
+    for rule in split_rules:
+        for bucket in CANDIDATES["bucketSize"]:
+            for tpb in CANDIDATES["threadsPerBlock"]:
+                ms, st = _time_config(clouds, queries, pc, qc, ks[pick], dim, dtype, bucket, tpb, rule, repeats)
+                trials.append({"bucketSize": bucket, "threadsPerBlock": tpb, "splitRule": rule, "ms": ms,
+                               "levels": st["levels"]})
     best = min(trials, key=lambda t: t["ms"])
     # the fixed level count must cover the batch's largest cloud, sampled or not
     levels = best["levels"]
     big = int(np.argmax(pcs))
     if big not in set(pick.tolist()):
         levels = max(levels, _levels_of(cloud_list[big], query_list[big], int(ks[big]), dim, dtype,
-                                        best["bucketSize"]))
+                                        best["bucketSize"], best["splitRule"]))
     choice = {"bucketSize": best["bucketSize"], "threadsPerBlock": best["threadsPerBlock"],
-              "maxLevels": max(8, levels + 8), "sample_ms": best["ms"]}
+              "splitRule": best["splitRule"], "maxLevels": max(8, levels + 8), "sample_ms": best["ms"]}
     _cache[key] = choice
     if cache_path:
         disk = {}

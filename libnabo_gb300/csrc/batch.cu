@@ -29,6 +29,7 @@ struct nabo_cuda_batch {
   int nClouds = 0;
   int64_t nTotal = 0;
   unsigned bucketSize = 8;
+  int splitRule = 0;  // 0: the reference's sliding midpoint; 1: median
   int maxLevels = 48;
   int blockSize = 128;
   int device = 0;
@@ -172,7 +173,8 @@ int build(nabo_cuda_batch* b, const void* clouds, cudaStream_t st) {
 #define NABO_B_CASE(TT, DD)                                                                                \
   if (b->dpad == DD) {                                                                                     \
     const int rc = build_forest<TT, DD>(static_cast<const TT*>(clouds), b->nTotal, b->dim, b->dim,        \
-                                        b->bucketSize, b->dOff, b->nClouds, b->maxLevels, st, &f);         \
+                                        b->bucketSize, b->dOff, b->nClouds, b->maxLevels, st, &f,          \
+                                        b->splitRule);                                                     \
     if (rc != kOk || !b->recs32) return rc;                                                                \
     return narrow_records<DD>(b->recs, b->nTotal, b->dim, b->recs32, b->coordMax, st);                   \
   }
@@ -405,9 +407,11 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
     p.bucketSize = params->bucketSize;
     p.threadsPerBlock = params->threadsPerBlock;
     p.pipelineChunks = params->pipelineChunks;
+    p.splitRule = params->splitRule;
   }
   if (p.pipelineChunks < 0 || p.pipelineChunks > 64)
     return set_error(kErrArgument, "pipelineChunks must be between 0 and 64");
+  if (p.splitRule != 0 && p.splitRule != 1) return set_error(kErrArgument, "splitRule must be 0 or 1");
   if (p.bucketSize < 2)
     return set_error(kErrArgument, "Requested bucket size " + std::to_string(p.bucketSize) + ", but must be larger than 2");
   int64_t total = 0;
@@ -425,6 +429,7 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
   b->bucketSize = p.bucketSize;
   b->maxLevels = maxLevels > 0 ? maxLevels : 48;
   b->blockSize = p.threadsPerBlock > 0 ? p.threadsPerBlock : 128;
+  b->splitRule = p.splitRule;
   b->groups = p.pipelineChunks > 0 ? p.pipelineChunks : 8;
   if (b->blockSize != 32 && b->blockSize != 64 && b->blockSize != 128) {
     delete b;

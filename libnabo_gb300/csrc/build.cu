@@ -349,8 +349,30 @@ __global__ void k_minmax(const Rec<T, D>* __restrict__ recs, int* __restrict__ s
   }
 }
 
+// Median-split trees (split rule 1): the cut is the median of the segment's
+// coordinates along the cut dimension, sampled at kMedianSamples evenly
+// spaced positions (the segment's points are in no particular order there).
+constexpr int kMedianSamples = 31;
+
 template <typename T>
-__global__ void k_cut(SegLevel<T> L, const LevelState* st) {
+__device__ T sampled_median(const T* __restrict__ val, int start, int count) {
+  T smp[kMedianSamples];
+  for (int j = 0; j < kMedianSamples; ++j)
+    smp[j] = val[start + (int)((int64_t)(2 * j + 1) * count / (2 * kMedianSamples))];
+  for (int i = 1; i < kMedianSamples; ++i) {  // insertion sort
+    const T x = smp[i];
+    int j = i - 1;
+    while (j >= 0 && x < smp[j]) {
+      smp[j + 1] = smp[j];
+      --j;
+    }
+    smp[j + 1] = x;
+  }
+  return smp[kMedianSamples / 2];
+}
+
+template <typename T>
+__global__ void k_cut(SegLevel<T> L, const LevelState* st, const T* __restrict__ val, int splitRule) {
   pdl_begin();
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= st->nseg) return;
@@ -358,8 +380,12 @@ __global__ void k_cut(SegLevel<T> L, const LevelState* st) {
   const T mn = ordered_val(L.mnK[s], T(0));
   const T mx = ordered_val(L.mxK[s], T(0));
   // (max + min) / 2 as the reference writes it (nabo/kdtree_cpu.cpp:135);
-  // halving is exact, so multiplying by 1/2 gives the same value.
-  const T ideal = Ar<T>::mul(Ar<T>::add(L.boxHi[(int64_t)s * kMaxDim + cd], L.boxLo[(int64_t)s * kMaxDim + cd]), T(0.5));
+  // halving is exact, so multiplying by 1/2 gives the same value. The
+  // median rule takes a point's coordinate, which lies in [mn, mx].
+  const T ideal = splitRule == 1
+                      ? sampled_median(val, L.start[s], L.count[s])
+                      : Ar<T>::mul(Ar<T>::add(L.boxHi[(int64_t)s * kMaxDim + cd], L.boxLo[(int64_t)s * kMaxDim + cd]),
+                                   T(0.5));
   T cut;
   int mode;
   if (ideal < mn) {
@@ -823,9 +849,33 @@ __device__ __forceinline__ void warp_partition_pass(Rec<T, D>* pts, int lo, int 
 // pre-order with an explicit stack (global scratch, written by lane 0). Each
 // split's min/max, counts and partition passes run across the lanes; node
 // records and bucket order come out as the reference's.
+// The lower median (rank count / 2) of the count values node[i].p.c[cd],
+// computed by the warp: each lane ranks its elements against all of them.
+template <typename T, int D>
+__device__ T warp_median(const Rec<T, D>* node, int count, int cd, int lane) {
+  const int want = count / 2;
+  bool found = false;
+  T med = T(0);
+  for (int i = lane; i < count; i += 32) {
+    const T v = node[i].p.c[cd];
+    int lt = 0, le = 0;
+    for (int j = 0; j < count; ++j) {
+      const T w = node[j].p.c[cd];
+      lt += w < v ? 1 : 0;
+      le += w <= v ? 1 : 0;
+    }
+    if (!found && lt <= want && want < le) {
+      found = true;
+      med = v;
+    }
+  }
+  const unsigned m = __ballot_sync(0xffffffffu, found);
+  return __shfl_sync(0xffffffffu, med, __ffs(m) - 1);
+}
+
 template <typename T, int D>
 __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, Node<T>* scratch,
-                        SmallStack<T> stk, int dim, unsigned bucketSize, int* counters) {
+                        SmallStack<T> stk, int dim, unsigned bucketSize, int* counters, int splitRule) {
   extern __shared__ __align__(16) unsigned char smallSmem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -875,8 +925,9 @@ __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, 
         hi[d] = stk.boxHi[(int64_t)e * kMaxDim + d];
       }
       const int cd = arg_max_extent(lo, hi, dim);
-      const T ideal = Ar<T>::mul(Ar<T>::add(hi[cd], lo[cd]), T(0.5));
       Rec<T, D>* node = pts + st;
+      const T ideal = splitRule == 1 ? warp_median(node, count, cd, lane)
+                                     : Ar<T>::mul(Ar<T>::add(hi[cd], lo[cd]), T(0.5));
       T mn = std::numeric_limits<T>::max(), mx = std::numeric_limits<T>::lowest();
       for (int i = lane; i < count; i += 32) {
         const T v = node[i].p.c[cd];
@@ -1184,7 +1235,7 @@ int pack_cloud(const T* dCloud, int64_t n, int64_t stride, int dim, cudaStream_t
 // graph; a tree needing more levels sets the overflow flag (f->status).
 template <typename T, int D>
 int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, const int64_t* dOff,
-                 int nClouds, int maxLevels, cudaStream_t stream, ForestOut* f) {
+                 int nClouds, int maxLevels, cudaStream_t stream, ForestOut* f, int splitRule) {
   using Key = typename KeyOf<T>::type;
   const int N = (int)n;
   const bool hostDriven = maxLevels < 0;
@@ -1302,7 +1353,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
     const int remap = level > 0 ? 1 : 0;
     NABO_CUDA_TRY(launch_pdl(k_prepare<T>, sg, 128, 0, stream, cur, st, dim));
     NABO_CUDA_TRY(launch_pdl(k_minmax<T, D>, grid, kBlock, 0, stream, recs, segOf, N, cur, nxt, remap, st, val));
-    NABO_CUDA_TRY(launch_pdl(k_cut<T>, sg, 128, 0, stream, cur, st));
+    NABO_CUDA_TRY(launch_pdl(k_cut<T>, sg, 128, 0, stream, cur, st, (const T*)val, splitRule));
     NABO_CUDA_TRY(launch_pdl(k_count<T>, grid, kBlock, 0, stream, val, segOf, N, cur, st));
     for (int pass = 1; pass <= 2; ++pass) {
       NABO_CUDA_TRY(launch_pdl(k_flag_sums<T>, scanBlocks, kBlock, 0, stream, val, segOf, N, cur, pass, tiles,
@@ -1339,7 +1390,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
     const size_t smem = (size_t)wpb * kSmallMax * (sizeof(Rec<T, D>) + sizeof(int));
     const int smallGrid = std::max(1, std::min(ceil_div(std::max(nSmallHost, 1), wpb), 16 * std::max(sms, 1)));
     k_small<T, D><<<smallGrid, 32 * wpb, smem, stream>>>(recs, small, counters + 1, scratchNodes, stk, dim,
-                                                         bucketSize, counters);
+                                                         bucketSize, counters, splitRule);
   }
   NABO_CUDA_TRY(cudaGetLastError());
   Node<T>* nodes = static_cast<Node<T>*>(f->nodes);
@@ -1360,7 +1411,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
 
 template <typename T, int D>
 int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, cudaStream_t stream,
-                 DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats) {
+                 DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats, int splitRule) {
   Scratch sc(stream);
   ForestOut f;
   Rec<T, D>* recs = nullptr;
@@ -1384,7 +1435,7 @@ int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   f.nodeCap = nodeCap;
   f.rootLo = rootBox;
   f.rootHi = rootBox + kMaxDim;
-  const int rc = build_forest<T, D>(dCloud, n, stride, dim, bucketSize, off, 1, -1, stream, &f);
+  const int rc = build_forest<T, D>(dCloud, n, stride, dim, bucketSize, off, 1, -1, stream, &f, splitRule);
   if (rc != kOk) return rc;
   int64_t hno[2];
   int hs[4];
@@ -1467,9 +1518,9 @@ template int narrow_records<16>(const void*, int64_t, int, void*, float*, cudaSt
 
 #define NABO_BUILD_INSTANTIATE(T, D)                                                                          \
   template int build_kdtree<T, D>(const T*, int64_t, int64_t, int, unsigned, cudaStream_t, DeviceCloud*,      \
-                                  double*, double*, BuildStats*);                                             \
+                                  double*, double*, BuildStats*, int);                                        \
   template int build_forest<T, D>(const T*, int64_t, int64_t, int, unsigned, const int64_t*, int, int,        \
-                                  cudaStream_t, ForestOut*);                                                  \
+                                  cudaStream_t, ForestOut*, int);                                             \
   template int pack_cloud<T, D>(const T*, int64_t, int64_t, int, cudaStream_t, DeviceCloud*);
 
 NABO_BUILD_INSTANTIATE(float, 2)

@@ -331,7 +331,7 @@ int build_any(nabo_cuda_search* h, const void* dCloud, int64_t stride, cudaStrea
     int rc = kOk;
     NABO_DISPATCH_RC(rc, h->c.dtype, h->c.dpad,
                      (build_kdtree<T, D>(static_cast<const T*>(dCloud), h->c.n, stride, h->c.dim, h->c.bucketSize,
-                                         st, &h->c, rootMin, rootMax, nullptr)));
+                                         st, &h->c, rootMin, rootMax, nullptr, h->c.splitRule)));
     if (rc == kOk && h->c.dtype == NABO_CUDA_FLOAT64) rc = narrow_cloud(h->c, st);
     return rc;
   }
@@ -395,9 +395,14 @@ int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int6
     p.queryOrdering = params->queryOrdering;
     p.traversal = params->traversal;
     p.pipelineChunks = params->pipelineChunks;
+    p.splitRule = params->splitRule;
   }
   if (p.pipelineChunks < 0 || p.pipelineChunks > kPipelineMaxChunks)
     return set_error(kErrArgument, "pipelineChunks must be between 0 and 64");
+  if (p.splitRule != 0 && p.splitRule != 1) return set_error(kErrArgument, "splitRule must be 0 or 1");
+  if (p.splitRule == 1 && (creationFlags & NABO_TOUCH_STATISTICS))
+    return set_error(kErrArgument, "the median-split tree is not the reference's tree: TOUCH_STATISTICS would not "
+                                   "count what the reference counts (use splitRule 0)");
   // NearestNeighbourSearch::create (nabo/nabo.cpp:137-138)
   if (dimIn <= 0) return set_error(kErrArgument, "Your space must have at least one dimension");
   if (searchType < 0 || searchType >= NABO_SEARCH_TYPE_COUNT) return set_error(kErrArgument, "Unknown search type");
@@ -443,6 +448,7 @@ int create_impl(int dtype, const void* cloud, bool cloudOnDevice, int rows, int6
   h->queryOrdering = p.queryOrdering;
   h->traversal = p.traversal;
   h->pipelineChunks = p.pipelineChunks;
+  h->c.splitRule = searchType == NABO_SEARCH_KDTREE_CUDA ? p.splitRule : 0;
   if (p.traversal < 0 || p.traversal > 2) {
     delete h;
     return set_error(kErrArgument, "traversal must be 0, 1 or 2");

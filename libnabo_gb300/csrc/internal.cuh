@@ -80,6 +80,7 @@ struct DeviceCloud {
   int dpad = 0;         // compiled record dimension (>= dim)
   int64_t n = 0;        // points
   unsigned bucketSize = 8;
+  int splitRule = 0;      // 0: the reference's sliding midpoint; 1: median (balanced)
   void* recs = nullptr;   // Rec<T,dpad>[n], leaf order (kd-tree) or cloud order (brute force)
   void* nodes = nullptr;  // Node<T>[nodeCount] (kd-tree only)
   int64_t nodeCount = 0;
@@ -104,9 +105,11 @@ struct BuildStats {
 // constructor (nabo/kdtree_cpu.cpp:109-272): same nodes, cut values and
 // bucket order. `rootMin/rootMax` receive the root box the reference uses
 // (with its max-bound initialisation), as doubles.
+// splitRule 1 cuts at the median of the widest dimension instead (a
+// balanced tree, not the reference's; see nabo_cuda_params::splitRule).
 template <typename T, int D>
 int build_kdtree(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, cudaStream_t stream,
-                 DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats);
+                 DeviceCloud* out, double* rootMin, double* rootMax, BuildStats* stats, int splitRule = 0);
 
 // Output buffers of a forest build (all device memory, allocated by the
 // caller): records (n), nodes (2n), nodeOffset (nClouds+1), root boxes
@@ -182,7 +185,7 @@ int narrow_records(const void* recs, int64_t n, int dim, void* recs32, float* co
 
 template <typename T, int D>
 int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned bucketSize, const int64_t* dOff,
-                 int nClouds, int maxLevels, cudaStream_t stream, ForestOut* f);
+                 int nClouds, int maxLevels, cudaStream_t stream, ForestOut* f, int splitRule = 0);
 
 // Packs the cloud into records in cloud order (brute force) and computes
 // its true bounds.
