@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--no-order", action="store_true", help="keep the queries in their given order")
     p.add_argument("--no-learned", action="store_true", help="skip the learned-radius form")
     p.add_argument("--train-queries", type=int, default=200000)
+    p.add_argument("--split-rules", default="0,1",
+                   help="batched workload: split rules the autotuner may choose (0 the reference's, 1 median)")
     p.add_argument("--traversal", type=int, default=0,
                    help="kd-tree traversal: 0/1 reference visit order (default), 2 warp packet")
     return p.parse_args()
@@ -489,10 +491,12 @@ def run_batched(args):
     pc = np.array([c.shape[0] for c in clouds], np.int64)
     qc = np.array([q.shape[0] for q in queries], np.int64)
     t0 = time.perf_counter()
-    choice = autotune.tune(clouds, queries, ks, sample=64, repeats=3)
+    choice = autotune.tune(clouds, queries, ks, sample=64, repeats=3,
+                           split_rules=tuple(int(r) for r in args.split_rules.split(",")))
     tune_s = time.perf_counter() - t0
     b = nb.BatchSearch(pc, bucketSize=choice["bucketSize"], threadsPerBlock=choice["threadsPerBlock"],
-                       maxLevels=choice["maxLevels"])
+                       maxLevels=choice["maxLevels"], splitRule=choice["splitRule"],
+                       lanesPerQuery=choice.get("lanesPerQuery", 1))
     b.set_queries(qc, ks)
     hc = np.concatenate(clouds)
     hq = np.concatenate(queries)
@@ -542,7 +546,9 @@ def run_batched(args):
     gd = b.split(out[1].cpu().numpy())
     checked, same = 0, True
     for c in range(0, len(clouds), max(1, len(clouds) // 8)):
-        oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        # the exact k smallest pairs (the reference's tree or the median-split
+        # one, whichever the autotuner chose, returns them)
+        oi, od, _ = O.bf_knn(clouds[c], queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
         same = same and np.array_equal(gi[c], oi) and np.array_equal(gd[c].view(np.uint32), od.view(np.uint32))
         checked += 1
     # end to end through the host-buffer call: clouds and queries from pinned
@@ -581,7 +587,9 @@ def run_batched(args):
         "config": {"workload": "batched512_3d", "clouds": len(clouds), "points": int(pc.sum()),
                    "queries": nq_total, "k": "per cloud from {1, 5, 16}", "selfMatch": False,
                    "bucketSize": choice["bucketSize"], "threadsPerBlock": choice["threadsPerBlock"],
+                   "splitRule": choice["splitRule"], "lanesPerQuery": choice.get("lanesPerQuery", 1),
                    "maxLevels": choice["maxLevels"], "autotune_s": tune_s,
+                   "autotune_trials": choice.get("trials"),
                    "step": "forest build + search, one CUDA graph launch",
                    "l2": "inputs larger than L2 (clouds + queries %.0f MB)" % ((hc.nbytes + hq.nbytes) / 1e6),
                    "parallelism": f"replicas x{world}"},

@@ -98,7 +98,11 @@ typedef struct nabo_cuda_params {
                               callers that need neither the reference's tree
                               nor its TOUCH_STATISTICS counts (refused with
                               NABO_TOUCH_STATISTICS); exact results */
-  int32_t reserved[1];
+  int32_t lanesPerQuery;   /* batched search with k <= 32: 1 (0 = default):
+                              one thread per query; 8: a group of 8 lanes
+                              per query (one traversal, the top-k spread
+                              over the group's registers); chosen by the
+                              autotuner, same results */
 } nabo_cuda_params;
 
 typedef struct nabo_cuda_search nabo_cuda_search; /* opaque */

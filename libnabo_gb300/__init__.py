@@ -545,7 +545,7 @@ class BatchSearch:
     """
 
     def __init__(self, point_counts, dim: int = 3, dtype=np.float32, bucketSize: int = 8, threadsPerBlock: int = 128,
-                 maxLevels: int = 48, pipelineChunks: int = 0, splitRule: int = 0):
+                 maxLevels: int = 48, pipelineChunks: int = 0, splitRule: int = 0, lanesPerQuery: int = 1):
         counts = np.ascontiguousarray(np.asarray(point_counts, dtype=np.int64))
         self.point_counts = counts
         self.dim = int(dim)
@@ -557,6 +557,7 @@ class BatchSearch:
         p.threadsPerBlock = int(threadsPerBlock)
         p.pipelineChunks = int(pipelineChunks)
         p.splitRule = int(splitRule)
+        p.lanesPerQuery = int(lanesPerQuery)
         _check(_lib.nabo_cuda_batch_create(_dtype_code(self.dtype), self.dim, len(counts), _ptr(counts),
                                            ctypes.byref(p), int(maxLevels), ctypes.byref(self._b)))
         self.query_counts = None

@@ -83,7 +83,7 @@ class nabo_cuda_params(ctypes.Structure):
         ("threadsPerBlock", ctypes.c_int32),
         ("pipelineChunks", ctypes.c_int32),
         ("splitRule", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 1),
+        ("lanesPerQuery", ctypes.c_int32),
     ]
 
 

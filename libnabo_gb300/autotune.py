@@ -3,8 +3,9 @@
 Times the batched build + search (one CUDA-graph launch) on a sample of the
 batch for every candidate configuration -- kd-tree bucket size, split rule
 (the reference's sliding midpoint, or the median: a balanced tree with the
-same layout), and threads per block of the search kernel -- and keeps the
-fastest. Every configuration returns the exact neighbours; only speed
+same layout), threads per query (one thread, or a group of 8 lanes sharing
+one traversal with the top-k spread over their registers) and threads per
+block of the search kernel -- and keeps the fastest. Every configuration returns the exact neighbours; only speed
 differs. The median split builds another tree than the reference's, so
 callers that need the reference's own trees pass ``split_rules=(0,)``. Choices are cached per workload shape (dimension, scalar
 type, largest k, point-count scale), in memory and optionally in a JSON file.
@@ -18,7 +19,8 @@ import time
 
 import numpy as np
 
-CANDIDATES = {"bucketSize": (4, 6, 8, 12, 16), "threadsPerBlock": (64, 128), "splitRule": (0, 1)}
+CANDIDATES = {"bucketSize": (4, 6, 8, 12, 16), "threadsPerBlock": (64, 128), "splitRule": (0, 1),
+              "lanesPerQuery": (1, 8)}
 _cache: dict = {}
 
 
@@ -27,11 +29,12 @@ def shape_key(point_counts, dim, dtype, k) -> str:
     return f"d{dim}-{np.dtype(dtype).name}-k{int(np.max(k))}-n2^{int(round(math.log2(max(mean, 1.0))))}"
 
 
-def _time_config(clouds, queries, pc, qc, ks, dim, dtype, bucket, tpb, rule, repeats):
+def _time_config(clouds, queries, pc, qc, ks, dim, dtype, bucket, tpb, rule, lanes, repeats):
     import torch
 
     from . import BatchSearch
-    b = BatchSearch(pc, dim=dim, dtype=dtype, bucketSize=bucket, threadsPerBlock=tpb, splitRule=rule)
+    b = BatchSearch(pc, dim=dim, dtype=dtype, bucketSize=bucket, threadsPerBlock=tpb, splitRule=rule,
+                    lanesPerQuery=lanes)
     b.set_queries(qc, ks)
     out = b._outputs(queries.device)
     b.run(clouds, queries, out=out)  # capture + first launch
@@ -90,12 +93,16 @@ def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int 
     queries = torch.from_numpy(np.concatenate([query_list[i] for i in pick]).astype(dtype)).cuda()
     trials = []
     t0 = time.perf_counter()
+    # lane groups apply to k <= 32 and run blocks of 128 threads
+    lane_choices = CANDIDATES["lanesPerQuery"] if int(np.max(ks)) <= 32 else (1,)
     for rule in split_rules:
         for bucket in CANDIDATES["bucketSize"]:
-            for tpb in CANDIDATES["threadsPerBlock"]:
-                ms, st = _time_config(clouds, queries, pc, qc, ks[pick], dim, dtype, bucket, tpb, rule, repeats)
-                trials.append({"bucketSize": bucket, "threadsPerBlock": tpb, "splitRule": rule, "ms": ms,
-                               "levels": st["levels"]})
+            for lanes in lane_choices:
+                for tpb in (CANDIDATES["threadsPerBlock"] if lanes == 1 else (128,)):
+                    ms, st = _time_config(clouds, queries, pc, qc, ks[pick], dim, dtype, bucket, tpb, rule, lanes,
+                                          repeats)
+                    trials.append({"bucketSize": bucket, "threadsPerBlock": tpb, "splitRule": rule,
+                                   "lanesPerQuery": lanes, "ms": ms, "levels": st["levels"]})
     best = min(trials, key=lambda t: t["ms"])
     # the fixed level count must cover the batch's largest cloud, sampled or not
     levels = best["levels"]
@@ -104,7 +111,8 @@ def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int 
         levels = max(levels, _levels_of(cloud_list[big], query_list[big], int(ks[big]), dim, dtype,
                                         best["bucketSize"], best["splitRule"]))
     choice = {"bucketSize": best["bucketSize"], "threadsPerBlock": best["threadsPerBlock"],
-              "splitRule": best["splitRule"], "maxLevels": max(8, levels + 8), "sample_ms": best["ms"]}
+              "splitRule": best["splitRule"], "lanesPerQuery": best["lanesPerQuery"],
+              "maxLevels": max(8, levels + 8), "sample_ms": best["ms"]}
     _cache[key] = choice
     if cache_path:
         disk = {}

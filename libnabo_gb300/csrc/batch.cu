@@ -30,6 +30,7 @@ struct nabo_cuda_batch {
   int64_t nTotal = 0;
   unsigned bucketSize = 8;
   int splitRule = 0;  // 0: the reference's sliding midpoint; 1: median
+  int lanesPerQuery = 1;
   int maxLevels = 48;
   int blockSize = 128;
   int device = 0;
@@ -224,6 +225,7 @@ BatchArgs batch_args(const nabo_cuda_batch* b, const void* query, double eps, un
   a.deepFail = b->status + 4;
   a.maxRadii = nullptr;
   a.fallbacks = nullptr;
+  a.lanesPerQuery = b->lanesPerQuery;
   return a;
 }
 
@@ -408,10 +410,13 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
     p.threadsPerBlock = params->threadsPerBlock;
     p.pipelineChunks = params->pipelineChunks;
     p.splitRule = params->splitRule;
+    p.lanesPerQuery = params->lanesPerQuery;
   }
   if (p.pipelineChunks < 0 || p.pipelineChunks > 64)
     return set_error(kErrArgument, "pipelineChunks must be between 0 and 64");
   if (p.splitRule != 0 && p.splitRule != 1) return set_error(kErrArgument, "splitRule must be 0 or 1");
+  if (p.lanesPerQuery != 0 && p.lanesPerQuery != 1 && p.lanesPerQuery != 8)
+    return set_error(kErrArgument, "lanesPerQuery must be 1 or 8");
   if (p.bucketSize < 2)
     return set_error(kErrArgument, "Requested bucket size " + std::to_string(p.bucketSize) + ", but must be larger than 2");
   int64_t total = 0;
@@ -430,6 +435,7 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
   b->maxLevels = maxLevels > 0 ? maxLevels : 48;
   b->blockSize = p.threadsPerBlock > 0 ? p.threadsPerBlock : 128;
   b->splitRule = p.splitRule;
+  b->lanesPerQuery = p.lanesPerQuery == 8 ? 8 : 1;
   b->groups = p.pipelineChunks > 0 ? p.pipelineChunks : 8;
   if (b->blockSize != 32 && b->blockSize != 64 && b->blockSize != 128) {
     delete b;

@@ -168,6 +168,7 @@ struct BatchArgs {
   // maxRadius, counted in *fallbacks (may be null).
   const void* maxRadii;
   int32_t* fallbacks;
+  int lanesPerQuery;            // 1: one thread per query; 8: a lane group (k <= 32)
 };
 template <typename T, int D>
 int knn_batch(const BatchArgs& b, cudaStream_t stream);

@@ -331,7 +331,14 @@ __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, ui
     unsigned mask = 0;
     if constexpr (std::is_same<T, float>::value) {
       // float: candidates as packed (dist2 bits, index) keys, one 64-bit
-      // compare against the head and one 64-bit select per insertion
+      // compare against min(head, radius key) -- the radius key is the
+      // largest key of distance maxRadius2, so d <= maxRadius2 && key <
+      // head is key < that minimum (a NaN radius accepts nothing: 0) --
+      // and one 64-bit select per insertion (4-9 % faster than separate
+      // radius and head tests on lidar scans)
+      const uint64_t radKey = maxRadius2 == maxRadius2 ? ((uint64_t(__float_as_uint(maxRadius2)) << 32) | 0xffffffffull) : 0ull;
+      const uint64_t thrKey =
+          (!want || radKey == 0ull) ? 0ull : (heap.key[0] <= radKey ? heap.key[0] : radKey + 1ull);
       uint64_t kj[kChunk];
 #pragma unroll
       for (int j = 0; j < kChunk; ++j) {
@@ -341,8 +348,7 @@ __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, ui
           load_rec(recs, (int64_t)st + base + j, r);
           const float d = dist2_seq(q, r);
           kj[j] = TopK<float, K>::make(d, r.p.idx);
-          const bool ok = want && d <= maxRadius2 && kj[j] < heap.key[0] && d > minDist;
-          mask |= ok ? (1u << j) : 0u;
+          mask |= (kj[j] < thrKey && d > minDist) ? (1u << j) : 0u;
         }
       }
       while (mask) {
@@ -807,24 +813,27 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_packet(KnnLaunch a) {
 // thread owns QT queries (blockDim.x apart) and their top-k, so each record
 // read from shared memory (a broadcast: every lane reads the same one) feeds
 // QT distances. The distance is the reference's separately rounded
-// sequential sum; a point is first compared with one float threshold,
+// sequential sum. Records are taken J at a time: the J x QT distances are
+// computed, each query's smallest is compared with one float threshold,
 // min(head, maxRadius^2) (NaN radius: NaN, which passes nothing), and only
-// the rare points at or below it take the exact test -- the reference's
+// when some distance is at or below its threshold -- rare once the heaps
+// are full -- do the group's points take the exact test, the reference's
 // radius and self-match rules and the (dist2, index) order against the head
 // (nabo/kdtree_cpu.cpp:392-396 with the lower index kept on ties). The
 // result, the k smallest pairs, does not depend on the order points are
 // offered in.
-template <typename T>
-__device__ __forceinline__ T bf_threshold(T head, T maxRadius2) {
-  return head < maxRadius2 ? head : maxRadius2;
-}
-
+//
 // With gridDim.y > 1 the points are split into chunks of `chunk` (a
 // multiple of the tile): block row y offers points [y*chunk, (y+1)*chunk) and
 // writes its k best to a.outIdx / a.outD2 + y*partStride, and
 // k_bf_merge combines the rows (for searches with too few queries to give
 // every SM several blocks).
-template <typename T, int D, int K, int QT>
+template <typename T>
+__device__ __forceinline__ T bf_threshold(T head, T maxRadius2) {
+  return head < maxRadius2 ? head : maxRadius2;
+}
+
+template <typename T, int D, int K, int QT, int J>
 __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a, int64_t chunk, int64_t partStride) {
   const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
   constexpr int kTile = (int)((24 * 1024) / sizeof(Rec<T, D>));
@@ -867,16 +876,35 @@ __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a, int64_t chu
       for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = __ldg(src + w);
     }
     __syncthreads();
-#pragma unroll 4
-    for (int j = 0; j < m; ++j) {
-      const Rec<T, D> r = tile[j];
+    for (int j0 = 0; j0 < m; j0 += J) {
+      T dist[J][QT];
+      T dmin[QT];
 #pragma unroll
-      for (int u = 0; u < QT; ++u) {
-        const T dist = dist2_seq(q[u], r);
-        if (dist <= thr[u]) {
-          if (dist <= maxRadius2[u] && heap[u].accepts(dist, r.p.idx) && dist > minDist) {
-            heap[u].insert(dist, r.p.idx);
-            thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
+      for (int jj = 0; jj < J; ++jj) {
+        const int j = j0 + jj < m ? j0 + jj : m - 1;  // a repeated point changes no minimum
+        const Rec<T, D> r = tile[j];
+#pragma unroll
+        for (int u = 0; u < QT; ++u) {
+          dist[jj][u] = dist2_seq(q[u], r);
+          dmin[u] = jj == 0 ? dist[jj][u] : (dist[jj][u] < dmin[u] ? dist[jj][u] : dmin[u]);
+        }
+      }
+      bool any = false;
+#pragma unroll
+      for (int u = 0; u < QT; ++u) any = any || dmin[u] <= thr[u];
+      if (any) {
+#pragma unroll
+        for (int jj = 0; jj < J; ++jj) {
+          if (j0 + jj < m) {
+            const int idx = tile[j0 + jj].p.idx;
+#pragma unroll
+            for (int u = 0; u < QT; ++u) {
+              const T d = dist[jj][u];
+              if (d <= thr[u] && d <= maxRadius2[u] && heap[u].accepts(d, idx) && d > minDist) {
+                heap[u].insert(d, idx);
+                thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
+              }
+            }
           }
         }
       }
@@ -914,11 +942,16 @@ __global__ void k_bf_merge(const int32_t* __restrict__ pIdx, const T* __restrict
   if (found) found[i] = f;
 }
 
-// Queries per thread of the brute force: more share each shared-memory read,
-// fewer keep long top-k lists in registers.
+// Shape of the brute force: QT queries per thread (more share each
+// shared-memory read, fewer keep long top-k lists in registers) and J
+// records per threshold test.
+// Measured on 100k x 100k 3-D points, k = 5 (kernel ms): QT x J = 2 x 4
+// 5.17, 2 x 8 5.72, 1 x 8 6.33, 4 x 4 6.83, 1 x 4 6.90, 4 x 8 7.88,
+// 8 x 2 8.49.
 template <typename T, int K>
-struct BfQueries {
-  static constexpr int value = sizeof(T) == 8 ? 1 : (K <= 8 ? 4 : (K <= 16 ? 2 : 1));
+struct BfShape {
+  static constexpr int QT = sizeof(T) == 8 ? 1 : (K <= 16 ? 2 : 1);
+  static constexpr int J = 4;
 };
 
 }  // namespace nabo_gb300

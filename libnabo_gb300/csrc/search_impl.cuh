@@ -298,9 +298,8 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
 // Brute force for k <= kMaxK. A search with too few queries to give every
 // SM several blocks splits the points into row chunks (block rows), each
 // writing its k best per query to scratch, merged by k_bf_merge.
-template <typename T, int D, int K>
+template <typename T, int D, int K, int QT = BfShape<T, K>::QT, int J = BfShape<T, K>::J>
 int launch_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
-  constexpr int QT = BfQueries<T, K>::value;
   constexpr int64_t kTile = (int64_t)((24 * 1024) / sizeof(Rec<T, D>));
   const int qBlocks = ceil_div(L.nq, 128 * QT);
   int dev = 0, sms = 148;
@@ -308,7 +307,7 @@ int launch_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
   const int64_t tiles = std::max<int64_t>(1, (L.n + kTile - 1) / kTile);
   int64_t rows = std::min<int64_t>({(4 * (int64_t)sms + qBlocks - 1) / qBlocks, tiles / 4, 64});
   if (rows <= 1) {
-    k_knn_bruteforce<T, D, K, QT><<<qBlocks, 128, 0, stream>>>(L, L.n, 0);
+    k_knn_bruteforce<T, D, K, QT, J><<<qBlocks, 128, 0, stream>>>(L, L.n, 0);
     return kOk;
   }
   const int64_t chunk = (tiles + rows - 1) / rows * kTile;
@@ -326,7 +325,7 @@ int launch_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
   P.outIdx = pIdx;
   P.outD2 = pD2;
   P.found = nullptr;
-  k_knn_bruteforce<T, D, K, QT><<<dim3(qBlocks, (unsigned)rows), 128, 0, stream>>>(P, chunk, stride);
+  k_knn_bruteforce<T, D, K, QT, J><<<dim3(qBlocks, (unsigned)rows), 128, 0, stream>>>(P, chunk, stride);
   k_bf_merge<T, K><<<ceil_div(L.nq, 128), 128, 0, stream>>>(pIdx, pD2, (int)rows, stride, L.nq, L.k, L.outIdx,
                                                            static_cast<T*>(L.outD2), L.found);
   scratch_free(pIdx, stream);
@@ -421,7 +420,7 @@ int order_batch(const BatchArgs& b, cudaStream_t stream) {
 template <typename T, int D>
 int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t stream) {
   if (end <= begin) return kOk;
-  const int K = round_k(b.kMax);
+  int K = round_k(b.kMax);
   if (K < 0 && b.kMax > kMaxWideK) return k_unsupported();
   int rc = kOk;
   KnnLaunch L;
@@ -463,6 +462,11 @@ int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t st
   if (K < 0) {  // some cloud wants more than kMaxK: the whole batch runs a lane group per query
     rc = launch_wide_kdtree<T, D, true>(L, b.kMax, kStackLarge, stream);
     if (rc != kOk) return rc == kNeedsSlab ? set_error(kErrInternal, "batched wide search stacks") : rc;
+  } else if (b.lanesPerQuery == 8) {  // 8 lanes per query, the top-k spread over them
+    rc = K <= 16 ? launch_wide_kdtree_as<T, D, 2, 8, true>(L, kStackLarge, stream)
+                 : launch_wide_kdtree_as<T, D, 4, 8, true>(L, kStackLarge, stream);
+    if (rc != kOk) return rc == kNeedsSlab ? set_error(kErrInternal, "batched group search stacks") : rc;
+    K = 0;
   }
 #define NABO_LAUNCH(KK)                                                                     \
   case KK:                                                                                  \

@@ -152,12 +152,20 @@ def test_autotuner_choice_is_exact():
     clouds, queries, ks = _batch_data(48, 2000, 60000, seed=6)
     choice = autotune.tune(clouds, queries, ks, sample=16, repeats=2)
     assert choice["bucketSize"] in autotune.CANDIDATES["bucketSize"]
+    assert {t["splitRule"] for t in choice["trials"]} == {0, 1}
+    assert {t["lanesPerQuery"] for t in choice["trials"]} == {1, 8}
     b, bi, bd = _run_batch(clouds, queries, ks, graph=True, bucketSize=choice["bucketSize"],
-                           threadsPerBlock=choice["threadsPerBlock"], maxLevels=choice["maxLevels"])
+                           threadsPerBlock=choice["threadsPerBlock"], maxLevels=choice["maxLevels"],
+                           splitRule=choice["splitRule"], lanesPerQuery=choice["lanesPerQuery"])
     assert b.status()["ok"]
     for c in range(0, len(clouds), 7):
-        oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        # the reference's tree (split rule 0) or the median-split tree (1):
+        # either returns the exact k smallest pairs
+        oi, od, _ = O.bf_knn(clouds[c], queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
         H.assert_identical(bi[c], bd[c], oi, od, f"tuned cloud {c}")
+    # restricted to the reference's trees on request
+    ref_only = autotune.tune(clouds, queries, ks, sample=8, repeats=1, split_rules=(0,))
+    assert ref_only["splitRule"] == 0
     again = autotune.tune(clouds, queries, ks, sample=16, repeats=2)
     assert again["cached"]
 
@@ -261,3 +269,14 @@ def test_host_run_argument_errors():
         b.run_host(np.concatenate(clouds), np.concatenate(queries), optionFlags=nb.ALLOW_SELF_MATCH)
     with pytest.raises(nb.NaboError, match="pipelineChunks"):
         nb.BatchSearch([c.shape[0] for c in clouds], pipelineChunks=65)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_lane_groups_per_query_are_exact(graph):
+    """Batches searched by 8-lane groups per query (k <= 32) return the
+    one-thread-per-query results."""
+    clouds, queries, ks = _batch_data(20, 300, 20000, seed=12)
+    _, bi, bd = _run_batch(clouds, queries, ks, graph=graph, lanesPerQuery=8)
+    _, ri, rd = _run_batch(clouds, queries, ks, graph=graph)
+    for c in range(len(clouds)):
+        H.assert_identical(bi[c], bd[c], ri[c], rd[c], f"lane groups cloud {c}")
