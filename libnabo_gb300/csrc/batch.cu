@@ -53,11 +53,8 @@ struct nabo_cuda_batch {
   uint32_t* hist = nullptr;
   uint32_t* cell = nullptr;
   uint32_t* rank = nullptr;
-  // trees taller than the search kernels' stacks: the queries handed to the
-  // deep search, their count, and its stacks
+  // trees taller than the search kernels' stacks: the deep search's stacks
   int64_t nMax = 0;  // points of the largest cloud
-  int32_t* ovfList = nullptr;
-  int32_t* ovfCount = nullptr;
   void* slab = nullptr;
   int64_t slabBytes = 0;
   // captured graph and the arguments it was captured with
@@ -118,10 +115,8 @@ void drop_graph(nabo_cuda_batch* b) {
 
 void free_query_plan(nabo_cuda_batch* b) {
   for (void* p : {(void*)b->dQOff, (void*)b->dOutOff, (void*)b->dK, (void*)b->order, (void*)b->hist,
-                  (void*)b->cell, (void*)b->rank, b->devQueries, (void*)b->devIdx, b->devD2, (void*)b->ovfList,
-                  (void*)b->ovfCount, b->slab})
+                  (void*)b->cell, (void*)b->rank, b->devQueries, (void*)b->devIdx, b->devD2, b->slab})
     if (p) cudaFree(p);
-  b->ovfList = b->ovfCount = nullptr;
   b->slab = nullptr;
   b->slabBytes = 0;
   b->dQOff = b->dOutOff = nullptr;
@@ -217,8 +212,6 @@ BatchArgs batch_args(const nabo_cuda_batch* b, const void* query, double eps, un
   a.blockSize = b->blockSize;
   a.recs32 = b->recs32;
   a.coordMax = b->coordMax;
-  a.ovfList = b->ovfList;
-  a.ovfCount = b->ovfCount;
   a.slab = b->slab;
   a.slabBytes = b->slabBytes;
   a.heightDev = b->status + 2;
@@ -526,9 +519,6 @@ int nabo_cuda_batch_set_queries(nabo_cuda_batch* b, const int64_t* queryCounts, 
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->cell, (size_t)std::max<int64_t>(nq, 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->rank, (size_t)std::max<int64_t>(nq, 1) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc((void**)&b->hist, (size_t)2 * b->nTotal * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->ovfList, (size_t)std::max<int64_t>(nq, 1) * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&b->ovfCount, sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMemset(b->ovfCount, 0, sizeof(int32_t));
   if (e == cudaSuccess) {
     // the deep search's stacks: room for one stack as tall as the largest
     // cloud (a tree's height is below its point count), 16 MiB at least so

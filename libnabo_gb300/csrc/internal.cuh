@@ -151,12 +151,10 @@ struct BatchArgs {
   int blockSize;                // threads per block of the search kernel
   const void* recs32;           // f64: float copies of recs, or null
   const float* coordMax;        // f64: device float, largest coordinate magnitude
-  // Trees taller than the search kernels' stacks (256 levels): the queries
-  // listed in ovfList (nq entries; *ovfCount, zero between searches) are
-  // searched again with stacks in `slab`, sized by *heightDev (the tallest
-  // tree); *deepFail is set to -1 if one stack does not fit the slab.
-  int32_t* ovfList;
-  int32_t* ovfCount;
+  // Trees taller than the search kernels' stacks (256 levels), which only
+  // the device knows of (*heightDev: the tallest tree): the search is then
+  // run by the deep kernel with stacks in `slab`; *deepFail is set to -1 if
+  // one stack does not fit the slab.
   void* slab;
   int64_t slabBytes;
   const int* heightDev;

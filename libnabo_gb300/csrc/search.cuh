@@ -238,22 +238,21 @@ struct KnnLaunch {
   int bClouds;
   // Trees taller than the compiled stacks (the reference's recursion has no
   // depth limit, nabo/kdtree_cpu.cpp:367-447):
-  //  - ovfList/ovfCount (the batch's local-stack kernels): a query whose
-  //    stack would overflow stops without writing anything and appends its
-  //    order position (+ ovfBase) to ovfList, for k_knn_kdtree_deep;
   //  - slab/slabBytes: traversal stacks in global memory for the deep
   //    kernels, `cap` entries per query (stackCap, or the tree height read
-  //    from *stackHeightDev plus one); list/listCount: the positions to
-  //    search (null: all nq).
-  int32_t* ovfList;
-  int32_t* ovfCount;
-  int64_t ovfBase;
+  //    from *stackHeightDev plus one);
+  //  - tallGate (batches, whose tree heights only the device knows): the
+  //    tallest tree's height. Kernels with stacks of tallGateLimit entries
+  //    return at once when it is larger; the deep kernels return at once
+  //    when it is not. Both are launched, and exactly one searches.
+  //  - deepFail: set to -1 by a deep kernel whose slab holds no stack.
   void* slab;
   int64_t slabBytes;
   int stackCap;
   const int* stackHeightDev;
-  const int32_t* list;
-  const int32_t* listCount;
+  const int* tallGate;
+  int tallGateLimit;
+  int32_t* deepFail;
 };
 
 // Leaf scan shared by the kernels: the bucket's records are read in chunks
@@ -494,14 +493,12 @@ struct SlabStack {
 // descend / leaf / pop so the lanes of a warp run each phase together: all
 // lanes descend until every lane stands on a leaf, then all scan their
 // leaves, then all pop. `cap` entries of `stk` are available; the caller
-// guarantees cap > tree height, except with OVF, where a push beyond cap
-// abandons the query (nothing written, false returned) so that a deep
-// launch can search it again. Adds the points examined to `touchedOut`.
+// guarantees cap >= tree height. Adds the points examined to `touchedOut`.
 // EXACT (epsilon 0, so maxError2 = 1 and rd * maxError2 = rd exactly): the
 // push test rd <= maxRadius2 && rd <= head is one compare against
 // min(maxRadius2, head), refreshed after each leaf; decisions are the same.
-template <typename T, int D, int K, bool EXACT, bool OVF, typename S>
-__device__ __forceinline__ bool knn_query(const KnnLaunch& a, int64_t t, S& stk, int cap, uint32_t& touchedOut) {
+template <typename T, int D, int K, bool EXACT, typename S>
+__device__ __forceinline__ void knn_query(const KnnLaunch& a, int64_t t, S& stk, int cap, uint32_t& touchedOut) {
   // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396): without
   // ALLOW_SELF_MATCH a point at distance <= epsilon is skipped; one compare
   // against -1 (everything passes) or epsilon
@@ -559,16 +556,9 @@ __device__ __forceinline__ bool knn_query(const KnnLaunch& a, int64_t t, S& stk,
         const uint32_t farN = newOff > T(0) ? node + 1 : right;
         const bool far = EXACT ? rdFar <= bound
                                : (rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head());
-        if constexpr (OVF) {
-          if (far) {
-            if (sp >= cap) return false;
-            stack_push(stk[sp++], rdFar, off, cd, newOff, farN);
-          }
-        } else {
-          // sp <= tree height < cap (checked by the caller); the test only
-          // makes the bound explicit
-          if (far && sp < cap) stack_push(stk[sp++], rdFar, off, cd, newOff, farN);
-        }
+        // sp <= tree height <= cap (checked by the caller); the test only
+        // makes the bound explicit
+        if (far && sp < cap) stack_push(stk[sp++], rdFar, off, cd, newOff, farN);
         node = nearN;
         nd = load_node(nodes, node);
       }
@@ -599,7 +589,6 @@ __device__ __forceinline__ bool knn_query(const KnnLaunch& a, int64_t t, S& stk,
   const int f = heap.store(k, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
   if (a.found) a.found[qi] = f;
   touchedOut += touched;
-  return true;
 }
 
 // The warp's TOUCH_STATISTICS counts summed into a.touched (every lane of
@@ -613,59 +602,54 @@ __device__ __forceinline__ void add_touched(const KnnLaunch& a, uint32_t touched
   }
 }
 
-// One thread per query, stack of STACK entries in local memory. With OVF
-// (batches, whose tree heights are known only on the device) a query whose
-// tree is taller than STACK is handed to k_knn_kdtree_deep through
-// a.ovfList.
-template <typename T, int D, int K, int STACK, bool EXACT, bool OVF>
+// One thread per query, stack of STACK entries in local memory.
+template <typename T, int D, int K, int STACK, bool EXACT>
 __device__ __forceinline__ void knn_kdtree_body(const KnnLaunch& a) {
+  if (a.tallGate && *a.tallGate > a.tallGateLimit) return;  // the deep kernel searches (uniform)
   const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   uint32_t touched = 0;
   if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
     LocalStack<T, D, STACK> stk;
-    if (!knn_query<T, D, K, EXACT, OVF>(a, t, stk, STACK, touched)) {
-      if constexpr (OVF) a.ovfList[atomicAdd(a.ovfCount, 1)] = (int32_t)(t + a.ovfBase);
-    }
+    knn_query<T, D, K, EXACT>(a, t, stk, STACK, touched);
   }
   add_touched(a, touched);
 }
 
-template <typename T, int D, int K, int STACK, bool EXACT, bool OVF>
+template <typename T, int D, int K, int STACK, bool EXACT>
 __global__ void __launch_bounds__(128) k_knn_kdtree(KnnLaunch a) {
-  knn_kdtree_body<T, D, K, STACK, EXACT, OVF>(a);
+  knn_kdtree_body<T, D, K, STACK, EXACT>(a);
 }
 
 // Double searches with a long top-k hold ~100 registers of heap alone;
 // limited to 128 registers a thread, 4 blocks share an SM, and the FP64 pipe
 // gets the extra warps it needs to hide its latency (12 % faster on 8-D
 // clouds, k = 32).
-template <typename T, int D, int K, int STACK, bool EXACT, bool OVF>
+template <typename T, int D, int K, int STACK, bool EXACT>
 __global__ void __launch_bounds__(128, 4) k_knn_kdtree_lean(KnnLaunch a) {
-  knn_kdtree_body<T, D, K, STACK, EXACT, OVF>(a);
+  knn_kdtree_body<T, D, K, STACK, EXACT>(a);
 }
 
 // Trees of any height: the stacks in a.slab, cap = a.stackCap entries per
 // query (or the tree height read from *a.stackHeightDev, plus one, for
 // batches whose heights the host does not know). As many threads as the
 // slab holds stacks search (the others idle), each taking every active-th
-// item of a.list (or of 0..nq-1). A slab too small for one stack searches
-// nothing and sets *a.ovfCount to -1.
+// query. A slab too small for one stack searches nothing and sets
+// *a.deepFail to -1.
 template <typename T, int D, int K, bool EXACT>
 __global__ void __launch_bounds__(128) k_knn_kdtree_deep(KnnLaunch a) {
+  if (a.tallGate && *a.tallGate <= a.tallGateLimit) return;  // the local-stack kernel searches (uniform)
   const int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t threads = (int64_t)gridDim.x * blockDim.x;
   const int cap = a.stackCap > 0 ? a.stackCap : (a.stackHeightDev ? *a.stackHeightDev + 1 : 0);
   int64_t active = cap > 0 ? a.slabBytes / ((int64_t)sizeof(StackRec<T, D>) * cap) : 0;
   if (active > threads) active = threads;
-  const int64_t count = a.list ? (int64_t)*a.listCount : a.nq;
-  if (active <= 0 && count > 0 && g == 0 && a.ovfCount) *a.ovfCount = -1;
+  if (active <= 0 && a.nq > 0 && g == 0 && a.deepFail) *a.deepFail = -1;
   uint32_t touched = 0;
   if (g < active) {
     SlabStack<T, D> stk{static_cast<StackRec<T, D>*>(a.slab) + g, active};
-    for (int64_t w = g; w < count; w += active) {
-      const int64_t t = a.list ? (int64_t)a.list[w] : w;
+    for (int64_t t = g; t < a.nq; t += active) {
       if (a.nqDevice && t >= (int64_t)*a.nqDevice) continue;
-      knn_query<T, D, K, EXACT, false>(a, t, stk, cap, touched);
+      knn_query<T, D, K, EXACT>(a, t, stk, cap, touched);
     }
   }
   add_touched(a, touched);
@@ -677,20 +661,20 @@ constexpr size_t deep_stack_bytes(int cap) {
   return sizeof(StackRec<T, D>) * (size_t)cap;
 }
 
-template <typename T, int D, int K, int STACK, bool EXACT, bool OVF>
+template <typename T, int D, int K, int STACK, bool EXACT>
 void launch_kdtree_as(int grid, int block, cudaStream_t stream, const KnnLaunch& L) {
   if constexpr (sizeof(T) == 8 && K >= 16)
-    k_knn_kdtree_lean<T, D, K, STACK, EXACT, OVF><<<grid, block, 0, stream>>>(L);
+    k_knn_kdtree_lean<T, D, K, STACK, EXACT><<<grid, block, 0, stream>>>(L);
   else
-    k_knn_kdtree<T, D, K, STACK, EXACT, OVF><<<grid, block, 0, stream>>>(L);
+    k_knn_kdtree<T, D, K, STACK, EXACT><<<grid, block, 0, stream>>>(L);
 }
 
-template <typename T, int D, int K, int STACK, bool OVF = false>
+template <typename T, int D, int K, int STACK>
 void launch_kdtree(int grid, int block, cudaStream_t stream, const KnnLaunch& L) {
   if (L.maxError2 == 1.0)
-    launch_kdtree_as<T, D, K, STACK, true, OVF>(grid, block, stream, L);
+    launch_kdtree_as<T, D, K, STACK, true>(grid, block, stream, L);
   else
-    launch_kdtree_as<T, D, K, STACK, false, OVF>(grid, block, stream, L);
+    launch_kdtree_as<T, D, K, STACK, false>(grid, block, stream, L);
 }
 
 template <typename T, int D, int K>
@@ -832,11 +816,14 @@ template <typename T>
 __device__ __forceinline__ T bf_threshold(T head, T maxRadius2) {
   return head < maxRadius2 ? head : maxRadius2;
 }
+__device__ __forceinline__ float fmin_t(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double fmin_t(double a, double b) { return fmin(a, b); }
 
 template <typename T, int D, int K, int QT, int J>
 __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a, int64_t chunk, int64_t partStride) {
   const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
-  constexpr int kTile = (int)((24 * 1024) / sizeof(Rec<T, D>));
+  // a multiple of J, so that a group never reads past the tile
+  constexpr int kTile = (int)((24 * 1024) / sizeof(Rec<T, D>)) / J * J;
   __shared__ Rec<T, D> tile[kTile];
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
   const T* __restrict__ query = static_cast<const T*>(a.query);
@@ -874,34 +861,45 @@ __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a, int64_t chu
       uint4* dst = reinterpret_cast<uint4*>(tile);
       const int words = m * RecSize<T, D>::chunks;
       for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = __ldg(src + w);
+      // the last group's missing points: NaN coordinates, whose distance
+      // passes no threshold and lowers no minimum (a group's first point
+      // is always a real one)
+      const int padEnd = (m + J - 1) / J * J;
+      for (int j = m + (int)threadIdx.x; j < padEnd; j += blockDim.x) {
+        Rec<T, D> r;
+#pragma unroll
+        for (int d = 0; d < D; ++d) r.p.c[d] = __builtin_nan("");
+        r.p.idx = -1;
+        tile[j] = r;
+      }
     }
     __syncthreads();
     for (int j0 = 0; j0 < m; j0 += J) {
-      T dist[J][QT];
+      // each query's smallest distance of the group (fmin ignores the NaN
+      // padding; the group's first point is a real one)
       T dmin[QT];
 #pragma unroll
       for (int jj = 0; jj < J; ++jj) {
-        const int j = j0 + jj < m ? j0 + jj : m - 1;  // a repeated point changes no minimum
-        const Rec<T, D> r = tile[j];
+        const Rec<T, D> r = tile[j0 + jj];
 #pragma unroll
         for (int u = 0; u < QT; ++u) {
-          dist[jj][u] = dist2_seq(q[u], r);
-          dmin[u] = jj == 0 ? dist[jj][u] : (dist[jj][u] < dmin[u] ? dist[jj][u] : dmin[u]);
+          const T d = dist2_seq(q[u], r);
+          dmin[u] = jj == 0 ? d : fmin_t(dmin[u], d);
         }
       }
       bool any = false;
 #pragma unroll
       for (int u = 0; u < QT; ++u) any = any || dmin[u] <= thr[u];
-      if (any) {
+      if (any) {  // rare once the heaps are full: the group again, exactly
 #pragma unroll
         for (int jj = 0; jj < J; ++jj) {
           if (j0 + jj < m) {
-            const int idx = tile[j0 + jj].p.idx;
+            const Rec<T, D> r = tile[j0 + jj];
 #pragma unroll
             for (int u = 0; u < QT; ++u) {
-              const T d = dist[jj][u];
-              if (d <= thr[u] && d <= maxRadius2[u] && heap[u].accepts(d, idx) && d > minDist) {
-                heap[u].insert(d, idx);
+              const T d = dist2_seq(q[u], r);
+              if (d <= thr[u] && d <= maxRadius2[u] && heap[u].accepts(d, r.p.idx) && d > minDist) {
+                heap[u].insert(d, r.p.idx);
                 thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
               }
             }

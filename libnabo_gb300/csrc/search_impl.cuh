@@ -62,7 +62,7 @@ constexpr size_t kWideSmemMax = 160 * 1024;
 // Internal: the search needs its stacks in global memory.
 constexpr int kNeedsSlab = -100;
 
-template <typename T, int D, int M, int G, bool OVF>
+template <typename T, int D, int M, int G>
 int launch_wide_kdtree_as(const KnnLaunch& L, int height, cudaStream_t stream) {
   const int cap = height + 1;
   // the groups' stacks in shared memory: smaller blocks for tall trees of
@@ -73,23 +73,23 @@ int launch_wide_kdtree_as(const KnnLaunch& L, int height, cudaStream_t stream) {
   if (smem > kWideSmemMax) return kNeedsSlab;
   cudaError_t e = cudaSuccess;
   if (smem > 48 * 1024)
-    e = cudaFuncSetAttribute(k_knn_kdtree_wide<T, D, M, G, OVF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute(k_knn_kdtree_wide<T, D, M, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)smem);
   if (e != cudaSuccess) return cuda_error(e, "wide kd-tree search shared memory");
   const int grid = ceil_div(L.nq, threads / G);
-  k_knn_kdtree_wide<T, D, M, G, OVF><<<grid, threads, smem, stream>>>(L, cap);
+  k_knn_kdtree_wide<T, D, M, G><<<grid, threads, smem, stream>>>(L, cap);
   return kOk;
 }
 
 // Launches the group-per-query kd-tree search for L.k (or the batch's
 // largest k) above kMaxK; `height` bounds the traversal stack. Returns
 // kNeedsSlab when one warp's stacks do not fit in shared memory.
-template <typename T, int D, bool OVF = false>
+template <typename T, int D>
 int launch_wide_kdtree(const KnnLaunch& L, int kMax, int height, cudaStream_t stream) {
   switch (wide_k(kMax)) {
 #define NABO_WIDE(KK) \
   case KK:            \
-    return launch_wide_kdtree_as<T, D, WideShape<KK>::M, WideShape<KK>::G, OVF>(L, height, stream);
+    return launch_wide_kdtree_as<T, D, WideShape<KK>::M, WideShape<KK>::G>(L, height, stream);
     NABO_WIDE_LIST(NABO_WIDE)
 #undef NABO_WIDE
   }
@@ -104,9 +104,9 @@ int64_t deep_unit_bytes(int kMax, int height) {
   return kMax > kMaxK ? wide_group_slab_bytes<T, D>(cap) : (int64_t)deep_stack_bytes<T, D>(cap);
 }
 
-// Launches the deep search over L (L.slab, L.slabBytes, the cap or the
-// device height, and optionally L.list set by the caller) with room for
-// `units` concurrent queries.
+// Launches the deep search over L (L.slab, L.slabBytes and the cap or the
+// device height set by the caller) with room for `units` concurrent
+// queries.
 template <typename T, int D>
 int launch_deep(const KnnLaunch& L, int kMax, int64_t units, cudaStream_t stream) {
   if (units < 1) units = 1;
@@ -184,15 +184,13 @@ KnnLaunch make_launch(const DeviceCloud& c, const KnnArgs& a, const int32_t* ord
   L.bK = nullptr;
   L.bOutOffset = nullptr;
   L.bClouds = 0;
-  L.ovfList = nullptr;
-  L.ovfCount = nullptr;
-  L.ovfBase = 0;
   L.slab = nullptr;
   L.slabBytes = 0;
   L.stackCap = 0;
   L.stackHeightDev = nullptr;
-  L.list = nullptr;
-  L.listCount = nullptr;
+  L.tallGate = nullptr;
+  L.tallGateLimit = 0;
+  L.deepFail = nullptr;
   return L;
 }
 
@@ -448,51 +446,44 @@ int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t st
   L.bClouds = b.nClouds;
   L.recs32 = b.recs32;
   L.coordMax = b.coordMax;
-  L.ovfList = b.ovfList;
-  L.ovfCount = b.ovfCount;
-  L.ovfBase = begin;
   L.maxRadii = b.maxRadii;
   L.fallbackRadius = b.maxRadii ? b.maxRadius : -1.0;
   L.fallbacks = b.fallbacks;
+  // The trees' heights are known only on the device: the kernels below keep
+  // stacks of kStackLarge entries and return at once if the tallest tree
+  // (read from the build's status) is taller; the deep kernel launched after
+  // them then searches the range with stacks in b.slab sized by that tree,
+  // and otherwise returns at once.
+  L.tallGate = b.heightDev;
+  L.tallGateLimit = kStackLarge;
   const int grid = ceil_div(L.nq, b.blockSize);
-  // The trees' heights are known only on the device: the kernels search
-  // with stacks of kStackLarge entries and list the queries of taller trees,
-  // which the deep kernel then searches with stacks in b.slab sized by the
-  // tallest tree (it returns at once when the list is empty).
   if (K < 0) {  // some cloud wants more than kMaxK: the whole batch runs a lane group per query
-    rc = launch_wide_kdtree<T, D, true>(L, b.kMax, kStackLarge, stream);
+    rc = launch_wide_kdtree<T, D>(L, b.kMax, kStackLarge, stream);
     if (rc != kOk) return rc == kNeedsSlab ? set_error(kErrInternal, "batched wide search stacks") : rc;
   } else if (b.lanesPerQuery == 8) {  // 8 lanes per query, the top-k spread over them
-    rc = K <= 16 ? launch_wide_kdtree_as<T, D, 2, 8, true>(L, kStackLarge, stream)
-                 : launch_wide_kdtree_as<T, D, 4, 8, true>(L, kStackLarge, stream);
+    rc = K <= 16 ? launch_wide_kdtree_as<T, D, 2, 8>(L, kStackLarge, stream)
+                 : launch_wide_kdtree_as<T, D, 4, 8>(L, kStackLarge, stream);
     if (rc != kOk) return rc == kNeedsSlab ? set_error(kErrInternal, "batched group search stacks") : rc;
     K = 0;
   }
 #define NABO_LAUNCH(KK)                                                                     \
   case KK:                                                                                  \
-    launch_kdtree<T, D, KK, kStackLarge, true>(grid, b.blockSize, stream, L);               \
+    launch_kdtree<T, D, KK, kStackLarge>(grid, b.blockSize, stream, L);                     \
     break;
   if (K > 0) switch (K) { NABO_K_LIST(NABO_LAUNCH) }
 #undef NABO_LAUNCH
   {
     KnnLaunch R = L;
-    R.nq = b.nq;
-    R.order = b.order;
-    R.ovfList = nullptr;
-    R.ovfBase = 0;
-    R.ovfCount = b.deepFail;
-    R.list = b.ovfList;
-    R.listCount = b.ovfCount;
     R.slab = b.slab;
     R.slabBytes = b.slabBytes;
     R.stackCap = 0;
     R.stackHeightDev = b.heightDev;
+    R.deepFail = b.deepFail;
     // enough threads for every stack the slab holds once trees are taller
     // than kStackLarge
     const int64_t units = std::max<int64_t>(1, b.slabBytes / deep_unit_bytes<T, D>(b.kMax, kStackLarge + 1));
-    rc = launch_deep<T, D>(R, b.kMax, units, stream);
+    rc = launch_deep<T, D>(R, b.kMax, std::min<int64_t>(units, L.nq), stream);
     if (rc != kOk) return rc;
-    NABO_CUDA_TRY(cudaMemsetAsync(b.ovfCount, 0, sizeof(int32_t), stream));
   }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "batched search launch");

@@ -229,12 +229,10 @@ __host__ __device__ inline int64_t wide_group_slab_bytes(int cap) {
 
 // One query (order position t) searched by the G-lane group: the
 // reference's visit order with the stack at sRd / sOff / sNode (cap
-// entries), written by the group's first lane and read by all its lanes.
-// With OVF a push beyond cap abandons the query (nothing written, false
-// returned, the same in every lane of the group); without it the caller
-// guarantees cap > tree height.
-template <typename T, int D, int M, int G, bool OVF>
-__device__ __forceinline__ bool wide_query(const KnnLaunch& a, int64_t t, T* sRd, T* sOff, uint32_t* sNode, int cap,
+// entries), written by the group's first lane and read by all its lanes;
+// the caller guarantees cap > tree height.
+template <typename T, int D, int M, int G>
+__device__ __forceinline__ void wide_query(const KnnLaunch& a, int64_t t, T* sRd, T* sOff, uint32_t* sNode, int cap,
                                            int g, unsigned gm, uint32_t& touchedOut) {
   // the reference's self-match rule (nabo/kdtree_cpu.cpp:392-396)
   const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
@@ -285,11 +283,7 @@ __device__ __forceinline__ bool wide_query(const KnnLaunch& a, int64_t t, T* sRd
         const uint32_t right = node_payload(nd.meta);
         const uint32_t nearN = newOff > T(0) ? right : node + 1;
         const uint32_t farN = newOff > T(0) ? node + 1 : right;
-        bool far = rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head();
-        if (far && sp >= cap) {
-          if constexpr (OVF) return false;
-          far = false;
-        }
+        const bool far = rdFar <= maxRadius2 && Ar<T>::mul(rdFar, maxError2) <= heap.head() && sp < cap;
         if (far) {
           if (g == 0) {
             sRd[sp] = rdFar;
@@ -333,15 +327,15 @@ __device__ __forceinline__ bool wide_query(const KnnLaunch& a, int64_t t, T* sRd
   const int f = heap.store(k, g, gm, a.outIdx + outBase, static_cast<T*>(a.outD2) + outBase);
   if (a.found && g == 0) a.found[qi] = f;
   touchedOut += touched;
-  return true;
 }
 
 // Reference-order kd-tree search, one G-lane group per query (blockDim.x / G
 // queries per block), stacks in shared memory; `cap` > the tree height
-// bounds them (with OVF, batches: a taller tree hands the query to
-// k_knn_kdtree_wide_deep through a.ovfList).
-template <typename T, int D, int M, int G, bool OVF>
+// bounds them (batches: returns at once when a.tallGate says a tree is
+// taller, k_knn_kdtree_wide_deep searching instead).
+template <typename T, int D, int M, int G>
 __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
+  if (a.tallGate && *a.tallGate > a.tallGateLimit) return;  // uniform
   extern __shared__ __align__(16) unsigned char wideSmem[];
   const int lane = threadIdx.x & 31;
   const int g = lane & (G - 1);  // lane within the group
@@ -354,23 +348,19 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_wide(KnnLaunch a, int cap) {
                           (size_t)group * cap;
   const int64_t t = (int64_t)blockIdx.x * groups + group;
   uint32_t touched = 0;
-  if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice)) {
-    if (!wide_query<T, D, M, G, OVF>(a, t, sRd, sOff, sNode, cap, g, gm, touched)) {
-      if constexpr (OVF) {
-        if (g == 0) a.ovfList[atomicAdd(a.ovfCount, 1)] = (int32_t)(t + a.ovfBase);
-      }
-    }
-  }
+  if (t < a.nq && (!a.nqDevice || t < (int64_t)*a.nqDevice))
+    wide_query<T, D, M, G>(a, t, sRd, sOff, sNode, cap, g, gm, touched);
   if (a.stats && g == 0 && touched) atomicAdd(a.touched, (unsigned long long)touched);
 }
 
 // Trees of any height, k above 32: each group's stack in its own region of
 // the global slab a.slab (cap = a.stackCap, or the height read from
 // *a.stackHeightDev plus one); as many groups as the slab holds search, each
-// taking every active-th item of a.list (or of 0..nq-1). A slab too small
-// for one stack searches nothing and sets *a.ovfCount to -1.
+// taking every active-th query. A slab too small for one stack searches
+// nothing and sets *a.deepFail to -1.
 template <typename T, int D, int M, int G>
 __global__ void __launch_bounds__(128) k_knn_kdtree_wide_deep(KnnLaunch a) {
+  if (a.tallGate && *a.tallGate <= a.tallGateLimit) return;  // uniform
   const int lane = threadIdx.x & 31;
   const int g = lane & (G - 1);
   const unsigned gm = group_mask<G>(lane);
@@ -380,18 +370,16 @@ __global__ void __launch_bounds__(128) k_knn_kdtree_wide_deep(KnnLaunch a) {
   const int64_t per = wide_group_slab_bytes<T, D>(cap);
   int64_t active = cap > 0 ? a.slabBytes / per : 0;
   if (active > groupsAll) active = groupsAll;
-  const int64_t count = a.list ? (int64_t)*a.listCount : a.nq;
-  if (active <= 0 && count > 0 && gid == 0 && g == 0 && a.ovfCount) *a.ovfCount = -1;
+  if (active <= 0 && a.nq > 0 && gid == 0 && g == 0 && a.deepFail) *a.deepFail = -1;
   uint32_t touched = 0;
   if (gid < active) {
     unsigned char* region = static_cast<unsigned char*>(a.slab) + gid * per;
     T* sRd = reinterpret_cast<T*>(region);
     T* sOff = sRd + cap;
     uint32_t* sNode = reinterpret_cast<uint32_t*>(sRd + (size_t)cap * (D + 1));
-    for (int64_t w = gid; w < count; w += active) {
-      const int64_t t = a.list ? (int64_t)a.list[w] : w;
+    for (int64_t t = gid; t < a.nq; t += active) {
       if (a.nqDevice && t >= (int64_t)*a.nqDevice) continue;
-      wide_query<T, D, M, G, false>(a, t, sRd, sOff, sNode, cap, g, gm, touched);
+      wide_query<T, D, M, G>(a, t, sRd, sOff, sNode, cap, g, gm, touched);
     }
   }
   if (a.stats && g == 0 && touched) atomicAdd(a.touched, (unsigned long long)touched);
