@@ -80,14 +80,17 @@ def workload(name: str, rank: int):
 
 
 def training_queries(name: str, q, count: int):
-    """Training queries for the radius network. Lidar: a random subset of the
-    transformed scan being searched (a query's k-th distance is dominated by
-    how far the scan transform moved it off the surface, so the network is fit
-    to the transform it serves); uniform: fresh samples of the same law."""
+    """Training queries for the radius network, disjoint from the timed ones.
+    Lidar: another frame -- the same scene scanned again with fresh range
+    noise, moved by the same pose change as the timed queries (a query's k-th
+    distance is dominated by how far that motion moved it off the surfaces),
+    as frame t trains the network a sensor loop uses on frame t + 1; uniform:
+    fresh samples of the same law."""
     from libnabo_gb300 import synthetic as S
     rng = np.random.default_rng(S.SEED_BASE + 4242)
     if name == "lidar":
-        return q[rng.choice(q.shape[0], min(count, q.shape[0]), replace=False)]
+        frame = S.lidar_queries(S.lidar_scan(noise_seed=S.SEED_BASE + 4244))
+        return frame[rng.choice(frame.shape[0], min(count, frame.shape[0]), replace=False)]
     return S.uniform(count, 3, seed=S.SEED_BASE + 4243)
 
 
@@ -338,7 +341,7 @@ def run_ours(args):
             learned = {"ms_per_step": learned_ms, "queries_per_s": world * nq / (learned_ms / 1e3),
                        "fallbacks": int(fb.item()), "fallback_rate": int(fb.item()) / nq,
                        "identical_to_plain": exact, "train_s": train_s, "train_queries": int(tr.shape[0]),
-                       "train_queries_from": "random subset of the searched queries" if args.workload == "lidar"
+                       "train_queries_from": "another frame of the scene (fresh range noise, same pose change), disjoint from the timed queries" if args.workload == "lidar"
                        else "independent samples of the query distribution",
                        "bounded_kernel_ms": statistics.mean(lkernel_ms),
                        "ideal_radius_kernel_ms": statistics.mean(ideal_kernel_ms),
@@ -775,6 +778,37 @@ def run_c4(args):
             learned[f"eps{eps}"] = entry
         learned["models"] = {np.dtype(x["dt"]).name: dict(x["model"].meta, train_queries=x["train_n"])
                              for x in batches}
+
+        # where the time goes, per scalar type (best of 2, epsilon 0): the
+        # plain search, the learned search, its network alone, and the bound
+        # of any radius predictor -- each query's exact k-th distance (a hair
+        # above) as its radius
+        def t_best(fn, reps=2):
+            best = float("inf")
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a0.record()
+                fn()
+                a1.record()
+                torch.cuda.synchronize()
+                best = min(best, a0.elapsed_time(a1))
+            return best
+
+        parts = {}
+        for j, x in enumerate(batches):
+            b, tq = x["b"], x["tq"]
+            tmp = b._outputs(dev)
+            dk2 = exact_out[j][1].view(-1, k)[:, -1]
+            ideal = (torch.sqrt(dk2) * (1 + 2.0 ** -20)).to(dk2.dtype).contiguous()
+            entry = {"plain_ms": t_best(lambda: b.knn(tq, out=tmp)),
+                     "learned_ms": t_best(lambda: b.knn_learned(x["model"], tq, out=tmp)),
+                     "network_ms": t_best(lambda: b.predict_radii(x["model"], tq)),
+                     "ideal_radius_ms": t_best(lambda: b.knn_radii(tq, ideal, out=tmp))}
+            entry["ideal_radius_identical"] = bool(torch.equal(tmp[0], exact_out[j][0])
+                                                   and torch.equal(tmp[1], exact_out[j][1]))
+            parts[np.dtype(x["dt"]).name] = entry
+        learned["per_type_eps0"] = parts
         learned["train_s"] = train_s
         learned["train_queries_from"] = "fresh draws from each cloud's mixture, disjoint from the timed queries"
     forms["learned"] = learned

@@ -19,7 +19,7 @@ import time
 
 import numpy as np
 
-CANDIDATES = {"bucketSize": (4, 6, 8, 12, 16), "threadsPerBlock": (64, 128), "splitRule": (0, 1),
+CANDIDATES = {"bucketSize": (4, 6, 8, 12, 16, 24, 32), "threadsPerBlock": (64, 128), "splitRule": (0, 1),
               "lanesPerQuery": (1, 8)}
 _cache: dict = {}
 

@@ -47,10 +47,14 @@ def _boxes(rng, count=20, within=60.0, size=(1.0, 10.0), ground=-1.7):
 
 def lidar_scan(seed: int = SEED_BASE + 1, n_azimuth: int = 25000, beams: int = 64, elev_deg=(-25.0, 15.0),
                ground: float = -1.7, n_boxes: int = 20, noise: float = 0.02, max_range: float = 120.0,
-               dtype=np.float32) -> np.ndarray:
-    """Returns an (n, 3) cloud of ray returns (rays that hit nothing are dropped)."""
+               dtype=np.float32, noise_seed: int | None = None) -> np.ndarray:
+    """Returns an (n, 3) cloud of ray returns (rays that hit nothing are dropped).
+    ``noise_seed`` draws the range noise from its own generator: the same
+    scene scanned again (another frame of a static scene)."""
     rng = np.random.default_rng(seed)
     lo, hi = _boxes(rng, n_boxes, ground=ground)
+    if noise_seed is not None:
+        rng = np.random.default_rng(noise_seed)
     elev = np.deg2rad(np.linspace(elev_deg[0], elev_deg[1], beams))
     az = np.linspace(0.0, 2.0 * np.pi, n_azimuth, endpoint=False)
     out = []

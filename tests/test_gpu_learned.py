@@ -27,11 +27,16 @@ def lidar():
 
 @pytest.fixture(scope="module")
 def lidar_model(lidar):
+    """A model trained on another frame of the scene (fresh range noise, the
+    same pose change): held-out queries, disjoint from every query the tests
+    evaluate it on."""
     nb = _nb()
+    from libnabo_gb300 import synthetic as S
     cloud, q = lidar
     s = nb.NearestNeighbourSearch(cloud, creationOptionFlags=nb.TOUCH_STATISTICS)
+    frame = S.lidar_queries(S.lidar_scan(n_azimuth=2400, noise_seed=99))
     rng = np.random.default_rng(0)
-    train = q[rng.choice(q.shape[0], 40000, replace=False)]
+    train = frame[rng.choice(frame.shape[0], 40000, replace=False)]
     m = nb.RadiusModel(s, train, k=10, maxRadius=1.0, epochs=12)
     return s, m
 
