@@ -349,10 +349,17 @@ __global__ void k_minmax(const Rec<T, D>* __restrict__ recs, int* __restrict__ s
   }
 }
 
-// Median-split trees (split rule 1): the cut is the median of the segment's
-// coordinates along the cut dimension, sampled at kMedianSamples evenly
-// spaced positions (the segment's points are in no particular order there).
+// Median-split trees (split rule 1): the cut is just above the median of the
+// segment's coordinates along the cut dimension (sampled at kMedianSamples
+// evenly spaced positions at the level-synchronous levels, where the
+// segment's points are in no particular order; exact in k_small). Just above
+// (the next representable value): points equal to the median go left and
+// hardly any point lies on the cut, so the build's second partition pass,
+// which only segments with points on their cut run, is skipped.
 constexpr int kMedianSamples = 31;
+
+__device__ __forceinline__ float next_up(float x) { return nextafterf(x, __builtin_huge_valf()); }
+__device__ __forceinline__ double next_up(double x) { return nextafter(x, __builtin_huge_val()); }
 
 template <typename T>
 __device__ T sampled_median(const T* __restrict__ val, int start, int count) {
@@ -383,7 +390,7 @@ __global__ void k_cut(SegLevel<T> L, const LevelState* st, const T* __restrict__
   // halving is exact, so multiplying by 1/2 gives the same value. The
   // median rule takes a point's coordinate, which lies in [mn, mx].
   const T ideal = splitRule == 1
-                      ? sampled_median(val, L.start[s], L.count[s])
+                      ? next_up(sampled_median(val, L.start[s], L.count[s]))
                       : Ar<T>::mul(Ar<T>::add(L.boxHi[(int64_t)s * kMaxDim + cd], L.boxLo[(int64_t)s * kMaxDim + cd]),
                                    T(0.5));
   T cut;
@@ -926,7 +933,7 @@ __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, 
       }
       const int cd = arg_max_extent(lo, hi, dim);
       Rec<T, D>* node = pts + st;
-      const T ideal = splitRule == 1 ? warp_median(node, count, cd, lane)
+      const T ideal = splitRule == 1 ? next_up(warp_median(node, count, cd, lane))
                                      : Ar<T>::mul(Ar<T>::add(hi[cd], lo[cd]), T(0.5));
       T mn = std::numeric_limits<T>::max(), mx = std::numeric_limits<T>::lowest();
       for (int i = lane; i < count; i += 32) {

@@ -294,8 +294,10 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
 }
 
 // Brute force for k <= kMaxK. A search with too few queries to give every
-// SM several blocks splits the points into row chunks (block rows), each
-// writing its k best per query to scratch, merged by k_bf_merge.
+// SM kBfBlocksPerSm blocks splits the points into row chunks (block rows),
+// each writing its k best per query to scratch, merged by k_bf_merge.
+// (At 4 blocks per SM, 100 k x 100 k ran 16 warps per SM at 74 % issue.)
+constexpr int kBfBlocksPerSm = 8;
 template <typename T, int D, int K, int QT = BfShape<T, K>::QT, int J = BfShape<T, K>::J>
 int launch_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
   constexpr int64_t kTile = (int64_t)((24 * 1024) / sizeof(Rec<T, D>));
@@ -303,7 +305,7 @@ int launch_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
   int dev = 0, sms = 148;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t tiles = std::max<int64_t>(1, (L.n + kTile - 1) / kTile);
-  int64_t rows = std::min<int64_t>({(4 * (int64_t)sms + qBlocks - 1) / qBlocks, tiles / 4, 64});
+  int64_t rows = std::min<int64_t>({(kBfBlocksPerSm * (int64_t)sms + qBlocks - 1) / qBlocks, tiles / 4, 64});
   if (rows <= 1) {
     k_knn_bruteforce<T, D, K, QT, J><<<qBlocks, 128, 0, stream>>>(L, L.n, 0);
     return kOk;
