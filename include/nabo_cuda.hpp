@@ -86,11 +86,19 @@ inline void check(int rc) {
 }
 }  // namespace detail
 
+// CloudType is what the cloud is held as: an owning matrix, a fixed-row
+// matrix (the reference's Matrix3X instantiation) or a non-owning mapped view
+// (its Map<const Matrix3X, Aligned>, nabo/nabo.cpp:181-186); it needs rows(),
+// cols() and a column-major data() with stride rows(). MatrixType is the
+// matrix of queries and squared distances, dynamic in both dimensions as the
+// reference's Matrix typedef (nabo/nabo.h:261); it defaults to CloudType for
+// owning dynamic clouds.
 template <typename T, typename CloudType = DenseMatrix<T>, typename IndexMatrixType = DenseMatrix<int>,
-          typename VectorType = DenseVector<T>, typename IndexVectorType = DenseVector<int>>
+          typename VectorType = DenseVector<T>, typename IndexVectorType = DenseVector<int>,
+          typename MatrixType = CloudType>
 class NearestNeighbourSearch {
  public:
-  using Matrix = CloudType;
+  using Matrix = MatrixType;
   using IndexMatrix = IndexMatrixType;
   using Vector = VectorType;
   using IndexVector = IndexVectorType;

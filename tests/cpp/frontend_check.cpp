@@ -57,6 +57,72 @@ static int errors() {
   return bad;
 }
 
+// Clouds held as the reference's other instantiations hold them
+// (nabo/nabo.cpp:181-186): a matrix with 3 rows fixed at compile time
+// (Matrix3X) and a non-owning view of a caller's column-major buffer
+// (Map<const Matrix3X, Aligned>); queries and distances stay dynamic.
+template <typename S>
+class Fixed3X {
+ public:
+  using Scalar = S;
+  explicit Fixed3X(long n) : n_(n), v_((size_t)(3 * n)) {}
+  static constexpr long rows() { return 3; }
+  long cols() const { return n_; }
+  const S* data() const { return v_.data(); }
+  S& operator()(long i) { return v_[(size_t)i]; }
+
+ private:
+  long n_;
+  std::vector<S> v_;
+};
+
+template <typename S>
+class ConstMap3X {
+ public:
+  using Scalar = S;
+  ConstMap3X(const S* p, long n) : p_(p), n_(n) {}
+  static constexpr long rows() { return 3; }
+  long cols() const { return n_; }
+  const S* data() const { return p_; }
+
+ private:
+  const S* p_;
+  long n_;
+};
+
+// The same search through a fixed-row cloud and through a mapped cloud:
+// results identical to the dense cloud's.
+template <typename T>
+static int other_cloud_types(const M<T>& cloud, const M<T>& query, const M<int>& idx, const M<T>& d2, int k) {
+  using V = nabo_cuda::DenseVector<T>;
+  using IV = nabo_cuda::DenseVector<int>;
+  using NNSFixed = nabo_cuda::NearestNeighbourSearch<T, Fixed3X<T>, M<int>, V, IV, M<T>>;
+  using NNSMap = nabo_cuda::NearestNeighbourSearch<T, ConstMap3X<T>, M<int>, V, IV, M<T>>;
+  static_assert(std::is_same<typename NNSMap::Matrix, M<T>>::value, "queries and distances stay dynamic");
+  int bad = 0;
+  Fixed3X<T> fixed(cloud.cols());
+  for (long i = 0; i < cloud.size(); ++i) fixed(i) = cloud(i);
+  const ConstMap3X<T> mapped(cloud.data(), cloud.cols());
+  M<int> i1(k, query.cols()), i2(k, query.cols());
+  M<T> e1(k, query.cols()), e2(k, query.cols());
+  NNSFixed* a = NNSFixed::createKDTreeLinearHeap(fixed);
+  NNSMap* b = NNSMap::createKDTreeLinearHeap(mapped);
+  a->knn(query, i1, e1, k, 0, NNSFixed::SORT_RESULTS, (T)1.0);
+  b->knn(query, i2, e2, k, 0, NNSMap::SORT_RESULTS, (T)1.0);
+  int diff1 = 0, diff2 = 0;
+  for (long i = 0; i < idx.size(); ++i) {
+    diff1 += (i1(i) != idx(i) || e1(i) != d2(i)) ? 1 : 0;
+    diff2 += (i2(i) != idx(i) || e2(i) != d2(i)) ? 1 : 0;
+  }
+  std::printf("%s Matrix3X-like cloud: %d differences\n", diff1 ? "FAIL" : "ok", diff1);
+  std::printf("%s Map<const Matrix3X>-like cloud: %d differences\n", diff2 ? "FAIL" : "ok", diff2);
+  bad += (diff1 ? 1 : 0) + (diff2 ? 1 : 0);
+  bad += (&b->cloud == &mapped) ? 0 : 1;  // held by reference, as the reference holds it
+  delete a;
+  delete b;
+  return bad;
+}
+
 template <typename T>
 static int search_type(const std::vector<float>& c, const std::vector<float>& q, const std::vector<float>& r, int n,
                        int nq, int k, int dim, FILE* out) {
@@ -71,6 +137,7 @@ static int search_type(const std::vector<float>& c, const std::vector<float>& q,
   M<T> d2(k, nq), d22(k, nq);
   const unsigned long touched = s->knn(query, idx, d2, k, 0, NNS::SORT_RESULTS, (T)1.0);
   s->knn(query, idx2, d22, radii, k, 0, 0);
+  int bad = dim == 3 ? other_cloud_types<T>(cloud, query, idx, d2, k) : 0;
   std::fwrite(idx.data(), 4, (size_t)idx.size(), out);
   std::fwrite(d2.data(), sizeof(T), (size_t)d2.size(), out);
   std::fwrite(idx2.data(), 4, (size_t)idx2.size(), out);
@@ -78,7 +145,6 @@ static int search_type(const std::vector<float>& c, const std::vector<float>& q,
   const uint64_t t64 = touched;
   std::fwrite(&t64, 8, 1, out);
   // the single-point overload (nabo/nabo.h:325) against the matrix call's columns
-  int bad = 0;
   {
     nabo_cuda::DenseVector<T> qv(dim + 1), dv;  // a longer vector: only the first dim entries count
     nabo_cuda::DenseVector<int> iv;

@@ -60,7 +60,9 @@ def test_cpp_frontend_search_matches_oracle(tmp_path):
         radii.tofile(f)
     r = subprocess.run([exe, "search", inp, out], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "FAIL" not in r.stdout and r.stdout.count("ok ") == 14, r.stdout
+    # 9 checks per scalar type, 2 of them through the Matrix3X-like and the
+    # mapped cloud types
+    assert "FAIL" not in r.stdout and r.stdout.count("ok ") == 18, r.stdout
     raw = open(out, "rb").read()
     off = 0
 
