@@ -577,43 +577,18 @@ __global__ void k_swap(Rec<T, D>* recs, T* val, const int* __restrict__ pairA, c
   }
 }
 
-// nabo/kdtree_cpu.cpp:180-223: leftCount rule, node, children.
+// Writes the split of segment s of the current level (node levelBase + s):
+// its node record and its two children, each either a segment of the next
+// level (more than kSmallMax points) or a small segment, with the child
+// boxes cut at `cut` along `cd` (nabo/kdtree_cpu.cpp:192-223). With
+// `childDims` the children's cut dimensions are also recorded (the median
+// split moves each point's next cut coordinate along with it).
 template <typename T>
-__global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, const LevelState* st, TopNodes<T> top,
-                           SmallSegs<T> small, int* counters, int dim, int segCap, int smallCap, int topCap) {
-  pdl_begin();
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nseg = st->nseg;
-  if (s >= nseg) return;
-  const int levelBase = st->levelBase;
-  const int nextLevelBase = levelBase + nseg;
-  const int level = st->level;
-  if (levelBase + s >= topCap) {
-    atomicOr(counters + 3, 1);
-    return;
-  }
+__device__ void emit_split(const SegLevel<T>& L, const SegLevel<T>& next, int s, int leftCount, int cd, T cut,
+                           const TopNodes<T>& top, const SmallSegs<T>& small, int* counters, int dim, int segCap,
+                           int smallCap, int node, int nextLevelBase, int level, bool childDims) {
   const int count = L.count[s];
   const int start = L.start[s];
-  const int br1 = L.lt[s];
-  const int br2 = br1 + L.eq[s];
-  const int mode = L.mode[s];
-  int leftCount;
-  if (mode == 1)
-    leftCount = 1;
-  else if (mode == 2)
-    leftCount = count - 1;
-  else if (br1 > count / 2)
-    leftCount = br1;
-  else if (br2 < count / 2)
-    leftCount = br2;
-  else
-    leftCount = count / 2;
-  // finite coordinates guarantee 1 <= leftCount < count; keep the split
-  // productive whatever happens
-  leftCount = leftCount < 1 ? 1 : (leftCount > count - 1 ? count - 1 : leftCount);
-  const int cd = L.cutDim[s];
-  const T cut = L.cut[s];
-  const int node = levelBase + s;
   top.dim[node] = cd;
   top.cut[node] = cut;
   L.leftCount[s] = leftCount;
@@ -663,7 +638,43 @@ __global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, const LevelState* st
       top.right[node] = ref;
       L.newRight[s] = newSeg;
     }
+    if (childDims && newSeg >= 0) next.cutDim[newSeg] = arg_max_extent(dLo, dHi, dim);
   }
+}
+
+// nabo/kdtree_cpu.cpp:180-223: leftCount rule, node, children.
+template <typename T>
+__global__ void k_finalize(SegLevel<T> L, SegLevel<T> next, const LevelState* st, TopNodes<T> top,
+                           SmallSegs<T> small, int* counters, int dim, int segCap, int smallCap, int topCap) {
+  pdl_begin();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nseg = st->nseg;
+  if (s >= nseg) return;
+  const int levelBase = st->levelBase;
+  if (levelBase + s >= topCap) {
+    atomicOr(counters + 3, 1);
+    return;
+  }
+  const int count = L.count[s];
+  const int br1 = L.lt[s];
+  const int br2 = br1 + L.eq[s];
+  const int mode = L.mode[s];
+  int leftCount;
+  if (mode == 1)
+    leftCount = 1;
+  else if (mode == 2)
+    leftCount = count - 1;
+  else if (br1 > count / 2)
+    leftCount = br1;
+  else if (br2 < count / 2)
+    leftCount = br2;
+  else
+    leftCount = count / 2;
+  // finite coordinates guarantee 1 <= leftCount < count; keep the split
+  // productive whatever happens
+  leftCount = leftCount < 1 ? 1 : (leftCount > count - 1 ? count - 1 : leftCount);
+  emit_split(L, next, s, leftCount, L.cutDim[s], L.cut[s], top, small, counters, dim, segCap, smallCap,
+             levelBase + s, levelBase + nseg, st->level, false);
 }
 
 // Closes a level: records its top-node range and makes the segments the
@@ -686,11 +697,300 @@ __global__ void k_advance(LevelState* st, int* counters, int* lvStart, int* lvCo
   counters[0] = 0;
 }
 
+// ---- median-split top levels (split rule 1): a stable partition by scatter
+//
+// The median-split tree is this library's own, so its top levels need not
+// reproduce the reference's in-place swaps. Each level scans two flags per
+// position of a large segment, coordinate <= m and coordinate < m (m the
+// segment's sampled median), keeps one of them per segment and moves every
+// record to its child's range, flagged records first, each side in position
+// order, into the other of two record arrays. Records whose child is a
+// small segment go straight to the final array that the small-segment phase
+// reads. Segment ids and cut coordinates travel with the records, so a
+// level reads each position's id and coordinate twice and its record once,
+// and writes its record, next id and next coordinate once: 6 launches and
+// about 56 bytes per position of a large segment per level, against 14
+// launches for the reference's rule. The arrays in use alternate with the
+// level's parity (LevelState::level), read on the device, so a fixed-level
+// build needs no host decision.
+constexpr int kItems = 4;               // consecutive positions per thread
+constexpr int kTile = kBlock * kItems;  // positions per block and tile
+
+template <typename T, int D>
+struct MedianBufs {
+  Rec<T, D>* rec[2];  // [n]
+  int* seg[2];        // [nPad]: segment of the level, -1 outside large segments
+  T* val[2];          // [nPad]: coordinate along the segment's cut dimension
+  // selects rather than indexing, which would copy the struct to local memory
+  __device__ Rec<T, D>* recs(int i) const { return i ? rec[1] : rec[0]; }
+  __device__ int* segs(int i) const { return i ? seg[1] : seg[0]; }
+  __device__ T* vals(int i) const { return i ? val[1] : val[0]; }
+};
+
+template <typename T>
+__device__ __forceinline__ void load4(const T* __restrict__ p, T (&v)[kItems]) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 x = *reinterpret_cast<const float4*>(p);
+    v[0] = x.x;
+    v[1] = x.y;
+    v[2] = x.z;
+    v[3] = x.w;
+  } else {
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+  }
+}
+
+template <typename T, int D>
+__device__ __forceinline__ T rec_coord(const Rec<T, D>& r, int cd) {
+  T v = r.p.c[0];
+#pragma unroll
+  for (int d = 1; d < D; ++d) v = d == cd ? r.p.c[d] : v;
+  return v;
+}
+
+// One tile's positions of a thread: segment ids, coordinates and the two
+// flags (x: v <= m, y: v < m; m = L.cut[s] holds the median until the
+// level's split is chosen).
+template <typename T>
+struct MedianItems {
+  int s[kItems];
+  T v[kItems];
+};
+
+template <typename T>
+__device__ __forceinline__ void median_load(const int* __restrict__ seg, const T* __restrict__ val, int64_t p0,
+                                            int64_t nPad, MedianItems<T>& it) {
+  if (p0 < nPad) {
+    const int4 s4 = *reinterpret_cast<const int4*>(seg + p0);
+    it.s[0] = s4.x;
+    it.s[1] = s4.y;
+    it.s[2] = s4.z;
+    it.s[3] = s4.w;
+    load4(val + p0, it.v);
+  } else {
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      it.s[i] = -1;
+      it.v[i] = T(0);
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ int2 median_flag(const SegLevel<T>& L, int s, T v) {
+  if (s < 0) return make_int2(0, 0);
+  const T m = L.cut[s];
+  return make_int2(v <= m ? 1 : 0, v < m ? 1 : 0);
+}
+
+// Level 0: each position's coordinate along its root segment's cut dimension.
+template <typename T, int D>
+__global__ void k_median_val0(MedianBufs<T, D> B, int64_t n, SegLevel<T> L, const LevelState* st) {
+  pdl_begin();
+  if (st->nseg == 0) return;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
+    const int s = B.seg[0][p];
+    if (s >= 0) B.val[0][p] = B.rec[0][p].p.c[L.cutDim[s]];
+  }
+}
+
+template <typename T, int D>
+__global__ void k_median_cut(SegLevel<T> L, const LevelState* st, MedianBufs<T, D> B) {
+  pdl_begin();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= st->nseg) return;
+  L.cut[s] = sampled_median(B.vals(st->level & 1), L.start[s], L.count[s]);
+}
+
+// Block b scans tiles [b * tiles, (b + 1) * tiles) in position order and
+// records, besides its totals, each segment's running flag counts at its
+// first position (exclusive) and last position (inclusive), as k_flag_sums.
+// The next tile's ids and coordinates are loaded before this tile's scan.
+template <typename T, int D>
+__global__ void k_median_sums(MedianBufs<T, D> B, int64_t nPad, SegLevel<T> L, int tiles, int2* blockSums,
+                              int2* segFirst, int2* segLast, const LevelState* st) {
+  pdl_begin();
+  if (st->nseg == 0) return;
+  const int par = st->level & 1;
+  const int* seg = B.segs(par);
+  const T* val = B.vals(par);
+  const int64_t first = (int64_t)blockIdx.x * tiles * kTile + threadIdx.x * kItems;
+  MedianItems<T> nxt;
+  median_load(seg, val, first, nPad, nxt);
+  int2 carry = make_int2(0, 0);
+  for (int t = 0; t < tiles; ++t) {
+    const MedianItems<T> it = nxt;
+    const int64_t p0 = first + (int64_t)t * kTile;
+    if (t + 1 < tiles) median_load(seg, val, p0 + kTile, nPad, nxt);
+    int2 f[kItems];
+    int2 sum = make_int2(0, 0);
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      f[i] = median_flag(L, it.s[i], it.v[i]);
+      sum = add2(sum, f[i]);
+    }
+    int2 total;
+    int2 ex = add2(block_excl_scan(sum, &total), carry);
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const int s = it.s[i];
+      if (s >= 0) {
+        const int64_t p = p0 + i;
+        const int st0 = L.start[s];
+        if (p == st0) segFirst[s] = ex;
+        if (p == st0 + L.count[s] - 1) segLast[s] = add2(ex, f[i]);
+      }
+      ex = add2(ex, f[i]);
+    }
+    carry = add2(carry, total);
+  }
+  if (threadIdx.x == 0) blockSums[blockIdx.x] = carry;
+}
+
+// Chooses each segment's split from its two flag totals and writes it:
+//   some point above the median  -> cut just above it, left = v <= m
+//   else some point below it     -> cut at it, left = v < m
+//   else (all equal)             -> cut at it, first half left by position
+// L.lt keeps the chosen flag's global rank at the segment's first position.
+template <typename T>
+__global__ void k_median_split(SegLevel<T> L, SegLevel<T> next, const LevelState* st, TopNodes<T> top,
+                               SmallSegs<T> small, int* counters, int dim, int segCap, int smallCap, int topCap,
+                               const int2* __restrict__ blockPrefix, const int2* __restrict__ segFirst,
+                               const int2* __restrict__ segLast, int perBlock) {
+  pdl_begin();
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nseg = st->nseg;
+  if (s >= nseg) return;
+  const int levelBase = st->levelBase;
+  if (levelBase + s >= topCap) {
+    atomicOr(counters + 3, 1);
+    return;
+  }
+  const int count = L.count[s];
+  const int start = L.start[s];
+  const int2 a = add2(blockPrefix[start / perBlock], segFirst[s]);
+  const int2 b = add2(blockPrefix[(start + count - 1) / perBlock], segLast[s]);
+  const int le = b.x - a.x, lt = b.y - a.y;
+  const T m = L.cut[s];
+  int mode, leftCount;
+  T cut;
+  if (le < count) {
+    mode = 0;
+    leftCount = le;
+    cut = next_up(m);
+    L.lt[s] = a.x;
+  } else if (lt > 0) {
+    mode = 1;
+    leftCount = lt;
+    cut = m;
+    L.lt[s] = a.y;
+  } else {
+    mode = 2;
+    leftCount = count / 2;
+    cut = m;
+  }
+  leftCount = leftCount < 1 ? 1 : (leftCount > count - 1 ? count - 1 : leftCount);
+  L.mode[s] = mode;
+  emit_split(L, next, s, leftCount, L.cutDim[s], cut, top, small, counters, dim, segCap, smallCap, levelBase + s,
+             levelBase + nseg, st->level, true);
+}
+
+// Moves every record of a large segment to its child's range: a record with
+// r flagged records before it in its segment goes to start + r when flagged,
+// to start + leftCount + (its offset - r) otherwise. Positions outside large
+// segments only mark themselves outside in the next level's id array.
+template <typename T, int D>
+__global__ void k_median_scatter(MedianBufs<T, D> B, Rec<T, D>* __restrict__ finalRecs, int64_t nPad,
+                                 SegLevel<T> L, SegLevel<T> next, int tiles, const int2* __restrict__ blockPrefix,
+                                 const LevelState* st) {
+  pdl_begin();
+  if (st->nseg == 0) return;
+  const int par = st->level & 1;
+  const int* seg = B.segs(par);
+  const T* val = B.vals(par);
+  const Rec<T, D>* src = B.recs(par);
+  Rec<T, D>* dst = B.recs(par ^ 1);
+  int* segN = B.segs(par ^ 1);
+  T* valN = B.vals(par ^ 1);
+  const int64_t first = (int64_t)blockIdx.x * tiles * kTile + threadIdx.x * kItems;
+  MedianItems<T> nxt;
+  median_load(seg, val, first, nPad, nxt);
+  int2 carry = blockPrefix[blockIdx.x];
+  for (int t = 0; t < tiles; ++t) {
+    const MedianItems<T> it = nxt;
+    const int64_t p0 = first + (int64_t)t * kTile;
+    if (t + 1 < tiles) median_load(seg, val, p0 + kTile, nPad, nxt);
+    int2 f[kItems];
+    int2 sum = make_int2(0, 0);
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      f[i] = median_flag(L, it.s[i], it.v[i]);
+      sum = add2(sum, f[i]);
+    }
+    int2 total;
+    int2 ex = add2(block_excl_scan(sum, &total), carry);
+    carry = add2(carry, total);
+    if (p0 >= nPad) continue;
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const int s = it.s[i];
+      const int64_t p = p0 + i;
+      if (s < 0) {
+        segN[p] = -1;
+      } else {
+        const int start = L.start[s];
+        const int mode = L.mode[s];
+        const int lc = L.leftCount[s];
+        const int loc = (int)(p - start);
+        int before;
+        bool left;
+        if (mode == 2) {
+          before = loc < lc ? loc : lc;
+          left = loc < lc;
+        } else {
+          before = (mode == 0 ? ex.x : ex.y) - L.lt[s];
+          left = (mode == 0 ? f[i].x : f[i].y) != 0;
+        }
+        const int64_t dest = start + (left ? before : lc + (loc - before));
+        const int child = left ? L.newLeft[s] : L.newRight[s];
+        Rec<T, D> r;
+        load_rec(src, p, r);
+        if (child >= 0) {
+          dst[dest] = r;
+          segN[dest] = child;
+          valN[dest] = rec_coord(r, next.cutDim[child]);
+        } else {
+          finalRecs[dest] = r;
+          segN[dest] = -1;
+        }
+      }
+      ex = add2(ex, f[i]);
+    }
+  }
+}
+
+// A fixed-level build that ran out of levels leaves records of unfinished
+// segments in the working arrays; they go to the final array, whose cloud
+// ranges then hold every point (the one-leaf-per-cloud fallback reads them).
+template <typename T, int D>
+__global__ void k_median_flush(MedianBufs<T, D> B, Rec<T, D>* finalRecs, int64_t n, const LevelState* st) {
+  if (st->nseg == 0) return;
+  const int par = st->level & 1;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    if (B.segs(par)[p] >= 0) finalRecs[p] = B.recs(par)[p];
+}
+
 // ---- forest set-up: clouds are contiguous point ranges [off[c], off[c+1])
 
 template <typename T, int D>
 __global__ void k_pack_forest(const T* __restrict__ cloud, int64_t n, int64_t stride, int dim,
-                              const int64_t* __restrict__ off, int nClouds, Rec<T, D>* __restrict__ recs) {
+                              const int64_t* __restrict__ off, int nClouds, Rec<T, D>* __restrict__ recs,
+                              Rec<T, D>* __restrict__ smallRoots) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (p >= n) return;
   Rec<T, D> r;
@@ -698,8 +998,12 @@ __global__ void k_pack_forest(const T* __restrict__ cloud, int64_t n, int64_t st
   for (int c = 0; c < RecSize<T, D>::chunks; ++c) r.v[c] = make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
   for (int d = 0; d < D; ++d) r.p.c[d] = d < dim ? cloud[p * stride + d] : T(0);
-  r.p.idx = (int32_t)(p - off[cloud_of(off, nClouds, p)]);
+  const int c = cloud_of(off, nClouds, p);
+  r.p.idx = (int32_t)(p - off[c]);
   recs[p] = r;
+  // the median split packs into a working array: clouds whose root is
+  // already a small segment also go to the final array
+  if (smallRoots && off[c + 1] - off[c] <= kSmallMax) smallRoots[p] = r;
 }
 
 // Per-cloud per-dimension min/max (ordered keys) and a non-finite flag.
@@ -785,11 +1089,12 @@ __global__ void k_forest_roots(const int64_t* __restrict__ off, int nClouds, con
   }
 }
 
-__global__ void k_init_segof(int* segOf, int64_t n, const int64_t* __restrict__ off, int nClouds,
+// Positions in [n, nPad) (the median split's padding) belong to no segment.
+__global__ void k_init_segof(int* segOf, int64_t n, int64_t nPad, const int64_t* __restrict__ off, int nClouds,
                              const int* __restrict__ rootSeg) {
   const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  segOf[p] = rootSeg[cloud_of(off, nClouds, p)];
+  if (p >= nPad) return;
+  segOf[p] = p < n ? rootSeg[cloud_of(off, nClouds, p)] : -1;
 }
 
 // ---------------------------------------------------------------------------
@@ -1248,7 +1553,21 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   const bool hostDriven = maxLevels < 0;
   Scratch sc(stream);
   Rec<T, D>* recs = static_cast<Rec<T, D>*>(f->recs);
-  k_pack_forest<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, dOff, nClouds, recs);
+  // the median split works in two record arrays of its own (positions
+  // padded to whole tiles) and leaves the final array to its scatter
+  const bool median = splitRule == 1;
+  const int64_t nPad = median ? (std::max<int64_t>(n, 1) + kTile - 1) / kTile * kTile : n;
+  MedianBufs<T, D> mb = {};
+  if (median) {
+    for (int i = 0; i < 2; ++i) {
+      NABO_CUDA_TRY(sc.get(&mb.rec[i], n));
+      NABO_CUDA_TRY(sc.get(&mb.seg[i], nPad));
+      NABO_CUDA_TRY(sc.get(&mb.val[i], nPad));
+    }
+  }
+  Rec<T, D>* packed = median ? mb.rec[0] : recs;
+  k_pack_forest<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, dOff, nClouds, packed,
+                                                                  median ? recs : nullptr);
 
   // per-cloud bounds
   Key* keys;
@@ -1256,7 +1575,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   NABO_CUDA_TRY(cudaMemsetAsync(f->status, 0, 4 * sizeof(int), stream));
   k_init_keys_forest<T><<<ceil_div(nClouds * kMaxDim, 256), 256, 0, stream>>>(keys, keys + nClouds * kMaxDim,
                                                                               nClouds);
-  k_bounds_forest<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(recs, n, dim, dOff, nClouds, keys,
+  k_bounds_forest<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(packed, n, dim, dOff, nClouds, keys,
                                                                    keys + nClouds * kMaxDim, f->status + 0);
   NABO_CUDA_TRY(cudaGetLastError());
   if (hostDriven) {
@@ -1288,15 +1607,20 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   // when a tree needs more (the split rule gives trees as tall as the cloud
   // is large on geometrically spaced coordinates)
   int lvCap = hostDriven ? 4096 : std::max(maxLevels, 1);
-  T* val;
-  NABO_CUDA_TRY(sc.get(&segOf, n));
-  NABO_CUDA_TRY(sc.get(&val, n));
+  T* val = nullptr;
+  pairA = pairB = nullptr;
+  if (median) {
+    segOf = mb.seg[0];
+  } else {
+    NABO_CUDA_TRY(sc.get(&segOf, n));
+    NABO_CUDA_TRY(sc.get(&val, n));
+    NABO_CUDA_TRY(sc.get(&pairA, pairCap));
+    NABO_CUDA_TRY(sc.get(&pairB, pairCap));
+  }
   NABO_CUDA_TRY(sc.get(&passTotal, 1));
   NABO_CUDA_TRY(sc.get(&blockSums, nb));
   NABO_CUDA_TRY(sc.get(&segFirst, segCap));
   NABO_CUDA_TRY(sc.get(&segLast, segCap));
-  NABO_CUDA_TRY(sc.get(&pairA, pairCap));
-  NABO_CUDA_TRY(sc.get(&pairB, pairCap));
   NABO_CUDA_TRY(sc.get(&counters, 4));
   NABO_CUDA_TRY(sc.get(&lv, 2 * (int64_t)lvCap));
   NABO_CUDA_TRY(sc.get(&rootRef, nClouds));
@@ -1326,7 +1650,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   k_forest_roots<T><<<ceil_div(nClouds, 128), 128, 0, stream>>>(
       dOff, nClouds, keys, keys + nClouds * kMaxDim, dim, cur, small, st, counters, rootRef, rootSeg,
       static_cast<T*>(f->rootLo), static_cast<T*>(f->rootHi));
-  k_init_segof<<<nb, kBlock, 0, stream>>>(segOf, n, dOff, nClouds, rootSeg);
+  k_init_segof<<<ceil_div(nPad, kBlock), kBlock, 0, stream>>>(segOf, n, nPad, dOff, nClouds, rootSeg);
   NABO_CUDA_TRY(cudaGetLastError());
 
   const int sg = ceil_div(segCap, 128);
@@ -1339,6 +1663,15 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   const int grid = std::max(1, std::min(nb, 8 * std::max(sms, 1)));
   const int tiles = ceil_div(nb, grid);
   const int scanBlocks = ceil_div(nb, tiles);
+  // median split: as many blocks as are resident at once, each scanning a
+  // contiguous run of mTiles tiles of kTile positions
+  const int mTilesTotal = (int)(nPad / kTile);
+  int mOcc = 0;
+  if (median)
+    NABO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mOcc, k_median_scatter<T, D>, kBlock, 0));
+  const int mGrid = std::max(1, std::min(mTilesTotal, std::max(mOcc, 1) * std::max(sms, 1)));
+  const int mTiles = ceil_div(mTilesTotal, mGrid);
+  const int mBlocks = ceil_div(mTilesTotal, mTiles);
   for (int level = 0; hostDriven || level < maxLevels; ++level) {
     if (hostDriven) {
       int nseg = 0;
@@ -1356,6 +1689,24 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
         lv = lv2;
         lvCap = grown;
       }
+    }
+    if (median) {
+      if (level == 0) {
+        NABO_CUDA_TRY(launch_pdl(k_prepare<T>, sg, 128, 0, stream, cur, st, dim));
+        NABO_CUDA_TRY(launch_pdl(k_median_val0<T, D>, grid, kBlock, 0, stream, mb, n, cur, st));
+      }
+      NABO_CUDA_TRY(launch_pdl(k_median_cut<T, D>, sg, 128, 0, stream, cur, st, mb));
+      NABO_CUDA_TRY(launch_pdl(k_median_sums<T, D>, mBlocks, kBlock, 0, stream, mb, nPad, cur, mTiles, blockSums,
+                               segFirst, segLast, st));
+      NABO_CUDA_TRY(launch_pdl(k_scan_block_sums, 1, kBlock, 0, stream, blockSums, mBlocks, passTotal, st));
+      NABO_CUDA_TRY(launch_pdl(k_median_split<T>, sg, 128, 0, stream, cur, nxt, st, top, small, counters, dim,
+                               (int)segCap, (int)smallCap, (int)topCap, (const int2*)blockSums,
+                               (const int2*)segFirst, (const int2*)segLast, mTiles * kTile));
+      NABO_CUDA_TRY(launch_pdl(k_median_scatter<T, D>, mBlocks, kBlock, 0, stream, mb, recs, nPad, cur, nxt, mTiles,
+                               (const int2*)blockSums, st));
+      NABO_CUDA_TRY(launch_pdl(k_advance, 1, 1, 0, stream, st, counters, lv, lv + lvCap, lvCap));
+      std::swap(cur, nxt);
+      continue;
     }
     const int remap = level > 0 ? 1 : 0;
     NABO_CUDA_TRY(launch_pdl(k_prepare<T>, sg, 128, 0, stream, cur, st, dim));
@@ -1376,6 +1727,8 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
     NABO_CUDA_TRY(launch_pdl(k_advance, 1, 1, 0, stream, st, counters, lv, lv + lvCap, lvCap));
     std::swap(cur, nxt);
   }
+
+  if (median) k_median_flush<T, D><<<grid, kBlock, 0, stream>>>(mb, recs, n, st);
 
   // small segments (their count is read on the device: grid for the most)
   Node<T>* scratchNodes;
