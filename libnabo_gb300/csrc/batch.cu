@@ -68,6 +68,7 @@ struct nabo_cuda_batch {
   // host-buffer runs: the plan's offsets on the host, device copies of the
   // inputs and results, two streams and the graph of the last page-locked call
   std::vector<int64_t> hQOff, hOutOff;
+  BatchClassPlan plan;  // search launches by compiled top-k size
   int groups = 8;
   void* devClouds = nullptr;
   void* devQueries = nullptr;
@@ -126,6 +127,45 @@ void free_query_plan(nabo_cuda_batch* b) {
   b->devIdx = nullptr;
   b->hQOff.clear();
   b->hOutOff.clear();
+  for (void* p : {(void*)b->plan.dRunCloud, (void*)b->plan.dRunPrefix})
+    if (p) cudaFree(p);
+  b->plan = BatchClassPlan();
+}
+
+// Groups the clouds by the top-k size compiled for their k (k <= 32; a
+// batch with a larger k searches all queries by lane groups instead).
+cudaError_t make_class_plan(nabo_cuda_batch* b, const std::vector<int32_t>& ks,
+                            const std::vector<int64_t>& qoff) {
+  BatchClassPlan& p = b->plan;
+  p = BatchClassPlan();
+  if (b->kMax > kMaxK) return cudaSuccess;
+  std::vector<int> sizes;
+  for (int32_t k : ks) sizes.push_back(round_k(k));
+  std::sort(sizes.begin(), sizes.end());
+  sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+  p.runPrefix.push_back(0);
+  for (int K : sizes) {
+    const int first = (int)p.runCloud.size();
+    for (int c = 0; c < b->nClouds; ++c) {
+      const int64_t cnt = qoff[(size_t)c + 1] - qoff[(size_t)c];
+      if (round_k(ks[(size_t)c]) != K || cnt == 0) continue;
+      p.runCloud.push_back(c);
+      p.runPrefix.push_back(p.runPrefix.back() + cnt);
+    }
+    if ((int)p.runCloud.size() == first) continue;
+    p.K.push_back(K);
+    p.runBegin.push_back(first);
+  }
+  p.groups = (int)p.K.size();
+  p.runBegin.push_back((int)p.runCloud.size());
+  if (p.groups == 0) return cudaSuccess;
+  cudaError_t e = cudaMalloc((void**)&p.dRunCloud, p.runCloud.size() * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&p.dRunPrefix, p.runPrefix.size() * sizeof(int64_t));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p.dRunCloud, p.runCloud.data(), p.runCloud.size() * sizeof(int32_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p.dRunPrefix, p.runPrefix.data(), p.runPrefix.size() * sizeof(int64_t), cudaMemcpyHostToDevice);
+  return e;
 }
 
 // f(T(), std::integral_constant<int, D>()) for the batch's scalar type and
@@ -219,6 +259,8 @@ BatchArgs batch_args(const nabo_cuda_batch* b, const void* query, double eps, un
   a.maxRadii = nullptr;
   a.fallbacks = nullptr;
   a.lanesPerQuery = b->lanesPerQuery;
+  a.classes = &b->plan;
+  a.hQOffset = b->hQOff.empty() ? nullptr : b->hQOff.data();
   return a;
 }
 
@@ -533,6 +575,11 @@ int nabo_cuda_batch_set_queries(nabo_cuda_batch* b, const int64_t* queryCounts, 
   if (e != cudaSuccess) {
     free_query_plan(b);
     return cuda_error(e, "batch query plan");
+  }
+  e = make_class_plan(b, ks, qoff);
+  if (e != cudaSuccess) {
+    free_query_plan(b);
+    return cuda_error(e, "batch query groups");
   }
   b->hQOff = std::move(qoff);
   b->hOutOff = std::move(ooff);

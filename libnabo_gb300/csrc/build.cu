@@ -1162,27 +1162,59 @@ __device__ __forceinline__ void warp_partition_pass(Rec<T, D>* pts, int lo, int 
 // split's min/max, counts and partition passes run across the lanes; node
 // records and bucket order come out as the reference's.
 // The lower median (rank count / 2) of the count values node[i].p.c[cd],
-// computed by the warp: each lane ranks its elements against all of them.
+// computed by the warp. Up to 64 values each lane ranks its own against all
+// of them (count^2 / 32 compares per lane). Above, a bitwise radix select
+// over the values' order-preserving keys, most significant bit first: each
+// round counts the remaining candidates whose next bit is 0 (one compare
+// per held value, summed across the warp) and keeps the half that holds
+// the wanted rank, 32 rounds for float and 64 for double whatever the count.
 template <typename T, int D>
 __device__ T warp_median(const Rec<T, D>* node, int count, int cd, int lane) {
-  const int want = count / 2;
-  bool found = false;
-  T med = T(0);
-  for (int i = lane; i < count; i += 32) {
-    const T v = node[i].p.c[cd];
-    int lt = 0, le = 0;
-    for (int j = 0; j < count; ++j) {
-      const T w = node[j].p.c[cd];
-      lt += w < v ? 1 : 0;
-      le += w <= v ? 1 : 0;
+  using Key = typename KeyOf<T>::type;
+  const int want0 = count / 2;
+  if (count <= 64) {
+    bool found = false;
+    T med = T(0);
+    for (int i = lane; i < count; i += 32) {
+      const T v = node[i].p.c[cd];
+      int lt = 0, le = 0;
+      for (int j = 0; j < count; ++j) {
+        const T w = node[j].p.c[cd];
+        lt += w < v ? 1 : 0;
+        le += w <= v ? 1 : 0;
+      }
+      if (!found && lt <= want0 && want0 < le) {
+        found = true;
+        med = v;
+      }
     }
-    if (!found && lt <= want && want < le) {
-      found = true;
-      med = v;
+    const unsigned m = __ballot_sync(0xffffffffu, found);
+    return __shfl_sync(0xffffffffu, med, __ffs(m) - 1);
+  }
+  constexpr int kPer = kSmallMax / 32;
+  constexpr int kBits = 8 * (int)sizeof(Key);
+  Key k[kPer];
+#pragma unroll
+  for (int j = 0; j < kPer; ++j) {
+    const int i = lane + 32 * j;
+    // padding sorts above every finite value's key, so it never holds the rank
+    k[j] = i < count ? ordered_key(node[i].p.c[cd]) : ~Key(0);
+  }
+  const int held = (count + 31) / 32;
+  Key prefix = 0;
+  int want = want0;
+  for (int b = kBits - 1; b >= 0; --b) {
+    const Key sel = prefix >> b;
+    int c = 0;
+#pragma unroll
+    for (int j = 0; j < kPer; ++j) c += (j < held && (k[j] >> b) == sel) ? 1 : 0;
+    c = __reduce_add_sync(0xffffffffu, c);
+    if (want >= c) {
+      want -= c;
+      prefix |= Key(1) << b;
     }
   }
-  const unsigned m = __ballot_sync(0xffffffffu, found);
-  return __shfl_sync(0xffffffffu, med, __ffs(m) - 1);
+  return ordered_val(prefix, T(0));
 }
 
 template <typename T, int D>

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "nabo_gb300.h"
@@ -125,6 +126,36 @@ struct ForestOut {
 };
 
 // A batched search over a forest (batch.cu).
+// Register top-k sizes compiled; a request for k uses the smallest K >= k.
+#define NABO_K_LIST(X) X(1) X(2) X(5) X(8) X(10) X(16) X(32)
+constexpr int kMaxK = 32;
+
+inline int round_k(int k) {
+#define NABO_ROUND(KK) \
+  if (k <= KK) return KK;
+  NABO_K_LIST(NABO_ROUND)
+#undef NABO_ROUND
+  return -1;
+}
+
+// Queries of a batch grouped by the top-k size compiled for their cloud's k
+// (1, 2, 5, 8, 10, 16 or 32): one search launch per group, so a k = 1 cloud
+// does not carry a 16-slot heap because another cloud wants 16. A group
+// lists its clouds that have queries ("runs", by cloud id); runPrefix holds
+// the running query count over all runs, group after group, so group g's
+// launch covers positions [runPrefix[runBegin[g]], runPrefix[runBegin[g+1]])
+// of that count, and run r's queries sit at leaf-order positions
+// [qOffset[c], qOffset[c+1]) of cloud c = runCloud[r].
+struct BatchClassPlan {
+  int groups = 0;
+  std::vector<int> K;                 // [groups]
+  std::vector<int> runBegin;          // [groups + 1]
+  std::vector<int32_t> runCloud;      // host copy
+  std::vector<int64_t> runPrefix;     // host copy, [runs + 1]
+  int32_t* dRunCloud = nullptr;       // device copies
+  int64_t* dRunPrefix = nullptr;
+};
+
 struct BatchArgs {
   const void* nodes;
   const void* recs;
@@ -167,6 +198,8 @@ struct BatchArgs {
   const void* maxRadii;
   int32_t* fallbacks;
   int lanesPerQuery;            // 1: one thread per query; 8: a lane group (k <= 32)
+  const BatchClassPlan* classes;  // null or no groups: one launch sized for the largest k
+  const int64_t* hQOffset;        // host copy of qOffset (to map a position range to clouds)
 };
 template <typename T, int D>
 int knn_batch(const BatchArgs& b, cudaStream_t stream);

@@ -236,6 +236,12 @@ struct KnnLaunch {
   const int32_t* bK;
   const int64_t* bOutOffset;
   int bClouds;
+  // one group of a batch's queries (see BatchClassPlan): thread t searches
+  // position runPrefix[runBegin] + t of the group's running query count;
+  // null runPrefix: thread t searches leaf-order position t
+  const int64_t* runPrefix;
+  const int32_t* runCloud;
+  int runBegin, runEnd;
   // Trees taller than the compiled stacks (the reference's recursion has no
   // depth limit, nabo/kdtree_cpu.cpp:367-447):
   //  - slab/slabBytes: traversal stacks in global memory for the deep
@@ -507,15 +513,34 @@ __device__ __forceinline__ void knn_query(const KnnLaunch& a, int64_t t, S& stk,
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
   const T* __restrict__ query = static_cast<const T*>(a.query);
   uint32_t touched = 0;  // a query touches at most the cloud's n < 2^31 points
-  const int64_t qi = a.order ? (int64_t)a.order[t] : t;
+  int64_t qi;
   int k = a.k;
   uint32_t root = 0;
-  int64_t outBase = qi * (int64_t)a.k;
-  if (a.bQueryOffset) {
-    const int c = cloud_of(a.bQueryOffset, a.bClouds, qi);
+  int64_t outBase;
+  if (a.runPrefix) {
+    const int64_t g = a.runPrefix[a.runBegin] + t;
+    int lo = a.runBegin, hi = a.runEnd - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (a.runPrefix[mid] <= g)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const int c = a.runCloud[lo];
+    qi = (int64_t)a.order[a.bQueryOffset[c] + (g - a.runPrefix[lo])];
     k = a.bK[c];
     root = (uint32_t)a.bNodeOffset[c];
     outBase = a.bOutOffset[c] + (qi - a.bQueryOffset[c]) * (int64_t)k;
+  } else {
+    qi = a.order ? (int64_t)a.order[t] : t;
+    outBase = qi * (int64_t)a.k;
+    if (a.bQueryOffset) {
+      const int c = cloud_of(a.bQueryOffset, a.bClouds, qi);
+      k = a.bK[c];
+      root = (uint32_t)a.bNodeOffset[c];
+      outBase = a.bOutOffset[c] + (qi - a.bQueryOffset[c]) * (int64_t)k;
+    }
   }
   T q[D];
 #pragma unroll

@@ -12,20 +12,9 @@
 
 namespace nabo_gb300 {
 
-// Register top-k sizes compiled; a request for k uses the smallest K >= k.
-#define NABO_K_LIST(X) X(1) X(2) X(5) X(8) X(10) X(16) X(32)
-constexpr int kMaxK = 32;
 // Traversal stack depths compiled; the tree's height selects one.
 constexpr int kStackSmall = 64;
 constexpr int kStackLarge = 256;
-
-inline int round_k(int k) {
-#define NABO_ROUND(KK) \
-  if (k <= KK) return KK;
-  NABO_K_LIST(NABO_ROUND)
-#undef NABO_ROUND
-  return -1;
-}
 
 // k above kMaxK: a group of lanes per query holding K slots (K compiled
 // below): 8 lanes for K = 64 and 128 (four queries share a warp's traversal
@@ -151,7 +140,7 @@ int launch_wide_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
 
 template <typename T, int D>
 KnnLaunch make_launch(const DeviceCloud& c, const KnnArgs& a, const int32_t* order) {
-  KnnLaunch L;
+  KnnLaunch L{};  // every field not set below is zero / null
   L.nodes = c.nodes;
   L.recs = c.recs;
   L.query = a.query;
@@ -470,9 +459,37 @@ int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t st
   }
 #define NABO_LAUNCH(KK)                                                                     \
   case KK:                                                                                  \
-    launch_kdtree<T, D, KK, kStackLarge>(grid, b.blockSize, stream, L);                     \
+    launch_kdtree<T, D, KK, kStackLarge>(g, b.blockSize, stream, G);                        \
     break;
-  if (K > 0) switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+  const BatchClassPlan* cp = b.classes;
+  if (K > 0 && cp && cp->groups > 0 && b.hQOffset) {
+    // one launch per group of clouds sharing a compiled top-k size, over the
+    // group's clouds whose queries lie in [begin, end)
+    const int64_t* qo = b.hQOffset;
+    for (int gi = 0; gi < cp->groups; ++gi) {
+      const int32_t* rc0 = cp->runCloud.data();
+      const int* r0p = std::lower_bound(rc0 + cp->runBegin[gi], rc0 + cp->runBegin[gi + 1], 0,
+                                        [&](int32_t c, int) { return qo[c] < begin; });
+      const int* r1p = std::lower_bound(r0p, rc0 + cp->runBegin[gi + 1], 0,
+                                        [&](int32_t c, int) { return qo[c + 1] <= end; });
+      const int r0 = (int)(r0p - rc0), r1 = (int)(r1p - rc0);
+      if (r1 <= r0) continue;
+      KnnLaunch G = L;
+      G.order = b.order;
+      G.runPrefix = cp->dRunPrefix;
+      G.runCloud = cp->dRunCloud;
+      G.runBegin = r0;
+      G.runEnd = r1;
+      G.nq = cp->runPrefix[(size_t)r1] - cp->runPrefix[(size_t)r0];
+      G.k = cp->K[(size_t)gi];
+      const int g = ceil_div(G.nq, b.blockSize);
+      switch (round_k(cp->K[(size_t)gi])) { NABO_K_LIST(NABO_LAUNCH) }
+    }
+  } else if (K > 0) {
+    KnnLaunch G = L;
+    const int g = grid;
+    switch (K) { NABO_K_LIST(NABO_LAUNCH) }
+  }
 #undef NABO_LAUNCH
   {
     KnnLaunch R = L;
