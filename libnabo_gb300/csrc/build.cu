@@ -974,6 +974,130 @@ __global__ void k_median_scatter(MedianBufs<T, D> B, Rec<T, D>* __restrict__ fin
   }
 }
 
+// Staging a tile (record, destination, next id and coordinate per slot)
+// within 47 KB of static shared memory: float records of up to 4
+// dimensions.
+template <typename T, int D>
+constexpr bool median_staging_fits() {
+  return (size_t)kTile * (sizeof(Rec<T, D>) + 2 * sizeof(int) + sizeof(T)) <= 47 * 1024;
+}
+
+// k_median_scatter with the tile's moves staged in shared memory: each
+// record, with its destination and next id and coordinate, goes to a slot
+// in destination order (the tile's flagged records first, each side in
+// position order, so every run of one segment and side is contiguous in
+// both), then the block writes the slots out, consecutive threads to
+// consecutive destinations.
+template <typename T, int D>
+__global__ void k_median_scatter_staged(MedianBufs<T, D> B, Rec<T, D>* __restrict__ finalRecs, int64_t nPad,
+                                        SegLevel<T> L, SegLevel<T> next, int tiles,
+                                        const int2* __restrict__ blockPrefix, const LevelState* st) {
+  // (instantiated only where the staging fits; see median_scatter)
+  constexpr int kStage = median_staging_fits<T, D>() ? kTile : 1;
+  __shared__ Rec<T, D> sRec[kStage];
+  __shared__ int sDest[kStage];
+  __shared__ int sChild[kStage];
+  __shared__ T sVal[kStage];
+  pdl_begin();
+  if (st->nseg == 0) return;
+  const int par = st->level & 1;
+  const int* seg = B.segs(par);
+  const T* val = B.vals(par);
+  const Rec<T, D>* src = B.recs(par);
+  Rec<T, D>* dst = B.recs(par ^ 1);
+  int* segN = B.segs(par ^ 1);
+  T* valN = B.vals(par ^ 1);
+  const int64_t first = (int64_t)blockIdx.x * tiles * kTile + threadIdx.x * kItems;
+  MedianItems<T> nxt;
+  median_load(seg, val, first, nPad, nxt);
+  int2 carry = blockPrefix[blockIdx.x];
+  for (int t = 0; t < tiles; ++t) {
+    const MedianItems<T> it = nxt;
+    const int64_t p0 = first + (int64_t)t * kTile;
+    if (t + 1 < tiles) median_load(seg, val, p0 + kTile, nPad, nxt);
+    int2 f[kItems];
+    int2 sum = make_int2(0, 0);
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      f[i] = median_flag(L, it.s[i], it.v[i]);
+      sum = add2(sum, f[i]);
+    }
+    int2 total;
+    int2 ex = add2(block_excl_scan(sum, &total), carry);
+    carry = add2(carry, total);
+    // destination of each held record and its side
+    int dest[kItems];
+    bool left[kItems];
+    int2 side = make_int2(0, 0);  // (left, right) records this thread moves
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      const int s = it.s[i];
+      dest[i] = -1;
+      left[i] = false;
+      if (s >= 0) {
+        const int64_t p = p0 + i;
+        const int start = L.start[s];
+        const int mode = L.mode[s];
+        const int lc = L.leftCount[s];
+        const int loc = (int)(p - start);
+        int before;
+        if (mode == 2) {
+          before = loc < lc ? loc : lc;
+          left[i] = loc < lc;
+        } else {
+          before = (mode == 0 ? ex.x : ex.y) - L.lt[s];
+          left[i] = (mode == 0 ? f[i].x : f[i].y) != 0;
+        }
+        dest[i] = start + (left[i] ? before : lc + (loc - before));
+        side = add2(side, make_int2(left[i] ? 1 : 0, left[i] ? 0 : 1));
+      } else if (p0 < nPad) {
+        segN[p0 + i] = -1;
+      }
+      ex = add2(ex, f[i]);
+    }
+    int2 sideTotal;
+    int2 slot = block_excl_scan(side, &sideTotal);
+    slot.y += sideTotal.x;  // rights after all lefts
+#pragma unroll
+    for (int i = 0; i < kItems; ++i) {
+      if (dest[i] < 0) continue;
+      const int s = it.s[i];
+      const int j = left[i] ? slot.x++ : slot.y++;
+      const int child = left[i] ? L.newLeft[s] : L.newRight[s];
+      Rec<T, D> r;
+      load_rec(src, p0 + i, r);
+      sRec[j] = r;
+      sChild[j] = child;
+      sDest[j] = dest[i];
+      if (child >= 0) sVal[j] = rec_coord(r, next.cutDim[child]);
+    }
+    __syncthreads();
+    const int moved = sideTotal.x + sideTotal.y;
+    for (int j = threadIdx.x; j < moved; j += blockDim.x) {
+      const int d = sDest[j];
+      const int child = sChild[j];
+      if (child >= 0) {
+        dst[d] = sRec[j];
+        segN[d] = child;
+        valN[d] = sVal[j];
+      } else {
+        finalRecs[d] = sRec[j];
+        segN[d] = -1;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The scatter kernel for this record size.
+template <typename T, int D>
+constexpr auto median_scatter() {
+  if constexpr (median_staging_fits<T, D>())
+    return k_median_scatter_staged<T, D>;
+  else
+    return k_median_scatter<T, D>;
+}
+
 // A fixed-level build that ran out of levels leaves records of unfinished
 // segments in the working arrays; they go to the final array, whose cloud
 // ranges then hold every point (the one-leaf-per-cloud fallback reads them).
@@ -1700,7 +1824,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   const int mTilesTotal = (int)(nPad / kTile);
   int mOcc = 0;
   if (median)
-    NABO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mOcc, k_median_scatter<T, D>, kBlock, 0));
+    NABO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&mOcc, median_scatter<T, D>(), kBlock, 0));
   const int mGrid = std::max(1, std::min(mTilesTotal, std::max(mOcc, 1) * std::max(sms, 1)));
   const int mTiles = ceil_div(mTilesTotal, mGrid);
   const int mBlocks = ceil_div(mTilesTotal, mTiles);
@@ -1734,7 +1858,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
       NABO_CUDA_TRY(launch_pdl(k_median_split<T>, sg, 128, 0, stream, cur, nxt, st, top, small, counters, dim,
                                (int)segCap, (int)smallCap, (int)topCap, (const int2*)blockSums,
                                (const int2*)segFirst, (const int2*)segLast, mTiles * kTile));
-      NABO_CUDA_TRY(launch_pdl(k_median_scatter<T, D>, mBlocks, kBlock, 0, stream, mb, recs, nPad, cur, nxt, mTiles,
+      NABO_CUDA_TRY(launch_pdl(median_scatter<T, D>(), mBlocks, kBlock, 0, stream, mb, recs, nPad, cur, nxt, mTiles,
                                (const int2*)blockSums, st));
       NABO_CUDA_TRY(launch_pdl(k_advance, 1, 1, 0, stream, st, counters, lv, lv + lvCap, lvCap));
       std::swap(cur, nxt);

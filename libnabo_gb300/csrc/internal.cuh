@@ -340,9 +340,14 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
                   int32_t* dOrder, cudaStream_t stream, const QueryChunks* chunks = nullptr);
 
 // Counting-sort placement: dHist holds per-cell counts (turned into offsets
-// in place), dCell/dRank each query's cell and rank inside it.
+// in place), dCell/dRank each query's cell and rank inside it. With binsDev
+// only the first min(bins, *binsDev) cells (a count the device holds) are
+// scanned; every cell at or past it must be empty.
 int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist, int64_t bins, int64_t nq,
-                   int32_t* dOrder, cudaStream_t stream);
+                   int32_t* dOrder, cudaStream_t stream, const int64_t* binsDev = nullptr);
+
+// Zeroes the first min(n, *nDev) entries (all n when nDev is null).
+int zero_u32(uint32_t* data, int64_t n, const int64_t* nDev, cudaStream_t stream);
 
 // Stable sort of element indices 0..n-1 (or of dVals, when given) by the
 // low `bits` bits of dKeys, written to dOrder; dKeys is clobbered.
@@ -351,6 +356,7 @@ int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaSt
 
 // Device-wide exclusive scan of uint32 values (in place), returns total via
 // a device pointer. Scratch is stream-ordered.
-int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t stream);
+int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t stream,
+                       const int64_t* nDev = nullptr);
 
 }  // namespace nabo_gb300

@@ -53,7 +53,15 @@ __device__ __forceinline__ uint32_t block_excl_scan_u32(uint32_t v, uint32_t* to
   return wpre + x - v;
 }
 
-__global__ void k_block_sums(const uint32_t* __restrict__ data, int64_t n, uint32_t* sums) {
+// The scans cover the first m = min(n, *nDev) entries when nDev is given
+// (a count only the device knows); blocks past m return at once.
+__device__ __forceinline__ int64_t live_count(int64_t n, const int64_t* nDev) {
+  return nDev ? min(n, *nDev) : n;
+}
+
+__global__ void k_block_sums(const uint32_t* __restrict__ data, int64_t n, uint32_t* sums, const int64_t* nDev) {
+  n = live_count(n, nDev);
+  if (blockIdx.x * (int64_t)kB >= n) return;
   const int64_t i = blockIdx.x * (int64_t)kB + threadIdx.x;
   const uint32_t v = i < n ? data[i] : 0u;
   uint32_t t;
@@ -63,7 +71,8 @@ __global__ void k_block_sums(const uint32_t* __restrict__ data, int64_t n, uint3
 
 // Single block: each thread scans a contiguous run of the block sums
 // serially, one block-wide scan of the runs' totals joins them.
-__global__ void k_scan_sums(uint32_t* sums, int nb, uint32_t* total) {
+__global__ void k_scan_sums(uint32_t* sums, int nb, uint32_t* total, const int64_t* nDev) {
+  if (nDev) nb = (int)min((int64_t)nb, (live_count((int64_t)nb * kB, nDev) + kB - 1) / kB);
   const int per = (nb + kB - 1) / kB;
   const int b0 = threadIdx.x * per;
   const int b1 = min(b0 + per, nb);
@@ -79,7 +88,9 @@ __global__ void k_scan_sums(uint32_t* sums, int nb, uint32_t* total) {
   if (threadIdx.x == 0 && total) *total = t;
 }
 
-__global__ void k_apply(uint32_t* data, int64_t n, const uint32_t* __restrict__ sums) {
+__global__ void k_apply(uint32_t* data, int64_t n, const uint32_t* __restrict__ sums, const int64_t* nDev) {
+  n = live_count(n, nDev);
+  if (blockIdx.x * (int64_t)kB >= n) return;
   const int64_t i = blockIdx.x * (int64_t)kB + threadIdx.x;
   const uint32_t v = i < n ? data[i] : 0u;
   uint32_t t;
@@ -354,7 +365,9 @@ __global__ void k_place(const uint32_t* __restrict__ cell, const uint32_t* __res
 // more than kRunSort queries keep arrival order; the order only affects
 // speed, never results.
 constexpr int kRunSort = 64;
-__global__ void k_sort_runs(const uint32_t* __restrict__ start, int64_t bins, int64_t nq, int32_t* order) {
+__global__ void k_sort_runs(const uint32_t* __restrict__ start, int64_t bins, int64_t nq, int32_t* order,
+                            const int64_t* binsDev) {
+  bins = live_count(bins, binsDev);
   const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (b >= bins) return;
   const int64_t s = start[b];
@@ -373,25 +386,40 @@ __global__ void k_sort_runs(const uint32_t* __restrict__ start, int64_t bins, in
 
 }  // namespace
 
-int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t stream) {
+__global__ void k_zero_u32(uint32_t* data, int64_t n, const int64_t* nDev) {
+  n = live_count(n, nDev);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    data[i] = 0u;
+}
+
+int scan_exclusive_u32(uint32_t* data, int64_t n, uint32_t* dTotal, cudaStream_t stream, const int64_t* nDev) {
   const int nb = ceil_div(n, kB);
   uint32_t* sums = nullptr;
   NABO_CUDA_TRY(scratch_alloc((void**)&sums, (size_t)std::max(nb, 1) * sizeof(uint32_t), stream));
-  k_block_sums<<<nb, kB, 0, stream>>>(data, n, sums);
-  k_scan_sums<<<1, kB, 0, stream>>>(sums, nb, dTotal);
-  k_apply<<<nb, kB, 0, stream>>>(data, n, sums);
+  k_block_sums<<<nb, kB, 0, stream>>>(data, n, sums, nDev);
+  k_scan_sums<<<1, kB, 0, stream>>>(sums, nb, dTotal, nDev);
+  k_apply<<<nb, kB, 0, stream>>>(data, n, sums, nDev);
   const cudaError_t e = cudaGetLastError();
   scratch_free(sums, stream);
   if (e != cudaSuccess) return cuda_error(e, "scan_exclusive_u32");
   return kOk;
 }
 
+int zero_u32(uint32_t* data, int64_t n, const int64_t* nDev, cudaStream_t stream) {
+  int device = 0, sms = 0;
+  NABO_CUDA_TRY(cudaGetDevice(&device));
+  NABO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  k_zero_u32<<<std::max(1, std::min(ceil_div(n, kB), 8 * std::max(sms, 1))), kB, 0, stream>>>(data, n, nDev);
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? kOk : cuda_error(e, "zero_u32");
+}
+
 int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist, int64_t bins, int64_t nq,
-                   int32_t* dOrder, cudaStream_t stream) {
-  const int rc = scan_exclusive_u32(dHist, bins, nullptr, stream);
+                   int32_t* dOrder, cudaStream_t stream, const int64_t* binsDev) {
+  const int rc = scan_exclusive_u32(dHist, bins, nullptr, stream, binsDev);
   if (rc != kOk) return rc;
   k_place<<<ceil_div(nq, kB), kB, 0, stream>>>(dCell, dRank, dHist, nq, dOrder);
-  k_sort_runs<<<ceil_div(bins, kB), kB, 0, stream>>>(dHist, bins, nq, dOrder);
+  k_sort_runs<<<ceil_div(bins, kB), kB, 0, stream>>>(dHist, bins, nq, dOrder, binsDev);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_error(e, "order_by_cells");
   return kOk;

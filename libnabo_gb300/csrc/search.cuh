@@ -844,12 +844,55 @@ __device__ __forceinline__ T bf_threshold(T head, T maxRadius2) {
 __device__ __forceinline__ float fmin_t(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ double fmin_t(double a, double b) { return fmin(a, b); }
 
+// Float brute force filters each group of J points before the reference's
+// distance: a = |p|^2 - 2 q.p, D fused multiply-adds per pair from |p|^2
+// (computed once per point as the tile is staged, kept in the record's index
+// slot, the index itself beside the tile) and -2q. With e the reference's
+// distance (separately rounded squares, nabo/kdtree_cpu.cpp:383-391), a
+// point it could accept has e <= thr, and then
+//   a <= thr - |q|^2 + g (thr + 2 P + 2 |q|^2)
+// with g = (D + 1) u / (1 - (D + 1) u), u = 2^-24, P the tile's largest
+// |p|^2 (the dot product's rounding, bounded with 2|q||p| <= |q|^2 + |p|^2,
+// plus e's own and |q|^2's). The test uses 2^-17 for g, over 4 times that
+// bound for D <= 16 and covering the rounding of the bound itself, so it
+// never drops a point that the exact pass would take; a group that passes
+// is computed again exactly, as before.
+template <int D>
+struct BfFilter {
+  float m2q[D];  // -2 q
+  float qn;      // |q|^2
+  float thrA;    // threshold on a
+  __device__ __forceinline__ void init(const float (&q)[D]) {
+    qn = 0.0f;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      m2q[d] = -2.0f * q[d];
+      qn = fmaf(q[d], q[d], qn);
+    }
+  }
+  // A NaN threshold (an idle slot, or a NaN radius) passes nothing. Where
+  // |p|^2, |q|^2 or the bound overflow, thrA is inf or NaN and the test
+  // below (!(a > thrA)) passes every group to the exact pass.
+  __device__ __forceinline__ void set(float thr, float pmax) {
+    thrA = thr != thr ? -__int_as_float(0x7f800000) : (thr - qn) + 0x1p-17f * (thr + 2.0f * pmax + 2.0f * qn);
+  }
+  __device__ __forceinline__ float eval(const Rec<float, D>& r) const {
+    float a = __int_as_float(r.p.idx);
+#pragma unroll
+    for (int d = 0; d < D; ++d) a = fmaf(m2q[d], r.p.c[d], a);
+    return a;
+  }
+};
+
 template <typename T, int D, int K, int QT, int J>
 __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a, int64_t chunk, int64_t partStride) {
+  constexpr bool kFilter = sizeof(T) == 4;
   const T minDist = a.allowSelf ? T(-1) : Ar<T>::eps();
   // a multiple of J, so that a group never reads past the tile
   constexpr int kTile = (int)((24 * 1024) / sizeof(Rec<T, D>)) / J * J;
   __shared__ Rec<T, D> tile[kTile];
+  __shared__ int32_t tileIdx[kFilter ? kTile : 1];  // filter: the points' indices
+  __shared__ float warpMax[4];                       // filter: largest |p|^2 per warp
   const Rec<T, D>* __restrict__ recs = static_cast<const Rec<T, D>*>(a.recs);
   const T* __restrict__ query = static_cast<const T*>(a.query);
   const int64_t base0 = (int64_t)blockIdx.x * blockDim.x * QT + threadIdx.x;
@@ -859,6 +902,7 @@ __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a, int64_t chu
   int64_t qi[QT];
   bool active[QT];
   TopK<T, K> heap[QT];
+  BfFilter<D> flt[kFilter ? QT : 1];
 #pragma unroll
   for (int u = 0; u < QT; ++u) {
     const int64_t t = base0 + (int64_t)u * blockDim.x;
@@ -875,57 +919,115 @@ __global__ void __launch_bounds__(128) k_knn_bruteforce(KnnLaunch a, int64_t chu
     if (!active[u]) maxRadius2[u] = __builtin_nan("");
     heap[u].init(a.k);
     thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
+    if constexpr (kFilter) flt[u].init(reinterpret_cast<const float(&)[D]>(q[u]));
   }
   const int64_t first = (int64_t)blockIdx.y * chunk;
   const int64_t last = first + chunk < a.n ? first + chunk : a.n;
   for (int64_t base = first; base < last; base += kTile) {
     const int m = (int)((last - base) < kTile ? (last - base) : kTile);
     __syncthreads();
-    {
+    if constexpr (kFilter) {
+      float pm = 0.0f;
+      for (int j = threadIdx.x; j < m; j += blockDim.x) {
+        Rec<T, D> r;
+        load_rec(recs, base + j, r);
+        float pn = 0.0f;
+#pragma unroll
+        for (int d = 0; d < D; ++d) pn = fmaf(r.p.c[d], r.p.c[d], pn);
+        tileIdx[j] = r.p.idx;
+        r.p.idx = __float_as_int(pn);
+        tile[j] = r;
+        pm = fmaxf(pm, pn);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) pm = fmaxf(pm, __shfl_xor_sync(0xffffffffu, pm, o));
+      if ((threadIdx.x & 31) == 0) warpMax[threadIdx.x >> 5] = pm;
+    } else {
       const uint4* src = reinterpret_cast<const uint4*>(recs + base);
       uint4* dst = reinterpret_cast<uint4*>(tile);
       const int words = m * RecSize<T, D>::chunks;
       for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = __ldg(src + w);
-      // the last group's missing points: NaN coordinates, whose distance
-      // passes no threshold and lowers no minimum (a group's first point
-      // is always a real one)
+    }
+    {
+      // the last group's missing points: NaN coordinates (and |p|^2), whose
+      // distance passes no threshold and lowers no minimum (a group's first
+      // point is always a real one)
       const int padEnd = (m + J - 1) / J * J;
       for (int j = m + (int)threadIdx.x; j < padEnd; j += blockDim.x) {
         Rec<T, D> r;
 #pragma unroll
         for (int d = 0; d < D; ++d) r.p.c[d] = __builtin_nan("");
-        r.p.idx = -1;
+        r.p.idx = kFilter ? __float_as_int(__builtin_nanf("")) : -1;
         tile[j] = r;
       }
     }
     __syncthreads();
-    for (int j0 = 0; j0 < m; j0 += J) {
-      // each query's smallest distance of the group (fmin ignores the NaN
-      // padding; the group's first point is a real one)
-      T dmin[QT];
+    if constexpr (kFilter) {
+      const float pmax = fmaxf(fmaxf(warpMax[0], warpMax[1]), fmaxf(warpMax[2], warpMax[3]));
 #pragma unroll
-      for (int jj = 0; jj < J; ++jj) {
-        const Rec<T, D> r = tile[j0 + jj];
-#pragma unroll
-        for (int u = 0; u < QT; ++u) {
-          const T d = dist2_seq(q[u], r);
-          dmin[u] = jj == 0 ? d : fmin_t(dmin[u], d);
-        }
-      }
-      bool any = false;
-#pragma unroll
-      for (int u = 0; u < QT; ++u) any = any || dmin[u] <= thr[u];
-      if (any) {  // rare once the heaps are full: the group again, exactly
+      for (int u = 0; u < QT; ++u) flt[u].set((float)thr[u], pmax);
+      for (int j0 = 0; j0 < m; j0 += J) {
+        float amin[QT];
 #pragma unroll
         for (int jj = 0; jj < J; ++jj) {
-          if (j0 + jj < m) {
-            const Rec<T, D> r = tile[j0 + jj];
+          const Rec<T, D> r = tile[j0 + jj];
 #pragma unroll
-            for (int u = 0; u < QT; ++u) {
-              const T d = dist2_seq(q[u], r);
-              if (d <= thr[u] && d <= maxRadius2[u] && heap[u].accepts(d, r.p.idx) && d > minDist) {
-                heap[u].insert(d, r.p.idx);
-                thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
+          for (int u = 0; u < QT; ++u) {
+            const float av = flt[u].eval(reinterpret_cast<const Rec<float, D>&>(r));
+            amin[u] = jj == 0 ? av : fminf(amin[u], av);
+          }
+        }
+        bool any = false;
+#pragma unroll
+        for (int u = 0; u < QT; ++u) any = any || !(amin[u] > flt[u].thrA);
+        if (any) {  // rare once the heaps are full: the group exactly
+#pragma unroll
+          for (int jj = 0; jj < J; ++jj) {
+            if (j0 + jj < m) {
+              const Rec<T, D> r = tile[j0 + jj];
+              const int idx = tileIdx[j0 + jj];
+#pragma unroll
+              for (int u = 0; u < QT; ++u) {
+                const T d = dist2_seq(q[u], r);
+                if (d <= thr[u] && d <= maxRadius2[u] && heap[u].accepts(d, idx) && d > minDist) {
+                  heap[u].insert(d, idx);
+                  thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
+                  flt[u].set((float)thr[u], pmax);
+                }
+              }
+            }
+          }
+        }
+      }
+    } else {
+      for (int j0 = 0; j0 < m; j0 += J) {
+        // each query's smallest distance of the group (fmin ignores the NaN
+        // padding; the group's first point is a real one)
+        T dmin[QT];
+#pragma unroll
+        for (int jj = 0; jj < J; ++jj) {
+          const Rec<T, D> r = tile[j0 + jj];
+#pragma unroll
+          for (int u = 0; u < QT; ++u) {
+            const T d = dist2_seq(q[u], r);
+            dmin[u] = jj == 0 ? d : fmin_t(dmin[u], d);
+          }
+        }
+        bool any = false;
+#pragma unroll
+        for (int u = 0; u < QT; ++u) any = any || dmin[u] <= thr[u];
+        if (any) {  // rare once the heaps are full: the group again, exactly
+#pragma unroll
+          for (int jj = 0; jj < J; ++jj) {
+            if (j0 + jj < m) {
+              const Rec<T, D> r = tile[j0 + jj];
+#pragma unroll
+              for (int u = 0; u < QT; ++u) {
+                const T d = dist2_seq(q[u], r);
+                if (d <= thr[u] && d <= maxRadius2[u] && heap[u].accepts(d, r.p.idx) && d > minDist) {
+                  heap[u].insert(d, r.p.idx);
+                  thr[u] = bf_threshold(heap[u].head(), maxRadius2[u]);
+                }
               }
             }
           }
@@ -968,12 +1070,16 @@ __global__ void k_bf_merge(const int32_t* __restrict__ pIdx, const T* __restrict
 // Shape of the brute force: QT queries per thread (more share each
 // shared-memory read, fewer keep long top-k lists in registers) and J
 // records per threshold test.
-// Measured on 100k x 100k 3-D points, k = 5 (kernel ms): QT x J = 2 x 4
-// 5.17, 2 x 8 5.72, 1 x 8 6.33, 4 x 4 6.83, 1 x 4 6.90, 4 x 8 7.88,
-// 8 x 2 8.49.
+// Float, with the |p|^2 - 2 q.p filter, 100k x 100k 3-D points (kernel ms,
+// k = 5 / k = 10): QT x J = 1 x 4 3.50 / 4.79, 1 x 8 3.51 / 5.06, 1 x 12
+// 3.76 / 5.95, 2 x 4 3.92 / 6.63, 3 x 4 4.54 / 8.17, 1 x 16 4.59 / 6.58,
+// 2 x 8 4.80 / 8.19, 4 x 4 5.89 / 10.97, 4 x 8 8.76 / 18.12.
+// Before the filter (separately rounded distances for every pair, k = 5):
+// 2 x 4 5.17, 2 x 8 5.72, 1 x 8 6.33, 4 x 4 6.83, 1 x 4 6.90, 4 x 8 7.88,
+// 8 x 2 8.49; double, which keeps that kernel, uses 1 x 4.
 template <typename T, int K>
 struct BfShape {
-  static constexpr int QT = sizeof(T) == 8 ? 1 : (K <= 16 ? 2 : 1);
+  static constexpr int QT = 1;
   static constexpr int J = 4;
 };
 

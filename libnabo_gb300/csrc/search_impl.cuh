@@ -398,12 +398,16 @@ int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t
 template <typename T, int D>
 int order_batch(const BatchArgs& b, cudaStream_t stream) {
   if (b.nq == 0) return kOk;
-  NABO_CUDA_TRY(cudaMemsetAsync(b.hist, 0, (size_t)b.nodeCap * sizeof(uint32_t), stream));
+  // the forest's node count (nodeOffset[nClouds]) is known on the device
+  // only; the histogram's cells past it stay unused
+  const int64_t* nodesDev = b.nodeOffset + b.nClouds;
+  const int zrc = zero_u32(b.hist, b.nodeCap, nodesDev, stream);
+  if (zrc != kOk) return zrc;
   k_leaf_cells<T, D><<<ceil_div(b.nq, 256), 256, 0, stream>>>(static_cast<const Node<T>*>(b.nodes),
                                                               static_cast<const T*>(b.query), b.nq, b.qStride, b.dim,
                                                               b.cell, b.rank, b.hist, b.qOffset, b.nodeOffset,
                                                               b.nClouds);
-  return order_by_cells(b.cell, b.rank, b.hist, b.nodeCap, b.nq, b.order, stream);
+  return order_by_cells(b.cell, b.rank, b.hist, b.nodeCap, b.nq, b.order, stream, nodesDev);
 }
 
 template <typename T, int D>

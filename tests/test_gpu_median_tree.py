@@ -28,10 +28,12 @@ def _clouds():
         "uniform_f32": (S.uniform(50000, 3, seed=3), S.uniform(8000, 3, seed=4)),
         "lidar_f32": (lidar, S.lidar_queries(lidar)[:8000]),
         "clusters8_f64": (c8, (c8[:6000] + np.random.default_rng(6).normal(0, 0.01, (6000, 8))).astype(np.float64)),
+        "uniform4_f32": (S.uniform(40000, 4, seed=7), S.uniform(6000, 4, seed=8)),
+        "uniform3_f64": (S.uniform(40000, 3, seed=9).astype(np.float64), S.uniform(6000, 3, seed=10).astype(np.float64)),
     }
 
 
-@pytest.mark.parametrize("name", ["uniform_f32", "lidar_f32", "clusters8_f64"])
+@pytest.mark.parametrize("name", ["uniform_f32", "lidar_f32", "clusters8_f64", "uniform4_f32", "uniform3_f64"])
 @pytest.mark.parametrize("k", [1, 10, 40])
 def test_median_tree_search_is_exact(name, k):
     nb = _nb()
