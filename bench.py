@@ -118,8 +118,22 @@ def profiled_traffic(label: str, k: int):
     return per_launch, nq
 
 
+def _nvtx_timed(push: bool) -> None:
+    """An NVTX range named "timed" around the timed steps, so that a profiler
+    can capture just their kernels (ncu --nvtx --nvtx-include "timed/")."""
+    try:
+        import torch
+        if push:
+            torch.cuda.nvtx.range_push("timed")
+        else:
+            torch.cuda.nvtx.range_pop()
+    except (ImportError, RuntimeError, AttributeError):
+        pass
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms, over the
+    timed steps (which it also marks with the "timed" NVTX range)."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -137,9 +151,11 @@ class ClockSampler:
                  "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+        _nvtx_timed(True)
         return self
 
     def __exit__(self, *exc):
+        _nvtx_timed(False)
         if self.proc is not None:
             self.proc.terminate()
             try:
