@@ -850,12 +850,13 @@ __device__ __forceinline__ double fmin_t(double a, double b) { return fmin(a, b)
 // slot, the index itself beside the tile) and -2q. With e the reference's
 // distance (separately rounded squares, nabo/kdtree_cpu.cpp:383-391), a
 // point it could accept has e <= thr, and then
-//   a <= thr - |q|^2 + g (thr + 2 P + 2 |q|^2)
-// with g = (D + 1) u / (1 - (D + 1) u), u = 2^-24, P the tile's largest
-// |p|^2 (the dot product's rounding, bounded with 2|q||p| <= |q|^2 + |p|^2,
-// plus e's own and |q|^2's). The test uses 2^-17 for g, over 4 times that
-// bound for D <= 16 and covering the rounding of the bound itself, so it
-// never drops a point that the exact pass would take; a group that passes
+//   a <= thr - |q|^2 + g (thr + 3 P + 2 |q|^2)
+// (the dot product's rounding, bounded with 2|q||p| <= |q|^2 + |p|^2, plus
+// e's own rounding and |q|^2's) with g = (D + 2) u / (1 - (D + 2) u),
+// u = 2^-24, and P the tile's largest |p|^2; the test's bound
+// thr - |q|^2 + 2^-17 (thr + 2 P + 2 |q|^2) exceeds that (g (thr + 3 P +
+// 2 |q|^2)) over 4 times for D <= 16 and covers its own rounding, so it
+// never drops a point that the exact pass would take. A group that passes
 // is computed again exactly, as before.
 template <int D>
 struct BfFilter {

@@ -285,7 +285,11 @@ int knn_kdtree(const DeviceCloud& c, const KnnArgs& a, cudaStream_t stream) {
 // Brute force for k <= kMaxK. A search with too few queries to give every
 // SM kBfBlocksPerSm blocks splits the points into row chunks (block rows),
 // each writing its k best per query to scratch, merged by k_bf_merge.
-// (At 4 blocks per SM, 100 k x 100 k ran 16 warps per SM at 74 % issue.)
+// (At 4 blocks per SM, 100 k x 100 k ran 16 warps per SM at 74 % issue.
+// Rows chosen from the kernel's real occupancy instead, to fill whole waves
+// (4 rows there instead of 2), measured slower, 3.50 -> 3.74 ms at k = 5 and
+// 4.79 -> 5.78 ms at k = 10: each row's top-k lists start empty, and more
+// of the points then meet a loose threshold.)
 constexpr int kBfBlocksPerSm = 8;
 template <typename T, int D, int K, int QT = BfShape<T, K>::QT, int J = BfShape<T, K>::J>
 int launch_bruteforce(const KnnLaunch& L, cudaStream_t stream) {
