@@ -788,17 +788,6 @@ __device__ __forceinline__ int2 median_flag(const SegLevel<T>& L, int s, T v) {
   return make_int2(v <= m ? 1 : 0, v < m ? 1 : 0);
 }
 
-// Level 0: each position's coordinate along its root segment's cut dimension.
-template <typename T, int D>
-__global__ void k_median_val0(MedianBufs<T, D> B, int64_t n, SegLevel<T> L, const LevelState* st) {
-  pdl_begin();
-  if (st->nseg == 0) return;
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x) {
-    const int s = B.seg[0][p];
-    if (s >= 0) B.val[0][p] = B.rec[0][p].p.c[L.cutDim[s]];
-  }
-}
-
 template <typename T, int D>
 __global__ void k_median_cut(SegLevel<T> L, const LevelState* st, MedianBufs<T, D> B) {
   pdl_begin();
@@ -1111,54 +1100,77 @@ __global__ void k_median_flush(MedianBufs<T, D> B, Rec<T, D>* finalRecs, int64_t
 
 // ---- forest set-up: clouds are contiguous point ranges [off[c], off[c+1])
 
+// Packs the clouds into records (index within the cloud) and reduces each
+// cloud's per-dimension min/max (ordered keys) and a non-finite flag, in
+// one pass. Block b takes the contiguous positions [b * chunk, (b + 1) *
+// chunk) a tile of kBlock at a time, following the clouds with a cursor (a
+// binary search once per thread); each lane keeps the running min/max of
+// its current cloud, and the warp flushes them (reduced across the lanes
+// of each cloud, one atomic per cloud and dimension) only when some lane's
+// cloud changes, and at the end. With `smallRoots`, points of clouds whose
+// root is already a small segment are also written there.
 template <typename T, int D>
-__global__ void k_pack_forest(const T* __restrict__ cloud, int64_t n, int64_t stride, int dim,
-                              const int64_t* __restrict__ off, int nClouds, Rec<T, D>* __restrict__ recs,
-                              Rec<T, D>* __restrict__ smallRoots) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  Rec<T, D> r;
-#pragma unroll
-  for (int c = 0; c < RecSize<T, D>::chunks; ++c) r.v[c] = make_uint4(0u, 0u, 0u, 0u);
-#pragma unroll
-  for (int d = 0; d < D; ++d) r.p.c[d] = d < dim ? cloud[p * stride + d] : T(0);
-  const int c = cloud_of(off, nClouds, p);
-  r.p.idx = (int32_t)(p - off[c]);
-  recs[p] = r;
-  // the median split packs into a working array: clouds whose root is
-  // already a small segment also go to the final array
-  if (smallRoots && off[c + 1] - off[c] <= kSmallMax) smallRoots[p] = r;
-}
-
-// Per-cloud per-dimension min/max (ordered keys) and a non-finite flag.
-template <typename T, int D>
-__global__ void k_bounds_forest(const Rec<T, D>* __restrict__ recs, int64_t n, int dim,
-                                const int64_t* __restrict__ off, int nClouds, typename KeyOf<T>::type* mnK,
-                                typename KeyOf<T>::type* mxK, int* nonFinite) {
+__global__ void k_pack_bounds(const T* __restrict__ cloud, int64_t n, int64_t stride, int dim,
+                              const int64_t* __restrict__ off, int nClouds, int64_t chunk,
+                              Rec<T, D>* __restrict__ recs, Rec<T, D>* __restrict__ smallRoots,
+                              typename KeyOf<T>::type* mnK, typename KeyOf<T>::type* mxK, int* nonFinite) {
   using Key = typename KeyOf<T>::type;
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int c = -1;
-  Rec<T, D> r;
-  if (p < n) {
-    c = cloud_of(off, nClouds, p);
-    load_rec(recs, p, r);
-  }
-  int bad = 0;
+  const int64_t begin = blockIdx.x * chunk;
+  const int64_t end = begin + chunk < n ? begin + chunk : n;
+  if (begin >= end) return;
+  int c = cloud_of(off, nClouds, begin + threadIdx.x < end ? begin + threadIdx.x : begin);
+  int cur = -1;  // cloud of the running min/max
+  Key kmin[D], kmax[D];
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    Key kmin = 0, kmax = 0;
-    if (c >= 0) {
-      kmin = kmax = ordered_key(r.p.c[d]);
-      bad |= (d < dim && !isfinite(r.p.c[d])) ? 1 : 0;
+    kmin[d] = ~Key(0);
+    kmax[d] = 0;
+  }
+  int bad = 0;
+  auto flush = [&]() {
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      bool tail;
+      const Key a = seg_warp_reduce(cur, kmin[d], MinOp(), &tail);
+      const Key b = seg_warp_reduce(cur, kmax[d], MaxOp(), &tail);
+      if (tail && cur >= 0 && d < dim) {
+        atomicMin(mnK + (int64_t)cur * kMaxDim + d, a);
+        atomicMax(mxK + (int64_t)cur * kMaxDim + d, b);
+      }
+      kmin[d] = ~Key(0);
+      kmax[d] = 0;
     }
-    bool tail;
-    kmin = seg_warp_reduce(c, kmin, MinOp(), &tail);
-    kmax = seg_warp_reduce(c, kmax, MaxOp(), &tail);
-    if (tail && c >= 0 && d < dim) {
-      atomicMin(mnK + (int64_t)c * kMaxDim + d, kmin);
-      atomicMax(mxK + (int64_t)c * kMaxDim + d, kmax);
+  };
+  for (int64_t p0 = begin; p0 < end; p0 += kBlock) {
+    const int64_t p = p0 + threadIdx.x;
+    int cp = -1;
+    Rec<T, D> r;
+    if (p < end) {
+      while (off[c + 1] <= p) ++c;
+      cp = c;
+#pragma unroll
+      for (int q = 0; q < RecSize<T, D>::chunks; ++q) r.v[q] = make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+      for (int d = 0; d < D; ++d) r.p.c[d] = d < dim ? cloud[p * stride + d] : T(0);
+      r.p.idx = (int32_t)(p - off[c]);
+      recs[p] = r;
+      if (smallRoots && off[c + 1] - off[c] <= kSmallMax) smallRoots[p] = r;
+    }
+    if (__any_sync(kFull, cp != cur)) {
+      flush();
+      cur = cp;
+    }
+    if (cp >= 0) {
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const Key k = ordered_key(r.p.c[d]);
+        kmin[d] = k < kmin[d] ? k : kmin[d];
+        kmax[d] = k > kmax[d] ? k : kmax[d];
+        bad |= (d < dim && !isfinite(r.p.c[d])) ? 1 : 0;
+      }
     }
   }
+  flush();
   if (__any_sync(kFull, bad) && (threadIdx.x & 31) == 0) atomicOr(nonFinite, 1);
 }
 
@@ -1211,14 +1223,32 @@ __global__ void k_forest_roots(const int64_t* __restrict__ off, int nClouds, con
     rootLo[(int64_t)c * kMaxDim + d] = lo[d];
     rootHi[(int64_t)c * kMaxDim + d] = hi[d];
   }
+  // the root segment's cut dimension (the median split reads it before
+  // any level kernel runs)
+  if (count > kSmallMax) L.cutDim[rootSeg[c]] = arg_max_extent(lo, hi, dim);
 }
 
-// Positions in [n, nPad) (the median split's padding) belong to no segment.
-__global__ void k_init_segof(int* segOf, int64_t n, int64_t nPad, const int64_t* __restrict__ off, int nClouds,
-                             const int* __restrict__ rootSeg) {
-  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (p >= nPad) return;
-  segOf[p] = p < n ? rootSeg[cloud_of(off, nClouds, p)] : -1;
+// Each position's root segment (-1 for a small root, and for the median
+// split's padding [n, nPad)), by contiguous block ranges with a cloud
+// cursor as in k_pack_bounds. With `val` (the median split) also the
+// position's coordinate along its root segment's cut dimension.
+template <typename T, int D>
+__global__ void k_init_segof(int* segOf, int64_t n, int64_t nPad, int64_t chunk, const int64_t* __restrict__ off,
+                             int nClouds, const int* __restrict__ rootSeg, const Rec<T, D>* __restrict__ recs,
+                             const int* __restrict__ cutDim, T* val) {
+  const int64_t begin = blockIdx.x * chunk;
+  const int64_t end = begin + chunk < nPad ? begin + chunk : nPad;
+  if (begin >= end) return;
+  int c = begin < n ? cloud_of(off, nClouds, begin + threadIdx.x < n ? begin + threadIdx.x : begin) : 0;
+  for (int64_t p = begin + threadIdx.x; p < end; p += kBlock) {
+    int s = -1;
+    if (p < n) {
+      while (off[c + 1] <= p) ++c;
+      s = rootSeg[c];
+      if (val && s >= 0) val[p] = recs[p].p.c[cutDim[s]];
+    }
+    segOf[p] = s;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1722,17 +1752,23 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
     }
   }
   Rec<T, D>* packed = median ? mb.rec[0] : recs;
-  k_pack_forest<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(dCloud, n, stride, dim, dOff, nClouds, packed,
-                                                                  median ? recs : nullptr);
+  // per-position passes over contiguous block ranges: 8 blocks per SM
+  int device = 0, sms = 0;
+  NABO_CUDA_TRY(cudaGetDevice(&device));
+  NABO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  const int rangeBlocks = std::max(1, std::min(ceil_div(std::max<int64_t>(n, 1), kBlock), 8 * std::max(sms, 1)));
+  const int64_t rangeChunk = (int64_t)ceil_div(ceil_div(std::max<int64_t>(n, 1), rangeBlocks), kBlock) * kBlock;
 
-  // per-cloud bounds
+  // records and per-cloud bounds in one pass
   Key* keys;
   NABO_CUDA_TRY(sc.get(&keys, 2 * (int64_t)nClouds * kMaxDim));
   NABO_CUDA_TRY(cudaMemsetAsync(f->status, 0, 4 * sizeof(int), stream));
   k_init_keys_forest<T><<<ceil_div(nClouds * kMaxDim, 256), 256, 0, stream>>>(keys, keys + nClouds * kMaxDim,
                                                                               nClouds);
-  k_bounds_forest<T, D><<<ceil_div(n, kBlock), kBlock, 0, stream>>>(packed, n, dim, dOff, nClouds, keys,
-                                                                   keys + nClouds * kMaxDim, f->status + 0);
+  if (n > 0)
+    k_pack_bounds<T, D><<<rangeBlocks, kBlock, 0, stream>>>(dCloud, n, stride, dim, dOff, nClouds, rangeChunk, packed,
+                                                            median ? recs : nullptr, keys, keys + nClouds * kMaxDim,
+                                                            f->status + 0);
   NABO_CUDA_TRY(cudaGetLastError());
   if (hostDriven) {
     int bad = 0;
@@ -1806,16 +1842,17 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   k_forest_roots<T><<<ceil_div(nClouds, 128), 128, 0, stream>>>(
       dOff, nClouds, keys, keys + nClouds * kMaxDim, dim, cur, small, st, counters, rootRef, rootSeg,
       static_cast<T*>(f->rootLo), static_cast<T*>(f->rootHi));
-  k_init_segof<<<ceil_div(nPad, kBlock), kBlock, 0, stream>>>(segOf, n, nPad, dOff, nClouds, rootSeg);
+  {
+    const int64_t segChunk = rangeChunk * ceil_div(nPad, rangeChunk * rangeBlocks);
+    k_init_segof<T, D><<<ceil_div(nPad, segChunk), kBlock, 0, stream>>>(
+        segOf, n, nPad, segChunk, dOff, nClouds, rootSeg, packed, cur.cutDim, median ? mb.val[0] : nullptr);
+  }
   NABO_CUDA_TRY(cudaGetLastError());
 
   const int sg = ceil_div(segCap, 128);
   // per-position passes: a fixed grid of 8 blocks per SM looping over tiles
   // of kBlock positions; the two scan passes give each block a contiguous
   // run of `tiles` tiles
-  int device = 0, sms = 0;
-  NABO_CUDA_TRY(cudaGetDevice(&device));
-  NABO_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
   const int grid = std::max(1, std::min(nb, 8 * std::max(sms, 1)));
   const int tiles = ceil_div(nb, grid);
   const int scanBlocks = ceil_div(nb, tiles);
@@ -1847,10 +1884,6 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
       }
     }
     if (median) {
-      if (level == 0) {
-        NABO_CUDA_TRY(launch_pdl(k_prepare<T>, sg, 128, 0, stream, cur, st, dim));
-        NABO_CUDA_TRY(launch_pdl(k_median_val0<T, D>, grid, kBlock, 0, stream, mb, n, cur, st));
-      }
       NABO_CUDA_TRY(launch_pdl(k_median_cut<T, D>, sg, 128, 0, stream, cur, st, mb));
       NABO_CUDA_TRY(launch_pdl(k_median_sums<T, D>, mBlocks, kBlock, 0, stream, mb, nPad, cur, mTiles, blockSums,
                                segFirst, segLast, st));

@@ -400,6 +400,63 @@ __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, ui
   }
 }
 
+// Ascending bitonic sort of B (a power of 2) keys held in registers: every
+// index is known at compile time, so a compare-exchange is one 64-bit
+// compare and two selects.
+template <int B>
+__device__ __forceinline__ void sort_keys(uint64_t (&s)[B]) {
+#pragma unroll
+  for (int k2 = 2; k2 <= B; k2 <<= 1) {
+#pragma unroll
+    for (int j = k2 >> 1; j > 0; j >>= 1) {
+#pragma unroll
+      for (int i = 0; i < B; ++i) {
+        const int l = i ^ j;
+        if (l > i) {
+          const uint64_t a = s[i], b = s[l];
+          const bool sw = ((i & k2) == 0) ? (a > b) : (a < b);
+          s[i] = sw ? b : a;
+          s[l] = sw ? a : b;
+        }
+      }
+    }
+  }
+}
+
+// A query's first leaf into its still empty top-k (float, k == K): the
+// first B points' keys -- those the leaf scan would not take (outside the
+// radius, a forbidden self match, or !want) as the empty key -- sorted by a
+// network and placed in the list as they are, then the rest of the leaf by
+// the normal scan. The list ends as if the points had been inserted one at
+// a time (it holds the K smallest keys, and the scan's order never matters
+// to that), for a fraction of the work: about 6 B log2(B)^2 / 4 integer
+// instructions against about 6 K per insertion.
+template <int D, int K>
+__device__ __forceinline__ void scan_first_leaf(const Rec<float, D>* __restrict__ recs, uint32_t st, uint32_t cnt,
+                                                const float (&q)[D], float maxRadius2, float minDist, bool want,
+                                                TopK<float, K>& heap, const LeafFilter<float, D>& flt) {
+  constexpr int B = K <= 10 ? 8 : 16;
+  constexpr uint64_t kEmpty = uint64_t(0x7f800000u) << 32;
+  const uint64_t radKey = maxRadius2 == maxRadius2 ? ((uint64_t(__float_as_uint(maxRadius2)) << 32) | 0xffffffffull) : 0ull;
+  const uint64_t thrKey = (!want || radKey == 0ull) ? 0ull : (kEmpty <= radKey ? kEmpty : radKey + 1ull);
+  uint64_t sk[B];
+#pragma unroll
+  for (int j = 0; j < B; ++j) {
+    sk[j] = kEmpty;
+    if ((uint32_t)j < cnt) {
+      Rec<float, D> r;
+      load_rec(recs, (int64_t)st + j, r);
+      const float d = dist2_seq(q, r);
+      const uint64_t key = TopK<float, K>::make(d, r.p.idx);
+      if (key < thrKey && d > minDist) sk[j] = key;
+    }
+  }
+  sort_keys(sk);
+#pragma unroll
+  for (int j = 0; j < K; ++j) heap.key[j] = (K - 1 - j < B) ? sk[(K - 1 - j) < B ? (K - 1 - j) : 0] : kEmpty;
+  if (cnt > (uint32_t)B) scan_leaf<float, D, K>(recs, st + B, cnt - B, q, maxRadius2, minDist, want, heap, flt);
+}
+
 // A pushed far child as 32-bit words [rd | off[0..D-1] | node] (a T is one
 // word for float, two for double) in 16-byte chunks: a push is one 128-bit
 // local store per chunk (a lone trailing word is stored alone), a pop reads
@@ -566,6 +623,7 @@ __device__ __forceinline__ void knn_query(const KnnLaunch& a, int64_t t, S& stk,
     int sp = 0;
     uint32_t node = root;
     T rd = T(0);
+    bool fresh = true;  // no leaf scanned yet: the top-k is empty
     for (;;) {
       // descend to a leaf, pushing far children
       // min(maxRadius2, head), where a NaN radius (which passes nothing) wins
@@ -589,7 +647,15 @@ __device__ __forceinline__ void knn_query(const KnnLaunch& a, int64_t t, S& stk,
       }
       // leaf
       const uint32_t cnt = node_payload(nd.meta);
-      scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap, flt);
+      if constexpr (std::is_same<T, float>::value && K >= 8) {
+        if (fresh && k == K)
+          scan_first_leaf<D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap, flt);
+        else
+          scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap, flt);
+      } else {
+        scan_leaf<T, D, K>(recs, node_start(nd), cnt, q, maxRadius2, minDist, true, heap, flt);
+      }
+      fresh = false;
       touched += cnt;
       // pop the next far child that can still hold a better neighbour
       bool more = false;
