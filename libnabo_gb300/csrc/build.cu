@@ -1373,7 +1373,8 @@ __device__ T warp_median(const Rec<T, D>* node, int count, int cd, int lane) {
 
 template <typename T, int D>
 __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, Node<T>* scratch,
-                        SmallStack<T> stk, int dim, unsigned bucketSize, int* counters, int splitRule) {
+                        SmallStack<T> stk, int dim, unsigned bucketSize, int* counters, int splitRule,
+                        int* nextSeg) {
   extern __shared__ __align__(16) unsigned char smallSmem[];
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
@@ -1384,7 +1385,13 @@ __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, 
   int* posR = posL + kSmallMax / 2;
   const int nS = *nSmall;
   int hmax = 0;
-  for (int sid = blockIdx.x * warps + warp; sid < nS; sid += gridDim.x * warps) {
+  // segments are taken one at a time from a counter (sizes differ up to 2x;
+  // a fixed assignment left warps idle at the end)
+  for (;;) {
+    int sid = 0;
+    if (lane == 0) sid = atomicAdd(nextSeg, 1);
+    sid = __shfl_sync(0xffffffffu, sid, 0);
+    if (sid >= nS) break;
     const int base = small.start[sid];
     const int segN = small.count[sid];
     for (int i = lane; i < segN; i += 32) pts[i] = recs[base + i];
@@ -1937,9 +1944,16 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   {
     const int wpb = small_warps_per_block<T, D>();
     const size_t smem = (size_t)wpb * kSmallMax * (sizeof(Rec<T, D>) + sizeof(int));
-    const int smallGrid = std::max(1, std::min(ceil_div(std::max(nSmallHost, 1), wpb), 16 * std::max(sms, 1)));
+    // one wave of resident blocks, its warps taking segments from a counter
+    int occ = 0;
+    NABO_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_small<T, D>, 32 * wpb, smem));
+    const int smallGrid =
+        std::max(1, std::min(ceil_div(std::max(nSmallHost, 1), wpb), std::max(occ, 1) * std::max(sms, 1)));
+    int* nextSeg;
+    NABO_CUDA_TRY(sc.get(&nextSeg, 1));
+    NABO_CUDA_TRY(cudaMemsetAsync(nextSeg, 0, sizeof(int), stream));
     k_small<T, D><<<smallGrid, 32 * wpb, smem, stream>>>(recs, small, counters + 1, scratchNodes, stk, dim,
-                                                         bucketSize, counters, splitRule);
+                                                         bucketSize, counters, splitRule, nextSeg);
   }
   NABO_CUDA_TRY(cudaGetLastError());
   Node<T>* nodes = static_cast<Node<T>*>(f->nodes);

@@ -364,7 +364,11 @@ __global__ void k_place(const uint32_t* __restrict__ cell, const uint32_t* __res
 // warps' result rows lie side by side and their stores coalesce. Cells with
 // more than kRunSort queries keep arrival order; the order only affects
 // speed, never results.
+// Runs of up to kRunRegs queries are loaded at once and sorted in registers
+// by a network (independent loads instead of a chain of dependent ones);
+// longer runs, up to kRunSort, by insertion in place.
 constexpr int kRunSort = 64;
+constexpr int kRunRegs = 16;
 __global__ void k_sort_runs(const uint32_t* __restrict__ start, int64_t bins, int64_t nq, int32_t* order,
                             const int64_t* binsDev) {
   bins = live_count(bins, binsDev);
@@ -373,6 +377,32 @@ __global__ void k_sort_runs(const uint32_t* __restrict__ start, int64_t bins, in
   const int64_t s = start[b];
   const int64_t e = b + 1 < bins ? (int64_t)start[b + 1] : nq;
   if (e - s < 2 || e - s > kRunSort) return;
+  if (e - s <= kRunRegs) {
+    const int len = (int)(e - s);
+    int32_t v[kRunRegs];
+#pragma unroll
+    for (int j = 0; j < kRunRegs; ++j) v[j] = j < len ? order[s + j] : INT_MAX;
+#pragma unroll
+    for (int k2 = 2; k2 <= kRunRegs; k2 <<= 1) {
+#pragma unroll
+      for (int jj = k2 >> 1; jj > 0; jj >>= 1) {
+#pragma unroll
+        for (int i = 0; i < kRunRegs; ++i) {
+          const int l = i ^ jj;
+          if (l > i) {
+            const int32_t lo = min(v[i], v[l]), hi = max(v[i], v[l]);
+            const bool up = (i & k2) == 0;
+            v[i] = up ? lo : hi;
+            v[l] = up ? hi : lo;
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kRunRegs; ++j)
+      if (j < len) order[s + j] = v[j];
+    return;
+  }
   for (int64_t i = s + 1; i < e; ++i) {
     const int32_t v = order[i];
     int64_t j = i - 1;
