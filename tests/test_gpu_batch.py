@@ -280,3 +280,37 @@ def test_lane_groups_per_query_are_exact(graph):
     _, ri, rd = _run_batch(clouds, queries, ks, graph=graph)
     for c in range(len(clouds)):
         H.assert_identical(bi[c], bd[c], ri[c], rd[c], f"lane groups cloud {c}")
+
+
+@pytest.mark.parametrize("split_rule", [0, 1])
+@pytest.mark.parametrize("chunks", [1, 3, 5])
+def test_k_size_launches_with_mixed_k_and_empty_clouds(split_rule, chunks):
+    """The search runs one launch per compiled top-k size (1, 2, 5, 8, 10,
+    16, 32) over run lists of its clouds. Clouds whose k is below their
+    group's size (3 and 4 in the 5-slot group, 9 in the 10-slot one),
+    clouds without queries (no run), and host runs whose cloud groups cut
+    every size's run list must all give the oracle's results."""
+    nb = _nb()
+    clouds, queries, _ = _batch_data(22, 300, 8000, seed=11)
+    ks = np.array([1, 2, 3, 5, 4, 7, 8, 9, 10, 12, 16, 20, 32, 1, 5, 16, 3, 9, 32, 2, 8, 10], np.int32)
+    ks = np.minimum(ks, [c.shape[0] - 1 for c in clouds]).astype(np.int32)
+    for c in (4, 13, 21):
+        queries[c] = queries[c][:0]
+    b = nb.BatchSearch([c.shape[0] for c in clouds], splitRule=split_rule, pipelineChunks=chunks, maxLevels=40)
+    b.set_queries([q.shape[0] for q in queries], ks)
+    di, dd = _device_flat(b, clouds, queries)
+    host, hold = _host_buffers(True)
+    hc, hq = host(np.concatenate(clouds)), host(np.concatenate(queries))
+    out = (host(np.zeros(b.result_entries, np.int32)), host(np.zeros(b.result_entries, np.float32)))
+    gi, gd = b.run_host(hc, hq, out=out)
+    H.assert_identical(gi[:, None], gd[:, None], di[:, None], dd[:, None], "host run vs device run")
+    for c in range(len(clouds)):
+        if queries[c].shape[0] == 0:
+            assert b.split(gi)[c].size == 0
+            continue
+        if split_rule == 0:
+            oi, od, _ = O.OracleTree(clouds[c]).knn(queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        else:
+            oi, od, _ = O.bf_knn(clouds[c], queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        H.assert_identical(b.split(gi)[c], b.split(gd)[c], oi, od, f"cloud {c} k={ks[c]} rule {split_rule}")
+    del hold
