@@ -672,6 +672,8 @@ def run_c4(args):
     import libnabo_gb300 as nb
     from oracle import oracle as O
 
+    from libnabo_gb300 import autotune
+
     dev = torch.device("cuda", 0)
     data = c4_workload(args.c4_clouds)
     k = 32
@@ -682,12 +684,23 @@ def run_c4(args):
             continue
         pc = np.array([c.shape[0] for c in clouds], np.int64)
         qc = np.array([q.shape[0] for q in queries], np.int64)
-        b = nb.BatchSearch(pc, dim=8, dtype=dt, bucketSize=8, maxLevels=64)
+        # the autotuner on 4 clouds, 25,000 queries each; one thread per
+        # query (8-lane groups measured 6-8x slower on these batches)
+        t0 = time.perf_counter()
+        choice = autotune.tune(clouds, queries, k, dim=8, dtype=dt, sample=4, repeats=2,
+                               split_rules=tuple(int(r) for r in args.split_rules.split(",")),
+                               max_queries_per_cloud=25000, lanes=(1,))
+        choice["autotune_s"] = time.perf_counter() - t0
+        b = nb.BatchSearch(pc, dim=8, dtype=dt, bucketSize=choice["bucketSize"],
+                           threadsPerBlock=choice["threadsPerBlock"], maxLevels=choice["maxLevels"],
+                           splitRule=choice["splitRule"])
         b.set_queries(qc, np.full(len(clouds), k, np.int32))
         tc = torch.from_numpy(np.concatenate(clouds)).to(dev)
         tq = torch.from_numpy(np.concatenate(queries)).to(dev)
         batches.append(dict(dt=dt, b=b, tc=tc, tq=tq, out=b._outputs(dev), clouds=clouds, queries=queries,
-                            train_queries=train_queries, points=int(pc.sum()), nq=int(qc.sum())))
+                            train_queries=train_queries, points=int(pc.sum()), nq=int(qc.sum()),
+                            choice={kk: choice[kk] for kk in ("bucketSize", "threadsPerBlock", "splitRule",
+                                                              "maxLevels", "autotune_s")}))
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -698,8 +711,10 @@ def run_c4(args):
     build_ms = e0.elapsed_time(e1)
     for x in batches:  # a tree deeper than 64 top levels: rebuild with room for it
         if x["b"].status()["flags"] & 2:
-            x["b"] = nb.BatchSearch([c.shape[0] for c in x["clouds"]], dim=8, dtype=x["dt"], bucketSize=8,
-                                    maxLevels=256)
+            x["b"] = nb.BatchSearch([c.shape[0] for c in x["clouds"]], dim=8, dtype=x["dt"],
+                                    bucketSize=x["choice"]["bucketSize"],
+                                    threadsPerBlock=x["choice"]["threadsPerBlock"], maxLevels=256,
+                                    splitRule=x["choice"]["splitRule"])
             x["b"].set_queries([q.shape[0] for q in x["queries"]], np.full(len(x["clouds"]), k, np.int32))
             x["b"].build(x["tc"])
     status = {np.dtype(x["dt"]).name: x["b"].status() for x in batches}
@@ -845,8 +860,10 @@ def run_c4(args):
         base = {"value": nqb / tb, "unit": "queries/s", "cores": O.num_threads(), "kind": "port",
                 "sample": f"search only, 2 smallest clouds of each type, 5000 queries each ({nqb} queries, eps 0)",
                 "touched_per_query": touched / nqb}
-    # checks on the smallest cloud of each type: exact at eps 0 (oracle,
-    # canonical ties), the (1+eps)^2 bound on squared distances at eps 0.5
+    # checks on the smallest cloud of each type: exact at eps 0 (the
+    # oracle's tree in canonical order for the reference's split rule, its
+    # brute force for the median split), the (1+eps)^2 bound on squared
+    # distances at eps 0.5
     checks = {}
     for j, x in enumerate(batches):
         c = int(np.argmin([cl.shape[0] for cl in x["clouds"]]))
@@ -854,7 +871,10 @@ def run_c4(args):
         gi = x["b"].split(exact_out[j][0].cpu().numpy())[c][sub]
         gd = x["b"].split(exact_out[j][1].cpu().numpy())[c][sub]
         ad = x["b"].split(approx_out[j][1].cpu().numpy())[c][sub]
-        oi, od, _ = O.OracleTree(x["clouds"][c]).knn(x["queries"][c][sub], k, mode=O.MODE_CANONICAL)
+        if x["choice"]["splitRule"] == 1:
+            oi, od, _ = O.bf_knn(x["clouds"][c], x["queries"][c][sub], k, mode=O.MODE_CANONICAL)
+        else:
+            oi, od, _ = O.OracleTree(x["clouds"][c]).knn(x["queries"][c][sub], k, mode=O.MODE_CANONICAL)
         checks[np.dtype(x["dt"]).name] = {
             "cloud": c, "points": int(x["clouds"][c].shape[0]), "queries_checked": 2000,
             "exact_identical": bool(np.array_equal(gi, oi) and np.array_equal(gd, od)),
@@ -866,7 +886,8 @@ def run_c4(args):
         "config": {"workload": "c4_8d", "clouds": sum(len(x["clouds"]) for x in batches),
                    "points": sum(x["points"] for x in batches), "queries": nq_total, "k": k, "dims": 8,
                    "per_type": {np.dtype(x["dt"]).name: {"clouds": len(x["clouds"]), "points": x["points"],
-                                                          "queries": x["nq"]} for x in batches},
+                                                          "queries": x["nq"], "autotuned": x["choice"]}
+                                for x in batches},
                    "step": "search of every query of both batches (trees built once)",
                    "l2": "inputs larger than L2"},
         "forms": forms, "build_ms": build_ms, "status": status, "checks": checks, "cpu_baseline": base,

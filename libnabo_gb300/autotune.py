@@ -70,13 +70,18 @@ def _levels_of(cloud, queries, k, dim, dtype, bucket, rule) -> int:
 
 
 def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int = 64, repeats: int = 3,
-         cache_path: str | None = None, seed: int = 0, split_rules=CANDIDATES["splitRule"]) -> dict:
-    """Best {bucketSize, threadsPerBlock, splitRule} for a batch (lists of (n_c, dim) arrays)."""
+         cache_path: str | None = None, seed: int = 0, split_rules=CANDIDATES["splitRule"],
+         max_queries_per_cloud: int | None = None, lanes=None) -> dict:
+    """Best {bucketSize, threadsPerBlock, splitRule, lanesPerQuery} for a batch (lists of (n_c, dim)
+    arrays), timed on `sample` of its clouds with at most `max_queries_per_cloud` of each one's
+    queries; `lanes` restricts the lanes-per-query candidates."""
     import torch
     ks = np.broadcast_to(np.asarray(k, dtype=np.int32), (len(cloud_list),))
     pcs = np.array([c.shape[0] for c in cloud_list], np.int64)
     split_rules = tuple(int(r) for r in split_rules)
+    lane_set = tuple(int(x) for x in (lanes if lanes is not None else CANDIDATES["lanesPerQuery"]))
     key = shape_key(pcs, dim, dtype, ks) + ("" if split_rules == (0, 1) else "-s" + "".join(map(str, split_rules)))
+    key += "" if lane_set == CANDIDATES["lanesPerQuery"] else "-l" + "".join(map(str, lane_set))
     if key in _cache:
         return dict(_cache[key], key=key, cached=True)
     if cache_path and os.path.exists(cache_path):
@@ -88,13 +93,14 @@ def tune(cloud_list, query_list, k, dim: int = 3, dtype=np.float32, sample: int 
     rng = np.random.default_rng(seed)
     pick = np.sort(rng.choice(len(cloud_list), min(sample, len(cloud_list)), replace=False))
     pc = pcs[pick]
-    qc = np.array([query_list[i].shape[0] for i in pick], np.int64)
+    qsub = [query_list[i][:max_queries_per_cloud] if max_queries_per_cloud else query_list[i] for i in pick]
+    qc = np.array([q.shape[0] for q in qsub], np.int64)
     clouds = torch.from_numpy(np.concatenate([cloud_list[i] for i in pick]).astype(dtype)).cuda()
-    queries = torch.from_numpy(np.concatenate([query_list[i] for i in pick]).astype(dtype)).cuda()
+    queries = torch.from_numpy(np.concatenate(qsub).astype(dtype)).cuda()
     trials = []
     t0 = time.perf_counter()
     # lane groups apply to k <= 32 and run blocks of 128 threads
-    lane_choices = CANDIDATES["lanesPerQuery"] if int(np.max(ks)) <= 32 else (1,)
+    lane_choices = lane_set if int(np.max(ks)) <= 32 else (1,)
     for rule in split_rules:
         for bucket in CANDIDATES["bucketSize"]:
             for lanes in lane_choices:
