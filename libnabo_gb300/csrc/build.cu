@@ -1315,35 +1315,52 @@ __device__ __forceinline__ void warp_partition_pass(Rec<T, D>* pts, int lo, int 
 // pre-order with an explicit stack (global scratch, written by lane 0). Each
 // split's min/max, counts and partition passes run across the lanes; node
 // records and bucket order come out as the reference's.
+// Ascending bitonic sort of 32 R keys held R per lane (element lane + 32 r),
+// across the warp: partners at distance below 32 are exchanged by shuffle,
+// at 32 inside the lane.
+template <int R, typename Key>
+__device__ __forceinline__ void warp_sort_keys(Key (&e)[R], int lane) {
+#pragma unroll
+  for (int k2 = 2; k2 <= 32 * R; k2 <<= 1) {
+#pragma unroll
+    for (int j = k2 >> 1; j > 0; j >>= 1) {
+      Key o[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) o[r] = j >= 32 ? e[r ^ (j >> 5)] : __shfl_xor_sync(0xffffffffu, e[r], j);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const int i = lane + 32 * r;
+        const bool keepMin = ((i & j) == 0) == ((i & k2) == 0);
+        e[r] = keepMin ? (o[r] < e[r] ? o[r] : e[r]) : (o[r] > e[r] ? o[r] : e[r]);
+      }
+    }
+  }
+}
+
 // The lower median (rank count / 2) of the count values node[i].p.c[cd],
-// computed by the warp. Up to 64 values each lane ranks its own against all
-// of them (count^2 / 32 compares per lane). Above, a bitwise radix select
-// over the values' order-preserving keys, most significant bit first: each
-// round counts the remaining candidates whose next bit is 0 (one compare
-// per held value, summed across the warp) and keeps the half that holds
-// the wanted rank, 32 rounds for float and 64 for double whatever the count.
+// computed by the warp over the values' order-preserving keys (padding
+// sorts above every finite value's key, so it never holds the rank). Up to
+// 64 values a bitonic sort across the warp (one or two keys per lane) and
+// the key at the rank; above, a bitwise radix select, most significant bit
+// first: each round counts the remaining candidates whose next bit is 0 (one
+// compare per held value, summed across the warp) and keeps the half that
+// holds the rank, 32 rounds for float and 64 for double.
 template <typename T, int D>
 __device__ T warp_median(const Rec<T, D>* node, int count, int cd, int lane) {
   using Key = typename KeyOf<T>::type;
   const int want0 = count / 2;
+  if (count <= 32) {
+    Key e[1] = {lane < count ? ordered_key(node[lane].p.c[cd]) : ~Key(0)};
+    warp_sort_keys<1>(e, lane);
+    return ordered_val(__shfl_sync(0xffffffffu, e[0], want0), T(0));
+  }
   if (count <= 64) {
-    bool found = false;
-    T med = T(0);
-    for (int i = lane; i < count; i += 32) {
-      const T v = node[i].p.c[cd];
-      int lt = 0, le = 0;
-      for (int j = 0; j < count; ++j) {
-        const T w = node[j].p.c[cd];
-        lt += w < v ? 1 : 0;
-        le += w <= v ? 1 : 0;
-      }
-      if (!found && lt <= want0 && want0 < le) {
-        found = true;
-        med = v;
-      }
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, found);
-    return __shfl_sync(0xffffffffu, med, __ffs(m) - 1);
+    Key e[2];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) e[r] = lane + 32 * r < count ? ordered_key(node[lane + 32 * r].p.c[cd]) : ~Key(0);
+    warp_sort_keys<2>(e, lane);
+    const Key m = __shfl_sync(0xffffffffu, want0 >= 32 ? e[1] : e[0], want0 & 31);
+    return ordered_val(m, T(0));
   }
   constexpr int kPer = kSmallMax / 32;
   constexpr int kBits = 8 * (int)sizeof(Key);
@@ -1849,7 +1866,7 @@ int build_forest(const T* dCloud, int64_t n, int64_t stride, int dim, unsigned b
   k_forest_roots<T><<<ceil_div(nClouds, 128), 128, 0, stream>>>(
       dOff, nClouds, keys, keys + nClouds * kMaxDim, dim, cur, small, st, counters, rootRef, rootSeg,
       static_cast<T*>(f->rootLo), static_cast<T*>(f->rootHi));
-  {
+  if (nPad > 0) {
     const int64_t segChunk = rangeChunk * ceil_div(nPad, rangeChunk * rangeBlocks);
     k_init_segof<T, D><<<ceil_div(nPad, segChunk), kBlock, 0, stream>>>(
         segOf, n, nPad, segChunk, dOff, nClouds, rootSeg, packed, cur.cutDim, median ? mb.val[0] : nullptr);
