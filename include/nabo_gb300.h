@@ -354,7 +354,7 @@ int nabo_cuda_batch_run(nabo_cuda_batch* b, const void* clouds, const void* quer
  * batch's own, allocated on first use. When all four buffers are
  * page-locked, one CUDA graph (captured as for nabo_cuda_batch_run) uploads
  * the queries during the build and searches the clouds in
- * params.pipelineChunks groups (0 = 4) of about equal result size, each
+ * params.pipelineChunks groups (0 = 8) of about equal result size, each
  * group's results downloaded while the next group is searched; otherwise
  * plain copies surround the device run. Results equal
  * nabo_cuda_batch_run's. Device calls on this batch still running on

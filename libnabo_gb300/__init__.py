@@ -695,7 +695,7 @@ class BatchSearch:
         (total_queries, dim), C order) into host result arrays; returns when
         they are filled. With page-locked arrays (e.g. pinned torch tensors'
         ``.numpy()``) the copies overlap the build and search inside one CUDA
-        graph (``pipelineChunks`` cloud groups, 0 = 4)."""
+        graph (``pipelineChunks`` cloud groups, 0 = 8)."""
         if self.query_counts is None:
             raise NaboError(1, "call set_queries first")
         c = np.ascontiguousarray(clouds, dtype=self.dtype)

@@ -69,7 +69,11 @@ struct nabo_cuda_batch {
   // inputs and results, two streams and the graph of the last page-locked call
   std::vector<int64_t> hQOff, hOutOff;
   BatchClassPlan plan;  // search launches by compiled top-k size
-  int groups = 4;
+  // two more streams and their events, for the plan's groups side by side
+  cudaStream_t aux[2] = {nullptr, nullptr};
+  cudaEvent_t evFork = nullptr;
+  cudaEvent_t evJoin[2] = {nullptr, nullptr};
+  int groups = 8;
   void* devClouds = nullptr;
   void* devQueries = nullptr;
   int32_t* devIdx = nullptr;
@@ -261,6 +265,11 @@ BatchArgs batch_args(const nabo_cuda_batch* b, const void* query, double eps, un
   a.lanesPerQuery = b->lanesPerQuery;
   a.classes = &b->plan;
   a.hQOffset = b->hQOff.empty() ? nullptr : b->hQOff.data();
+  a.aux[0] = b->aux[0];
+  a.aux[1] = b->aux[1];
+  a.evFork = b->evFork;
+  a.evJoin[0] = b->evJoin[0];
+  a.evJoin[1] = b->evJoin[1];
   return a;
 }
 
@@ -471,10 +480,11 @@ int nabo_cuda_batch_create(int dtype, int dim, int nClouds, const int64_t* point
   b->blockSize = p.threadsPerBlock > 0 ? p.threadsPerBlock : 128;
   b->splitRule = p.splitRule;
   b->lanesPerQuery = p.lanesPerQuery == 8 ? 8 : 1;
-  // 4 groups: host run of 512 clouds, 22 M queries, median of 10 calls: 2 groups
-  // 25.65 ms, 4 24.40, 8 24.67, 16 25.83 (each group searches with one launch
-  // per compiled top-k size)
-  b->groups = p.pipelineChunks > 0 ? p.pipelineChunks : 4;
+  // 8 groups: host run of 512 clouds, 22 M queries, median of 10 calls, each
+  // group searching with one launch per compiled top-k size side by side:
+  // 2 groups 25.05 ms, 4 23.46, 8 23.00, 16 23.29 (those launches one after
+  // another: 25.65, 24.40, 24.67, 25.83)
+  b->groups = p.pipelineChunks > 0 ? p.pipelineChunks : 8;
   if (b->blockSize != 32 && b->blockSize != 64 && b->blockSize != 128) {
     delete b;
     return set_error(kErrArgument, "threads per block must be 32, 64 or 128");
@@ -517,8 +527,10 @@ int nabo_cuda_batch_destroy(nabo_cuda_batch* b) {
   for (void* p : {(void*)b->dOff, b->recs, b->nodes, (void*)b->nodeOffset, b->rootBox, (void*)b->status, b->recs32,
                   (void*)b->coordMax, b->devClouds})
     if (p) cudaFree(p);
-  for (cudaStream_t st : {b->hostStream, b->copyStream})
+  for (cudaStream_t st : {b->hostStream, b->copyStream, b->aux[0], b->aux[1]})
     if (st) cudaStreamDestroy(st);
+  for (cudaEvent_t ev : {b->evFork, b->evJoin[0], b->evJoin[1]})
+    if (ev) cudaEventDestroy(ev);
   delete b;
   return kOk;
 }
@@ -580,6 +592,14 @@ int nabo_cuda_batch_set_queries(nabo_cuda_batch* b, const int64_t* queryCounts, 
     return cuda_error(e, "batch query plan");
   }
   e = make_class_plan(b, ks, qoff);
+  if (e == cudaSuccess && b->plan.groups > 1 && !b->evFork) {
+    // made once per batch, kept until it is destroyed
+    for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+      e = cudaStreamCreateWithFlags(&b->aux[i], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->evJoin[i], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->evFork, cudaEventDisableTiming);
+  }
   if (e != cudaSuccess) {
     free_query_plan(b);
     return cuda_error(e, "batch query groups");

@@ -200,6 +200,11 @@ struct BatchArgs {
   int lanesPerQuery;            // 1: one thread per query; 8: a lane group (k <= 32)
   const BatchClassPlan* classes;  // null or no groups: one launch sized for the largest k
   const int64_t* hQOffset;        // host copy of qOffset (to map a position range to clouds)
+  // streams and events for running the groups' launches side by side (all
+  // null: one after the other on the caller's stream)
+  cudaStream_t aux[2];
+  cudaEvent_t evFork;
+  cudaEvent_t evJoin[2];
 };
 template <typename T, int D>
 int knn_batch(const BatchArgs& b, cudaStream_t stream);

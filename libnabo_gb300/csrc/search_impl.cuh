@@ -469,12 +469,23 @@ int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t st
   case KK:                                                                                  \
     launch_kdtree<T, D, KK, kStackLarge>(g, b.blockSize, stream, G);                        \
     break;
+#define NABO_LAUNCH_ON(KK)                                                                  \
+  case KK:                                                                                  \
+    launch_kdtree<T, D, KK, kStackLarge>(g, b.blockSize, gs, G);                            \
+    break;
   const BatchClassPlan* cp = b.classes;
   if (K > 0 && cp && cp->groups > 0 && b.hQOffset) {
     // one launch per group of clouds sharing a compiled top-k size, over the
-    // group's clouds whose queries lie in [begin, end)
+    // group's clouds whose queries lie in [begin, end). The largest size
+    // goes first on the caller's stream, the others side by side on two
+    // more (forked from and joined back into it), so that their blocks fill
+    // the SMs the register-heavy largest one leaves free and its tail.
     const int64_t* qo = b.hQOffset;
-    for (int gi = 0; gi < cp->groups; ++gi) {
+    const bool fork = cp->groups > 1 && b.aux[0] && b.aux[1] && b.evFork && b.evJoin[0] && b.evJoin[1];
+    bool used[2] = {false, false};
+    int next = 0;
+    if (fork) NABO_CUDA_TRY(cudaEventRecord(b.evFork, stream));
+    for (int gi = cp->groups - 1; gi >= 0; --gi) {
       const int32_t* rc0 = cp->runCloud.data();
       const int* r0p = std::lower_bound(rc0 + cp->runBegin[gi], rc0 + cp->runBegin[gi + 1], 0,
                                         [&](int32_t c, int) { return qo[c] < begin; });
@@ -491,7 +502,19 @@ int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t st
       G.nq = cp->runPrefix[(size_t)r1] - cp->runPrefix[(size_t)r0];
       G.k = cp->K[(size_t)gi];
       const int g = ceil_div(G.nq, b.blockSize);
-      switch (round_k(cp->K[(size_t)gi])) { NABO_K_LIST(NABO_LAUNCH) }
+      cudaStream_t gs = stream;
+      if (fork && gi != cp->groups - 1) {
+        const int a = next++ & 1;
+        gs = b.aux[a];
+        if (!used[a]) NABO_CUDA_TRY(cudaStreamWaitEvent(gs, b.evFork, 0));
+        used[a] = true;
+      }
+      switch (round_k(cp->K[(size_t)gi])) { NABO_K_LIST(NABO_LAUNCH_ON) }
+    }
+    for (int a = 0; a < 2; ++a) {
+      if (!used[a]) continue;
+      NABO_CUDA_TRY(cudaEventRecord(b.evJoin[a], b.aux[a]));
+      NABO_CUDA_TRY(cudaStreamWaitEvent(stream, b.evJoin[a], 0));
     }
   } else if (K > 0) {
     KnnLaunch G = L;
@@ -499,6 +522,7 @@ int search_batch(const BatchArgs& b, int64_t begin, int64_t end, cudaStream_t st
     switch (K) { NABO_K_LIST(NABO_LAUNCH) }
   }
 #undef NABO_LAUNCH
+#undef NABO_LAUNCH_ON
   {
     KnnLaunch R = L;
     R.slab = b.slab;
