@@ -38,3 +38,26 @@ def test_cached_choice_needs_no_timing(tmp_path):
     again = A.tune(clouds, queries, [5, 16])  # now from memory, no file
     assert again["cached"] and again["bucketSize"] == 12
     A._cache.clear()
+
+
+def test_restricted_candidates_are_cached_under_their_own_key(tmp_path):
+    """A tuning restricted to some split rules or lanes per query is stored
+    apart from the unrestricted one (a restricted run must not answer an
+    unrestricted request, nor the reverse)."""
+    A = _autotune()
+    clouds = [np.zeros((1000, 8), np.float32), np.zeros((3000, 8), np.float32)]
+    queries = [c[:10] for c in clouds]
+    base = A.shape_key([1000, 3000], 8, np.float32, 32)
+    path = tmp_path / "tune.json"
+    path.write_text(json.dumps({
+        base: {"bucketSize": 8, "threadsPerBlock": 128, "maxLevels": 30, "sample_ms": 2.0},
+        base + "-l1": {"bucketSize": 16, "threadsPerBlock": 128, "maxLevels": 30, "sample_ms": 2.0},
+        base + "-s1-l1": {"bucketSize": 24, "threadsPerBlock": 64, "maxLevels": 30, "sample_ms": 2.0}}))
+    A._cache.clear()
+    got = A.tune(clouds, queries, 32, dim=8, cache_path=str(path), lanes=(1,), max_queries_per_cloud=5)
+    assert got["cached"] and got["key"] == base + "-l1" and got["bucketSize"] == 16
+    got = A.tune(clouds, queries, 32, dim=8, cache_path=str(path), split_rules=(1,), lanes=(1,))
+    assert got["key"] == base + "-s1-l1" and got["bucketSize"] == 24
+    got = A.tune(clouds, queries, 32, dim=8, cache_path=str(path))
+    assert got["key"] == base and got["bucketSize"] == 8
+    A._cache.clear()
