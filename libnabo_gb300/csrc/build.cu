@@ -1426,7 +1426,9 @@ __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, 
     __syncwarp();
     int sp = 1;
     int emitted = 0;
-    T lo[kMaxDim], hi[kMaxDim];
+    // the node's cell over the compiled dimensions (registers; entries past
+    // `dim` stay 0 and never win the widest-extent test)
+    T lo[D], hi[D];
     while (sp > 0) {
       --sp;
       const int e = base + sp;
@@ -1442,14 +1444,30 @@ __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, 
         __syncwarp();
         continue;
       }
-      for (int d = 0; d < dim; ++d) {
-        lo[d] = stk.boxLo[(int64_t)e * kMaxDim + d];
-        hi[d] = stk.boxHi[(int64_t)e * kMaxDim + d];
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        lo[d] = d < dim ? stk.boxLo[(int64_t)e * kMaxDim + d] : T(0);
+        hi[d] = d < dim ? stk.boxHi[(int64_t)e * kMaxDim + d] : T(0);
       }
-      const int cd = arg_max_extent(lo, hi, dim);
+      // argMax of the extents as arg_max_extent (first strict maximum)
+      int cd = 0;
+      T lcd = lo[0], hcd = hi[0];
+      {
+        T best = T(0);
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          const T ext = Ar<T>::sub(hi[d], lo[d]);
+          if (d < dim && ext > best) {
+            best = ext;
+            cd = d;
+            lcd = lo[d];
+            hcd = hi[d];
+          }
+        }
+      }
       Rec<T, D>* node = pts + st;
       const T ideal = splitRule == 1 ? next_up(warp_median(node, count, cd, lane))
-                                     : Ar<T>::mul(Ar<T>::add(hi[cd], lo[cd]), T(0.5));
+                                     : Ar<T>::mul(Ar<T>::add(hcd, lcd), T(0.5));
       T mn = std::numeric_limits<T>::max(), mx = std::numeric_limits<T>::lowest();
       for (int i = lane; i < count; i += 32) {
         const T v = node[i].p.c[cd];
@@ -1504,18 +1522,24 @@ __global__ void k_small(Rec<T, D>* recs, SmallSegs<T> small, const int* nSmall, 
         stk.count[f] = count - leftCount;
         stk.parent[f] = local;
         stk.depth[f] = depth + 1;
-        for (int d = 0; d < dim; ++d) {
-          stk.boxLo[(int64_t)f * kMaxDim + d] = d == cd ? cut : lo[d];
-          stk.boxHi[(int64_t)f * kMaxDim + d] = hi[d];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          if (d < dim) {
+            stk.boxLo[(int64_t)f * kMaxDim + d] = d == cd ? cut : lo[d];
+            stk.boxHi[(int64_t)f * kMaxDim + d] = hi[d];
+          }
         }
         f = base + sp + 1;
         stk.start[f] = st;
         stk.count[f] = leftCount;
         stk.parent[f] = -1;
         stk.depth[f] = depth + 1;
-        for (int d = 0; d < dim; ++d) {
-          stk.boxLo[(int64_t)f * kMaxDim + d] = lo[d];
-          stk.boxHi[(int64_t)f * kMaxDim + d] = d == cd ? cut : hi[d];
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          if (d < dim) {
+            stk.boxLo[(int64_t)f * kMaxDim + d] = lo[d];
+            stk.boxHi[(int64_t)f * kMaxDim + d] = d == cd ? cut : hi[d];
+          }
         }
       }
       sp += 2;
