@@ -24,16 +24,20 @@ def _clouds():
     from libnabo_gb300 import synthetic as S
     lidar = S.lidar_scan(n_azimuth=2400)
     c8, _, _ = S.clusters(30000, 8, 5, dtype=np.float64)
+    c16, _, _ = S.clusters(20000, 16, 6, dtype=np.float32)
     return {
         "uniform_f32": (S.uniform(50000, 3, seed=3), S.uniform(8000, 3, seed=4)),
         "lidar_f32": (lidar, S.lidar_queries(lidar)[:8000]),
         "clusters8_f64": (c8, (c8[:6000] + np.random.default_rng(6).normal(0, 0.01, (6000, 8))).astype(np.float64)),
         "uniform4_f32": (S.uniform(40000, 4, seed=7), S.uniform(6000, 4, seed=8)),
+        "uniform2_f32": (S.uniform(40000, 2, seed=11), S.uniform(6000, 2, seed=12)),
+        "clusters16_f32": (c16, (c16[:5000] + np.random.default_rng(13).normal(0, 0.01, (5000, 16))).astype(np.float32)),
         "uniform3_f64": (S.uniform(40000, 3, seed=9).astype(np.float64), S.uniform(6000, 3, seed=10).astype(np.float64)),
     }
 
 
-@pytest.mark.parametrize("name", ["uniform_f32", "lidar_f32", "clusters8_f64", "uniform4_f32", "uniform3_f64"])
+@pytest.mark.parametrize("name", ["uniform_f32", "lidar_f32", "clusters8_f64", "uniform4_f32", "uniform3_f64",
+                                  "uniform2_f32", "clusters16_f32"])
 @pytest.mark.parametrize("k", [1, 10, 40])
 def test_median_tree_search_is_exact(name, k):
     nb = _nb()
@@ -202,3 +206,29 @@ def test_median_tree_batch_with_ties_small_roots_and_level_limit(graph, levels):
             bucket = clouds[c].shape[0] if levels == 2 else 8
             assert_valid_tree(b.export_tree(c), clouds[c], bucket, label)
             assert_exact_up_to_ties(clouds[c], queries[c], int(ks[c]), bi[c], bd[c], label)
+
+
+def test_median_tree_batch_8d_is_exact():
+    """An 8-D float batch with the median split (the C4 batches' choice for
+    float): records of 48 bytes take the unstaged scatter."""
+    import torch
+    nb = _nb()
+    from libnabo_gb300 import synthetic as S
+    clouds, queries = [], []
+    for i, n in enumerate((2000, 9000, 300, 25000)):
+        c, centres, sig = S.clusters(n, 8, 70 + i, dtype=np.float32)
+        q, _, _ = S.clusters(700, 8, 90 + i, dtype=np.float32, centres=centres, sigmas=sig)
+        clouds.append(c)
+        queries.append(q)
+    ks = np.array([32, 5, 16, 32], np.int32)
+    b = nb.BatchSearch([c.shape[0] for c in clouds], dim=8, splitRule=1, bucketSize=16, maxLevels=40)
+    b.set_queries([q.shape[0] for q in queries], ks)
+    b.build(torch.from_numpy(np.concatenate(clouds)).cuda())
+    idx, d2 = b.knn(torch.from_numpy(np.concatenate(queries)).cuda())
+    torch.cuda.synchronize()
+    assert b.status()["ok"], b.status()
+    bi, bd = b.split(idx.cpu().numpy()), b.split(d2.cpu().numpy())
+    for c in range(len(clouds)):
+        assert_valid_tree(b.export_tree(c), clouds[c], 16, f"8-D median batch cloud {c}")
+        oi, od, _ = O.bf_knn(clouds[c], queries[c], int(ks[c]), mode=O.MODE_CANONICAL)
+        H.assert_identical(bi[c], bd[c], oi, od, f"8-D median batch cloud {c}")
