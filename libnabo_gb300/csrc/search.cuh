@@ -88,6 +88,110 @@ struct TopK {
   }
 };
 
+// double lists of 16 or more entries in the kd-tree search: a binary
+// max-heap of (dist2 bits, index) in shared memory, slot-major with one
+// column per thread (blocks of at most kHeapThreads threads), the root kept
+// in registers for the accept test. Held in registers, such a list (3
+// registers an entry) spilled under the search kernel's register cap, and
+// every insertion walked the spilled entries through local memory (8-D,
+// k = 32: 2.2 G local loads a launch). Here an insertion sifts down at most
+// log2(k) levels. The entries and their order are those of TopK: the k
+// smallest (dist2, index) pairs, empty entries (+inf, -1), written out in
+// ascending order.
+constexpr int kHeapThreads = 128;
+template <int K>
+struct SmemTopK {
+  unsigned long long* d;  // entry j of this thread's list at d[j * kHeapThreads]
+  int* ix;
+  int n;
+  unsigned long long rootD;
+  int rootI;
+  static __device__ __forceinline__ bool greater(unsigned long long da, int ia, unsigned long long db, int ib) {
+    return da > db || (da == db && ia > ib);
+  }
+  static __device__ __forceinline__ unsigned long long bits(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+  }
+  __device__ __forceinline__ void init(int k) {
+    __shared__ unsigned long long sd[K * kHeapThreads];
+    __shared__ int si[K * kHeapThreads];
+    d = sd + threadIdx.x;
+    ix = si + threadIdx.x;
+    n = k < K ? k : K;
+    rootD = bits(Ar<double>::inf());
+    rootI = -1;
+    for (int j = 0; j < n; ++j) {
+      d[j * kHeapThreads] = rootD;
+      ix[j * kHeapThreads] = -1;
+    }
+  }
+  __device__ __forceinline__ double head() const { return __longlong_as_double((long long)rootD); }
+  __device__ __forceinline__ bool accepts(double dist, int idx) const { return greater(rootD, rootI, bits(dist), idx); }
+  // The root (the largest entry) drops out and (x, xi) sifts down from it
+  // within the first m entries.
+  __device__ __forceinline__ void sift(unsigned long long x, int xi, int m) {
+    int j = 0;
+    for (;;) {
+      const int l = 2 * j + 1;
+      if (l >= m) break;
+      int c = l;
+      unsigned long long cd = d[l * kHeapThreads];
+      int ci = ix[l * kHeapThreads];
+      if (l + 1 < m) {
+        const unsigned long long rd = d[(l + 1) * kHeapThreads];
+        const int ri = ix[(l + 1) * kHeapThreads];
+        if (greater(rd, ri, cd, ci)) {
+          c = l + 1;
+          cd = rd;
+          ci = ri;
+        }
+      }
+      if (!greater(cd, ci, x, xi)) break;
+      d[j * kHeapThreads] = cd;
+      ix[j * kHeapThreads] = ci;
+      j = c;
+    }
+    d[j * kHeapThreads] = x;
+    ix[j * kHeapThreads] = xi;
+  }
+  // Drops the largest entry and inserts (dist, idx); requires accepts(dist, idx).
+  __device__ __forceinline__ void insert(double dist, int idx) {
+    sift(bits(dist), idx, n);
+    rootD = d[0];
+    rootI = ix[0];
+  }
+  __device__ __forceinline__ int count(int) const {
+    int c = 0;
+    for (int j = 0; j < n; ++j) c += ix[j * kHeapThreads] >= 0 ? 1 : 0;
+    return c;
+  }
+  // Writes the entries in ascending order (the largest last), emptying the
+  // heap; returns how many are valid.
+  __device__ __forceinline__ int store(int, int32_t* __restrict__ oi, double* __restrict__ od) {
+    int found = 0;
+    for (int m = n; m > 0; --m) {
+      const unsigned long long top = d[0];
+      const int ti = ix[0];
+      oi[m - 1] = ti;
+      od[m - 1] = __longlong_as_double((long long)top);
+      found += ti >= 0 ? 1 : 0;
+      if (m > 1) sift(d[(m - 1) * kHeapThreads], ix[(m - 1) * kHeapThreads], m - 1);
+    }
+    return found;
+  }
+};
+
+// The list the kd-tree search keeps: shared-memory heaps for double lists
+// of 16 or more entries, registers otherwise.
+template <typename T, int K>
+struct SearchHeap {
+  using type = TopK<T, K>;
+};
+template <int K>
+struct SearchHeap<double, K> {
+  using type = std::conditional_t<(K >= 16), SmemTopK<K>, TopK<double, K>>;
+};
+
 // float: one 64-bit key per entry, (bit pattern of dist2) << 32 | index.
 // Distances are >= 0, where the IEEE bit pattern orders like the value, so
 // one unsigned comparison orders (dist2, index). An empty slot is
@@ -327,9 +431,9 @@ struct LeafFilter<double, D> {
   }
 };
 
-template <typename T, int D, int K>
+template <typename T, int D, int K, typename H>
 __device__ __forceinline__ void scan_leaf(const Rec<T, D>* __restrict__ recs, uint32_t st, uint32_t cnt,
-                                          const T (&q)[D], T maxRadius2, T minDist, bool want, TopK<T, K>& heap,
+                                          const T (&q)[D], T maxRadius2, T minDist, bool want, H& heap,
                                           const LeafFilter<T, D>& flt) {
   constexpr int kChunk = 4;
   for (uint32_t base = 0; base < cnt; base += kChunk) {
@@ -612,7 +716,7 @@ __device__ __forceinline__ void knn_query(const KnnLaunch& a, int64_t t, S& stk,
     mayFall = a.fallbackRadius >= 0.0 && (double)r < a.fallbackRadius;
   }
   const T maxError2 = (T)a.maxError2;
-  TopK<T, K> heap;
+  typename SearchHeap<T, K>::type heap;
   heap.init(k);
   LeafFilter<T, D> flt;
   flt.init(a.recs32, a.coordMax, q);
