@@ -161,15 +161,26 @@ __device__ __forceinline__ uint32_t morton_key(const T* __restrict__ q, int64_t 
 }
 
 // ---- stable LSD radix sort of (key, value) pairs, 10-bit digits.
-// Each warp owns a tile of `rounds` x 32 consecutive elements. Pass p:
-// k_radix_hist counts the tile's digits; the counts, laid out digit-major
-// ([digit][tile]), are scanned into the tile's first output slot per digit;
-// k_radix_scatter walks the tile in element order, 32 at a time, ranking
-// equal digits inside the 32 with __match_any_sync, so equal keys keep their
-// order (stability, which LSD needs across passes).
+// A block of kTileWarps warps owns a tile of kTile consecutive elements,
+// warp w the w-th run of kWarpRounds x 32 of them. Pass p: k_tile_hist
+// counts the tile's digits into hist[tile][digit] (tile-major, so each
+// block writes one contiguous row); k_tile_scan turns every digit's column
+// into exclusive prefixes over the tiles and the digit totals;
+// k_tile_scatter re-counts each warp's run into a warp-private histogram,
+// offsets the warps of the tile one after another, and walks each run in
+// element order, 32 at a time, ranking equal digits inside the 32 with
+// __match_any_sync, so equal keys keep their order (stability, which LSD
+// needs across passes).
 constexpr int kRadixBits = 10;
 constexpr int kRadix = 1 << kRadixBits;
-constexpr int kSortWarps = 4;
+constexpr int kTileWarps = 8;
+constexpr int kTileThreads = 32 * kTileWarps;
+constexpr int kWarpRounds = 16;
+constexpr int kWarpSpan = 32 * kWarpRounds;
+constexpr int kTile = kTileWarps * kWarpSpan;
+constexpr int kDigitsPerThread = kRadix / kTileThreads;
+static_assert(kRadix % kTileThreads == 0, "digits split evenly over the tile's threads");
+static_assert(kTileThreads == kB, "block_excl_scan_u32 scans kB threads");
 
 // Adds each distinct digit of the 32 live lanes once (equal digits are
 // common: the keys are spatially sorted after the first pass).
@@ -181,75 +192,67 @@ __device__ __forceinline__ void count_digit(uint32_t* h, bool act, uint32_t d) {
   }
 }
 
-// Loads of kPre rounds are issued before their processing, so a warp
-// keeps that many memory requests in flight (there are few warps: one per
-// tile).
-constexpr int kPre = 8;
+// Element u of the calling lane's run: all of a warp's loads are issued
+// before any is used, so each warp keeps kWarpRounds requests in flight.
+__device__ __forceinline__ int64_t run_index(int u) {
+  return (int64_t)blockIdx.x * kTile + (threadIdx.x >> 5) * kWarpSpan + u * 32 + (threadIdx.x & 31);
+}
 
-__global__ void k_radix_hist(const uint32_t* __restrict__ key, int64_t n, int shift, int rounds, int64_t nTiles,
-                             uint32_t* hist) {
-  extern __shared__ uint32_t sh[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t tile = (int64_t)blockIdx.x * kSortWarps + warp;
-  if (tile >= nTiles) return;  // warp-uniform
-  uint32_t* h = sh + warp * kRadix;
-  for (int d = lane; d < kRadix; d += 32) h[d] = 0u;
-  __syncwarp();
-  const int64_t base = tile * rounds * 32;
-  for (int r0 = 0; r0 < rounds; r0 += kPre) {
-    if (base + (int64_t)r0 * 32 >= n) break;  // warp-uniform
-    uint32_t kk[kPre];
+// Writes the block's digit counts as the tile's row of hist.
+__device__ __forceinline__ void store_tile_row(const uint32_t* h, uint32_t* hist) {
+  __syncthreads();
+  uint32_t* row = hist + (int64_t)blockIdx.x * kRadix;
+  for (int d = threadIdx.x; d < kRadix; d += kTileThreads) row[d] = h[d];
+}
+
+__global__ void __launch_bounds__(kTileThreads) k_tile_hist(const uint32_t* __restrict__ key, int64_t n, int shift,
+                                                            uint32_t* hist) {
+  __shared__ uint32_t h[kRadix];
+  for (int d = threadIdx.x; d < kRadix; d += kTileThreads) h[d] = 0u;
+  __syncthreads();
+  uint32_t kk[kWarpRounds];
 #pragma unroll
-    for (int u = 0; u < kPre; ++u) {
-      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
-      kk[u] = i < n ? key[i] : 0u;
-    }
-#pragma unroll
-    for (int u = 0; u < kPre; ++u) {
-      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
-      count_digit(h, i < n, (kk[u] >> shift) & (kRadix - 1));
-    }
+  for (int u = 0; u < kWarpRounds; ++u) {
+    const int64_t i = run_index(u);
+    kk[u] = i < n ? key[i] : 0u;
   }
-  __syncwarp();
-  for (int d = lane; d < kRadix; d += 32) hist[(int64_t)d * nTiles + tile] = h[d];
+#pragma unroll
+  for (int u = 0; u < kWarpRounds; ++u) count_digit(h, run_index(u) < n, (kk[u] >> shift) & (kRadix - 1));
+  store_tile_row(h, hist);
 }
 
 // Morton keys of the queries, in the radix sort's tile layout, with the
 // first pass's digit counts.
 template <typename T>
-__global__ void k_morton_tiles(const T* __restrict__ q, int64_t n, int64_t qStride, CellParams p, int rounds,
-                               int64_t nTiles, uint32_t* key, uint32_t* hist) {
-  extern __shared__ uint32_t sh[];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t tile = (int64_t)blockIdx.x * kSortWarps + warp;
-  if (tile >= nTiles) return;  // warp-uniform
-  uint32_t* h = sh + warp * kRadix;
-  for (int d = lane; d < kRadix; d += 32) h[d] = 0u;
-  __syncwarp();
-  const int64_t base = tile * rounds * 32;
-  for (int r0 = 0; r0 < rounds; r0 += kPre) {
-    if (base + (int64_t)r0 * 32 >= n) break;  // warp-uniform
-    uint32_t kk[kPre];
-    if (p.dims <= 3) {
-      T c[kPre][3];
+__global__ void __launch_bounds__(kTileThreads) k_morton_tiles(const T* __restrict__ q, int64_t n, int64_t qStride,
+                                                               CellParams p, uint32_t* key, uint32_t* hist) {
+  __shared__ uint32_t h[kRadix];
+  for (int d = threadIdx.x; d < kRadix; d += kTileThreads) h[d] = 0u;
+  __syncthreads();
+  constexpr int kHalf = kWarpRounds / 2;  // coordinates of half the run in flight at once
 #pragma unroll
-      for (int u = 0; u < kPre; ++u) {
-        const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+  for (int r0 = 0; r0 < kWarpRounds; r0 += kHalf) {
+    uint32_t kk[kHalf];
+    if (p.dims <= 3) {
+      T c[kHalf][3];
+#pragma unroll
+      for (int u = 0; u < kHalf; ++u) {
+        const int64_t i = run_index(r0 + u);
 #pragma unroll
         for (int d = 0; d < 3; ++d) c[u][d] = (i < n && d < p.dims) ? q[i * qStride + d] : T(0);
       }
 #pragma unroll
-      for (int u = 0; u < kPre; ++u) kk[u] = morton_key3(c[u], p);
+      for (int u = 0; u < kHalf; ++u) kk[u] = morton_key3(c[u], p);
     } else {
 #pragma unroll
-      for (int u = 0; u < kPre; ++u) {
-        const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+      for (int u = 0; u < kHalf; ++u) {
+        const int64_t i = run_index(r0 + u);
         kk[u] = i < n ? morton_key(q, i, qStride, p) : 0u;
       }
     }
 #pragma unroll
-    for (int u = 0; u < kPre; ++u) {
-      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
+    for (int u = 0; u < kHalf; ++u) {
+      const int64_t i = run_index(r0 + u);
       if (p.nChunks > 1) {
         uint32_t cid = 0;
         for (int c = 0; c + 1 < p.nChunks; ++c) cid += i >= p.chunkEnd[c] ? 1u : 0u;
@@ -259,94 +262,115 @@ __global__ void k_morton_tiles(const T* __restrict__ q, int64_t n, int64_t qStri
       count_digit(h, i < n, kk[u] & (kRadix - 1));
     }
   }
-  __syncwarp();
-  for (int d = lane; d < kRadix; d += 32) hist[(int64_t)d * nTiles + tile] = h[d];
+  store_tile_row(h, hist);
 }
 
-// One block per digit: exclusive scan, in place, of the digit's counts over
-// the tiles (hist[digit][tile]); the digit's total goes to total[digit].
-__global__ void k_digit_scan(uint32_t* hist, int64_t nTiles, uint32_t* total) {
-  uint32_t* row = hist + (int64_t)blockIdx.x * nTiles;
-  const int64_t per = (nTiles + kB - 1) / kB;
-  const int64_t b0 = threadIdx.x * per;
-  const int64_t b1 = b0 + per < nTiles ? b0 + per : nTiles;
+// Block b handles digits [32 b, 32 b + 32), one per lane; warp g of the
+// block covers a contiguous range of tiles, so every load reads 32
+// consecutive counts of one tile's row. Rewrites hist[tile][digit] in place
+// as the count of the digit in the earlier tiles; the digit's total goes to
+// total[digit].
+constexpr int kScanGroups = 32;
+__global__ void __launch_bounds__(32 * kScanGroups) k_tile_scan(uint32_t* hist, int64_t nTiles, uint32_t* total) {
+  __shared__ uint32_t part[kScanGroups][32];
+  const int lane = threadIdx.x & 31, g = threadIdx.x >> 5;
+  const int d = blockIdx.x * 32 + lane;
+  const int64_t per = (nTiles + kScanGroups - 1) / kScanGroups;
+  const int64_t t0 = g * per;
+  const int64_t t1 = t0 + per < nTiles ? t0 + per : nTiles;
   uint32_t run = 0;
-  for (int64_t i = b0; i < b1; ++i) run += row[i];
-  uint32_t t;
-  uint32_t carry = block_excl_scan_u32(run, &t);
-  for (int64_t i = b0; i < b1; ++i) {
-    const uint32_t v = row[i];
-    row[i] = carry;
+  for (int64_t t = t0; t < t1; ++t) run += hist[t * kRadix + d];
+  part[g][lane] = run;
+  __syncthreads();
+  uint32_t carry = 0;
+  for (int h = 0; h < g; ++h) carry += part[h][lane];
+  if (g == kScanGroups - 1) total[d] = carry + run;
+  for (int64_t t = t0; t < t1; ++t) {
+    const uint32_t v = hist[t * kRadix + d];
+    hist[t * kRadix + d] = carry;
     carry += v;
   }
-  if (threadIdx.x == 0) total[blockIdx.x] = t;
 }
 
-__global__ void k_radix_scatter(const uint32_t* __restrict__ keyIn, const uint32_t* __restrict__ valIn, int64_t n,
-                                int shift, int rounds, int64_t nTiles, const uint32_t* __restrict__ offs,
-                                const uint32_t* __restrict__ total, uint32_t* keyOut, uint32_t* valOut) {
-  extern __shared__ uint32_t sh[];
+// offs = the scanned hist (hist[tile][digit] = the digit's count in the
+// earlier tiles), total = the digit totals.
+__global__ void __launch_bounds__(kTileThreads)
+    k_tile_scatter(const uint32_t* __restrict__ keyIn, const uint32_t* __restrict__ valIn, int64_t n, int shift,
+                   const uint32_t* __restrict__ offs, const uint32_t* __restrict__ total, uint32_t* keyOut,
+                   uint32_t* valOut) {
+  __shared__ uint32_t wh[kTileWarps][kRadix];  // counts, then first output slots, per warp and digit
+  __shared__ uint32_t first[kRadix];           // the tile's first output slot per digit
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t tile = (int64_t)blockIdx.x * kSortWarps + warp;
-  if (tile >= nTiles) return;  // warp-uniform
-  uint32_t* h = sh + warp * kRadix;
-  // first slot of each digit for this tile: the totals of the smaller
-  // digits (lane l sums digits [32 l, 32 l + 32), a warp scan joins the
-  // lanes) plus the earlier tiles' counts of the digit
+  uint32_t kk[kWarpRounds], vv[kWarpRounds];
+#pragma unroll
+  for (int u = 0; u < kWarpRounds; ++u) {
+    const int64_t i = run_index(u);
+    kk[u] = i < n ? keyIn[i] : 0u;
+    vv[u] = i < n ? (valIn ? valIn[i] : (uint32_t)i) : 0u;
+  }
+  // the tile's first slot per digit: the totals of the smaller digits
+  // (thread t holds digits [kDigitsPerThread t, kDigitsPerThread (t+1)))
+  // plus the earlier tiles' counts of the digit
   {
-    constexpr int kPer = kRadix / 32;
-    uint32_t tv[kPer];
+    uint32_t tv[kDigitsPerThread];
     uint32_t run = 0;
 #pragma unroll
-    for (int j = 0; j < kPer; ++j) {
-      tv[j] = total[lane * kPer + j];
+    for (int j = 0; j < kDigitsPerThread; ++j) {
+      tv[j] = total[threadIdx.x * kDigitsPerThread + j];
       run += tv[j];
     }
-    uint32_t inc = run;
+    uint32_t all;
+    uint32_t carry = block_excl_scan_u32(run, &all);
+    const uint32_t* row = offs + (int64_t)blockIdx.x * kRadix;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-      if (lane >= o) inc += y;
-    }
-    uint32_t carry = inc - run;
-#pragma unroll
-    for (int j = 0; j < kPer; ++j) {
-      const int d = lane * kPer + j;
-      h[d] = carry + offs[(int64_t)d * nTiles + tile];
+    for (int j = 0; j < kDigitsPerThread; ++j) {
+      const int d = threadIdx.x * kDigitsPerThread + j;
+      first[d] = carry + row[d];
       carry += tv[j];
     }
   }
+  for (int d = lane; d < kRadix; d += 32) wh[warp][d] = 0u;
   __syncwarp();
-  const uint32_t below = (1u << lane) - 1u;
-  const int64_t base = tile * rounds * 32;
-  for (int r0 = 0; r0 < rounds; r0 += kPre) {
-    if (base + (int64_t)r0 * 32 >= n) break;  // warp-uniform
-    uint32_t kk[kPre], vv[kPre];
+  // each warp counts its own run; the equal-digit peers of every round are
+  // kept for the ranking below
+  unsigned peers[kWarpRounds];
 #pragma unroll
-    for (int u = 0; u < kPre; ++u) {
-      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
-      kk[u] = i < n ? keyIn[i] : 0u;
-      vv[u] = i < n ? (valIn ? valIn[i] : (uint32_t)i) : 0u;
-    }
-#pragma unroll
-    for (int u = 0; u < kPre; ++u) {
-      const int64_t i = base + (int64_t)(r0 + u) * 32 + lane;
-      const bool act = i < n;
-      const unsigned live = __ballot_sync(0xffffffffu, act);
-      if (live == 0u) break;  // warp-uniform: the tile's tail is past n
+  for (int u = 0; u < kWarpRounds; ++u) {
+    const bool act = run_index(u) < n;
+    const unsigned live = __ballot_sync(0xffffffffu, act);
+    peers[u] = 0u;
+    if (act) {
       const uint32_t d = (kk[u] >> shift) & (kRadix - 1);
-      uint32_t peers = 0u, pos = 0u;
-      if (act) {
-        peers = __match_any_sync(live, d);
-        pos = h[d] + __popc(peers & below);
-      }
-      __syncwarp();
-      if (act && lane == 31 - __clz(peers)) h[d] += __popc(peers);
-      __syncwarp();
-      if (act) {
-        if (keyOut) keyOut[pos] = kk[u];
-        valOut[pos] = vv[u];
-      }
+      peers[u] = __match_any_sync(live, d);
+      if (lane == __ffs(peers[u]) - 1) atomicAdd(&wh[warp][d], (uint32_t)__popc(peers[u]));
+    }
+  }
+  __syncthreads();
+  // warps of the tile one after another: warp w's first slot per digit
+#pragma unroll
+  for (int j = 0; j < kDigitsPerThread; ++j) {
+    const int d = threadIdx.x * kDigitsPerThread + j;
+    uint32_t run = first[d];
+#pragma unroll
+    for (int w = 0; w < kTileWarps; ++w) {
+      const uint32_t c = wh[w][d];
+      wh[w][d] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  const uint32_t below = (1u << lane) - 1u;
+#pragma unroll
+  for (int u = 0; u < kWarpRounds; ++u) {
+    const bool act = peers[u] != 0u;  // an active lane is its own peer
+    const uint32_t d = (kk[u] >> shift) & (kRadix - 1);
+    const uint32_t pos = act ? wh[warp][d] + __popc(peers[u] & below) : 0u;
+    __syncwarp();
+    if (act && lane == 31 - __clz(peers[u])) wh[warp][d] += __popc(peers[u]);
+    __syncwarp();
+    if (act) {
+      if (keyOut) keyOut[pos] = kk[u];
+      valOut[pos] = vv[u];
     }
   }
 }
@@ -457,17 +481,14 @@ int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist
 
 namespace {
 
-// Tiles of at least 32 rounds of 32 elements, few enough that the
-// [digit][tile] counts stay below 2^26 entries.
+// One block per tile of kTile elements; the [tile][digit] counts take one
+// byte per element.
 struct SortPlan {
-  int rounds = 32;
   int64_t nTiles = 0;
   int blocks = 0;
-  size_t smem = (size_t)kSortWarps * kRadix * sizeof(uint32_t);
   explicit SortPlan(int64_t n) {
-    while (ceil_div(n, (int64_t)rounds * 32) * (int64_t)kRadix > (int64_t(1) << 26)) rounds *= 2;
-    nTiles = ceil_div(n, (int64_t)rounds * 32);
-    blocks = (int)ceil_div(nTiles, (int64_t)kSortWarps);
+    nTiles = ceil_div(n, (int64_t)kTile);
+    blocks = (int)nTiles;
   }
 };
 
@@ -490,12 +511,11 @@ int radix_passes(uint32_t* dKeys, int64_t n, int bits, const uint32_t* dVals, in
   for (int p = 0; p < passes && rc == kOk; ++p) {
     const int shift = p * kRadixBits;
     const bool last = p == passes - 1;
-    if (p > 0 || !firstCounted)
-      k_radix_hist<<<P.blocks, 32 * kSortWarps, P.smem, stream>>>(kin, n, shift, P.rounds, P.nTiles, hist);
-    k_digit_scan<<<kRadix, kB, 0, stream>>>(hist, P.nTiles, totals);
+    if (p > 0 || !firstCounted) k_tile_hist<<<P.blocks, kTileThreads, 0, stream>>>(kin, n, shift, hist);
+    k_tile_scan<<<kRadix / 32, 32 * kScanGroups, 0, stream>>>(hist, P.nTiles, totals);
     uint32_t* vout = last ? reinterpret_cast<uint32_t*>(dOrder) : vbuf[p & 1];
-    k_radix_scatter<<<P.blocks, 32 * kSortWarps, P.smem, stream>>>(kin, vin, n, shift, P.rounds, P.nTiles, hist,
-                                                                    totals, last ? nullptr : kout, vout);
+    k_tile_scatter<<<P.blocks, kTileThreads, 0, stream>>>(kin, vin, n, shift, hist, totals,
+                                                           last ? nullptr : kout, vout);
     e = cudaGetLastError();
     if (e != cudaSuccess) rc = cuda_error(e, "radix sort");
     std::swap(kin, kout);
@@ -553,8 +573,7 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
   if (e == cudaSuccess) e = scratch_alloc((void**)&hist, (size_t)(kRadix * P.nTiles) * sizeof(uint32_t), stream);
   int rc = e == cudaSuccess ? kOk : cuda_error(e, "order scratch");
   if (rc == kOk) {
-    k_morton_tiles<T><<<P.blocks, 32 * kSortWarps, P.smem, stream>>>(dQuery, nq, qStride, p, P.rounds, P.nTiles,
-                                                                      keys, hist);
+    k_morton_tiles<T><<<P.blocks, kTileThreads, 0, stream>>>(dQuery, nq, qStride, p, keys, hist);
     rc = radix_passes(keys, nq, p.bits * p.dims + chunkBits, nullptr, dOrder, P, hist, true, stream);
   }
   if (keys) scratch_free(keys, stream);
