@@ -24,7 +24,7 @@ namespace nabo_gb300 {
 namespace {
 
 constexpr int kB = 256;
-constexpr int kMortonDims = 10;
+constexpr int kMortonDims = 3;
 
 __device__ __forceinline__ uint32_t block_excl_scan_u32(uint32_t v, uint32_t* total) {
   __shared__ uint32_t sw[kB / 32];
@@ -119,7 +119,20 @@ __device__ __forceinline__ uint32_t spread3_10(uint32_t x) {
   return x;
 }
 
-// Morton code of up to 3 coordinates already loaded.
+// bit b of x (x < 2^16) to bit 2b
+__device__ __forceinline__ uint32_t spread2_16(uint32_t x) {
+  x &= 0xffffu;
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+// Morton code of up to 3 coordinates already loaded: bit b of dimension d
+// lands at b * dims + (dims - 1 - d). order_queries() keeps dims <= 3 and
+// bits <= 30 / dims (fewer when the chunk number takes the top of the key),
+// so one of the spread forms below always applies.
 template <typename T>
 __device__ __forceinline__ uint32_t morton_key3(const T (&x)[3], const CellParams& p) {
   uint32_t c[3];
@@ -130,34 +143,9 @@ __device__ __forceinline__ uint32_t morton_key3(const T (&x)[3], const CellParam
     v = fminf(fmaxf(v, 0.0f), maxc);  // NaN -> 0
     c[d] = d < p.dims ? (uint32_t)v : 0u;
   }
-  if (p.dims == 3 && p.bits == 10) return (spread3_10(c[0]) << 2) | (spread3_10(c[1]) << 1) | spread3_10(c[2]);
-  uint32_t k = 0;
-  for (int b = p.bits - 1; b >= 0; --b)
-    for (int d = 0; d < p.dims; ++d) k = (k << 1) | ((c[d] >> b) & 1u);
-  return k;
-}
-
-// Morton code: bit b of dimension d lands at b * dims + (dims - 1 - d).
-template <typename T>
-__device__ __forceinline__ uint32_t morton_key(const T* __restrict__ q, int64_t i, int64_t qStride,
-                                               const CellParams& p) {
-  uint32_t c[kMortonDims];
-  const float maxc = (float)((1u << p.bits) - 1u);
-#pragma unroll
-  for (int d = 0; d < kMortonDims; ++d) {
-    if (d < p.dims) {
-      float v = ((float)q[i * qStride + d] - p.lo[d]) * p.scale[d];
-      v = fminf(fmaxf(v, 0.0f), maxc);  // NaN -> 0
-      c[d] = (uint32_t)v;
-    } else {
-      c[d] = 0;
-    }
-  }
-  if (p.dims == 3 && p.bits == 10) return (spread3_10(c[0]) << 2) | (spread3_10(c[1]) << 1) | spread3_10(c[2]);
-  uint32_t k = 0;
-  for (int b = p.bits - 1; b >= 0; --b)
-    for (int d = 0; d < p.dims; ++d) k = (k << 1) | ((c[d] >> b) & 1u);
-  return k;
+  if (p.dims == 3) return (spread3_10(c[0]) << 2) | (spread3_10(c[1]) << 1) | spread3_10(c[2]);
+  if (p.dims == 2) return (spread2_16(c[0]) << 1) | spread2_16(c[1]);
+  return c[0] & ((1u << p.bits) - 1u);  // maxc may round up to 2^bits in float
 }
 
 // ---- stable LSD radix sort of (key, value) pairs, 10-bit digits.
@@ -175,7 +163,7 @@ constexpr int kRadixBits = 10;
 constexpr int kRadix = 1 << kRadixBits;
 constexpr int kTileWarps = 8;
 constexpr int kTileThreads = 32 * kTileWarps;
-constexpr int kWarpRounds = 16;
+constexpr int kWarpRounds = 8;
 constexpr int kWarpSpan = 32 * kWarpRounds;
 constexpr int kTile = kTileWarps * kWarpSpan;
 constexpr int kDigitsPerThread = kRadix / kTileThreads;
@@ -229,27 +217,19 @@ __global__ void __launch_bounds__(kTileThreads) k_morton_tiles(const T* __restri
   __shared__ uint32_t h[kRadix];
   for (int d = threadIdx.x; d < kRadix; d += kTileThreads) h[d] = 0u;
   __syncthreads();
-  constexpr int kHalf = kWarpRounds / 2;  // coordinates of half the run in flight at once
+  constexpr int kHalf = kWarpRounds > 8 ? kWarpRounds / 2 : kWarpRounds;  // coordinates in flight at once
 #pragma unroll
   for (int r0 = 0; r0 < kWarpRounds; r0 += kHalf) {
     uint32_t kk[kHalf];
-    if (p.dims <= 3) {
-      T c[kHalf][3];
+    T c[kHalf][3];
 #pragma unroll
-      for (int u = 0; u < kHalf; ++u) {
-        const int64_t i = run_index(r0 + u);
+    for (int u = 0; u < kHalf; ++u) {
+      const int64_t i = run_index(r0 + u);
 #pragma unroll
-        for (int d = 0; d < 3; ++d) c[u][d] = (i < n && d < p.dims) ? q[i * qStride + d] : T(0);
-      }
-#pragma unroll
-      for (int u = 0; u < kHalf; ++u) kk[u] = morton_key3(c[u], p);
-    } else {
-#pragma unroll
-      for (int u = 0; u < kHalf; ++u) {
-        const int64_t i = run_index(r0 + u);
-        kk[u] = i < n ? morton_key(q, i, qStride, p) : 0u;
-      }
+      for (int d = 0; d < 3; ++d) c[u][d] = (i < n && d < p.dims) ? q[i * qStride + d] : T(0);
     }
+#pragma unroll
+    for (int u = 0; u < kHalf; ++u) kk[u] = morton_key3(c[u], p);
 #pragma unroll
     for (int u = 0; u < kHalf; ++u) {
       const int64_t i = run_index(r0 + u);
@@ -481,33 +461,74 @@ int order_by_cells(const uint32_t* dCell, const uint32_t* dRank, uint32_t* dHist
 
 namespace {
 
-// One block per tile of kTile elements; the [tile][digit] counts take one
-// byte per element.
+// One block per tile of kTile elements; the [tile][digit] counts take
+// 4 kRadix / kTile bytes per element. (Tiles of 2048: 562 blocks for a
+// million keys, twice the warps of 4096-element tiles to hide the ranking
+// loop's shared-memory latency.) The sort's scratch is one allocation (a call makes one
+// stream-ordered allocation and one free instead of six of each): the
+// keys when the sort makes them, the counts, the digit totals, a second
+// key array and two value arrays, each on a 256-byte boundary.
 struct SortPlan {
   int64_t nTiles = 0;
   int blocks = 0;
-  explicit SortPlan(int64_t n) {
+  size_t offKeys = 0, offHist = 0, offTotals = 0, offK2 = 0, offV1 = 0, offV2 = 0, bytes = 0;
+  SortPlan(int64_t n, bool ownKeys) {
     nTiles = ceil_div(n, (int64_t)kTile);
     blocks = (int)nTiles;
+    const auto take = [this](size_t b) {
+      const size_t at = bytes;
+      bytes += (b + 255) & ~size_t(255);
+      return at;
+    };
+    const size_t row = (size_t)n * sizeof(uint32_t);
+    if (ownKeys) offKeys = take(row);
+    offHist = take((size_t)nTiles * kRadix * sizeof(uint32_t));
+    offTotals = take((size_t)kRadix * sizeof(uint32_t));
+    offK2 = take(row);
+    offV1 = take(row);
+    offV2 = take(row);
+  }
+};
+
+struct SortScratch {
+  void* block = nullptr;
+  uint32_t *keys = nullptr, *hist = nullptr, *totals = nullptr, *k2 = nullptr, *v1 = nullptr, *v2 = nullptr;
+  cudaError_t alloc(const SortPlan& P, bool ownKeys, cudaStream_t stream) {
+    const cudaError_t e = scratch_alloc(&block, P.bytes, stream);
+    if (e != cudaSuccess) {
+      block = nullptr;
+      return e;
+    }
+    char* b = static_cast<char*>(block);
+    const auto at = [b](size_t off) { return reinterpret_cast<uint32_t*>(b + off); };
+    if (ownKeys) keys = at(P.offKeys);
+    hist = at(P.offHist);
+    totals = at(P.offTotals);
+    k2 = at(P.offK2);
+    v1 = at(P.offV1);
+    v2 = at(P.offV2);
+    return cudaSuccess;
+  }
+  void release(cudaStream_t stream) {
+    if (block) scratch_free(block, stream);
+    block = nullptr;
   }
 };
 
 // The radix passes over dKeys (clobbered). Pass 0 takes the values from
 // dVals or, if null, the element indices; its digit counts are already in
-// `hist` when `firstCounted`. The last pass writes the values to dOrder.
+// S.hist when `firstCounted`. The last pass writes the values to dOrder.
 int radix_passes(uint32_t* dKeys, int64_t n, int bits, const uint32_t* dVals, int32_t* dOrder, const SortPlan& P,
-                 uint32_t* hist, bool firstCounted, cudaStream_t stream) {
+                 const SortScratch& S, bool firstCounted, cudaStream_t stream) {
   const int passes = std::max(1, (bits + kRadixBits - 1) / kRadixBits);
-  uint32_t *k2 = nullptr, *v1 = nullptr, *v2 = nullptr, *totals = nullptr;
-  cudaError_t e = scratch_alloc((void**)&totals, (size_t)kRadix * sizeof(uint32_t), stream);
-  if (e == cudaSuccess) e = scratch_alloc((void**)&k2, (size_t)n * sizeof(uint32_t), stream);
-  if (e == cudaSuccess) e = scratch_alloc((void**)&v1, (size_t)n * sizeof(uint32_t), stream);
-  if (e == cudaSuccess) e = scratch_alloc((void**)&v2, (size_t)n * sizeof(uint32_t), stream);
-  int rc = e == cudaSuccess ? kOk : cuda_error(e, "sort scratch");
+  uint32_t* hist = S.hist;
+  uint32_t* totals = S.totals;
+  int rc = kOk;
+  cudaError_t e = cudaSuccess;
   uint32_t* kin = dKeys;
-  uint32_t* kout = k2;
+  uint32_t* kout = S.k2;
   const uint32_t* vin = dVals;
-  uint32_t* vbuf[2] = {v1, v2};
+  uint32_t* vbuf[2] = {S.v1, S.v2};
   for (int p = 0; p < passes && rc == kOk; ++p) {
     const int shift = p * kRadixBits;
     const bool last = p == passes - 1;
@@ -521,8 +542,6 @@ int radix_passes(uint32_t* dKeys, int64_t n, int bits, const uint32_t* dVals, in
     std::swap(kin, kout);
     vin = vout;
   }
-  for (void* ptr : {(void*)k2, (void*)v1, (void*)v2, (void*)totals})
-    if (ptr) scratch_free(ptr, stream);
   return rc;
 }
 
@@ -531,11 +550,11 @@ int radix_passes(uint32_t* dKeys, int64_t n, int bits, const uint32_t* dVals, in
 int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaStream_t stream, const uint32_t* dVals) {
   if (n <= 0) return kOk;
   if (n > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
-  const SortPlan P(n);
-  uint32_t* hist = nullptr;
-  NABO_CUDA_TRY(scratch_alloc((void**)&hist, (size_t)(kRadix * P.nTiles) * sizeof(uint32_t), stream));
-  const int rc = radix_passes(dKeys, n, bits, dVals, dOrder, P, hist, false, stream);
-  scratch_free(hist, stream);
+  const SortPlan P(n, false);
+  SortScratch S;
+  NABO_CUDA_TRY(S.alloc(P, false, stream));
+  const int rc = radix_passes(dKeys, n, bits, dVals, dOrder, P, S, false, stream);
+  S.release(stream);
   return rc;
 }
 
@@ -544,8 +563,9 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
                   int32_t* dOrder, cudaStream_t stream, const QueryChunks* chunks) {
   if (nq <= 0) return kOk;
   if (nq > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
+  if (dim < 1 || dim > kMortonDims) return set_error(kErrInternal, "Morton order: 1 to 3 dimensions");
   CellParams p;
-  p.dims = std::min(dim, kMortonDims);
+  p.dims = dim;
   p.bits = 30 / p.dims;
   p.shift = 0;
   p.nChunks = chunks && chunks->n > 1 ? std::min(chunks->n, kMaxQueryChunks) : 0;
@@ -567,17 +587,13 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
       p.scale[d] = 0.0f;
     }
   }
-  const SortPlan P(nq);
-  uint32_t *keys = nullptr, *hist = nullptr;
-  cudaError_t e = scratch_alloc((void**)&keys, (size_t)nq * sizeof(uint32_t), stream);
-  if (e == cudaSuccess) e = scratch_alloc((void**)&hist, (size_t)(kRadix * P.nTiles) * sizeof(uint32_t), stream);
-  int rc = e == cudaSuccess ? kOk : cuda_error(e, "order scratch");
-  if (rc == kOk) {
-    k_morton_tiles<T><<<P.blocks, kTileThreads, 0, stream>>>(dQuery, nq, qStride, p, keys, hist);
-    rc = radix_passes(keys, nq, p.bits * p.dims + chunkBits, nullptr, dOrder, P, hist, true, stream);
-  }
-  if (keys) scratch_free(keys, stream);
-  if (hist) scratch_free(hist, stream);
+  const SortPlan P(nq, true);
+  SortScratch S;
+  const cudaError_t e = S.alloc(P, true, stream);
+  if (e != cudaSuccess) return cuda_error(e, "order scratch");
+  k_morton_tiles<T><<<P.blocks, kTileThreads, 0, stream>>>(dQuery, nq, qStride, p, S.keys, S.hist);
+  const int rc = radix_passes(S.keys, nq, p.bits * p.dims + chunkBits, nullptr, dOrder, P, S, true, stream);
+  S.release(stream);
   return rc;
 }
 
