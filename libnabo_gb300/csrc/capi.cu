@@ -350,8 +350,9 @@ int knn_given_order_any(const nabo_cuda_search* h, const KnnArgs& a, const int32
 }
 
 int chunk_order_any(const nabo_cuda_search* h, const void* query, int64_t nq, int64_t qStride,
-                    const QueryChunks& chunks, int32_t* order, cudaStream_t st) {
-  NABO_DISPATCH(h->c.dtype, h->c.dpad, (knn_chunk_order<T, D>(h->c, query, nq, qStride, chunks, order, st)));
+                    const QueryChunks& chunks, int32_t* order, cudaStream_t st, void* copyOut) {
+  NABO_DISPATCH(h->c.dtype, h->c.dpad,
+                (knn_chunk_order<T, D>(h->c, query, nq, qStride, chunks, order, st, copyOut)));
 }
 
 void free_events(nabo_cuda_search* s) {
@@ -771,6 +772,17 @@ bool is_pinned(const void* p) {
   return attr.type == cudaMemoryTypeHost;
 }
 
+// The device address of a page-locked host buffer mapped into the device's
+// address space, else nullptr.
+const void* mapped_host(const void* p) {
+  cudaPointerAttributes attr;
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
 // Large host-buffer searches whose result buffers are pinned: the queries
 // are uploaded and ordered once, then searched in pipelineChunks
 // consecutive chunks of shrinking size (the last chunk's download is the
@@ -813,11 +825,17 @@ int pipeline_enqueue(const nabo_cuda_search* s, const PipeRes* pr, cudaStream_t 
   if (e == cudaSuccess) e = scratch_alloc((void**)&dd, outN * es, main);
   if (e == cudaSuccess) e = scratch_alloc((void**)&dt, sizeof(unsigned long long), main);
   if (e == cudaSuccess && ordered) e = scratch_alloc((void**)&order, (size_t)nq * sizeof(int32_t), main);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dq, query, qBytes, cudaMemcpyHostToDevice, main);
+  // With query ordering and a device-mapped page-locked query buffer, the
+  // Morton kernel reads the queries over the host link and writes them to
+  // the device copy as it goes: the upload and the key pass in one.
+  const void* hostQuery = ordered ? mapped_host(query) : nullptr;
+  if (e == cudaSuccess && !hostQuery) e = cudaMemcpyAsync(dq, query, qBytes, cudaMemcpyHostToDevice, main);
   if (e == cudaSuccess && maxRadii) e = cudaMemcpyAsync(dr, maxRadii, (size_t)nq * es, cudaMemcpyHostToDevice, main);
   if (e == cudaSuccess) e = cudaMemsetAsync(dt, 0, sizeof(unsigned long long), main);
   if (e != cudaSuccess) rc = cuda_error(e, "knn pipeline setup");
-  if (rc == kOk && ordered) rc = chunk_order_any(s, dq, nq, qStride, chunks, order, main);
+  if (rc == kOk && ordered)
+    rc = hostQuery ? chunk_order_any(s, hostQuery, nq, qStride, chunks, order, main, dq)
+                   : chunk_order_any(s, dq, nq, qStride, chunks, order, main, nullptr);
   if (rc == kOk && cudaEventRecord(ready, main) != cudaSuccess) rc = cuda_error(cudaGetLastError(), "knn pipeline");
   for (int c = 0; c < chunks.n && rc == kOk; ++c) {
     const int64_t c0 = c ? chunks.end[c - 1] : 0, c1 = chunks.end[c];

@@ -279,7 +279,7 @@ template <typename T, int D>
 int knn_kdtree_given_order(const DeviceCloud& c, const KnnArgs& a, const int32_t* order, cudaStream_t stream);
 template <typename T, int D>
 int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, const QueryChunks& chunks,
-                    int32_t* order, cudaStream_t stream);
+                    int32_t* order, cudaStream_t stream, void* copyOut = nullptr);
 template <typename T, int D>
 int knn_leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, int32_t* order,
                    cudaStream_t stream);
@@ -339,10 +339,12 @@ int radius_model_k(const RadiusModel& m);
 // (a stable sort by Morton code). With chunks (n > 1) the permutation is
 // chunk-major: chunk c's queries come before those of chunk c+1, in Morton
 // order among themselves (the chunk number takes the top bits of a 32-bit
-// key, so more chunks leave a coarser curve).
+// key, so more chunks leave a coarser curve). With copyOut, the first dim
+// coordinates of each query row are also written there at the same
+// offsets (dQuery may then be a device-mapped page-locked host buffer).
 template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
-                  int32_t* dOrder, cudaStream_t stream, const QueryChunks* chunks = nullptr);
+                  int32_t* dOrder, cudaStream_t stream, const QueryChunks* chunks = nullptr, T* copyOut = nullptr);
 
 // Counting-sort placement: dHist holds per-cell counts (turned into offsets
 // in place), dCell/dRank each query's cell and rank inside it. With binsDev

@@ -210,10 +210,14 @@ __global__ void __launch_bounds__(kTileThreads) k_tile_hist(const uint32_t* __re
 }
 
 // Morton keys of the queries, in the radix sort's tile layout, with the
-// first pass's digit counts.
+// first pass's digit counts. With copyOut, the coordinates read (the first
+// dims of each row) are also written there at the same offsets: q may then
+// be page-locked host memory read over the host link, and the kernel is the
+// queries' upload too.
 template <typename T>
 __global__ void __launch_bounds__(kTileThreads) k_morton_tiles(const T* __restrict__ q, int64_t n, int64_t qStride,
-                                                               CellParams p, uint32_t* key, uint32_t* hist) {
+                                                               CellParams p, uint32_t* key, uint32_t* hist,
+                                                               T* __restrict__ copyOut) {
   __shared__ uint32_t h[kRadix];
   for (int d = threadIdx.x; d < kRadix; d += kTileThreads) h[d] = 0u;
   __syncthreads();
@@ -227,6 +231,15 @@ __global__ void __launch_bounds__(kTileThreads) k_morton_tiles(const T* __restri
       const int64_t i = run_index(r0 + u);
 #pragma unroll
       for (int d = 0; d < 3; ++d) c[u][d] = (i < n && d < p.dims) ? q[i * qStride + d] : T(0);
+    }
+    if (copyOut) {
+#pragma unroll
+      for (int u = 0; u < kHalf; ++u) {
+        const int64_t i = run_index(r0 + u);
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+          if (i < n && d < p.dims) copyOut[i * qStride + d] = c[u][d];
+      }
     }
 #pragma unroll
     for (int u = 0; u < kHalf; ++u) kk[u] = morton_key3(c[u], p);
@@ -560,7 +573,7 @@ int sort_order_u32(uint32_t* dKeys, int64_t n, int bits, int32_t* dOrder, cudaSt
 
 template <typename T>
 int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const double* lo, const double* hi,
-                  int32_t* dOrder, cudaStream_t stream, const QueryChunks* chunks) {
+                  int32_t* dOrder, cudaStream_t stream, const QueryChunks* chunks, T* copyOut) {
   if (nq <= 0) return kOk;
   if (nq > (int64_t)INT32_MAX) return set_error(kErrUnsupported, "sort: too many elements");
   if (dim < 1 || dim > kMortonDims) return set_error(kErrInternal, "Morton order: 1 to 3 dimensions");
@@ -591,7 +604,7 @@ int order_queries(const T* dQuery, int64_t nq, int64_t qStride, int dim, const d
   SortScratch S;
   const cudaError_t e = S.alloc(P, true, stream);
   if (e != cudaSuccess) return cuda_error(e, "order scratch");
-  k_morton_tiles<T><<<P.blocks, kTileThreads, 0, stream>>>(dQuery, nq, qStride, p, S.keys, S.hist);
+  k_morton_tiles<T><<<P.blocks, kTileThreads, 0, stream>>>(dQuery, nq, qStride, p, S.keys, S.hist, copyOut);
   const int rc = radix_passes(S.keys, nq, p.bits * p.dims + chunkBits, nullptr, dOrder, P, S, true, stream);
   S.release(stream);
   return rc;
@@ -610,8 +623,8 @@ QueryChunks shrinking_chunks(int64_t nq, int n) {
 }
 
 template int order_queries<float>(const float*, int64_t, int64_t, int, const double*, const double*, int32_t*,
-                                  cudaStream_t, const QueryChunks*);
+                                  cudaStream_t, const QueryChunks*, float*);
 template int order_queries<double>(const double*, int64_t, int64_t, int, const double*, const double*, int32_t*,
-                                   cudaStream_t, const QueryChunks*);
+                                   cudaStream_t, const QueryChunks*, double*);
 
 }  // namespace nabo_gb300

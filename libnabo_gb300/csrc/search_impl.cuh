@@ -385,12 +385,14 @@ int knn_leaf_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t 
 
 // Chunk-major Morton order (first by chunk, then along the curve) for a
 // search split into consecutive query chunks, one launch each; clouds of up
-// to 3 dimensions.
+// to 3 dimensions. With copyOut the queries are copied there as they are
+// read (see order_queries).
 template <typename T, int D>
 int knn_chunk_order(const DeviceCloud& c, const void* query, int64_t nq, int64_t qStride, const QueryChunks& chunks,
-                    int32_t* order, cudaStream_t stream) {
+                    int32_t* order, cudaStream_t stream, void* copyOut) {
   if (c.dim > 3) return set_error(kErrUnsupported, "chunked query order: more than 3 dimensions");
-  return order_queries<T>(static_cast<const T*>(query), nq, qStride, c.dim, c.lo, c.hi, order, stream, &chunks);
+  return order_queries<T>(static_cast<const T*>(query), nq, qStride, c.dim, c.lo, c.hi, order, stream, &chunks,
+                          static_cast<T*>(copyOut));
 }
 
 // Batched search over a forest: leaf order of all queries (each in its
@@ -557,6 +559,6 @@ int knn_batch(const BatchArgs& b, cudaStream_t stream) {
   template int knn_bruteforce<T, D>(const DeviceCloud&, const KnnArgs&, cudaStream_t); \
   template int knn_kdtree_given_order<T, D>(const DeviceCloud&, const KnnArgs&, const int32_t*, cudaStream_t); \
   template int knn_chunk_order<T, D>(const DeviceCloud&, const void*, int64_t, int64_t, const QueryChunks&, int32_t*, \
-                                     cudaStream_t);
+                                     cudaStream_t, void*);
 
 }  // namespace nabo_gb300
